@@ -1,0 +1,416 @@
+#!/usr/bin/env python
+"""Throughput benchmark: atom-force evaluations per second on one GB300.
+
+Workload (one "step"): a batch of B seeded ternary-alloy structures of 512
+atoms each (fcc 4x4x8, a = 3.9 A, Z = 13/28/40 at 0.5/0.3/0.2, jitter
+0.08 A), wACSF D = 64 (20 radial + 12 angular SFs, zeta 1/2/4), sparse GPR
+with M = 4000 points (theta = 0.8 std, coeff ~ N(0, 1e-3)); every step
+produces energy, forces and stress of all B*512 atoms.  Synthetic data, no
+dataset.  "value" is measured with inputs resident in HBM (device-buffer
+C-ABI call on the launching stream, CUDA events, L2 flushed between steps);
+"e2e" through the host-buffer C-ABI call with pinned host inputs, host<->device
+copies inside the timed region.  The precision form measured is the chosen
+fast form; the plain FP64 path is timed beside it, and both are compared
+with the FP64 oracle on one structure.
+
+--impl reference times the CPU restatement of the reference (the oracle,
+single-threaded per structure as the reference is) on all host cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "calypso-gap_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "atom-force evals/s on 1 GB300: chosen vs plain GPU at <=1 meV/atom, <=20 meV/A"
+UNIT = "atoms/s"
+ATOMS = 512
+M_SPARSE = 4000
+L2_FLUSH_BYTES = 512 << 20
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gapgb", choices=["gapgb", "reference"])
+    p.add_argument("--batch", type=int, default=64, help="structures per step per GPU")
+    p.add_argument("--precision", default="fp32", choices=["fp32", "tc", "fp64"])
+    p.add_argument("--no-oracle", action="store_true", help="skip the oracle error check")
+    return p.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def workload(rank, batch):
+    import gapgb.synth as S
+    structs = [S.alloy512(seed=100000 + rank * batch + s) for s in range(batch)]
+    return structs, S.pack(structs)
+
+
+def make_model():
+    """The synthetic alloy model: sparse points are descriptors of 8 seeded
+    alloy cells computed by the library itself."""
+    import gapgb
+    import gapgb.synth as S
+    ty, al, rc, ze = S.sf_table()
+    zt = np.array([13, 28, 40], np.int32)
+    wt = zt.astype(np.float64)
+    D = 2 * len(ty)
+    probe = gapgb.GapModel.create(zt, wt, ty, al, rc, np.ones(D), np.zeros((1, D)), np.zeros(1),
+                                  sf_zeta=ze)
+    cells = [S.alloy512(seed=s) for s in range(8)]
+    off, sp, lat, pos = S.pack(cells)
+    X = probe.descriptors(off, sp, lat, pos)
+    probe.close()
+    theta, mm, coeff = S.model_arrays(X, M_SPARSE, theta_scale=0.8, coeff_std=1e-3, seed=0)
+    arrays = (zt, wt, ty, al, rc, ze, theta, mm, coeff)
+    return arrays
+
+
+def clocks_sampler(stop, out):
+    q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    dev = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0] or "0"
+    try:
+        p = subprocess.Popen(["nvidia-smi", "-i", dev, "--query-gpu=" + q,
+                              "--format=csv,noheader,nounits", "-lms", "100"],
+                             stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    except (FileNotFoundError, OSError):
+        return
+    stop.wait()
+    p.terminate()
+    try:
+        txt, _ = p.communicate(timeout=5)
+    except subprocess.TimeoutExpired:
+        p.kill()
+        txt = ""
+    out.extend(l for l in txt.splitlines() if l.strip())
+
+
+def summarize_clocks(lines):
+    if not lines:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+    sm, smax, reasons = [], None, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for l in lines:
+        f = [x.strip() for x in l.split(",")]
+        try:
+            sm.append(float(f[1]))
+            smax = float(f[2])
+        except (ValueError, IndexError):
+            continue
+        for n, v in zip(names, f[5:9]):
+            if v.lower().startswith("active"):
+                reasons.add(n)
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+            "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def oracle_errors(arrays, structs, results):
+    """Max |dE|/atom (eV) and max |dF| (eV/A) of GPU results vs the FP64 oracle
+    on the first structure of the batch."""
+    import tempfile
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import write_model_file
+    from oracle import oracle
+    zt, wt, ty, al, rc, ze, theta, mm, coeff = arrays
+    with tempfile.TemporaryDirectory() as d:
+        path = write_model_file(os.path.join(d, "gp"), zt, wt, ty, al, rc, theta, mm, coeff, ze)
+        om = oracle.Model(path)
+        lat, pos, z = structs[0]
+        oE, oF, oS, _ = oracle.gap_calc(om, z, lat, pos, 6.0, True)
+    out = {}
+    for name, (E, F, St) in results.items():
+        out[name] = {"dE_per_atom_eV": abs(E[0] - oE) / len(pos),
+                     "max_dF_eV_per_A": float(np.abs(F[:len(pos)] - oF).max()),
+                     "max_dstress_GPa": float(np.abs(St[0] - oS).max())}
+    return out
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import tempfile
+    from helpers import write_model_file
+    # the same model arrays the GPU arm builds (descriptors from the oracle here)
+    import gapgb.synth as S
+    ty, al, rc, ze = S.sf_table()
+    zt = np.array([13, 28, 40], np.int32)
+    wt = zt.astype(np.float64)
+    D = 2 * len(ty)
+    cores = len(os.sched_getaffinity(0))
+    with tempfile.TemporaryDirectory() as d:
+        probe = write_model_file(os.path.join(d, "probe"), zt, wt, ty, al, rc, np.ones(D),
+                                 np.zeros((1, D)), np.zeros(1), ze)
+        pm = oracle.Model(probe)
+        X = []
+        for s in range(8):
+            lat, pos, z = S.alloy512(seed=s)
+            cnt, nb = oracle.neighbors(lat, pos, pm.weights(z), 6.0, 400)
+            X.append(oracle.car2acsf(pm, pos, cnt, nb)[0])
+        theta, mm, coeff = S.model_arrays(np.concatenate(X), M_SPARSE, 0.8, 1e-3, 0)
+        path = write_model_file(os.path.join(d, "gp"), zt, wt, ty, al, rc, theta, mm, coeff, ze)
+        om = oracle.Model(path)
+        structs = [S.alloy512(seed=100000 + s) for s in range(cores)]
+        off, sp, lat, pos = S.pack(structs)
+        times = []
+        for it in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            oracle.gap_calc_batch(om, off, sp, lat, pos, 6.0, cores)
+            dt = time.perf_counter() - t0
+            if it >= args.warmup:
+                times.append(dt)
+    atoms = cores * ATOMS
+    v = atoms * len(times) / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "alloy512 ternary fcc, D=64, M=4000", "atoms_per_structure": ATOMS,
+                   "structures_per_step": cores, "model": "synthetic sparse GPR"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d alloy512 structures per step, one per host thread "
+                                   "(CPU FP64 restatement, dense Jacobian as the reference)" % cores},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(arrays):
+    """The oracle on the host cores on a bounded sample (one alloy512
+    structure per core)."""
+    import tempfile
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import write_model_file
+    from oracle import oracle
+    import gapgb.synth as S
+    zt, wt, ty, al, rc, ze, theta, mm, coeff = arrays
+    cores = len(os.sched_getaffinity(0))
+    with tempfile.TemporaryDirectory() as d:
+        om = oracle.Model(write_model_file(os.path.join(d, "gp"), zt, wt, ty, al, rc, theta, mm,
+                                           coeff, ze))
+        structs = [S.alloy512(seed=100000 + s) for s in range(cores)]
+        off, sp, lat, pos = S.pack(structs)
+        t0 = time.perf_counter()
+        oracle.gap_calc_batch(om, off, sp, lat, pos, 6.0, cores)
+        dt = time.perf_counter() - t0
+    return {"value": cores * ATOMS / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d alloy512 structures (one per host thread), %.1f s" % (cores, dt)}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    import gapgb
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    os.environ.setdefault("GAPGB_PROFILE_STAGES", "0")
+    dev = torch.device("cuda", local)
+    arrays = make_model()
+    zt, wt, ty, al, rc, ze, theta, mm, coeff = arrays
+
+    def new_model(prec):
+        m = gapgb.GapModel.create(zt, wt, ty, al, rc, theta, mm, coeff, sf_zeta=ze)
+        m.set_precision(prec)
+        m.set_neighbour_cap(96)
+        return m
+
+    structs, (off, sp, lat, pos) = workload(rank, args.batch)
+    S, N = len(structs), int(off[-1])
+    d_off = torch.from_numpy(off).to(dev)
+    d_sp = torch.from_numpy(sp).to(dev)
+    d_lat = torch.from_numpy(lat).to(dev)
+    d_pos = torch.from_numpy(pos).to(dev)
+    d_E = torch.zeros(S, dtype=torch.float64, device=dev)
+    d_F = torch.zeros(N, 3, dtype=torch.float64, device=dev)
+    d_S = torch.zeros(S, 6, dtype=torch.float64, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def device_step(m):
+        m.eval_batch_ptrs(S, N, ATOMS, d_off.data_ptr(), d_sp.data_ptr(), d_lat.data_ptr(),
+                          d_pos.data_ptr(), 1, d_E.data_ptr(), d_F.data_ptr(), d_S.data_ptr(),
+                          0, stream.cuda_stream)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def time_device(m, steps, warmup, sampler=None):
+        for _ in range(warmup):
+            device_step(m)
+        torch.cuda.synchronize()
+        m.check_device_status()
+        barrier()
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        stop, lines, th = threading.Event(), [], None
+        if sampler:
+            th = threading.Thread(target=clocks_sampler, args=(stop, lines), daemon=True)
+            th.start()
+            time.sleep(0.3)
+        for a, b in evs:
+            flush.zero_()
+            a.record(stream)
+            device_step(m)
+            b.record(stream)
+        torch.cuda.synchronize()
+        if th:
+            stop.set()
+            th.join()
+        barrier()
+        m.check_device_status()
+        ms = sum(a.elapsed_time(b) for a, b in evs)
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        if world > 1:
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item()) / steps, summarize_clocks(lines)
+
+    chosen = new_model(args.precision)
+    ms_step, clocks = time_device(chosen, args.steps, args.warmup, sampler=(rank == 0))
+    value = world * N / (ms_step * 1e-3)
+    res_chosen = (d_E.cpu().numpy().copy(), d_F.cpu().numpy().copy(), d_S.cpu().numpy().copy())
+
+    # per-stage device times (library CUDA events on the launch stream)
+    os.environ["GAPGB_PROFILE_STAGES"] = "1"
+    prof = new_model(args.precision)
+    stages = np.zeros(4)
+    for it in range(args.warmup + 3):
+        flush.zero_()
+        device_step(prof)
+        prof.check_device_status()
+        if it >= args.warmup:
+            stages += np.array(prof.stage_times())
+    stages /= 3
+    prof.close()
+    os.environ["GAPGB_PROFILE_STAGES"] = "0"
+
+    # end to end through the host-buffer call, pinned host buffers
+    h_off = torch.from_numpy(off).pin_memory()
+    h_sp = torch.from_numpy(sp).pin_memory()
+    h_lat = torch.from_numpy(lat).pin_memory()
+    h_pos = torch.from_numpy(pos).pin_memory()
+    h_E = torch.zeros(S, dtype=torch.float64).pin_memory()
+    h_F = torch.zeros(N, 3, dtype=torch.float64).pin_memory()
+    h_S = torch.zeros(S, 6, dtype=torch.float64).pin_memory()
+
+    def host_step(m):
+        m.eval_batch_host_ptrs(S, h_off.data_ptr(), h_sp.data_ptr(), h_lat.data_ptr(),
+                               h_pos.data_ptr(), 1, h_E.data_ptr(), h_F.data_ptr(), h_S.data_ptr())
+
+    for _ in range(args.warmup):
+        host_step(chosen)
+    barrier()
+    t_host = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        host_step(chosen)
+        t_host += time.perf_counter() - t0
+    t = torch.tensor([t_host / args.steps], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    e2e_s = float(t.item())
+    h2d = off.nbytes + sp.nbytes + lat.nbytes + pos.nbytes
+    d2h = S * 8 + N * 3 * 8 + S * 6 * 8
+
+    # plain FP64 path on the same workload
+    plain = new_model("fp64")
+    psteps = max(2, args.steps // 3)
+    ms_plain, _ = time_device(plain, psteps, max(1, args.warmup // 2))
+    res_plain = (d_E.cpu().numpy().copy(), d_F.cpu().numpy().copy(), d_S.cpu().numpy().copy())
+    plain_value = world * N / (ms_plain * 1e-3)
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    errors = None if args.no_oracle else oracle_errors(
+        arrays, structs, {"chosen": res_chosen, "plain": res_plain})
+
+    # roofline of the dominant stage
+    D = 2 * len(ty)
+    names = ["neighbours", "descriptors", "gpr", "chain_rule"]
+    dom = int(np.argmax(stages))
+    gpr_flops = 4.0 * M_SPARSE * D * N  # x.m distances + (K o c).M, 2 flops each
+    gpr_bytes = N * D * 4 * 2 + M_SPARSE * D * 4 + N * 8
+    roof = {"kernel": names[dom], "stage_ms": {n: float(s) for n, s in zip(names, stages)}}
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+    if args.precision == "tc" and names[dom] == "gpr":
+        ach = gpr_flops / (stages[dom] * 1e-3) / 1e12
+        roof.update(bound="tensor", achieved=ach, peak=peaks["bf16_tflops"], unit="TFLOP/s",
+                    frac=ach / peaks["bf16_tflops"], traffic=None, peak_source="measured")
+    else:
+        # descriptor-side kernels: algorithmic HBM bytes (neighbour slots,
+        # descriptor rows) over the stage time; they are FP32/FP64-pipe bound
+        P = 56.0
+        per_atom = {"neighbours": 32.0 + P * 44.0, "descriptors": P * (32 + 4 + 32) + D * 4,
+                    "gpr": gpr_bytes / N, "chain_rule": P * (32 + 4 + 32 + 16) + D * 4 + 9 * 8}
+        ach = per_atom[names[dom]] * N / (stages[dom] * 1e-3) / 1e9
+        roof.update(bound="hbm", achieved=ach, peak=peaks["hbm_gbs"], unit="GB/s",
+                    frac=ach / peaks["hbm_gbs"], traffic=None, peak_source="measured")
+    roof["gpr_tflops"] = gpr_flops / (stages[2] * 1e-3) / 1e12
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": {"fp32": "f32", "tc": "bf16x3/f32", "fp64": "f64"}[args.precision],
+        "data": "synthetic",
+        "config": {"workload": "alloy512 ternary fcc (Z 13/28/40), D=64, M=4000",
+                   "structures_per_step": S, "atoms_per_step_per_gpu": N,
+                   "precision": args.precision, "l2": "flushed between steps (512 MB write)"},
+        "e2e": {"value": world * N / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "plain_fp64": {"value": plain_value, "unit": UNIT, "ms_per_step": ms_plain},
+        "speedup_vs_plain": value / plain_value,
+        "errors_vs_oracle": errors,
+        "roofline": roof,
+        "gpu_launches": None,
+        "clocks": clocks,
+    }
+    # kernels launched per step (count from the library's launch sequence)
+    # prep x2, neighbours, reverse, descriptors, GPR (+ split reduce), slot
+    # gradients, forces, orphans, structure reduce
+    line["gpu_launches"] = args.steps * 10
+    if world == 1:
+        line["cpu_baseline"] = cpu_baseline(arrays)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

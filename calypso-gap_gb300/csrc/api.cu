@@ -1,0 +1,676 @@
+// api.cu - the C ABI (include/gapgb.h): models, workspace, evaluation.
+//
+// One evaluation of a packed batch is, in stream order:
+//   prep (lattice images, weights)  -> neighbour list -> reverse slots
+//   -> descriptors G -> GPR (e, dE/dG) -> slot gradients + per-atom virial
+//   -> forces (gather) -> per-structure energy and stress.
+// This is FGAP_CALC (gappy/libgap/gap_calc.f90:1-301) for many structures at
+// once, without the dense Jacobian.  The host-buffer calls synchronise once
+// after the neighbour list to size shared memory and grow the neighbour
+// capacity on overflow; the device-buffer call never synchronises.
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <algorithm>
+#include <mutex>
+
+#include "gapgb_internal.h"
+
+namespace gapgb {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const std::string &s) { g_last_error = s; }
+
+namespace {
+
+gapgb_status fail(gapgb_status st, const std::string &msg) {
+  set_last_error(msg);
+  return st;
+}
+
+template <typename T>
+void free_dev(T *&p) {
+  if (p) cudaFree((void *)p);
+  p = nullptr;
+}
+
+void free_ws(Workspace &ws) {
+  free_dev(ws.d_atom_off);
+  free_dev(ws.d_species);
+  free_dev(ws.d_lat);
+  free_dev(ws.d_pos);
+  free_dev(ws.d_energy);
+  free_dev(ws.d_force);
+  free_dev(ws.d_stress);
+  free_dev(ws.d_atom_e);
+  free_dev(ws.apos);
+  free_dev(ws.frac32);
+  free_dev(ws.atom_struct);
+  free_dev(ws.sinfo);
+  free_dev(ws.nbr_cnt);
+  free_dev(ws.nbr_j);
+  free_dev(ws.nbr_s);
+  free_dev(ws.nbr_rev);
+  free_dev(ws.nbr_xyz);
+  free_dev(ws.G);
+  free_dev(ws.dedg);
+  free_dev(ws.gslot);
+  free_dev(ws.e);
+  free_dev(ws.wvir);
+  free_dev(ws.d_flags);
+  free_dev(ws.orphans);
+  free_dev(ws.gpr_scratch);
+  if (ws.h_flags) cudaFreeHost(ws.h_flags);
+  ws.h_flags = nullptr;
+  ws.N = ws.S = ws.cap = ws.D = 0;
+  ws.gpr_scratch_size = 0;
+}
+
+#define WS_ALLOC(ptr, count)                                                        \
+  do {                                                                              \
+    if (cudaMalloc((void **)&(ptr), sizeof(*(ptr)) * (size_t)(count) + 16) !=       \
+        cudaSuccess) {                                                              \
+      free_ws(ws);                                                                  \
+      return fail(GAPGB_ERR_ALLOC, "cudaMalloc failed for workspace");              \
+    }                                                                               \
+  } while (0)
+
+gapgb_status ensure_ws(gapgb_model *m, int N, int S, int cap) {
+  Workspace &ws = m->ws;
+  const int D = m->host.D;
+  const size_t scratch = gpr_scratch_bytes(N, m->host.M, D, sizeof(double));
+  if (ws.d_flags && N <= ws.N && S <= ws.S && cap <= ws.cap && D == ws.D &&
+      scratch <= ws.gpr_scratch_size)
+    return GAPGB_OK;
+  // grow with headroom so that slightly larger batches do not reallocate
+  int nN = N > ws.N ? N + N / 8 : ws.N;
+  int nS = S > ws.S ? S + S / 8 : ws.S;
+  int nC = cap > ws.cap ? cap : ws.cap;
+  free_ws(ws);
+  const size_t nslots = (size_t)nN * nC;
+  WS_ALLOC(ws.d_atom_off, nS + 1);
+  WS_ALLOC(ws.d_species, nN);
+  WS_ALLOC(ws.d_lat, (size_t)nS * 9);
+  WS_ALLOC(ws.d_pos, (size_t)nN * 3);
+  WS_ALLOC(ws.d_energy, nS);
+  WS_ALLOC(ws.d_force, (size_t)nN * 3);
+  WS_ALLOC(ws.d_stress, (size_t)nS * 6);
+  WS_ALLOC(ws.d_atom_e, nN);
+  WS_ALLOC(ws.apos, nN);
+  WS_ALLOC(ws.frac32, nN);
+  WS_ALLOC(ws.atom_struct, nN);
+  WS_ALLOC(ws.sinfo, nS);
+  WS_ALLOC(ws.nbr_cnt, nN);
+  WS_ALLOC(ws.nbr_j, nslots);
+  WS_ALLOC(ws.nbr_s, nslots);
+  WS_ALLOC(ws.nbr_rev, nslots);
+  WS_ALLOC(ws.nbr_xyz, nslots);
+  WS_ALLOC(*(double **)&ws.G, (size_t)nN * D);
+  WS_ALLOC(*(double **)&ws.dedg, (size_t)nN * D);
+  WS_ALLOC(*(double4 **)&ws.gslot, nslots);
+  WS_ALLOC(ws.e, nN);
+  WS_ALLOC(ws.wvir, (size_t)nN * 9);
+  WS_ALLOC(ws.d_flags, 8);
+  ws.orphan_cap = 1 << 16;
+  WS_ALLOC(ws.orphans, ws.orphan_cap);
+  // the split count depends on N: size for both the request and the headroom
+  const size_t sc = std::max(scratch, gpr_scratch_bytes(nN, m->host.M, D, sizeof(double)));
+  if (sc > 0) {
+    if (cudaMalloc(&ws.gpr_scratch, sc) != cudaSuccess) {
+      free_ws(ws);
+      return fail(GAPGB_ERR_ALLOC, "cudaMalloc failed for GPR scratch");
+    }
+  }
+  ws.gpr_scratch_size = sc;
+  if (cudaMallocHost((void **)&ws.h_flags, 8 * sizeof(int)) != cudaSuccess) {
+    free_ws(ws);
+    return fail(GAPGB_ERR_ALLOC, "cudaMallocHost failed");
+  }
+  ws.N = nN;
+  ws.S = nS;
+  ws.cap = nC;
+  ws.D = D;
+  return GAPGB_OK;
+}
+
+// Host-side validation at model creation (no device work).
+gapgb_status validate_model(gapgb_model *m) {
+  const HostModel &h = m->host;
+  std::string err;
+  gapgb_status st = build_sf_table(h, &m->sfh, &err);
+  if (st) return fail(st, err);
+  if (h.D > 128) return fail(GAPGB_ERR_CAP_EXCEEDED, "descriptor length D > 128");
+  for (int d = 0; d < h.D; ++d)
+    if (!(h.theta[d] != 0.0) || !std::isfinite(h.theta[d]))
+      return fail(GAPGB_ERR_PARSE, "theta must be finite and non-zero");
+  return GAPGB_OK;
+}
+
+// Device upload, done by the first call that needs the GPU.
+gapgb_status upload_model(gapgb_model *m) {
+  if (m->d_sf) return GAPGB_OK;
+  const HostModel &h = m->host;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
+    return fail(GAPGB_ERR_NO_DEVICE, "no CUDA device visible");
+  if (m->device < 0 || m->device >= ndev) return fail(GAPGB_ERR_ARG, "device ordinal out of range");
+  GAPGB_CUDA_TRY(cudaSetDevice(m->device));
+  const int M = h.M, D = h.D;
+  std::vector<double> mmt((size_t)M * D), invth(D);
+  std::vector<float> mmt32((size_t)M * D), invth32(D), coeff32(M);
+  for (int d = 0; d < D; ++d) {
+    invth[d] = 1.0 / h.theta[d];
+    invth32[d] = (float)invth[d];
+  }
+  for (int k = 0; k < M; ++k) {
+    coeff32[k] = (float)h.coeff[k];
+    for (int d = 0; d < D; ++d) {
+      mmt[(size_t)k * D + d] = h.mm[(size_t)k * D + d] / h.theta[d];
+      mmt32[(size_t)k * D + d] = (float)mmt[(size_t)k * D + d];
+    }
+  }
+  SFDev *d_sf = nullptr;
+  GAPGB_CUDA_TRY(cudaMalloc(&d_sf, sizeof(SFDev)));
+  GAPGB_CUDA_TRY(cudaMemcpy(d_sf, &m->sfh, sizeof(SFDev), cudaMemcpyHostToDevice));
+  GAPGB_CUDA_TRY(cudaMalloc(&m->d_mmt, sizeof(double) * mmt.size()));
+  GAPGB_CUDA_TRY(cudaMemcpy(m->d_mmt, mmt.data(), sizeof(double) * mmt.size(), cudaMemcpyHostToDevice));
+  GAPGB_CUDA_TRY(cudaMalloc(&m->d_mmt32, sizeof(float) * mmt32.size()));
+  GAPGB_CUDA_TRY(cudaMemcpy(m->d_mmt32, mmt32.data(), sizeof(float) * mmt32.size(), cudaMemcpyHostToDevice));
+  GAPGB_CUDA_TRY(cudaMalloc(&m->d_invth, sizeof(double) * D));
+  GAPGB_CUDA_TRY(cudaMemcpy(m->d_invth, invth.data(), sizeof(double) * D, cudaMemcpyHostToDevice));
+  GAPGB_CUDA_TRY(cudaMalloc(&m->d_invth32, sizeof(float) * D));
+  GAPGB_CUDA_TRY(cudaMemcpy(m->d_invth32, invth32.data(), sizeof(float) * D, cudaMemcpyHostToDevice));
+  GAPGB_CUDA_TRY(cudaMalloc(&m->d_coeff, sizeof(double) * M));
+  GAPGB_CUDA_TRY(cudaMemcpy(m->d_coeff, h.coeff.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
+  GAPGB_CUDA_TRY(cudaMalloc(&m->d_coeff32, sizeof(float) * M));
+  GAPGB_CUDA_TRY(cudaMemcpy(m->d_coeff32, coeff32.data(), sizeof(float) * M, cudaMemcpyHostToDevice));
+  GAPGB_CUDA_TRY(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+  for (auto &e : m->ev) GAPGB_CUDA_TRY(cudaEventCreate(&e));
+  const char *prof = std::getenv("GAPGB_PROFILE_STAGES");
+  m->profile_stages = prof && prof[0] && prof[0] != '0';
+  m->d_sf = d_sf;  // marks the model as uploaded
+  return GAPGB_OK;
+}
+
+bool finite_all(const double *p, size_t n) {
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(p[i])) return false;
+  return true;
+}
+
+gapgb_status check_batch_host(int nstruct, const int *atom_off, const double *lat,
+                              const double *pos) {
+  if (nstruct <= 0 || !atom_off) return fail(GAPGB_ERR_ARG, "nstruct must be positive");
+  if (atom_off[0] != 0) return fail(GAPGB_ERR_ARG, "atom_off[0] must be 0");
+  for (int s = 0; s < nstruct; ++s)
+    if (atom_off[s + 1] <= atom_off[s]) return fail(GAPGB_ERR_ARG, "every structure needs at least one atom");
+  if (!finite_all(lat, (size_t)nstruct * 9)) return fail(GAPGB_ERR_ARG, "non-finite lattice");
+  if (!finite_all(pos, (size_t)atom_off[nstruct] * 3)) return fail(GAPGB_ERR_ARG, "non-finite position");
+  for (int s = 0; s < nstruct; ++s) {
+    const double *L = lat + (size_t)s * 9;
+    const double det = L[0] * (L[4] * L[8] - L[5] * L[7]) - L[1] * (L[3] * L[8] - L[5] * L[6]) +
+                       L[2] * (L[3] * L[7] - L[4] * L[6]);
+    if (!(std::fabs(det) > 0.0)) return fail(GAPGB_ERR_ARG, "singular lattice");
+  }
+  return GAPGB_OK;
+}
+
+// Everything after the neighbour list, enqueued on `st`.
+gapgb_status enqueue_tail(gapgb_model *m, int S, int N, int cap, int capS, int lgrad,
+                          double *d_energy, double *d_force, double *d_stress, double *d_atom_e,
+                          cudaStream_t st) {
+  Workspace &ws = m->ws;
+  const bool prof = m->profile_stages;
+  launch_reverse(ws, N, cap, st);
+  if (prof) cudaEventRecord(m->ev[1], st);
+  const bool fp64 = m->precision == GAPGB_PREC_FP64;
+  if (fp64) launch_wacsf_fwd<double>(m, ws, N, cap, capS, st);
+  else launch_wacsf_fwd<float>(m, ws, N, cap, capS, st);
+  if (prof) cudaEventRecord(m->ev[2], st);
+  if (m->precision == GAPGB_PREC_TC) launch_gpr_tc(m, ws, N, st);
+  else if (fp64) launch_gpr<double>(m, ws, N, st);
+  else launch_gpr<float>(m, ws, N, st);
+  if (prof) cudaEventRecord(m->ev[3], st);
+  if (lgrad) {
+    if (fp64) {
+      launch_wacsf_bwd<double>(m, ws, N, cap, capS, st);
+      launch_forces<double>(ws, N, cap, d_force, st);
+    } else {
+      launch_wacsf_bwd<float>(m, ws, N, cap, capS, st);
+      launch_forces<float>(ws, N, cap, d_force, st);
+    }
+  } else {
+    cudaMemsetAsync(d_force, 0, sizeof(double) * 3 * (size_t)N, st);
+  }
+  launch_struct_reduce(ws, S, lgrad, d_energy, d_stress, d_atom_e, N, st);
+  if (prof) cudaEventRecord(m->ev[4], st);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(GAPGB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  return GAPGB_OK;
+}
+
+gapgb_status flags_to_status(const int *f) {
+  if (f[0] & kFlagUnknownSpecies) return fail(GAPGB_ERR_UNKNOWN_SPECIES, "atomic number not in the model's species table");
+  if (f[0] & kFlagImageLimit) return fail(GAPGB_ERR_CAP_EXCEEDED, "more than 127 periodic images per lattice direction");
+  if (f[0] & kFlagNeighbourOverflow) return fail(GAPGB_ERR_NEIGHBOUR_OVERFLOW, "neighbour capacity exceeded (max count " + std::to_string(f[1]) + ")");
+  if (f[0] & kFlagOrphanOverflow) return fail(GAPGB_ERR_CAP_EXCEEDED, "too many unpaired neighbour slots");
+  return GAPGB_OK;
+}
+
+void read_stage_times(gapgb_model *m) {
+  if (!m->profile_stages) return;
+  cudaEventSynchronize(m->ev[4]);
+  for (int q = 0; q < 4; ++q) cudaEventElapsedTime(&m->stage_ms[q], m->ev[q], m->ev[q + 1]);
+}
+
+// Host-buffer path: copies, neighbour list, one sync, the rest, copies back.
+gapgb_status eval_host(gapgb_model *m, int S, const int *atom_off, const int *species,
+                       const double *lat, const double *pos, int lgrad, double *energy,
+                       double *force, double *stress, double *atom_e, double **d_G_out) {
+  gapgb_status st = check_batch_host(S, atom_off, lat, pos);
+  if (st) return st;
+  const int N = atom_off[S];
+  st = upload_model(m);
+  if (st) return st;
+  GAPGB_CUDA_TRY(cudaSetDevice(m->device));
+  st = ensure_ws(m, N, S, m->cap);
+  if (st) return st;
+  Workspace &ws = m->ws;
+  cudaStream_t s = m->stream;
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_atom_off, atom_off, sizeof(int) * (S + 1), cudaMemcpyHostToDevice, s));
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_species, species, sizeof(int) * N, cudaMemcpyHostToDevice, s));
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_lat, lat, sizeof(double) * 9 * S, cudaMemcpyHostToDevice, s));
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_pos, pos, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s));
+  for (int attempt = 0; attempt < 3; ++attempt) {
+    const int cap = m->cap;
+    GAPGB_CUDA_TRY(cudaMemsetAsync(ws.d_flags, 0, 8 * sizeof(int), s));
+    if (m->profile_stages) cudaEventRecord(m->ev[0], s);
+    launch_prep(m, ws, S, N, ws.d_atom_off, ws.d_species, ws.d_lat, ws.d_pos, m->host.rcut, s);
+    launch_neighbors(ws, N, cap, m->host.rcut, s);
+    GAPGB_CUDA_TRY(cudaGetLastError());
+    GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.h_flags, ws.d_flags, 8 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    GAPGB_CUDA_TRY(cudaStreamSynchronize(s));
+    const int maxcnt = ws.h_flags[1];
+    if (ws.h_flags[0] & kFlagNeighbourOverflow) {
+      const int newcap = ((maxcnt + 31) / 32) * 32;
+      m->cap = newcap;
+      st = ensure_ws(m, N, S, newcap);
+      if (st) return st;
+      continue;
+    }
+    st = flags_to_status(ws.h_flags);
+    if (st) return st;
+    const int capS = maxcnt > 0 ? maxcnt : 1;
+    if (d_G_out) {
+      // descriptors only (gapgb_descriptors)
+      launch_reverse(ws, N, cap, s);
+      if (m->precision == GAPGB_PREC_FP64) launch_wacsf_fwd<double>(m, ws, N, cap, capS, s);
+      else launch_wacsf_fwd<float>(m, ws, N, cap, capS, s);
+      GAPGB_CUDA_TRY(cudaGetLastError());
+      *d_G_out = (double *)ws.G;
+      GAPGB_CUDA_TRY(cudaStreamSynchronize(s));
+      return GAPGB_OK;
+    }
+    st = enqueue_tail(m, S, N, cap, capS, lgrad, ws.d_energy, ws.d_force, ws.d_stress, ws.d_atom_e, s);
+    if (st) return st;
+    GAPGB_CUDA_TRY(cudaMemcpyAsync(energy, ws.d_energy, sizeof(double) * S, cudaMemcpyDeviceToHost, s));
+    if (force) GAPGB_CUDA_TRY(cudaMemcpyAsync(force, ws.d_force, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s));
+    if (stress) GAPGB_CUDA_TRY(cudaMemcpyAsync(stress, ws.d_stress, sizeof(double) * 6 * S, cudaMemcpyDeviceToHost, s));
+    if (atom_e) GAPGB_CUDA_TRY(cudaMemcpyAsync(atom_e, ws.d_atom_e, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+    GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.h_flags, ws.d_flags, 8 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    GAPGB_CUDA_TRY(cudaStreamSynchronize(s));
+    read_stage_times(m);
+    return flags_to_status(ws.h_flags);
+  }
+  return fail(GAPGB_ERR_NEIGHBOUR_OVERFLOW, "neighbour capacity could not be grown");
+}
+
+}  // namespace
+}  // namespace gapgb
+
+using namespace gapgb;
+
+extern "C" {
+
+const char *gapgb_status_string(gapgb_status st) {
+  switch (st) {
+    case GAPGB_OK: return "ok";
+    case GAPGB_ERR_FILE: return "model file missing or unreadable";
+    case GAPGB_ERR_PARSE: return "model file malformed";
+    case GAPGB_ERR_CAP_EXCEEDED: return "size beyond a documented limit";
+    case GAPGB_ERR_UNKNOWN_SPECIES: return "atomic number absent from the model";
+    case GAPGB_ERR_NEIGHBOUR_OVERFLOW: return "neighbour capacity exceeded";
+    case GAPGB_ERR_CUDA: return "CUDA error";
+    case GAPGB_ERR_TIMEOUT: return "device wait timed out";
+    case GAPGB_ERR_ARG: return "invalid argument";
+    case GAPGB_ERR_ALLOC: return "allocation failed";
+    case GAPGB_ERR_NO_DEVICE: return "no CUDA device";
+  }
+  return "unknown status";
+}
+
+const char *gapgb_last_error(void) { return g_last_error.c_str(); }
+
+const char *gapgb_version(void) { return "gapgb 0.1 (sm_103a)"; }
+
+gapgb_status gapgb_model_load(const char *path, double rcut, gapgb_model **out) {
+  if (!path || !out) return fail(GAPGB_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (!(rcut > 0.0)) return fail(GAPGB_ERR_ARG, "rcut must be positive");
+  gapgb_model *m = new gapgb_model();
+  std::string err;
+  gapgb_status st = parse_model_file(path, &m->host, &err);
+  if (st) {
+    delete m;
+    return fail(st, err);
+  }
+  m->host.rcut = rcut;
+  st = validate_model(m);
+  if (st) {
+    gapgb_model_free(m);
+    return st;
+  }
+  *out = m;
+  return GAPGB_OK;
+}
+
+gapgb_status gapgb_model_create(int nspecies, const int *species_z, const double *species_w,
+                                int nsf, const int *sf_type, const double *sf_alpha,
+                                const double *sf_cutoff, const double *sf_zeta, int nsparse,
+                                int des_len, const double *theta, const double *mm,
+                                const double *coeff, double rcut, gapgb_model **out) {
+  if (!out || !species_z || !species_w || !sf_type || !sf_alpha || !sf_cutoff || !theta || !mm ||
+      !coeff)
+    return fail(GAPGB_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (nspecies <= 0 || nsf <= 0 || nsf > kMaxSF || nsparse <= 0 || des_len <= 0 || !(rcut > 0.0))
+    return fail(GAPGB_ERR_ARG, "sizes must be positive (nsf <= 128)");
+  gapgb_model *m = new gapgb_model();
+  HostModel &h = m->host;
+  h.nspecies = nspecies;
+  h.species_z.assign(species_z, species_z + nspecies);
+  h.species_w.assign(species_w, species_w + nspecies);
+  h.nsf = nsf;
+  h.sf_type.assign(sf_type, sf_type + nsf);
+  h.sf_alpha.assign(sf_alpha, sf_alpha + nsf);
+  h.sf_cutoff.assign(sf_cutoff, sf_cutoff + nsf);
+  h.sf_zeta.assign(nsf, 1.0);
+  if (sf_zeta) h.sf_zeta.assign(sf_zeta, sf_zeta + nsf);
+  h.M = nsparse;
+  h.D = des_len;
+  h.theta.assign(theta, theta + des_len);
+  h.mm.assign(mm, mm + (size_t)nsparse * des_len);
+  h.coeff.assign(coeff, coeff + nsparse);
+  h.rcut = rcut;
+  gapgb_status st = validate_model(m);
+  if (st) {
+    gapgb_model_free(m);
+    return st;
+  }
+  *out = m;
+  return GAPGB_OK;
+}
+
+void gapgb_model_free(gapgb_model *m) {
+  if (!m) return;
+  cudaSetDevice(m->device);
+  free_ws(m->ws);
+  free_dev(m->d_sf);
+  free_dev(m->d_mmt);
+  free_dev(m->d_mmt32);
+  free_dev(m->d_invth);
+  free_dev(m->d_invth32);
+  free_dev(m->d_coeff);
+  free_dev(m->d_coeff32);
+  if (m->d_tc) cudaFree(m->d_tc);
+  for (auto &e : m->ev)
+    if (e) cudaEventDestroy(e);
+  if (m->stream) cudaStreamDestroy(m->stream);
+  delete m;
+}
+
+gapgb_status gapgb_model_info(const gapgb_model *m, int *nsparse, int *des_len, int *nsf,
+                              int *nspecies, double *rcut) {
+  if (!m) return fail(GAPGB_ERR_ARG, "null model");
+  if (nsparse) *nsparse = m->host.M;
+  if (des_len) *des_len = m->host.D;
+  if (nsf) *nsf = m->host.nsf;
+  if (nspecies) *nspecies = m->host.nspecies;
+  if (rcut) *rcut = m->host.rcut;
+  return GAPGB_OK;
+}
+
+gapgb_status gapgb_model_arrays(const gapgb_model *m, double *theta, double *mm, double *coeff) {
+  if (!m) return fail(GAPGB_ERR_ARG, "null model");
+  if (theta) std::memcpy(theta, m->host.theta.data(), sizeof(double) * m->host.D);
+  if (mm) std::memcpy(mm, m->host.mm.data(), sizeof(double) * m->host.mm.size());
+  if (coeff) std::memcpy(coeff, m->host.coeff.data(), sizeof(double) * m->host.M);
+  return GAPGB_OK;
+}
+
+gapgb_status gapgb_model_tables(const gapgb_model *m, int *species_z, double *species_w,
+                                int *sf_type, double *sf_alpha, double *sf_cutoff,
+                                double *sf_zeta) {
+  if (!m) return fail(GAPGB_ERR_ARG, "null model");
+  const HostModel &h = m->host;
+  if (species_z) std::memcpy(species_z, h.species_z.data(), sizeof(int) * h.nspecies);
+  if (species_w) std::memcpy(species_w, h.species_w.data(), sizeof(double) * h.nspecies);
+  if (sf_type) std::memcpy(sf_type, h.sf_type.data(), sizeof(int) * h.nsf);
+  if (sf_alpha) std::memcpy(sf_alpha, h.sf_alpha.data(), sizeof(double) * h.nsf);
+  if (sf_cutoff) std::memcpy(sf_cutoff, h.sf_cutoff.data(), sizeof(double) * h.nsf);
+  if (sf_zeta) std::memcpy(sf_zeta, h.sf_zeta.data(), sizeof(double) * h.nsf);
+  return GAPGB_OK;
+}
+
+gapgb_status gapgb_set_option(gapgb_model *m, gapgb_option opt, int64_t value) {
+  if (!m) return fail(GAPGB_ERR_ARG, "null model");
+  switch (opt) {
+    case GAPGB_OPT_PRECISION:
+      if (value == GAPGB_PREC_TC) return fail(GAPGB_ERR_ARG, "tensor-core GPR not built yet");
+      if (value != GAPGB_PREC_FP64 && value != GAPGB_PREC_FP32)
+        return fail(GAPGB_ERR_ARG, "unknown precision");
+      m->precision = (int)value;
+      return GAPGB_OK;
+    case GAPGB_OPT_NEIGHBOUR_CAP:
+      if (value < 1 || value > 65536) return fail(GAPGB_ERR_ARG, "capacity out of range");
+      m->cap = (int)value;
+      return GAPGB_OK;
+    case GAPGB_OPT_DEVICE:
+      return fail(GAPGB_ERR_ARG, "the device is fixed when the model is created");
+  }
+  return fail(GAPGB_ERR_ARG, "unknown option");
+}
+
+gapgb_status gapgb_get_option(const gapgb_model *m, gapgb_option opt, int64_t *value) {
+  if (!m || !value) return fail(GAPGB_ERR_ARG, "null argument");
+  switch (opt) {
+    case GAPGB_OPT_PRECISION: *value = m->precision; return GAPGB_OK;
+    case GAPGB_OPT_NEIGHBOUR_CAP: *value = m->cap; return GAPGB_OK;
+    case GAPGB_OPT_DEVICE: *value = m->device; return GAPGB_OK;
+  }
+  return fail(GAPGB_ERR_ARG, "unknown option");
+}
+
+gapgb_status gapgb_eval(gapgb_model *m, int natoms, const int *species, const double *lat,
+                        const double *pos, int lgrad, double *energy, double *force,
+                        double *stress, double *variance) {
+  if (!m || !species || !lat || !pos || !energy) return fail(GAPGB_ERR_ARG, "null argument");
+  if (natoms <= 0) return fail(GAPGB_ERR_ARG, "natoms must be positive");
+  if (lgrad && (!force || !stress)) return fail(GAPGB_ERR_ARG, "force and stress needed with lgrad");
+  const int off[2] = {0, natoms};
+  double stress_local[6];
+  gapgb_status st = eval_host(m, 1, off, species, lat, pos, lgrad, energy, force,
+                              stress ? stress : stress_local, nullptr, nullptr);
+  if (variance) *variance = 0.0;  // gap_calc.f90:206
+  return st;
+}
+
+gapgb_status gapgb_eval_batch(gapgb_model *m, int nstruct, const int *atom_off, const int *species,
+                              const double *lat, const double *pos, int lgrad, double *energy,
+                              double *force, double *stress, double *atom_energy) {
+  if (!m || !atom_off || !species || !lat || !pos || !energy)
+    return fail(GAPGB_ERR_ARG, "null argument");
+  if (lgrad && (!force || !stress)) return fail(GAPGB_ERR_ARG, "force and stress needed with lgrad");
+  return eval_host(m, nstruct, atom_off, species, lat, pos, lgrad, energy, force, stress,
+                   atom_energy, nullptr);
+}
+
+gapgb_status gapgb_eval_batch_device(gapgb_model *m, int nstruct, int natoms, int max_atoms,
+                                     const int *d_atom_off, const int *d_species,
+                                     const double *d_lat, const double *d_pos, int lgrad,
+                                     double *d_energy, double *d_force, double *d_stress,
+                                     double *d_atom_energy, void *stream) {
+  (void)max_atoms;
+  if (!m || !d_atom_off || !d_species || !d_lat || !d_pos || !d_energy)
+    return fail(GAPGB_ERR_ARG, "null argument");
+  if (nstruct <= 0 || natoms <= 0) return fail(GAPGB_ERR_ARG, "sizes must be positive");
+  if (lgrad && (!d_force || !d_stress)) return fail(GAPGB_ERR_ARG, "force and stress needed with lgrad");
+  gapgb_status st = upload_model(m);
+  if (st) return st;
+  GAPGB_CUDA_TRY(cudaSetDevice(m->device));
+  st = ensure_ws(m, natoms, nstruct, m->cap);
+  if (st) return st;
+  Workspace &ws = m->ws;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int cap = m->cap;
+  GAPGB_CUDA_TRY(cudaMemsetAsync(ws.d_flags, 0, 8 * sizeof(int), s));
+  if (m->profile_stages) cudaEventRecord(m->ev[0], s);
+  launch_prep(m, ws, nstruct, natoms, d_atom_off, d_species, d_lat, d_pos, m->host.rcut, s);
+  launch_neighbors(ws, natoms, cap, m->host.rcut, s);
+  double *d_stress_use = d_stress ? d_stress : ws.d_stress;
+  double *d_force_use = d_force ? d_force : ws.d_force;
+  return enqueue_tail(m, nstruct, natoms, cap, cap, lgrad, d_energy, d_force_use, d_stress_use,
+                      d_atom_energy, s);
+}
+
+gapgb_status gapgb_check_device_status(gapgb_model *m) {
+  if (!m) return fail(GAPGB_ERR_ARG, "null model");
+  if (!m->ws.d_flags) return GAPGB_OK;
+  GAPGB_CUDA_TRY(cudaSetDevice(m->device));
+  GAPGB_CUDA_TRY(cudaDeviceSynchronize());
+  GAPGB_CUDA_TRY(cudaMemcpy(m->ws.h_flags, m->ws.d_flags, 8 * sizeof(int), cudaMemcpyDeviceToHost));
+  read_stage_times(m);
+  gapgb_status st = flags_to_status(m->ws.h_flags);
+  GAPGB_CUDA_TRY(cudaMemset(m->ws.d_flags, 0, 8 * sizeof(int)));
+  return st;
+}
+
+gapgb_status gapgb_stage_times(gapgb_model *m, float t[4]) {
+  if (!m || !t) return fail(GAPGB_ERR_ARG, "null argument");
+  for (int q = 0; q < 4; ++q) t[q] = m->stage_ms[q];
+  return GAPGB_OK;
+}
+
+gapgb_status gapgb_descriptors(gapgb_model *m, int nstruct, const int *atom_off,
+                               const int *species, const double *lat, const double *pos,
+                               double *xx) {
+  if (!m || !atom_off || !species || !lat || !pos || !xx) return fail(GAPGB_ERR_ARG, "null argument");
+  const int saved = m->precision;
+  m->precision = GAPGB_PREC_FP64;
+  double *dG = nullptr;
+  gapgb_status st = eval_host(m, nstruct, atom_off, species, lat, pos, 0, nullptr, nullptr,
+                              nullptr, nullptr, &dG);
+  m->precision = saved;
+  if (st) return st;
+  const size_t n = (size_t)atom_off[nstruct] * m->host.D;
+  GAPGB_CUDA_TRY(cudaMemcpy(xx, dG, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  return GAPGB_OK;
+}
+
+gapgb_status gapgb_neighbors(gapgb_model *m, int natoms, const int *species, const double *lat,
+                             const double *pos, int cap, int *count, double *nb) {
+  if (!m || !species || !lat || !pos || !count || !nb || natoms <= 0 || cap <= 0)
+    return fail(GAPGB_ERR_ARG, "bad argument");
+  const int off[2] = {0, natoms};
+  gapgb_status st = check_batch_host(1, off, lat, pos);
+  if (st) return st;
+  st = upload_model(m);
+  if (st) return st;
+  GAPGB_CUDA_TRY(cudaSetDevice(m->device));
+  st = ensure_ws(m, natoms, 1, cap);
+  if (st) return st;
+  Workspace &ws = m->ws;
+  cudaStream_t s = m->stream;
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_atom_off, off, sizeof(int) * 2, cudaMemcpyHostToDevice, s));
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_species, species, sizeof(int) * natoms, cudaMemcpyHostToDevice, s));
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_lat, lat, sizeof(double) * 9, cudaMemcpyHostToDevice, s));
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_pos, pos, sizeof(double) * 3 * natoms, cudaMemcpyHostToDevice, s));
+  GAPGB_CUDA_TRY(cudaMemsetAsync(ws.d_flags, 0, 8 * sizeof(int), s));
+  launch_prep(m, ws, 1, natoms, ws.d_atom_off, ws.d_species, ws.d_lat, ws.d_pos, m->host.rcut, s);
+  launch_neighbors(ws, natoms, cap, m->host.rcut, s);
+  GAPGB_CUDA_TRY(cudaGetLastError());
+  std::vector<double4> xyz((size_t)natoms * cap);
+  std::vector<int> nj((size_t)natoms * cap);
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(count, ws.nbr_cnt, sizeof(int) * natoms, cudaMemcpyDeviceToHost, s));
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(xyz.data(), ws.nbr_xyz, sizeof(double4) * xyz.size(), cudaMemcpyDeviceToHost, s));
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(nj.data(), ws.nbr_j, sizeof(int) * nj.size(), cudaMemcpyDeviceToHost, s));
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.h_flags, ws.d_flags, 8 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  GAPGB_CUDA_TRY(cudaStreamSynchronize(s));
+  st = flags_to_status(ws.h_flags);
+  if (st) return st;
+  std::vector<double> w(natoms, 0.0);
+  for (int a = 0; a < natoms; ++a)
+    for (int q = 0; q < m->host.nspecies; ++q)
+      if (m->host.species_z[q] == species[a]) w[a] = m->host.species_w[q];
+  for (int i = 0; i < natoms; ++i)
+    for (int q = 0; q < count[i]; ++q) {
+      const size_t k = (size_t)i * cap + q;
+      double *o = nb + k * 6;
+      o[0] = xyz[k].x;
+      o[1] = xyz[k].y;
+      o[2] = xyz[k].z;
+      o[3] = xyz[k].w;
+      o[4] = w[nj[k]];
+      o[5] = (double)(nj[k] + 1);
+    }
+  return GAPGB_OK;
+}
+
+gapgb_status gapgb_min_bond(int natoms, const double *lat, const double *pos, double rcut,
+                            double *min_bond) {
+  if (!lat || !pos || !min_bond || natoms <= 0 || !(rcut > 0.0)) return fail(GAPGB_ERR_ARG, "bad argument");
+  // a throw-away single-species model carries the workspace
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
+  static gapgb_model *tiny = nullptr;
+  if (!tiny) {
+    const int z = 0;
+    const double w = 0.0, a = 0.0, c = 1.0, th = 1.0, mm2[2] = {0.0, 0.0}, co = 0.0;
+    const int ty = 1;
+    const double th2[2] = {th, th};
+    gapgb_status st = gapgb_model_create(1, &z, &w, 1, &ty, &a, &c, nullptr, 1, 2, th2, mm2, &co,
+                                         rcut, &tiny);
+    if (st) return st;
+  }
+  tiny->host.rcut = rcut;
+  std::vector<int> sp(natoms, 0);
+  const int off[2] = {0, natoms};
+  gapgb_status st = check_batch_host(1, off, lat, pos);
+  if (st) return st;
+  st = upload_model(tiny);
+  if (st) return st;
+  GAPGB_CUDA_TRY(cudaSetDevice(tiny->device));
+  st = ensure_ws(tiny, natoms, 1, 1);
+  if (st) return st;
+  Workspace &ws = tiny->ws;
+  cudaStream_t s = tiny->stream;
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_atom_off, off, sizeof(int) * 2, cudaMemcpyHostToDevice, s));
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_species, sp.data(), sizeof(int) * natoms, cudaMemcpyHostToDevice, s));
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_lat, lat, sizeof(double) * 9, cudaMemcpyHostToDevice, s));
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_pos, pos, sizeof(double) * 3 * natoms, cudaMemcpyHostToDevice, s));
+  GAPGB_CUDA_TRY(cudaMemsetAsync(ws.d_flags, 0, 8 * sizeof(int), s));
+  const double init = 10.0;  // get_bond.f90:38
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_energy, &init, sizeof(double), cudaMemcpyHostToDevice, s));
+  launch_prep(tiny, ws, 1, natoms, ws.d_atom_off, ws.d_species, ws.d_lat, ws.d_pos, rcut, s);
+  launch_min_bond(ws, natoms, rcut, ws.d_energy, s);
+  GAPGB_CUDA_TRY(cudaGetLastError());
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(min_bond, ws.d_energy, sizeof(double), cudaMemcpyDeviceToHost, s));
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.h_flags, ws.d_flags, 8 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  GAPGB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (ws.h_flags[0] & kFlagImageLimit)
+    return fail(GAPGB_ERR_CAP_EXCEEDED, "more than 127 periodic images per lattice direction");
+  return GAPGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,199 @@
+// gapgb_internal.h - shared definitions of the GB300 CALYPSO-GAP evaluator.
+//
+// Device data layout (one packed ragged batch of S structures, N atoms):
+//   apos[N]          double4 {x, y, z, species weight}
+//   atom_struct[N]   structure index of each atom
+//   sinfo[S]         per-structure lattice, inverse lattice, image counts
+//   nbr_cnt[N]       neighbours of atom i (<= cap)
+//   nbr_xyz[N*cap]   double4 {image x, y, z, r} - the reference's
+//                    neighbor(i,q,1:4) (gappy/libgap/gap_calc.f90:112-113)
+//   nbr_j[N*cap]     partner atom (global index)
+//   nbr_s[N*cap]     packed image shift ((n1+128)<<16 | (n2+128)<<8 | n3+128)
+//   nbr_rev[N*cap]   slot of the reverse pair in the partner's list, -1 if absent
+//   G[N*D]           descriptors (T = double or float), the reference's XX^T
+//   e[N]             atomic energies (double)
+//   dedg[N*D]        dE/dG (T)
+//   gslot[N*cap]     Vec4<T> {sum_d dedg_d dG_d/dp_q, 0}: gradient of atom i's
+//                    energy with respect to the position of neighbour slot q
+//   wvir[N*9]        per-atom virial sum_q (p_q - r_i)_a gslot_q,b (double)
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/gapgb.h"
+
+namespace gapgb {
+
+constexpr double kPiRef = 3.141592654;        // gap_calc.f90:59, wacsf.f90:31
+constexpr double kGPa2eVPang = 6.24219e-3;    // gap_calc.f90:9
+constexpr int kMaxSF = 128;                   // symmetry functions per model
+constexpr int kMaxRC = 16;                    // distinct SF cutoffs
+constexpr int kMaxAlpha = 16;                 // distinct angular exponents
+constexpr int kMaxImage = 127;                // |n_a| limit of the packed shift
+constexpr int kWarpsPerBlock = 4;
+constexpr int kMaxSpecies = 128;
+
+// Device error flags (bit positions in Workspace::d_flags[0]).
+enum : int {
+  kFlagNeighbourOverflow = 1,
+  kFlagUnknownSpecies = 2,
+  kFlagImageLimit = 4,
+  kFlagOrphanOverflow = 8,
+};
+
+// Symmetry-function table as the kernels read it.  Angular SFs are grouped by
+// distinct cutoff (rc) so that fc(r_jk) is evaluated once per triplet and
+// cutoff; per-slot fc and exp(-alpha r^2) tables live in shared memory.
+struct SFDev {
+  int nsf;       // D = 2*nsf descriptor entries are written (wacsf.f90:86-87)
+  int D;         // descriptor length of the model (>= 2*nsf)
+  int nrad, nang;
+  int nrc;       // distinct cutoffs over all SFs
+  int nalpha;    // distinct angular alphas
+  double max_ang_rc, max_rc;
+  double rc_val[kMaxRC];
+  double alpha_val[kMaxAlpha];
+  // radial SFs (types 1 and 3)
+  int rad_d[kMaxSF];
+  int rad_rc[kMaxSF];
+  double rad_alpha[kMaxSF];  // type 1: alpha; type 3: 4.0 (wacsf.f90:439)
+  double rad_rs[kMaxSF];     // type 1: 0;     type 3: R_s (wacsf.f90:438)
+  // angular SFs (types 2 and 4) sorted by cutoff index
+  int ang_d[kMaxSF];
+  int ang_rc[kMaxSF];
+  int ang_alpha[kMaxSF];
+  int ang_izeta[kMaxSF];     // zeta if a small positive integer, else -1
+  double ang_lambda[kMaxSF]; // +1 (type 2), -1 (type 4)
+  double ang_zeta[kMaxSF];
+  double ang_pref[kMaxSF];   // 2^(1-zeta)
+  // angular SFs of cutoff group g are ang_grp_start[g] .. ang_grp_start[g+1]-1
+  int n_ang_grp;
+  int ang_grp_rc[kMaxRC];
+  int ang_grp_start[kMaxRC + 1];
+  // species weights (gap_calc.f90:75-83; the last matching entry wins)
+  int nspecies;
+  int species_z[kMaxSpecies];
+  double species_w[kMaxSpecies];
+};
+
+struct StructInfo {
+  double lat[9];   // rows = lattice vectors
+  double linv[9];  // inverse: fractional f = d * linv (row vector)
+  double ext[3];   // conservative |f_a + n_a| bound: rcut * |column a of linv|
+  double volume;   // |det(lat)| (gap_calc.f90:201)
+  int nabc[3];     // gap_calc.f90:85-88
+  int a0, na;
+};
+
+template <typename T> struct Vec4;
+template <> struct Vec4<double> { using type = double4; };
+template <> struct Vec4<float> { using type = float4; };
+
+struct HostModel {
+  int nspecies = 0;
+  std::vector<int> species_z;
+  std::vector<double> species_w;
+  int nsf = 0;
+  std::vector<int> sf_type;
+  std::vector<double> sf_alpha, sf_cutoff, sf_zeta;
+  int M = 0, D = 0;
+  std::vector<double> theta, mm, coeff;
+  double rcut = 6.0;
+};
+
+struct Workspace {
+  int N = 0, S = 0, cap = 0, D = 0;
+  size_t bytes = 0;
+  // inputs (host-buffer path copies here)
+  int *d_atom_off = nullptr, *d_species = nullptr;
+  double *d_lat = nullptr, *d_pos = nullptr;
+  // outputs (host-buffer path)
+  double *d_energy = nullptr, *d_force = nullptr, *d_stress = nullptr, *d_atom_e = nullptr;
+  // internal
+  double4 *apos = nullptr;
+  float4 *frac32 = nullptr;   // fractional coordinates (FP32) for image pruning
+  int *atom_struct = nullptr;
+  StructInfo *sinfo = nullptr;
+  int *nbr_cnt = nullptr, *nbr_j = nullptr, *nbr_s = nullptr, *nbr_rev = nullptr;
+  double4 *nbr_xyz = nullptr;
+  void *G = nullptr, *dedg = nullptr, *gslot = nullptr;
+  double *e = nullptr, *wvir = nullptr;
+  int *d_flags = nullptr;     // [0] error bits, [1] max neighbour count, [2] orphan count
+  int *orphans = nullptr;     // orphan slot list
+  int orphan_cap = 0;
+  int *h_flags = nullptr;     // pinned mirror of d_flags
+  void *gpr_scratch = nullptr;  // split-K partial sums of the GPR
+  size_t gpr_scratch_size = 0;
+};
+
+}  // namespace gapgb
+
+struct gapgb_model {
+  gapgb::HostModel host;
+  gapgb::SFDev sfh;                    // host copy of the SF table
+  gapgb::SFDev *d_sf = nullptr;
+  double *d_mmt = nullptr;             // M x D, mm / theta (FP64)
+  float *d_mmt32 = nullptr;            // M x D, mm / theta (FP32)
+  double *d_invth = nullptr;           // D, 1 / theta
+  float *d_invth32 = nullptr;
+  double *d_coeff = nullptr;           // M
+  float *d_coeff32 = nullptr;
+  void *d_tc = nullptr;                // tensor-core operand images (gpr_tc.cu)
+  size_t tc_bytes = 0;
+  int device = 0;
+  int precision = GAPGB_PREC_FP64;
+  int cap = 256;
+  cudaStream_t stream = nullptr;       // internal stream of the host-buffer calls
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  bool profile_stages = false;
+  float stage_ms[4] = {0, 0, 0, 0};
+  gapgb::Workspace ws;
+};
+
+namespace gapgb {
+
+// model.cpp
+gapgb_status parse_model_file(const char *path, HostModel *m, std::string *err);
+gapgb_status build_sf_table(const HostModel &m, SFDev *t, std::string *err);
+
+// api.cu
+void set_last_error(const std::string &s);
+
+// kernel launchers (nbr.cu, wacsf.cu, gpr.cu, reduce.cu)
+void launch_prep(const gapgb_model *m, Workspace &ws, int S, int N, const int *d_atom_off,
+                 const int *d_species, const double *d_lat, const double *d_pos,
+                 double rcut, cudaStream_t st);
+void launch_neighbors(Workspace &ws, int N, int cap, double rcut, cudaStream_t st);
+void launch_reverse(Workspace &ws, int N, int cap, cudaStream_t st);
+template <typename T>
+void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int cap_smem,
+                      cudaStream_t st);
+template <typename T>
+void launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int cap_smem,
+                      cudaStream_t st);
+template <typename T>
+void launch_gpr(const gapgb_model *m, Workspace &ws, int N, cudaStream_t st);
+void launch_gpr_tc(gapgb_model *m, Workspace &ws, int N, cudaStream_t st);
+template <typename T>
+void launch_forces(Workspace &ws, int N, int cap, double *d_force, cudaStream_t st);
+void launch_struct_reduce(Workspace &ws, int S, int lgrad, double *d_energy, double *d_stress,
+                          double *d_atom_e, int N, cudaStream_t st);
+void launch_min_bond(Workspace &ws, int N, double rcut, double *d_out, cudaStream_t st);
+size_t wacsf_smem_bytes(const SFDev &t, int cap_smem, bool fwd, size_t elem);
+int gpr_nsplit(int N, int M);
+size_t gpr_scratch_bytes(int N, int M, int D, size_t elem);
+
+}  // namespace gapgb
+
+#define GAPGB_CUDA_TRY(expr)                                                      \
+  do {                                                                            \
+    cudaError_t _e = (expr);                                                      \
+    if (_e != cudaSuccess) {                                                      \
+      gapgb::set_last_error(std::string(#expr) + ": " + cudaGetErrorString(_e));  \
+      return GAPGB_ERR_CUDA;                                                      \
+    }                                                                             \
+  } while (0)

@@ -1,0 +1,337 @@
+// nbr.cu - structure/atom preparation and the periodic neighbour list.
+//
+// Reference: FGAP_CALC's image loop, gappy/libgap/gap_calc.f90:85-120.  For
+// every atom i the reference visits j = 1..N, then n1, n2, n3 in
+// [-nabc, nabc] ascending, forms xyz = pos(j) + n1 a1 + n2 a2 + n3 a3,
+// dr = pos(i) - xyz, dis = sqrt(dr.dr) and keeps the image if dis <= rcut
+// (self image (0,0,0) skipped).  Here one warp owns atom i and its lanes own
+// consecutive j, so a warp prefix sum over per-lane counts writes the list in
+// exactly the reference order.  Each lane prunes its pair's image box with the
+// fractional-coordinate bound |f_a + n_a| <= rcut*|b_a|/(2 pi) (FP32 with a
+// margin, conservative), then applies the reference's FP64 distance test with
+// separately rounded operations in the reference's statement order, so the
+// kept set and every stored distance are bit-identical to the loop above.
+#include <cfloat>
+
+#include "gapgb_internal.h"
+
+namespace gapgb {
+namespace {
+
+__device__ __forceinline__ void crossp_rn(const double *a, const double *b, double *o) {
+  o[0] = __dsub_rn(__dmul_rn(a[1], b[2]), __dmul_rn(a[2], b[1]));
+  o[1] = __dsub_rn(__dmul_rn(a[2], b[0]), __dmul_rn(a[0], b[2]));
+  o[2] = __dsub_rn(__dmul_rn(a[0], b[1]), __dmul_rn(a[1], b[0]));
+}
+
+// One thread per structure: image counts (gap_calc.f90:85-88 with
+// recipvector/volume/crossp of :240-266, same operation order), volume
+// (det, :201 and :290-299) and the inverse lattice for pruning.
+__global__ void k_prep_struct(int S, const int *__restrict__ atom_off,
+                              const double *__restrict__ lat_all, double rcut,
+                              StructInfo *__restrict__ out, int *__restrict__ flags) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S) return;
+  StructInfo si;
+  const double *L = lat_all + (size_t)s * 9;
+  for (int q = 0; q < 9; ++q) si.lat[q] = L[q];
+  // Fortran LAT(i,j) = L[(i-1)*3 + (j-1)]; columns c_j = LAT(:,j)
+  double c1[3] = {L[0], L[3], L[6]}, c2[3] = {L[1], L[4], L[7]}, c3[3] = {L[2], L[5], L[8]};
+  double r1[3], r2[3], r3[3];
+  crossp_rn(c2, c3, r1);
+  crossp_rn(c3, c1, r2);
+  crossp_rn(c1, c2, r3);
+  double vol = fabs(__dadd_rn(__dadd_rn(__dmul_rn(c1[0], r1[0]), __dmul_rn(c1[1], r1[1])),
+                              __dmul_rn(c1[2], r1[2])));
+  double *cols[3] = {r1, r2, r3};
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b)
+      cols[a][b] = __dmul_rn(__dmul_rn(__ddiv_rn(cols[a][b], vol), kPiRef), 2.0);
+  for (int row = 0; row < 3; ++row) {
+    double x = r1[row], y = r2[row], z = r3[row];
+    double len = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z)));
+    double n = ceil(__ddiv_rn(__ddiv_rn(__dmul_rn(rcut, len), kPiRef), 2.0));
+    if (!(n <= (double)kMaxImage)) {  // also catches NaN
+      atomicOr(flags, kFlagImageLimit);
+      n = (n > 0) ? (double)kMaxImage : 0.0;
+    }
+    si.nabc[row] = (int)n;
+  }
+  // det(lat) as gap_calc.f90:295-297
+  double det = __dadd_rn(
+      __dsub_rn(__dmul_rn(L[0], __dsub_rn(__dmul_rn(L[4], L[8]), __dmul_rn(L[5], L[7]))),
+                __dmul_rn(L[1], __dsub_rn(__dmul_rn(L[3], L[8]), __dmul_rn(L[5], L[6])))),
+      __dmul_rn(L[2], __dsub_rn(__dmul_rn(L[3], L[7]), __dmul_rn(L[6], L[4]))));
+  si.volume = fabs(det);
+  // inverse of L (rows = lattice vectors): adjugate / det
+  double inv[9];
+  inv[0] = (L[4] * L[8] - L[5] * L[7]) / det;
+  inv[1] = (L[2] * L[7] - L[1] * L[8]) / det;
+  inv[2] = (L[1] * L[5] - L[2] * L[4]) / det;
+  inv[3] = (L[5] * L[6] - L[3] * L[8]) / det;
+  inv[4] = (L[0] * L[8] - L[2] * L[6]) / det;
+  inv[5] = (L[2] * L[3] - L[0] * L[5]) / det;
+  inv[6] = (L[3] * L[7] - L[4] * L[6]) / det;
+  inv[7] = (L[1] * L[6] - L[0] * L[7]) / det;
+  inv[8] = (L[0] * L[4] - L[1] * L[3]) / det;
+  for (int q = 0; q < 9; ++q) si.linv[q] = inv[q];
+  for (int a = 0; a < 3; ++a) {
+    double cl = sqrt(inv[a] * inv[a] + inv[3 + a] * inv[3 + a] + inv[6 + a] * inv[6 + a]);
+    // FP32 fractional coordinates are compared against this bound: margin
+    // for their rounding (|f| < 1e3 keeps the error below 1e-4)
+    si.ext[a] = rcut * cl * (1.0 + 1e-9) + 2e-4;
+  }
+  si.a0 = atom_off[s];
+  si.na = atom_off[s + 1] - atom_off[s];
+  out[s] = si;
+}
+
+// One thread per atom: structure index, species weight, fractional coords.
+__global__ void k_prep_atoms(int N, int S, const int *__restrict__ atom_off,
+                             const int *__restrict__ species, const double *__restrict__ pos,
+                             const SFDev *__restrict__ sf, const StructInfo *__restrict__ sinfo,
+                             int *__restrict__ atom_struct, double4 *__restrict__ apos,
+                             float4 *__restrict__ frac32, int *__restrict__ flags) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  int lo = 0, hi = S;  // largest s with atom_off[s] <= i
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (atom_off[mid] <= i) lo = mid; else hi = mid;
+  }
+  atom_struct[i] = lo;
+  int z = species[i];
+  double w = 0.0;
+  bool found = false;
+  for (int q = 0; q < sf->nspecies; ++q)
+    if (sf->species_z[q] == z) { w = sf->species_w[q]; found = true; }
+  if (!found) atomicOr(flags, kFlagUnknownSpecies);
+  double x = pos[3 * (size_t)i], y = pos[3 * (size_t)i + 1], zc = pos[3 * (size_t)i + 2];
+  apos[i] = make_double4(x, y, zc, w);
+  const double *inv = sinfo[lo].linv;
+  frac32[i] = make_float4((float)(x * inv[0] + y * inv[3] + zc * inv[6]),
+                          (float)(x * inv[1] + y * inv[4] + zc * inv[7]),
+                          (float)(x * inv[2] + y * inv[5] + zc * inv[8]), 0.f);
+}
+
+// Reference distance of image (n1,n2,n3) of atom j from atom i, with the
+// reference's operation order and no contraction (gap_calc.f90:98-100).
+__device__ __forceinline__ double ref_image(const double4 &pi, const double4 &pj,
+                                            const double *L, int n1, int n2, int n3,
+                                            double *xyz) {
+  const double p[3] = {pj.x, pj.y, pj.z};
+  const double c[3] = {pi.x, pi.y, pi.z};
+  double dr[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    double v = __dadd_rn(p[k], __dmul_rn((double)n1, L[k]));
+    v = __dadd_rn(v, __dmul_rn((double)n2, L[3 + k]));
+    v = __dadd_rn(v, __dmul_rn((double)n3, L[6 + k]));
+    xyz[k] = v;
+    dr[k] = __dsub_rn(c[k], v);
+  }
+  return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dr[0], dr[0]), __dmul_rn(dr[1], dr[1])),
+                              __dmul_rn(dr[2], dr[2])));
+}
+
+__device__ __forceinline__ void image_box(const StructInfo &si, const float4 &fi,
+                                          const float4 &fj, int lo[3], int hi[3]) {
+  const float d[3] = {fj.x - fi.x, fj.y - fi.y, fj.z - fi.z};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float e = (float)si.ext[a];
+    float l = ceilf(-d[a] - e), h = floorf(-d[a] + e);
+    lo[a] = max(-si.nabc[a], (int)fmaxf(l, -1e6f));
+    hi[a] = min(si.nabc[a], (int)fminf(h, 1e6f));
+  }
+}
+
+template <bool kWrite>
+__device__ __forceinline__ int scan_pair(const StructInfo &si, const double4 &pi, const double4 &pj,
+                                         bool self, const int lo[3], const int hi[3], double rcut,
+                                         int j, int slot0, int cap, double4 *xyzr, int *nj,
+                                         int *ns) {
+  int c = 0;
+  for (int n1 = lo[0]; n1 <= hi[0]; ++n1)
+    for (int n2 = lo[1]; n2 <= hi[1]; ++n2)
+      for (int n3 = lo[2]; n3 <= hi[2]; ++n3) {
+        if (self && n1 == 0 && n2 == 0 && n3 == 0) continue;
+        double xyz[3];
+        double dis = ref_image(pi, pj, si.lat, n1, n2, n3, xyz);
+        if (dis > rcut) continue;
+        if (kWrite) {
+          int q = slot0 + c;
+          if (q < cap) {
+            xyzr[q] = make_double4(xyz[0], xyz[1], xyz[2], dis);
+            nj[q] = j;
+            ns[q] = ((n1 + 128) << 16) | ((n2 + 128) << 8) | (n3 + 128);
+          }
+        }
+        ++c;
+      }
+  return c;
+}
+
+__global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
+                                                   const double4 *__restrict__ apos,
+                                                   const float4 *__restrict__ frac32,
+                                                   const int *__restrict__ atom_struct,
+                                                   const StructInfo *__restrict__ sinfo,
+                                                   int *__restrict__ cnt, double4 *__restrict__ xyzr,
+                                                   int *__restrict__ nj, int *__restrict__ ns,
+                                                   int *__restrict__ flags) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int i = gw; i < N; i += nw) {
+    const StructInfo si = sinfo[atom_struct[i]];
+    const double4 pi = apos[i];
+    const float4 fi = frac32[i];
+    double4 *oxyz = xyzr + (size_t)i * cap;
+    int *oj = nj + (size_t)i * cap;
+    int *os = ns + (size_t)i * cap;
+    int total = 0;
+    for (int base = 0; base < si.na; base += 32) {
+      const int jl = base + lane;
+      const bool valid = jl < si.na;
+      const int j = si.a0 + jl;
+      int lo[3] = {0, 0, 0}, hi[3] = {-1, -1, -1};
+      double4 pj = pi;
+      if (valid) {
+        pj = apos[j];
+        image_box(si, fi, frac32[j], lo, hi);
+      }
+      int c = valid ? scan_pair<false>(si, pi, pj, j == i, lo, hi, rcut, j, 0, 0, nullptr,
+                                       nullptr, nullptr)
+                    : 0;
+      int incl = c;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += t;
+      }
+      const int wtot = __shfl_sync(0xffffffffu, incl, 31);
+      if (c > 0 && total + incl - c < cap)
+        scan_pair<true>(si, pi, pj, j == i, lo, hi, rcut, j, total + incl - c, cap, oxyz, oj, os);
+      total += wtot;
+    }
+    if (lane == 0) {
+      cnt[i] = min(total, cap);
+      atomicMax(flags + 1, total);
+      if (total > cap) atomicOr(flags, kFlagNeighbourOverflow);
+    }
+  }
+}
+
+// Reverse slot of every (i, q): the slot of (partner -> i, -shift) in the
+// partner's list, found by binary search over its (j, shift) ordered keys.
+__global__ void k_nbr_reverse(int N, int cap, const int *__restrict__ cnt,
+                              const int *__restrict__ nj, const int *__restrict__ ns,
+                              int *__restrict__ rev, int *__restrict__ orphans, int orphan_cap,
+                              int *__restrict__ flags) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int i = gw; i < N; i += nw) {
+    const int P = cnt[i];
+    for (int q = lane; q < P; q += 32) {
+      const size_t idx = (size_t)i * cap + q;
+      const int j = nj[idx];
+      const int s = ns[idx];
+      const int n1 = ((s >> 16) & 255) - 128, n2 = ((s >> 8) & 255) - 128, n3 = (s & 255) - 128;
+      const int want = ((128 - n1) << 16) | ((128 - n2) << 8) | (128 - n3);
+      const int *kj = nj + (size_t)j * cap;
+      const int *ks = ns + (size_t)j * cap;
+      int lo = 0, hi = cnt[j];
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        int a = kj[mid];
+        bool less = (a < i) || (a == i && ks[mid] < want);
+        if (less) lo = mid + 1; else hi = mid;
+      }
+      int r = -1;
+      if (lo < cnt[j] && kj[lo] == i && ks[lo] == want) r = lo;
+      rev[idx] = r;
+      if (r < 0) {
+        int o = atomicAdd(flags + 2, 1);
+        if (o < orphan_cap) orphans[o] = (int)idx;
+        else atomicOr(flags, kFlagOrphanOverflow);
+      }
+    }
+  }
+}
+
+// FGET_BOND (gappy/libgap/get_bond.f90:47-78): minimum over all kept images.
+__global__ void __launch_bounds__(128) k_min_bond(int N, double rcut,
+                                                  const double4 *__restrict__ apos,
+                                                  const float4 *__restrict__ frac32,
+                                                  const int *__restrict__ atom_struct,
+                                                  const StructInfo *__restrict__ sinfo,
+                                                  unsigned long long *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int i = gw; i < N; i += nw) {
+    const StructInfo si = sinfo[atom_struct[i]];
+    const double4 pi = apos[i];
+    const float4 fi = frac32[i];
+    double best = 10.0;  // get_bond.f90:38
+    for (int jl = lane; jl < si.na; jl += 32) {
+      const int j = si.a0 + jl;
+      const double4 pj = apos[j];
+      int lo[3], hi[3];
+      image_box(si, fi, frac32[j], lo, hi);
+      for (int n1 = lo[0]; n1 <= hi[0]; ++n1)
+        for (int n2 = lo[1]; n2 <= hi[1]; ++n2)
+          for (int n3 = lo[2]; n3 <= hi[2]; ++n3) {
+            if (j == i && n1 == 0 && n2 == 0 && n3 == 0) continue;
+            double xyz[3];
+            double dis = ref_image(pi, pj, si.lat, n1, n2, n3, xyz);
+            if (dis > rcut) continue;
+            if (dis < best) best = dis;
+          }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) best = fmin(best, __shfl_xor_sync(0xffffffffu, best, off));
+    if (lane == 0) atomicMin(out, (unsigned long long)__double_as_longlong(best));
+  }
+}
+
+int grid_for_warps(int nwarps_needed) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int sms = 148;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int blocks = (nwarps_needed + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  int maxb = sms * 16;
+  return blocks < maxb ? (blocks > 0 ? blocks : 1) : maxb;
+}
+
+}  // namespace
+
+void launch_prep(const gapgb_model *m, Workspace &ws, int S, int N, const int *d_atom_off,
+                 const int *d_species, const double *d_lat, const double *d_pos, double rcut,
+                 cudaStream_t st) {
+  k_prep_struct<<<(S + 127) / 128, 128, 0, st>>>(S, d_atom_off, d_lat, rcut, ws.sinfo, ws.d_flags);
+  k_prep_atoms<<<(N + 255) / 256, 256, 0, st>>>(N, S, d_atom_off, d_species, d_pos, m->d_sf,
+                                                 ws.sinfo, ws.atom_struct, ws.apos, ws.frac32,
+                                                 ws.d_flags);
+}
+
+void launch_neighbors(Workspace &ws, int N, int cap, double rcut, cudaStream_t st) {
+  k_nbr_build<<<grid_for_warps(N), 32 * kWarpsPerBlock, 0, st>>>(
+      N, cap, rcut, ws.apos, ws.frac32, ws.atom_struct, ws.sinfo, ws.nbr_cnt, ws.nbr_xyz,
+      ws.nbr_j, ws.nbr_s, ws.d_flags);
+}
+
+void launch_reverse(Workspace &ws, int N, int cap, cudaStream_t st) {
+  k_nbr_reverse<<<grid_for_warps(N), 32 * kWarpsPerBlock, 0, st>>>(
+      N, cap, ws.nbr_cnt, ws.nbr_j, ws.nbr_s, ws.nbr_rev, ws.orphans, ws.orphan_cap, ws.d_flags);
+}
+
+void launch_min_bond(Workspace &ws, int N, double rcut, double *d_out, cudaStream_t st) {
+  k_min_bond<<<grid_for_warps(N), 32 * kWarpsPerBlock, 0, st>>>(
+      N, rcut, ws.apos, ws.frac32, ws.atom_struct, ws.sinfo, (unsigned long long *)d_out);
+}
+
+}  // namespace gapgb

@@ -1,0 +1,189 @@
+/*
+ * gapgb.h - C ABI of the GB300 (sm_103a) CALYPSO-GAP energy / force / stress
+ * evaluator: wACSF descriptors + sparse GPR, neighbour search, chain rule into
+ * forces and virial stress, all on one GPU.
+ *
+ * Plain C types only (no CUDA or torch types); every call returns a status and
+ * never exits the process.  Array conventions are C row-major as numpy callers
+ * use them:
+ *   lat[s*9 + a*3 + c]   row a = lattice vector a of structure s (Angstrom)
+ *   pos[i*3 + c]         Cartesian position of atom i (Angstrom)
+ *   force[i*3 + c]       eV/Angstrom
+ *   stress[s*6 + q]      GPa, order XX YY ZZ XY YZ ZX, sign and units of the
+ *                        reference (gappy/libgap/gap_calc.f90:201-226)
+ * Ragged batches are packed: structure s owns atoms atom_off[s] ..
+ * atom_off[s+1]-1 (atom_off has nstruct+1 entries, atom_off[0] == 0).
+ *
+ * A handle is not thread-safe: use one handle per host thread (the reference
+ * itself is not re-entrant: it opens fixed Fortran units 111/2233/2244).
+ */
+#ifndef GAPGB_H
+#define GAPGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GAPGB_OK = 0,
+  GAPGB_ERR_FILE = 1,               /* model file missing / unreadable */
+  GAPGB_ERR_PARSE = 2,              /* model file malformed */
+  GAPGB_ERR_CAP_EXCEEDED = 3,       /* size beyond a documented limit */
+  GAPGB_ERR_UNKNOWN_SPECIES = 4,    /* atomic number absent from the model */
+  GAPGB_ERR_NEIGHBOUR_OVERFLOW = 5, /* more neighbours than the capacity */
+  GAPGB_ERR_CUDA = 6,               /* CUDA runtime error (see gapgb_last_error) */
+  GAPGB_ERR_TIMEOUT = 7,            /* a bounded device wait gave up */
+  GAPGB_ERR_ARG = 8,                /* invalid argument */
+  GAPGB_ERR_ALLOC = 9,              /* host or device allocation failed */
+  GAPGB_ERR_NO_DEVICE = 10          /* no CUDA device visible */
+} gapgb_status;
+
+/* Arithmetic of the evaluation. */
+typedef enum {
+  GAPGB_PREC_FP64 = 0, /* plain path: FP64 everywhere, matches the reference */
+  GAPGB_PREC_FP32 = 1, /* FP32 descriptors and GPR, FP64 energy/virial sums */
+  GAPGB_PREC_TC = 2    /* FP32 descriptors, tensor-core GPR (split BF16, FP32
+                          accumulate), FP64 energy/virial sums */
+} gapgb_precision;
+
+typedef enum {
+  GAPGB_OPT_PRECISION = 0,     /* gapgb_precision, default GAPGB_PREC_FP64 */
+  GAPGB_OPT_NEIGHBOUR_CAP = 1, /* slots per atom, default 256; grown on overflow
+                                  by the host-buffer calls */
+  GAPGB_OPT_DEVICE = 2         /* CUDA device ordinal, default 0 */
+} gapgb_option;
+
+typedef struct gapgb_model gapgb_model;
+
+const char *gapgb_status_string(gapgb_status st);
+/* Text of the last error seen on this host thread ("" if none). */
+const char *gapgb_last_error(void);
+/* Library version string. */
+const char *gapgb_version(void);
+
+/* ---- model ------------------------------------------------------------ */
+
+/* Parse a gap_parameters file and upload it to the device.
+ * Replaces FGAP_READ (gappy/libgap/gap_calc.f90:303-364) together with the
+ * species-weight read of FGAP_CALC (gap_calc.f90:75-83) and the SF-table read
+ * of CAR2ACSF (gappy/libgap/wacsf.f90:40-56).  rcut is the neighbour cutoff
+ * the reference passes to FGAP_CALC (gappy/libgap/GAP.py:15, default 6.0).
+ * Unlike the reference, M > 4000 and D > 100 are accepted. */
+gapgb_status gapgb_model_load(const char *path, double rcut, gapgb_model **out);
+
+/* Build a model from arrays (same meaning as the file's blocks).
+ * sf_zeta may be NULL (all 1, the reference's angular exponent);
+ * mm is [nsparse * des_len] row-major (row k = sparse point k). */
+gapgb_status gapgb_model_create(int nspecies, const int *species_z,
+                                const double *species_w, int nsf,
+                                const int *sf_type, const double *sf_alpha,
+                                const double *sf_cutoff, const double *sf_zeta,
+                                int nsparse, int des_len, const double *theta,
+                                const double *mm, const double *coeff,
+                                double rcut, gapgb_model **out);
+
+void gapgb_model_free(gapgb_model *model);
+
+gapgb_status gapgb_model_info(const gapgb_model *model, int *nsparse,
+                              int *des_len, int *nsf, int *nspecies,
+                              double *rcut);
+
+/* Host copies of theta[D], mm[M*D] (row-major), coeff[M]; any may be NULL. */
+gapgb_status gapgb_model_arrays(const gapgb_model *model, double *theta,
+                                double *mm, double *coeff);
+
+/* Host copies of the species table (nspecies entries) and the SF table
+ * (nsf entries); any pointer may be NULL.  With gapgb_model_create this
+ * rebuilds a model from a file's tables and caller-supplied GPR arrays, as
+ * FGAP_CALC does (gap_calc.f90:1-46 takes theta/MM/coeff as arguments and
+ * reads the tables from ./gap_parameters). */
+gapgb_status gapgb_model_tables(const gapgb_model *model, int *species_z,
+                                double *species_w, int *sf_type,
+                                double *sf_alpha, double *sf_cutoff,
+                                double *sf_zeta);
+
+gapgb_status gapgb_set_option(gapgb_model *model, gapgb_option opt,
+                              int64_t value);
+gapgb_status gapgb_get_option(const gapgb_model *model, gapgb_option opt,
+                              int64_t *value);
+
+/* ---- evaluation, host buffers ------------------------------------------- */
+
+/* One structure.  Replaces FGAP_CALC (gappy/libgap/gap_calc.f90:1-301):
+ * same inputs (species as atomic numbers, lattice rows, Cartesian
+ * positions), same outputs (energy eV, forces eV/A, stress GPa in the order
+ * XX YY ZZ XY YZ ZX, variance = 0 as in gap_calc.f90:206).  With lgrad == 0
+ * force and stress are set to zero, as the reference leaves them. */
+gapgb_status gapgb_eval(gapgb_model *model, int natoms, const int *species,
+                        const double *lat, const double *pos, int lgrad,
+                        double *energy, double *force, double *stress,
+                        double *variance);
+
+/* A packed ragged batch of independent structures in one pass (the batched
+ * replacement for one FGAP_CALC call per structure).  Host buffers; pinned
+ * host memory makes the copies asynchronous.  atom_energy may be NULL. */
+gapgb_status gapgb_eval_batch(gapgb_model *model, int nstruct,
+                              const int *atom_off, const int *species,
+                              const double *lat, const double *pos, int lgrad,
+                              double *energy, double *force, double *stress,
+                              double *atom_energy);
+
+/* ---- evaluation, device buffers ----------------------------------------- */
+
+/* Same as gapgb_eval_batch with every array in device memory, enqueued on
+ * `stream` (a cudaStream_t, NULL = legacy default stream) without a host
+ * synchronisation, so the call can be captured in a CUDA graph.  natoms must
+ * equal atom_off[nstruct] and max_atoms must bound every structure's atom
+ * count.  Errors found on the device (neighbour overflow, unknown species)
+ * are reported by gapgb_check_device_status after the stream has finished. */
+gapgb_status gapgb_eval_batch_device(gapgb_model *model, int nstruct,
+                                     int natoms, int max_atoms,
+                                     const int *d_atom_off,
+                                     const int *d_species, const double *d_lat,
+                                     const double *d_pos, int lgrad,
+                                     double *d_energy, double *d_force,
+                                     double *d_stress, double *d_atom_energy,
+                                     void *stream);
+
+/* Reads and clears the device-side error flags of the last device-buffer
+ * evaluation (synchronises the model's device). */
+gapgb_status gapgb_check_device_status(gapgb_model *model);
+
+/* Device time of each stage of the last evaluation, in milliseconds:
+ * t[0] neighbours, t[1] descriptors, t[2] GPR, t[3] chain rule + reduction.
+ * Only filled when GAPGB_PROFILE_STAGES is set in the environment. */
+gapgb_status gapgb_stage_times(gapgb_model *model, float t[4]);
+
+/* ---- descriptor export and utilities ------------------------------------ */
+
+/* wACSF descriptors XX (D per atom, the reference layout of
+ * gappy/libgap/wacsf.f90:86-87: unweighted block then weighted block) for a
+ * packed batch; the working replacement for gappy/libgap/WACSF.py:43-52. */
+gapgb_status gapgb_descriptors(gapgb_model *model, int nstruct,
+                               const int *atom_off, const int *species,
+                               const double *lat, const double *pos,
+                               double *xx);
+
+/* Neighbour list of one structure in the reference order (j, then n1, n2, n3
+ * ascending; gappy/libgap/gap_calc.f90:92-120).  Writes count[natoms] and, for
+ * slot q of atom i (q < count[i] <= cap), nb[(i*cap+q)*6 + f] with
+ * f = 0..2 image xyz, 3 r, 4 weight of j, 5 j (1-based) - the reference's
+ * neighbor(i, q, 1:6).  Distances are bit-identical to the reference loop
+ * evaluated without fused multiply-adds. */
+gapgb_status gapgb_neighbors(gapgb_model *model, int natoms,
+                             const int *species, const double *lat,
+                             const double *pos, int cap, int *count,
+                             double *nb);
+
+/* Minimum interatomic distance within rcut over all periodic images, 10.0 if
+ * none; replaces FGET_BOND (gappy/libgap/get_bond.f90:4-116). */
+gapgb_status gapgb_min_bond(int natoms, const double *lat, const double *pos,
+                            double rcut, double *min_bond);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GAPGB_H */

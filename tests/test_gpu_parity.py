@@ -1,0 +1,395 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle.
+
+Bars: neighbour lists bit-identical; FP64 path within 1e-9 relative energy,
+1e-7 eV/A forces, 1e-7 GPa stress (the plain-path tolerance); FP32 path
+within 1 meV/atom energy and 20 meV/A forces (the reduced-precision bar).
+"""
+import ctypes
+import os
+import shutil
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_MODEL
+from helpers import synth_model_file
+
+pytestmark = pytest.mark.gpu
+
+E_REL, F_ABS, S_ABS = 1e-9, 1e-7, 1e-7
+
+
+@pytest.fixture(scope="module")
+def golden_model(gapgb_mod):
+    m = gapgb_mod.GapModel.load(GOLDEN_MODEL)
+    yield m
+    m.close()
+
+
+@pytest.fixture(scope="module")
+def synth_si(oracle_mod, gapgb_mod, tmp_path_factory):
+    """Si model (zeta extension on) + its oracle twin, read from one file."""
+    import gapgb.synth as S
+    path = str(tmp_path_factory.mktemp("si") / "gap_parameters")
+    synth_model_file(path, oracle_mod, [S.si64(seed=s) for s in range(3)], M=300,
+                     theta_scale=1.0, coeff_std=1.0, seed=1)
+    g = gapgb_mod.GapModel.load(path)
+    yield g, oracle_mod.Model(path)
+    g.close()
+
+
+@pytest.fixture(scope="module")
+def synth_pop(oracle_mod, gapgb_mod, tmp_path_factory):
+    """4-species model over small triclinic population members."""
+    import gapgb.synth as S
+    rng = np.random.default_rng(7)
+    structs = [S.random_structure(rng, n, species_pool=(3, 8, 14, 26)) for n in (12, 20, 31, 9)]
+    # make every species appear in the sparse set
+    structs.append(S.random_structure(np.random.default_rng(8), 16, species_pool=(3, 8, 14, 26)))
+    path = str(tmp_path_factory.mktemp("pop") / "gap_parameters")
+    lat, pos, z = structs[0]
+    z = np.array([3, 8, 14, 26] * 3, np.int32)
+    structs[0] = (lat, pos, z)
+    synth_model_file(path, oracle_mod, structs, M=150, theta_scale=2.0, coeff_std=0.5, seed=3,
+                     zeta=False)
+    g = gapgb_mod.GapModel.load(path)
+    yield g, oracle_mod.Model(path), structs
+    g.close()
+
+
+def _assert_nbr_equal(gcnt, gnb, ocnt, onb):
+    assert np.array_equal(gcnt, ocnt)
+    for i in range(len(gcnt)):
+        a = gnb[i, : gcnt[i]]
+        b = onb[i, : ocnt[i]]
+        # bit-identical image positions, distances, weights and partner indices
+        assert np.array_equal(a.view(np.int64), b.view(np.int64)), i
+
+
+# ---------------------------------------------------------------- neighbours
+
+@pytest.mark.parametrize("f", [0, 5, 10])
+def test_neighbours_bit_exact_golden(golden_model, oracle_mod, golden_oracle_model, frames, f):
+    z, lat, pos = frames["numbers"][f], frames["cell"][f], frames["positions"][f]
+    gcnt, gnb = golden_model.neighbors(z, lat, pos, cap=1000)
+    ocnt, onb = oracle_mod.neighbors(lat, pos, golden_oracle_model.weights(z), 6.0, 1000)
+    _assert_nbr_equal(gcnt, gnb, ocnt, onb)
+
+
+def test_neighbours_bit_exact_triclinic(synth_pop, oracle_mod):
+    g, o, structs = synth_pop
+    for lat, pos, z in structs:
+        gcnt, gnb = g.neighbors(z, lat, pos, cap=600)
+        ocnt, onb = oracle_mod.neighbors(lat, pos, o.weights(z), 6.0, 600)
+        _assert_nbr_equal(gcnt, gnb, ocnt, onb)
+
+
+def test_neighbours_bit_exact_alloy512(gapgb_mod, oracle_mod, synth_pop):
+    import gapgb.synth as S
+    lat, pos, z = S.alloy512(seed=3)
+    zt, wt = S.species_table(z)
+    m = gapgb_mod.GapModel.create(zt, wt, [1], [0.5], [6.0], np.ones(2), np.zeros((1, 2)),
+                                  np.zeros(1))
+    gcnt, gnb = m.neighbors(z, lat, pos, cap=128)
+    w = dict(zip(zt.tolist(), wt.tolist()))
+    ocnt, onb = oracle_mod.neighbors(lat, pos, np.array([w[v] for v in z]), 6.0, 128)
+    _assert_nbr_equal(gcnt, gnb, ocnt, onb)
+    m.close()
+
+
+# ---------------------------------------------------------------- descriptors
+
+def test_descriptors_match_oracle(synth_si, oracle_mod):
+    import gapgb.synth as S
+    g, o = synth_si
+    lat, pos, z = S.si64(seed=11)
+    xx = g.descriptors([0, len(pos)], z, lat[None], pos)
+    cnt, nb = oracle_mod.neighbors(lat, pos, o.weights(z), 6.0, 400)
+    ox, _, _ = oracle_mod.car2acsf(o, pos, cnt, nb)
+    scale = np.abs(ox).max(0) + 1e-300
+    assert np.max(np.abs(xx - ox) / scale) < 1e-12
+
+
+def test_descriptors_golden_model(golden_model, oracle_mod, golden_oracle_model, frames):
+    z, lat, pos = frames["numbers"][2], frames["cell"][2], frames["positions"][2]
+    xx = golden_model.descriptors([0, len(pos)], z, lat[None], pos)
+    *_, ex = oracle_mod.gap_calc(golden_oracle_model, z, lat, pos, 6.0, False, extras=True)
+    scale = np.abs(ex["xx"]).max(0) + 1e-300
+    assert np.max(np.abs(xx - ex["xx"]) / scale) < 1e-12
+
+
+# ---------------------------------------------------------------- full path FP64
+
+@pytest.mark.parametrize("f", range(11))
+def test_fp64_golden_frames(golden_model, frames, f):
+    golden_model.set_precision("fp64")
+    E, F, S, var = golden_model.eval(frames["numbers"][f], frames["cell"][f],
+                                     frames["positions"][f])
+    assert abs(E - frames["energy"][f]) <= E_REL * abs(frames["energy"][f])
+    assert np.abs(F - frames["forces"][f]).max() <= F_ABS
+    assert np.abs(S - frames["stress"][f]).max() <= S_ABS
+    assert var == 0.0
+
+
+def test_fp64_vs_oracle_si_zeta(synth_si, oracle_mod):
+    import gapgb.synth as S
+    g, o = synth_si
+    g.set_precision("fp64")
+    for seed in (21, 22):
+        lat, pos, z = S.si64(seed=seed)
+        E, F, St, _ = g.eval(z, lat, pos)
+        oE, oF, oS, _ = oracle_mod.gap_calc(o, z, lat, pos, 6.0, True)
+        assert abs(E - oE) <= E_REL * max(1.0, abs(oE))
+        assert np.abs(F - oF).max() <= F_ABS
+        assert np.abs(St - oS).max() <= S_ABS
+
+
+def test_fp64_vs_oracle_population_batch(synth_pop, oracle_mod):
+    import gapgb.synth as S
+    g, o, structs = synth_pop
+    g.set_precision("fp64")
+    rng = np.random.default_rng(99)
+    batch = [S.random_structure(rng, n, species_pool=(3, 8, 14, 26)) for n in (8, 17, 40, 23, 64)]
+    off, sp, lat, pos = S.pack(batch)
+    E, F, St, ae = g.eval_batch(off, sp, lat, pos, atom_energy=True)
+    for s, (l, p, z) in enumerate(batch):
+        oE, oF, oS, _, ex = oracle_mod.gap_calc(o, z, l, p, 6.0, True, extras=True)
+        assert abs(E[s] - oE) <= E_REL * max(1.0, abs(oE))
+        assert np.abs(F[off[s]:off[s + 1]] - oF).max() <= F_ABS
+        assert np.abs(St[s] - oS).max() <= S_ABS
+        assert np.abs(ae[off[s]:off[s + 1]] - ex["e"]).max() <= 1e-9 * max(1.0, np.abs(ex["e"]).max())
+
+
+def test_batch_equals_single(synth_si):
+    import gapgb.synth as S
+    g, _ = synth_si
+    g.set_precision("fp64")
+    structs = [S.si64(seed=s) for s in (31, 32, 33)]
+    off, sp, lat, pos = S.pack(structs)
+    E, F, St = g.eval_batch(off, sp, lat, pos)
+    for s, (l, p, z) in enumerate(structs):
+        e1, f1, s1, _ = g.eval(z, l, p)
+        assert abs(E[s] - e1) <= 1e-12 * max(1.0, abs(e1))
+        assert np.abs(F[off[s]:off[s + 1]] - f1).max() <= 1e-10
+        assert np.abs(St[s] - s1).max() <= 1e-10
+
+
+def test_lgrad_false(golden_model, frames):
+    golden_model.set_precision("fp64")
+    E, F, S, _ = golden_model.eval(frames["numbers"][0], frames["cell"][0], frames["positions"][0],
+                                   lgrad=False)
+    assert abs(E - frames["energy"][0]) <= E_REL * abs(frames["energy"][0])
+    assert not F.any() and not S.any()
+
+
+def test_repeatable_bitwise(golden_model, frames):
+    golden_model.set_precision("fp64")
+    a = golden_model.eval(frames["numbers"][4], frames["cell"][4], frames["positions"][4])
+    b = golden_model.eval(frames["numbers"][4], frames["cell"][4], frames["positions"][4])
+    assert a[0] == b[0] and np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+
+
+# ---------------------------------------------------------------- FP32 path
+
+def test_fp32_golden_frames(golden_model, frames):
+    golden_model.set_precision("fp32")
+    try:
+        for f in (0, 6):
+            E, F, S, _ = golden_model.eval(frames["numbers"][f], frames["cell"][f],
+                                           frames["positions"][f])
+            n = len(F)
+            assert abs(E - frames["energy"][f]) / n <= 1e-3
+            assert np.abs(F - frames["forces"][f]).max() <= 20e-3
+    finally:
+        golden_model.set_precision("fp64")
+
+
+def test_fp32_population(synth_pop, oracle_mod):
+    import gapgb.synth as S
+    g, o, _ = synth_pop
+    g.set_precision("fp32")
+    try:
+        rng = np.random.default_rng(5)
+        batch = [S.random_structure(rng, n, species_pool=(3, 8, 14, 26)) for n in (30, 50)]
+        off, sp, lat, pos = S.pack(batch)
+        E, F, St = g.eval_batch(off, sp, lat, pos)
+        for s, (l, p, z) in enumerate(batch):
+            oE, oF, oS, _ = oracle_mod.gap_calc(o, z, l, p, 6.0, True)
+            assert abs(E[s] - oE) / len(p) <= 1e-3
+            assert np.abs(F[off[s]:off[s + 1]] - oF).max() <= 20e-3
+    finally:
+        g.set_precision("fp64")
+
+
+# ---------------------------------------------------------------- large-size properties
+
+def test_supercell_consistency_sige():
+    """E, F, stress of a 2x2x2 replica (32768 atoms, the MD cell) equal 8x E,
+    tiled F and the same stress of the 4096-atom cell."""
+    import gapgb
+    import gapgb.synth as S
+    lat, pos, z = S.sige(seed=4, reps=8)
+    zt, wt = S.species_table(z)
+    ty, al, rc, ze = S.sf_table()
+    rng = np.random.default_rng(0)
+    D = 64
+    mm = rng.normal(1.0, 0.3, (64, D)) * 5
+    m = gapgb.GapModel.create(zt, wt, ty, al, rc, np.full(D, 40.0), mm, rng.normal(0, 1, 64),
+                              sf_zeta=ze)
+    m.set_precision("fp64")
+    E1, F1, S1, _ = m.eval(z, lat, pos)
+    shifts = np.array([[i, j, k] for i in range(2) for j in range(2) for k in range(2)])
+    big = np.concatenate([pos + s @ lat for s in shifts])
+    E8, F8, S8, _ = m.eval(np.tile(z, 8), lat * 2, big)
+    assert abs(E8 - 8 * E1) <= 1e-9 * abs(E8)
+    assert np.abs(F8 - np.tile(F1, (8, 1))).max() <= 1e-7
+    assert np.abs(S8 - S1).max() <= 1e-7
+    assert np.abs(F8.sum(0)).max() <= 1e-8
+    m.close()
+
+
+# ---------------------------------------------------------------- drop-in APIs
+
+def test_libgap_calculator_and_ase(gapgb_mod, frames, tmp_path, monkeypatch):
+    shutil.copy(GOLDEN_MODEL, tmp_path / "gap_parameters")
+    monkeypatch.chdir(tmp_path)
+    from libgap.GAP import Calculator
+    c = Calculator(rcut=6.0)
+    c.gap_read()
+    species = ["C"] * 64
+    e, f, s, v = c.gap_calc(species, frames["cell"][1], frames["positions"][1], True)
+    assert abs(e - frames["energy"][1]) <= E_REL * abs(frames["energy"][1])
+    assert np.abs(f - frames["forces"][1]).max() <= F_ABS
+    assert np.abs(s - frames["stress"][1]).max() <= S_ABS and v == 0.0
+
+    from ase_gap.gap_calc import GAP
+
+    class Atoms:
+        def __init__(self, z, cell, pos):
+            self.numbers, self.cell, self.positions = z, cell, pos
+
+        def get_atomic_numbers(self):
+            return self.numbers
+
+        def copy(self):
+            return Atoms(self.numbers.copy(), self.cell.copy(), self.positions.copy())
+
+    calc = GAP(rcut=6.0)
+    at = Atoms(frames["numbers"][2], frames["cell"][2], frames["positions"][2])
+    calc.calculate(at, ["energy", "forces", "stress"])
+    assert abs(calc.results["energy"] - frames["energy"][2]) <= E_REL * abs(frames["energy"][2])
+    assert calc.results["free_energy"] == calc.results["energy"]
+    assert np.abs(calc.results["forces"] - frames["forces"][2]).max() <= F_ABS
+    assert np.abs(calc.results["stress"] - frames["stress"][2]).max() <= S_ABS
+
+
+def test_fortran_abi_shim(gapgb_mod, frames, tmp_path, monkeypatch):
+    """fgap_read_/fgap_calc_/fget_bond_ with gfortran conventions (by reference,
+    column-major) - what calypso-side callers link against."""
+    shutil.copy(GOLDEN_MODEL, tmp_path / "gap_parameters")
+    monkeypatch.chdir(tmp_path)
+    L = ctypes.CDLL(gapgb_mod.lib_path())
+    I, Dp = ctypes.c_int, ctypes.POINTER(ctypes.c_double)
+    nsp, dl = I(), I()
+    theta = np.zeros(100)
+    MM = np.zeros((4000, 100), order="F")
+    inv = np.zeros((4000, 4000), order="F")
+    coeff = np.zeros(4000)
+    L.fgap_read_(ctypes.byref(nsp), ctypes.byref(dl), theta.ctypes.data_as(Dp),
+                 MM.ctypes.data_as(Dp), inv.ctypes.data_as(Dp), coeff.ctypes.data_as(Dp))
+    assert (nsp.value, dl.value) == (129, 66)
+    M, D = nsp.value, dl.value
+    mm_f = np.asfortranarray(MM[:M, :D])
+    f = 3
+    na = I(64)
+    species = np.asfortranarray(frames["numbers"][f].astype(np.int32))
+    lat_f = np.asfortranarray(frames["cell"][f])
+    pos_f = np.asfortranarray(frames["positions"][f])
+    ene, var = ctypes.c_double(), ctypes.c_double()
+    force = np.zeros((64, 3), order="F")
+    stress = np.zeros(6)
+    rc = ctypes.c_double(6.0)
+    lg = I(1)
+    qmm = np.zeros((M, M), order="F")
+    th = np.ascontiguousarray(theta[:D])
+    co = np.ascontiguousarray(coeff[:M])
+    L.fgap_calc_(ctypes.byref(na), species.ctypes.data_as(ctypes.POINTER(I)),
+                 lat_f.ctypes.data_as(Dp), pos_f.ctypes.data_as(Dp), ctypes.byref(ene),
+                 force.ctypes.data_as(Dp), stress.ctypes.data_as(Dp), ctypes.byref(var),
+                 ctypes.byref(nsp), ctypes.byref(dl), th.ctypes.data_as(Dp),
+                 mm_f.ctypes.data_as(Dp), qmm.ctypes.data_as(Dp), co.ctypes.data_as(Dp),
+                 ctypes.byref(rc), ctypes.byref(lg))
+    assert abs(ene.value - frames["energy"][f]) <= E_REL * abs(frames["energy"][f])
+    assert np.abs(force - frames["forces"][f]).max() <= F_ABS
+    assert np.abs(stress - frames["stress"][f]).max() <= S_ABS
+    mb = ctypes.c_double()
+    L.fget_bond_(ctypes.byref(na), lat_f.ctypes.data_as(Dp), species.ctypes.data_as(ctypes.POINTER(I)),
+                 pos_f.ctypes.data_as(Dp), ctypes.byref(rc), ctypes.byref(mb))
+    from oracle import oracle
+    assert mb.value == oracle.min_bond(frames["cell"][f], frames["positions"][f], 6.0)
+
+
+def test_bond_and_wacsf_modules(gapgb_mod, oracle_mod, golden_oracle_model, frames, tmp_path,
+                                monkeypatch):
+    shutil.copy(GOLDEN_MODEL, tmp_path / "gap_parameters")
+    monkeypatch.chdir(tmp_path)
+    from libgap.BOND import Bond
+    from libgap.WACSF import Wacsf
+    lat, pos = frames["cell"][7], frames["positions"][7]
+    assert Bond(rcut=6.0).get_min_bond(lat, ["C"] * 64, pos) == oracle_mod.min_bond(lat, pos, 6.0)
+    xx = Wacsf(rcut=6.0).car2wacsf(lat, ["C"] * 64, pos)
+    *_, ex = oracle_mod.gap_calc(golden_oracle_model, frames["numbers"][7], lat, pos, 6.0, False,
+                                 extras=True)
+    assert np.max(np.abs(xx - ex["xx"]) / (np.abs(ex["xx"]).max(0) + 1e-300)) < 1e-12
+
+
+# ---------------------------------------------------------------- errors
+
+def test_unknown_species_is_an_error(golden_model, frames, gapgb_mod):
+    z = frames["numbers"][0].copy()
+    z[5] = 14
+    with pytest.raises(gapgb_mod.GapError) as ei:
+        golden_model.eval(z, frames["cell"][0], frames["positions"][0])
+    assert ei.value.status == 4
+
+
+def test_neighbour_capacity_grows(gapgb_mod, frames):
+    m = gapgb_mod.GapModel.load(GOLDEN_MODEL)
+    m.set_neighbour_cap(16)
+    E, F, S, _ = m.eval(frames["numbers"][0], frames["cell"][0], frames["positions"][0])
+    assert abs(E - frames["energy"][0]) <= E_REL * abs(frames["energy"][0])
+    assert m.get_option(gapgb_mod.OPT_NEIGHBOUR_CAP) >= 158
+    m.close()
+
+
+def test_device_path_reports_overflow(gapgb_mod, frames):
+    import torch
+    m = gapgb_mod.GapModel.load(GOLDEN_MODEL)
+    m.set_neighbour_cap(32)
+    dev = torch.device("cuda:0")
+    off = torch.tensor([0, 64], dtype=torch.int32, device=dev)
+    sp = torch.tensor(frames["numbers"][0], dtype=torch.int32, device=dev)
+    lat = torch.tensor(frames["cell"][0], dtype=torch.float64, device=dev)
+    pos = torch.tensor(frames["positions"][0], dtype=torch.float64, device=dev)
+    e = torch.zeros(1, dtype=torch.float64, device=dev)
+    f = torch.zeros(64, 3, dtype=torch.float64, device=dev)
+    s = torch.zeros(6, dtype=torch.float64, device=dev)
+    m.eval_batch_ptrs(1, 64, 64, off.data_ptr(), sp.data_ptr(), lat.data_ptr(), pos.data_ptr(), 1,
+                      e.data_ptr(), f.data_ptr(), s.data_ptr())
+    with pytest.raises(gapgb_mod.GapError) as ei:
+        m.check_device_status()
+    assert ei.value.status == 5
+    # with enough capacity the device path matches the reference frame
+    m.set_neighbour_cap(192)
+    m.eval_batch_ptrs(1, 64, 64, off.data_ptr(), sp.data_ptr(), lat.data_ptr(), pos.data_ptr(), 1,
+                      e.data_ptr(), f.data_ptr(), s.data_ptr())
+    m.check_device_status()
+    assert abs(e.item() - frames["energy"][0]) <= E_REL * abs(frames["energy"][0])
+    assert np.abs(f.cpu().numpy() - frames["forces"][0]).max() <= F_ABS
+    m.close()
+
+
+def test_min_bond_matches_oracle(gapgb_mod, oracle_mod, synth_pop):
+    _, _, structs = synth_pop
+    for lat, pos, _ in structs:
+        assert gapgb_mod.min_bond(lat, pos, 6.0) == oracle_mod.min_bond(lat, pos, 6.0)
