@@ -47,7 +47,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gapgb", choices=["gapgb", "reference"])
     p.add_argument("--batch", type=int, default=64, help="structures per step per GPU")
-    p.add_argument("--precision", default="fp32", choices=["fp32", "tc", "fp64"])
+    p.add_argument("--precision", default="fp32", choices=["fp32", "tc", "fp64", "mixed"])
     p.add_argument("--no-oracle", action="store_true", help="skip the oracle error check")
     return p.parse_args()
 
@@ -387,7 +387,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": {"fp32": "f32", "tc": "bf16x3/f32", "fp64": "f64"}[args.precision],
+        "dtype": {"fp32": "f32", "tc": "bf16x3/f32", "fp64": "f64", "mixed": "f32/f64"}[args.precision],
         "data": "synthetic",
         "config": {"workload": "alloy512 ternary fcc (Z 13/28/40), D=64, M=4000",
                    "structures_per_step": S, "atoms_per_step_per_gpu": N,
@@ -404,7 +404,7 @@ def main():
     # kernels launched per step (count from the library's launch sequence)
     # prep x2, neighbours, reverse, descriptors, GPR (+ split reduce), slot
     # gradients, forces, orphans, structure reduce
-    line["gpu_launches"] = args.steps * 10
+    line["gpu_launches"] = args.steps * 11
     if world == 1:
         line["cpu_baseline"] = cpu_baseline(arrays)
     print(json.dumps(line), flush=True)

@@ -229,8 +229,9 @@ gapgb_status enqueue_tail(gapgb_model *m, int S, int N, int cap, int capS, int l
   else launch_wacsf_fwd<float>(m, ws, N, cap, capS, st);
   if (prof) cudaEventRecord(m->ev[2], st);
   if (m->precision == GAPGB_PREC_TC) launch_gpr_tc(m, ws, N, st);
-  else if (fp64) launch_gpr<double>(m, ws, N, st);
-  else launch_gpr<float>(m, ws, N, st);
+  else if (fp64) launch_gpr<double, double>(m, ws, N, st);
+  else if (m->precision == GAPGB_PREC_MIXED) launch_gpr<double, float>(m, ws, N, st);
+  else launch_gpr<float, float>(m, ws, N, st);
   if (prof) cudaEventRecord(m->ev[3], st);
   if (lgrad) {
     if (fp64) {
@@ -468,7 +469,7 @@ gapgb_status gapgb_set_option(gapgb_model *m, gapgb_option opt, int64_t value) {
   switch (opt) {
     case GAPGB_OPT_PRECISION:
       if (value == GAPGB_PREC_TC) return fail(GAPGB_ERR_ARG, "tensor-core GPR not built yet");
-      if (value != GAPGB_PREC_FP64 && value != GAPGB_PREC_FP32)
+      if (value != GAPGB_PREC_FP64 && value != GAPGB_PREC_FP32 && value != GAPGB_PREC_MIXED)
         return fail(GAPGB_ERR_ARG, "unknown precision");
       m->precision = (int)value;
       return GAPGB_OK;

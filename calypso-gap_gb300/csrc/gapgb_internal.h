@@ -175,7 +175,7 @@ void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
 template <typename T>
 void launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int cap_smem,
                       cudaStream_t st);
-template <typename T>
+template <typename T, typename TG>
 void launch_gpr(const gapgb_model *m, Workspace &ws, int N, cudaStream_t st);
 void launch_gpr_tc(gapgb_model *m, Workspace &ws, int N, cudaStream_t st);
 template <typename T>

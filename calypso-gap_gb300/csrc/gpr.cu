@@ -8,13 +8,18 @@
 // With x' = x / theta and m' = m / theta (m' precomputed at model load):
 //   K_ik = exp(-0.5 |x'_i - m'_k|^2),  dedg_id = -(1/theta_d) sum_k (x'_id - m'_kd) w_ik,
 // w_ik = K_ik c_k.  The differences are formed directly (no |x|^2+|m|^2-2x.m
-// expansion), so there is no cancellation beyond the reference's own.
+// expansion), so there is no cancellation beyond the reference's own; e_i is
+// accumulated in FP64 with the coefficients in FP64 in every form.
 //
-// Block = 32 atoms x a range of sparse points; tiles of 64 sparse points are
-// staged in shared memory.  Phase A: each thread forms 8 (atom, point) kernel
-// values; phase B: each thread accumulates 8 descriptor components of dE/dG.
-// Small batches split the sparse points over blockIdx.y and a fixed-order
-// reduction sums the partial results (deterministic).
+// T is the arithmetic type, TG the storage type of G and dE/dG (the mixed
+// form reads FP32 descriptors and runs the GPR in FP64).
+//
+// Tiling: a block of 256 threads owns 64 atoms and walks the sparse points in
+// tiles of 64 staged in shared memory.  Phase A: thread (ty, tx) forms the
+// 4 x 4 kernel values of atoms ty+16a and points tx+16b (8 shared loads per
+// 16 difference-square-adds).  Phase B: the same thread accumulates dE/dG of
+// atoms ty+16a and descriptor components tx+16b.  Small batches split the
+// sparse points over blockIdx.y; a fixed-order reduction sums the partials.
 #include <type_traits>
 
 #include "gapgb_internal.h"
@@ -22,108 +27,134 @@
 namespace gapgb {
 namespace {
 
-constexpr int kBM = 32;
+constexpr int kBM = 64;
 constexpr int kBK = 64;
-constexpr int kMaxV = 16;  // D <= 8 * kMaxV
 
 __device__ __forceinline__ double g_exp(double x) { return exp(x); }
 __device__ __forceinline__ float g_exp(float x) { return expf(x); }
 
-template <typename T>
+template <typename T, typename TG, int NB>
 __global__ void __launch_bounds__(256)
-    k_gpr(int N, int M, int D, int klen, const T *__restrict__ G, const T *__restrict__ mmt,
-          const T *__restrict__ invth, const T *__restrict__ coeff, double *__restrict__ e_out,
-          T *__restrict__ dedg_out) {
+    k_gpr(int N, int M, int D, int klen, const TG *__restrict__ G, const T *__restrict__ mmt,
+          const T *__restrict__ invth, const double *__restrict__ coeff,
+          double *__restrict__ e_out, T *__restrict__ dedg_out) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  T *xs = reinterpret_cast<T *>(smraw);     // [kBM][D+1]
-  T *ms = xs + kBM * (D + 1);               // [kBK][D+1]
-  T *ws = ms + kBK * (D + 1);               // [kBM][kBK+1]
-  const int t = threadIdx.x;
+  const int ld = D + 1;
+  T *xs = reinterpret_cast<T *>(smraw);  // [kBM][D+1]
+  T *ms = xs + kBM * ld;                 // [kBK][D+1]
+  T *ws = ms + kBK * ld;                 // [kBM][kBK+1]
+  const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
   const int i0 = blockIdx.x * kBM;
   const int kbeg = blockIdx.y * klen;
   const int kend = min(M, kbeg + klen);
   for (int q = t; q < kBM * D; q += 256) {
     const int r = q / D, d = q - r * D;
     const int i = i0 + r;
-    xs[r * (D + 1) + d] = (i < N) ? G[(size_t)i * D + d] * invth[d] : (T)0;
+    xs[r * ld + d] = (i < N) ? (T)G[(size_t)i * D + d] * invth[d] : (T)0;
   }
-  const int ia = t >> 3, sub = t & 7;
-  double epart = 0.0;
-  T acc[kMaxV];
-  T xr[kMaxV];
-#pragma unroll
-  for (int v = 0; v < kMaxV; ++v) acc[v] = (T)0;
   __syncthreads();
+  T xr[4][NB];
+  T acc[4][NB];
 #pragma unroll
-  for (int v = 0; v < kMaxV; ++v) {
-    const int d = sub + 8 * v;
-    xr[v] = (d < D) ? xs[ia * (D + 1) + d] : (T)0;
-  }
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int d = tx + 16 * b;
+      xr[a][b] = (d < D) ? xs[(ty + 16 * a) * ld + d] : (T)0;
+      acc[a][b] = (T)0;
+    }
+  double epart[4] = {0.0, 0.0, 0.0, 0.0};
   for (int k0 = kbeg; k0 < kend; k0 += kBK) {
     for (int q = t; q < kBK * D; q += 256) {
       const int r = q / D, d = q - r * D;
       const int k = k0 + r;
-      ms[r * (D + 1) + d] = (k < kend) ? mmt[(size_t)k * D + d] : (T)0;
+      ms[r * ld + d] = (k < kend) ? mmt[(size_t)k * D + d] : (T)0;
     }
     __syncthreads();
-    // phase A: kernel values
-    const T *xrow = xs + ia * (D + 1);
-#pragma unroll 2
-    for (int u = 0; u < kBK / 8; ++u) {
-      const int kk = sub + 8 * u;
-      const T *mrow = ms + kk * (D + 1);
-      T s = (T)0;
+    // phase A: 4 x 4 kernel values per thread
+    T s[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) s[a][b] = (T)0;
 #pragma unroll 4
-      for (int d = 0; d < D; ++d) {
-        const T df = xrow[d] - mrow[d];
-        s += df * df;
+    for (int d = 0; d < D; ++d) {
+      T xv[4], mv[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) xv[a] = xs[(ty + 16 * a) * ld + d];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) mv[b] = ms[(tx + 16 * b) * ld + d];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const T df = xv[a] - mv[b];
+          s[a][b] += df * df;
+        }
+    }
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int k = k0 + tx + 16 * b;
+      const double c = (k < kend) ? coeff[k] : 0.0;
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        const T K = g_exp((T)-0.5 * s[a][b]);
+        const double w = (double)K * c;
+        epart[a] += w;
+        ws[(ty + 16 * a) * (kBK + 1) + tx + 16 * b] = (T)w;
       }
-      const int k = k0 + kk;
-      T w = (T)0;
-      if (k < kend) w = g_exp((T)-0.5 * s) * coeff[k];
-      ws[ia * (kBK + 1) + kk] = w;
-      epart += (double)w;
     }
     __syncthreads();
     // phase B: dE/dG partial sums
-    const T *wrow = ws + ia * (kBK + 1);
     const int kn = min(kBK, kend - k0);
     for (int kk = 0; kk < kn; ++kk) {
-      const T w = wrow[kk];
-      const T *mrow = ms + kk * (D + 1);
+      T w[4], mv[NB];
 #pragma unroll
-      for (int v = 0; v < kMaxV; ++v) {
-        const int d = sub + 8 * v;
-        if (d < D) acc[v] += (xr[v] - mrow[d]) * w;
+      for (int a = 0; a < 4; ++a) w[a] = ws[(ty + 16 * a) * (kBK + 1) + kk];
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        const int d = tx + 16 * b;
+        mv[b] = (d < D) ? ms[kk * ld + d] : (T)0;
       }
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < NB; ++b) acc[a][b] += (xr[a][b] - mv[b]) * w[a];
     }
     __syncthreads();
   }
-  epart += __shfl_xor_sync(0xffffffffu, epart, 1);
-  epart += __shfl_xor_sync(0xffffffffu, epart, 2);
-  epart += __shfl_xor_sync(0xffffffffu, epart, 4);
-  const int i = i0 + ia;
-  if (i < N) {
-    const size_t base = (size_t)blockIdx.y * N + i;
-    if (sub == 0) e_out[base] = epart;
+  // e: reduce over the 16 threads (tx) that share an atom row
 #pragma unroll
-    for (int v = 0; v < kMaxV; ++v) {
-      const int d = sub + 8 * v;
-      if (d < D) dedg_out[base * D + d] = -acc[v] * invth[d];
+  for (int a = 0; a < 4; ++a) {
+    double v = epart[a];
+#pragma unroll
+    for (int off = 1; off < 16; off <<= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    epart[a] = v;
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int i = i0 + ty + 16 * a;
+    if (i >= N) continue;
+    const size_t base = (size_t)blockIdx.y * N + i;
+    if (tx == 0) e_out[base] = epart[a];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int d = tx + 16 * b;
+      if (d < D) dedg_out[base * D + d] = -acc[a][b] * invth[d];
     }
   }
 }
 
-template <typename T>
+template <typename T, typename TG>
 __global__ void k_gpr_reduce(int N, int D, int nsplit, const double *__restrict__ e_part,
                              const T *__restrict__ dedg_part, double *__restrict__ e,
-                             T *__restrict__ dedg) {
+                             TG *__restrict__ dedg) {
   const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   const size_t nd = (size_t)N * D;
   if (tid < nd) {
     T s = (T)0;
     for (int p = 0; p < nsplit; ++p) s += dedg_part[(size_t)p * nd + tid];
-    dedg[tid] = s;
+    dedg[tid] = (TG)s;
   }
   if (tid < (size_t)N) {
     double s = 0.0;
@@ -147,12 +178,13 @@ int gpr_nsplit(int N, int M) {
 }
 
 size_t gpr_scratch_bytes(int N, int M, int D, size_t elem) {
+  // partial e and dE/dG of every split (one split still stages here so that
+  // the reduction also casts to the storage type)
   const int ns = gpr_nsplit(N, M);
-  if (ns <= 1) return 0;
   return (size_t)ns * N * sizeof(double) + (size_t)ns * N * D * elem;
 }
 
-template <typename T>
+template <typename T, typename TG>
 void launch_gpr(const gapgb_model *m, Workspace &ws, int N, cudaStream_t st) {
   const int M = m->host.M, D = m->host.D;
   const int ns = gpr_nsplit(N, M);
@@ -160,26 +192,26 @@ void launch_gpr(const gapgb_model *m, Workspace &ws, int N, cudaStream_t st) {
   const int klen = ((kt + ns - 1) / ns) * kBK;
   const int nsp = (M + klen - 1) / klen;
   const size_t smem = ((size_t)(kBM + kBK) * (D + 1) + (size_t)kBM * (kBK + 1)) * sizeof(T);
-  auto fn = k_gpr<T>;
-  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  const T *mmt = std::is_same<T, double>::value ? (const T *)m->d_mmt : (const T *)m->d_mmt32;
-  const T *invth = std::is_same<T, double>::value ? (const T *)m->d_invth : (const T *)m->d_invth32;
-  const T *coeff = std::is_same<T, double>::value ? (const T *)m->d_coeff : (const T *)m->d_coeff32;
+  constexpr bool f64 = std::is_same<T, double>::value;
+  const T *mmt = f64 ? (const T *)m->d_mmt : (const T *)m->d_mmt32;
+  const T *invth = f64 ? (const T *)m->d_invth : (const T *)m->d_invth32;
   dim3 grid((N + kBM - 1) / kBM, nsp);
-  if (nsp == 1) {
-    fn<<<grid, 256, smem, st>>>(N, M, D, klen, (const T *)ws.G, mmt, invth, coeff, ws.e,
-                                (T *)ws.dedg);
-  } else {
-    double *e_part = reinterpret_cast<double *>(ws.gpr_scratch);
-    T *d_part = reinterpret_cast<T *>(e_part + (size_t)nsp * N);
-    fn<<<grid, 256, smem, st>>>(N, M, D, klen, (const T *)ws.G, mmt, invth, coeff, e_part, d_part);
-    const size_t nd = (size_t)N * D;
-    k_gpr_reduce<T><<<(unsigned)((nd + 255) / 256), 256, 0, st>>>(N, D, nsp, e_part, d_part, ws.e,
-                                                                    (T *)ws.dedg);
-  }
+  double *e_part = reinterpret_cast<double *>(ws.gpr_scratch);
+  T *d_part = reinterpret_cast<T *>(e_part + (size_t)nsp * N);
+  const TG *G = (const TG *)ws.G;
+  auto run = [&](auto fn) {
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    fn<<<grid, 256, smem, st>>>(N, M, D, klen, G, mmt, invth, m->d_coeff, e_part, d_part);
+  };
+  if (D <= 64) run(k_gpr<T, TG, 4>);
+  else run(k_gpr<T, TG, 8>);
+  const size_t nd = (size_t)N * D;
+  k_gpr_reduce<T, TG><<<(unsigned)((nd + 255) / 256), 256, 0, st>>>(N, D, nsp, e_part, d_part,
+                                                                     ws.e, (TG *)ws.dedg);
 }
 
-template void launch_gpr<double>(const gapgb_model *, Workspace &, int, cudaStream_t);
-template void launch_gpr<float>(const gapgb_model *, Workspace &, int, cudaStream_t);
+template void launch_gpr<double, double>(const gapgb_model *, Workspace &, int, cudaStream_t);
+template void launch_gpr<float, float>(const gapgb_model *, Workspace &, int, cudaStream_t);
+template void launch_gpr<double, float>(const gapgb_model *, Workspace &, int, cudaStream_t);
 
 }  // namespace gapgb

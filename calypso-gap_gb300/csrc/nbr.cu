@@ -146,9 +146,22 @@ __device__ __forceinline__ void image_box(const StructInfo &si, const float4 &fi
   }
 }
 
+// FP32 screen of an image: squared Cartesian length of (f_j - f_i + n) L.
+// Candidates farther than rcut + margin cannot pass the exact test (the
+// margin covers the FP32 rounding of the fractional coordinates).
+__device__ __forceinline__ float screen_r2(const float *L32, const float fd[3], int n1, int n2,
+                                           int n3) {
+  const float a = fd[0] + (float)n1, b = fd[1] + (float)n2, c = fd[2] + (float)n3;
+  const float x = a * L32[0] + b * L32[3] + c * L32[6];
+  const float y = a * L32[1] + b * L32[4] + c * L32[7];
+  const float z = a * L32[2] + b * L32[5] + c * L32[8];
+  return x * x + y * y + z * z;
+}
+
 template <bool kWrite>
 __device__ __forceinline__ int scan_pair(const StructInfo &si, const double4 &pi, const double4 &pj,
                                          bool self, const int lo[3], const int hi[3], double rcut,
+                                         const float *L32, const float fd[3], float r2max,
                                          int j, int slot0, int cap, double4 *xyzr, int *nj,
                                          int *ns) {
   int c = 0;
@@ -156,6 +169,7 @@ __device__ __forceinline__ int scan_pair(const StructInfo &si, const double4 &pi
     for (int n2 = lo[1]; n2 <= hi[1]; ++n2)
       for (int n3 = lo[2]; n3 <= hi[2]; ++n3) {
         if (self && n1 == 0 && n2 == 0 && n3 == 0) continue;
+        if (screen_r2(L32, fd, n1, n2, n3) > r2max) continue;
         double xyz[3];
         double dis = ref_image(pi, pj, si.lat, n1, n2, n3, xyz);
         if (dis > rcut) continue;
@@ -187,6 +201,16 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
     const StructInfo si = sinfo[atom_struct[i]];
     const double4 pi = apos[i];
     const float4 fi = frac32[i];
+    float L32[9];
+    float lsum = 0.f;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      L32[q] = (float)si.lat[q];
+      lsum += fabsf(L32[q]);
+    }
+    // FP32 screen bound: rcut plus the fractional rounding margin in Angstrom
+    const float rs = (float)rcut + 2.5e-4f * lsum + 1e-3f;
+    const float r2max = rs * rs;
     double4 *oxyz = xyzr + (size_t)i * cap;
     int *oj = nj + (size_t)i * cap;
     int *os = ns + (size_t)i * cap;
@@ -197,12 +221,17 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
       const int j = si.a0 + jl;
       int lo[3] = {0, 0, 0}, hi[3] = {-1, -1, -1};
       double4 pj = pi;
+      float fd[3] = {0.f, 0.f, 0.f};
       if (valid) {
         pj = apos[j];
-        image_box(si, fi, frac32[j], lo, hi);
+        const float4 fj = frac32[j];
+        fd[0] = fj.x - fi.x;
+        fd[1] = fj.y - fi.y;
+        fd[2] = fj.z - fi.z;
+        image_box(si, fi, fj, lo, hi);
       }
-      int c = valid ? scan_pair<false>(si, pi, pj, j == i, lo, hi, rcut, j, 0, 0, nullptr,
-                                       nullptr, nullptr)
+      int c = valid ? scan_pair<false>(si, pi, pj, j == i, lo, hi, rcut, L32, fd, r2max, j, 0, 0,
+                                       nullptr, nullptr, nullptr)
                     : 0;
       int incl = c;
 #pragma unroll
@@ -212,7 +241,8 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
       }
       const int wtot = __shfl_sync(0xffffffffu, incl, 31);
       if (c > 0 && total + incl - c < cap)
-        scan_pair<true>(si, pi, pj, j == i, lo, hi, rcut, j, total + incl - c, cap, oxyz, oj, os);
+        scan_pair<true>(si, pi, pj, j == i, lo, hi, rcut, L32, fd, r2max, j, total + incl - c, cap,
+                        oxyz, oj, os);
       total += wtot;
     }
     if (lane == 0) {

@@ -11,9 +11,9 @@ import numpy as np
 
 from . import build as _build
 
-PREC_FP64, PREC_FP32, PREC_TC = 0, 1, 2
+PREC_FP64, PREC_FP32, PREC_TC, PREC_MIXED = 0, 1, 2, 3
 OPT_PRECISION, OPT_NEIGHBOUR_CAP, OPT_DEVICE = 0, 1, 2
-PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "tc": PREC_TC}
+PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "tc": PREC_TC, "mixed": PREC_MIXED}
 
 STATUS = {
     0: "OK", 1: "ERR_FILE", 2: "ERR_PARSE", 3: "ERR_CAP_EXCEEDED", 4: "ERR_UNKNOWN_SPECIES",

@@ -45,8 +45,10 @@ typedef enum {
 typedef enum {
   GAPGB_PREC_FP64 = 0, /* plain path: FP64 everywhere, matches the reference */
   GAPGB_PREC_FP32 = 1, /* FP32 descriptors and GPR, FP64 energy/virial sums */
-  GAPGB_PREC_TC = 2    /* FP32 descriptors, tensor-core GPR (split BF16, FP32
+  GAPGB_PREC_TC = 2,   /* FP32 descriptors, tensor-core GPR (split BF16, FP32
                           accumulate), FP64 energy/virial sums */
+  GAPGB_PREC_MIXED = 3 /* FP32 descriptors and gradients, FP64 GPR (for models
+                          whose coefficients cancel strongly) */
 } gapgb_precision;
 
 typedef enum {

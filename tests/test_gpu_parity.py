@@ -191,10 +191,12 @@ def test_repeatable_bitwise(golden_model, frames):
 
 # ---------------------------------------------------------------- FP32 path
 
-def test_fp32_golden_frames(golden_model, frames):
-    golden_model.set_precision("fp32")
+def test_mixed_golden_frames(golden_model, frames):
+    """The trained model's coefficients cancel ~2.4e4-fold: FP32 kernel values
+    miss 1 meV/atom there, FP32 descriptors with the FP64 GPR do not."""
+    golden_model.set_precision("mixed")
     try:
-        for f in (0, 6):
+        for f in range(11):
             E, F, S, _ = golden_model.eval(frames["numbers"][f], frames["cell"][f],
                                            frames["positions"][f])
             n = len(F)
