@@ -53,6 +53,8 @@ void free_ws(Workspace &ws) {
   free_dev(ws.nbr_s);
   free_dev(ws.nbr_rev);
   free_dev(ws.nbr_xyz);
+  free_dev(ws.nbr_d32);
+  free_dev(ws.nbr_w32);
   free_dev(ws.G);
   free_dev(ws.dedg);
   free_dev(ws.gslot);
@@ -106,6 +108,8 @@ gapgb_status ensure_ws(gapgb_model *m, int N, int S, int cap) {
   WS_ALLOC(ws.nbr_s, nslots);
   WS_ALLOC(ws.nbr_rev, nslots);
   WS_ALLOC(ws.nbr_xyz, nslots);
+  WS_ALLOC(ws.nbr_d32, nslots);
+  WS_ALLOC(ws.nbr_w32, nslots);
   WS_ALLOC(*(double **)&ws.G, (size_t)nN * D);
   WS_ALLOC(*(double **)&ws.dedg, (size_t)nN * D);
   WS_ALLOC(*(double4 **)&ws.gslot, nslots);
@@ -173,6 +177,12 @@ gapgb_status upload_model(gapgb_model *m) {
   SFDev *d_sf = nullptr;
   GAPGB_CUDA_TRY(cudaMalloc(&d_sf, sizeof(SFDev)));
   GAPGB_CUDA_TRY(cudaMemcpy(d_sf, &m->sfh, sizeof(SFDev), cudaMemcpyHostToDevice));
+  const SFT<double> t64 = make_sft<double>(m->sfh);
+  const SFT<float> t32 = make_sft<float>(m->sfh);
+  GAPGB_CUDA_TRY(cudaMalloc(&m->d_sft64, sizeof(t64)));
+  GAPGB_CUDA_TRY(cudaMemcpy(m->d_sft64, &t64, sizeof(t64), cudaMemcpyHostToDevice));
+  GAPGB_CUDA_TRY(cudaMalloc(&m->d_sft32, sizeof(t32)));
+  GAPGB_CUDA_TRY(cudaMemcpy(m->d_sft32, &t32, sizeof(t32), cudaMemcpyHostToDevice));
   GAPGB_CUDA_TRY(cudaMalloc(&m->d_mmt, sizeof(double) * mmt.size()));
   GAPGB_CUDA_TRY(cudaMemcpy(m->d_mmt, mmt.data(), sizeof(double) * mmt.size(), cudaMemcpyHostToDevice));
   GAPGB_CUDA_TRY(cudaMalloc(&m->d_mmt32, sizeof(float) * mmt32.size()));
@@ -418,6 +428,8 @@ void gapgb_model_free(gapgb_model *m) {
   cudaSetDevice(m->device);
   free_ws(m->ws);
   free_dev(m->d_sf);
+  free_dev(m->d_sft64);
+  free_dev(m->d_sft32);
   free_dev(m->d_mmt);
   free_dev(m->d_mmt32);
   free_dev(m->d_invth);

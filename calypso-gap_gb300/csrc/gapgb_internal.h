@@ -80,6 +80,67 @@ struct SFDev {
   double species_w[kMaxSpecies];
 };
 
+// The SF table in the arithmetic type of a descriptor kernel (no FP64 in the
+// FP32 kernels' loops).  Radial and angular entries as in SFDev; angular
+// entries sorted by cutoff group.
+constexpr int kAngChunk = 16;  // angular SFs accumulated in registers per pass
+template <typename T>
+struct SFT {
+  int nsf, D, nrad, nang, nrc, nalpha, n_ang_grp;
+  T max_ang_rc;
+  T rc_val[kMaxRC];
+  T pi_over_rc[kMaxRC];
+  T alpha_val[kMaxAlpha];
+  int rad_d[kMaxSF];
+  int rad_rc[kMaxSF];
+  T rad_alpha[kMaxSF];
+  T rad_rs[kMaxSF];
+  int ang_d[kMaxSF];
+  // rc | alpha << 8 | izeta << 16 | (lambda < 0) << 24 (izeta 0: non-integer zeta)
+  int ang_code[kMaxSF];
+  T ang_lambda[kMaxSF];
+  T ang_zeta[kMaxSF];
+  T ang_pref[kMaxSF];
+  int ang_grp_rc[kMaxRC];
+  int ang_grp_start[kMaxRC + 1];
+};
+
+template <typename T>
+inline SFT<T> make_sft(const SFDev &s) {
+  SFT<T> t{};
+  t.nsf = s.nsf;
+  t.D = s.D;
+  t.nrad = s.nrad;
+  t.nang = s.nang;
+  t.nrc = s.nrc;
+  t.nalpha = s.nalpha;
+  t.n_ang_grp = s.n_ang_grp;
+  t.max_ang_rc = (T)s.max_ang_rc;
+  for (int q = 0; q < s.nrc; ++q) {
+    t.rc_val[q] = (T)s.rc_val[q];
+    t.pi_over_rc[q] = (T)(kPiRef / s.rc_val[q]);
+  }
+  for (int q = 0; q < s.nalpha; ++q) t.alpha_val[q] = (T)s.alpha_val[q];
+  for (int q = 0; q < s.nrad; ++q) {
+    t.rad_d[q] = s.rad_d[q];
+    t.rad_rc[q] = s.rad_rc[q];
+    t.rad_alpha[q] = (T)s.rad_alpha[q];
+    t.rad_rs[q] = (T)s.rad_rs[q];
+  }
+  for (int q = 0; q < s.nang; ++q) {
+    t.ang_d[q] = s.ang_d[q];
+    const int iz = s.ang_izeta[q] > 0 ? s.ang_izeta[q] : 0;
+    t.ang_code[q] = s.ang_rc[q] | (s.ang_alpha[q] << 8) | (iz << 16) |
+                    (s.ang_lambda[q] < 0 ? (1 << 24) : 0);
+    t.ang_lambda[q] = (T)s.ang_lambda[q];
+    t.ang_zeta[q] = (T)s.ang_zeta[q];
+    t.ang_pref[q] = (T)s.ang_pref[q];
+  }
+  for (int g = 0; g < s.n_ang_grp; ++g) t.ang_grp_rc[g] = s.ang_grp_rc[g];
+  for (int g = 0; g <= s.n_ang_grp; ++g) t.ang_grp_start[g] = s.ang_grp_start[g];
+  return t;
+}
+
 struct StructInfo {
   double lat[9];   // rows = lattice vectors
   double linv[9];  // inverse: fractional f = d * linv (row vector)
@@ -120,6 +181,8 @@ struct Workspace {
   StructInfo *sinfo = nullptr;
   int *nbr_cnt = nullptr, *nbr_j = nullptr, *nbr_s = nullptr, *nbr_rev = nullptr;
   double4 *nbr_xyz = nullptr;
+  float4 *nbr_d32 = nullptr;  // FP32 {p_q - r_i, r} of every slot (FP32 kernels)
+  float *nbr_w32 = nullptr;   // FP32 weight of every slot's atom
   void *G = nullptr, *dedg = nullptr, *gslot = nullptr;
   double *e = nullptr, *wvir = nullptr;
   int *d_flags = nullptr;     // [0] error bits, [1] max neighbour count, [2] orphan count
@@ -136,6 +199,8 @@ struct gapgb_model {
   gapgb::HostModel host;
   gapgb::SFDev sfh;                    // host copy of the SF table
   gapgb::SFDev *d_sf = nullptr;
+  gapgb::SFT<double> *d_sft64 = nullptr;
+  gapgb::SFT<float> *d_sft32 = nullptr;
   double *d_mmt = nullptr;             // M x D, mm / theta (FP64)
   float *d_mmt32 = nullptr;            // M x D, mm / theta (FP32)
   double *d_invth = nullptr;           // D, 1 / theta

@@ -37,6 +37,7 @@ template <typename T, typename TG, int NB>
 __global__ void __launch_bounds__(256)
     k_gpr(int N, int M, int D, int klen, const TG *__restrict__ G, const T *__restrict__ mmt,
           const T *__restrict__ invth, const double *__restrict__ coeff,
+          const float *__restrict__ coeff32,
           double *__restrict__ e_out, T *__restrict__ dedg_out) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int ld = D + 1;
@@ -63,7 +64,11 @@ __global__ void __launch_bounds__(256)
       xr[a][b] = (d < D) ? xs[(ty + 16 * a) * ld + d] : (T)0;
       acc[a][b] = (T)0;
     }
+  // e partial sums: FP64 in the FP64 form; in the FP32 form a compensated
+  // FP32 pair (hi + lo), which keeps the FP64 pipe out of the inner loop
   double epart[4] = {0.0, 0.0, 0.0, 0.0};
+  float ehi[4] = {0.f, 0.f, 0.f, 0.f}, elo[4] = {0.f, 0.f, 0.f, 0.f};
+  constexpr bool kF64 = std::is_same<T, double>::value;
   for (int k0 = kbeg; k0 < kend; k0 += kBK) {
     for (int q = t; q < kBK * D; q += 256) {
       const int r = q / D, d = q - r * D;
@@ -95,13 +100,26 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
       const int k = k0 + tx + 16 * b;
-      const double c = (k < kend) ? coeff[k] : 0.0;
+      if (kF64) {
+        const double c = (k < kend) ? coeff[k] : 0.0;
 #pragma unroll
-      for (int a = 0; a < 4; ++a) {
-        const T K = g_exp((T)-0.5 * s[a][b]);
-        const double w = (double)K * c;
-        epart[a] += w;
-        ws[(ty + 16 * a) * (kBK + 1) + tx + 16 * b] = (T)w;
+        for (int a = 0; a < 4; ++a) {
+          const T K = g_exp((T)-0.5 * s[a][b]);
+          const double w = (double)K * c;
+          epart[a] += w;
+          ws[(ty + 16 * a) * (kBK + 1) + tx + 16 * b] = (T)w;
+        }
+      } else {
+        const float c = (k < kend) ? coeff32[k] : 0.f;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          const float w = (float)g_exp((T)-0.5 * s[a][b]) * c;
+          const float t = ehi[a] + w;  // two-sum of (ehi, w)
+          const float bb = t - ehi[a];
+          elo[a] += (ehi[a] - (t - bb)) + (w - bb);
+          ehi[a] = t;
+          ws[(ty + 16 * a) * (kBK + 1) + tx + 16 * b] = (T)w;
+        }
       }
     }
     __syncthreads();
@@ -126,7 +144,7 @@ __global__ void __launch_bounds__(256)
   // e: reduce over the 16 threads (tx) that share an atom row
 #pragma unroll
   for (int a = 0; a < 4; ++a) {
-    double v = epart[a];
+    double v = kF64 ? epart[a] : (double)ehi[a] + (double)elo[a];
 #pragma unroll
     for (int off = 1; off < 16; off <<= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
     epart[a] = v;
@@ -201,7 +219,8 @@ void launch_gpr(const gapgb_model *m, Workspace &ws, int N, cudaStream_t st) {
   const TG *G = (const TG *)ws.G;
   auto run = [&](auto fn) {
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    fn<<<grid, 256, smem, st>>>(N, M, D, klen, G, mmt, invth, m->d_coeff, e_part, d_part);
+    fn<<<grid, 256, smem, st>>>(N, M, D, klen, G, mmt, invth, m->d_coeff, m->d_coeff32, e_part,
+                                d_part);
   };
   if (D <= 64) run(k_gpr<T, TG, 4>);
   else run(k_gpr<T, TG, 8>);

@@ -163,7 +163,7 @@ __device__ __forceinline__ int scan_pair(const StructInfo &si, const double4 &pi
                                          bool self, const int lo[3], const int hi[3], double rcut,
                                          const float *L32, const float fd[3], float r2max,
                                          int j, int slot0, int cap, double4 *xyzr, int *nj,
-                                         int *ns) {
+                                         int *ns, float4 *d32, float *w32) {
   int c = 0;
   for (int n1 = lo[0]; n1 <= hi[0]; ++n1)
     for (int n2 = lo[1]; n2 <= hi[1]; ++n2)
@@ -179,6 +179,10 @@ __device__ __forceinline__ int scan_pair(const StructInfo &si, const double4 &pi
             xyzr[q] = make_double4(xyz[0], xyz[1], xyz[2], dis);
             nj[q] = j;
             ns[q] = ((n1 + 128) << 16) | ((n2 + 128) << 8) | (n3 + 128);
+            // deltaxj = -(pos(i) - xyz) (wacsf.f90:90), rounded once to FP32
+            d32[q] = make_float4((float)(xyz[0] - pi.x), (float)(xyz[1] - pi.y),
+                                 (float)(xyz[2] - pi.z), (float)dis);
+            w32[q] = (float)pj.w;
           }
         }
         ++c;
@@ -193,6 +197,7 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
                                                    const StructInfo *__restrict__ sinfo,
                                                    int *__restrict__ cnt, double4 *__restrict__ xyzr,
                                                    int *__restrict__ nj, int *__restrict__ ns,
+                                                   float4 *__restrict__ d32, float *__restrict__ w32,
                                                    int *__restrict__ flags) {
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -214,6 +219,8 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
     double4 *oxyz = xyzr + (size_t)i * cap;
     int *oj = nj + (size_t)i * cap;
     int *os = ns + (size_t)i * cap;
+    float4 *od = d32 + (size_t)i * cap;
+    float *ow = w32 + (size_t)i * cap;
     int total = 0;
     for (int base = 0; base < si.na; base += 32) {
       const int jl = base + lane;
@@ -231,7 +238,7 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
         image_box(si, fi, fj, lo, hi);
       }
       int c = valid ? scan_pair<false>(si, pi, pj, j == i, lo, hi, rcut, L32, fd, r2max, j, 0, 0,
-                                       nullptr, nullptr, nullptr)
+                                       nullptr, nullptr, nullptr, nullptr, nullptr)
                     : 0;
       int incl = c;
 #pragma unroll
@@ -242,7 +249,7 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
       const int wtot = __shfl_sync(0xffffffffu, incl, 31);
       if (c > 0 && total + incl - c < cap)
         scan_pair<true>(si, pi, pj, j == i, lo, hi, rcut, L32, fd, r2max, j, total + incl - c, cap,
-                        oxyz, oj, os);
+                        oxyz, oj, os, od, ow);
       total += wtot;
     }
     if (lane == 0) {
@@ -351,7 +358,7 @@ void launch_prep(const gapgb_model *m, Workspace &ws, int S, int N, const int *d
 void launch_neighbors(Workspace &ws, int N, int cap, double rcut, cudaStream_t st) {
   k_nbr_build<<<grid_for_warps(N), 32 * kWarpsPerBlock, 0, st>>>(
       N, cap, rcut, ws.apos, ws.frac32, ws.atom_struct, ws.sinfo, ws.nbr_cnt, ws.nbr_xyz,
-      ws.nbr_j, ws.nbr_s, ws.d_flags);
+      ws.nbr_j, ws.nbr_s, ws.nbr_d32, ws.nbr_w32, ws.d_flags);
 }
 
 void launch_reverse(Workspace &ws, int N, int cap, cudaStream_t st) {

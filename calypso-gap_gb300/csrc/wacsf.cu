@@ -21,10 +21,12 @@
 //
 // Work layout: one warp per centre atom.  The warp stages its neighbour
 // slots (relative vectors, distances, weights) and per-slot tables
-// fc(r_q), fc'(r_q) for every distinct cutoff and exp(-alpha r_q^2) for every
-// distinct angular alpha in shared memory.  Forward: lanes take slots
-// (radial) and pairs of the upper triangle (angular) and accumulate into a
-// per-lane column of a shared [D][32] array, summed in lane order at the end.
+// fc(r_q), fc'(r_q) (zero beyond each cutoff, so a term outside a cutoff
+// contributes exactly zero) and exp(-alpha r_q^2) in shared memory; the block
+// stages the SF table in the kernel's arithmetic type.
+// Forward: radial SFs one per lane over the slots in order (registers);
+// angular SFs in chunks of 16 register accumulators per lane over the pairs
+// of the upper triangle, summed over lanes by a fixed shuffle tree.
 // Backward: radial terms by slot (each lane owns its slots); angular pairs in
 // the rounds of a round-robin tournament schedule, in which every slot
 // appears in at most one pair per round, so lanes update slot gradients in
@@ -45,36 +47,61 @@ __device__ __forceinline__ void t_sincos(float x, float *s, float *c) { sincosf(
 __device__ __forceinline__ double t_pow(double x, double y) { return pow(x, y); }
 __device__ __forceinline__ float t_pow(float x, float y) { return powf(x, y); }
 
-// pref * base^zeta and its derivative with respect to base.
+// Non-integer zeta (rare): kept out of line so that the unrolled SF loops
+// stay small.
 template <typename T>
-__device__ __forceinline__ void ang_factor(T base, int iz, T zeta, T pref, T *A, T *dA) {
+__device__ __noinline__ T pow_general(T base, T zeta, T *dA) {
+  const T b = base > (T)0 ? base : (T)0;
+  const T p = t_pow(b, zeta - (T)1);
+  *dA = zeta * p;
+  return p * b;
+}
+
+// base^zeta and its derivative with respect to base (2^(1-zeta) applied by
+// the caller); iz = integer zeta, 0 for a non-integer zeta.
+template <typename T>
+__device__ __forceinline__ void ang_pow(T base, int iz, T zeta, T *A, T *dA) {
   if (iz == 1) {
     *A = base;
     *dA = (T)1;
   } else if (iz > 1) {
     T p = base;
     for (int t = 2; t < iz; ++t) p *= base;  // base^(iz-1)
-    *dA = pref * (T)iz * p;
-    *A = pref * p * base;
+    *dA = (T)iz * p;
+    *A = p * base;
   } else {
-    T b = base > (T)0 ? base : (T)0;
-    T p = t_pow(b, zeta - (T)1);
-    *dA = pref * zeta * p;
-    *A = pref * p * b;
+    *A = pow_general<T>(base, zeta, dA);
   }
 }
 
 template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+__host__ __device__ constexpr size_t kTableBytes(size_t s) { return (s + 15) / 16 * 16; }
+
+template <typename T>
 struct Layout {
-  T *dx, *dy, *dz, *r, *w, *fc, *dfc, *ea, *ec, *acc, *gx, *gy, *gz, *dg;
+  T *dx, *dy, *dz, *r, *w, *fc, *dfc, *ea, *Fp, *Ep, *gx, *gy, *gz, *dg, *cA, *cB;
 };
 
 template <typename T>
-__device__ __forceinline__ Layout<T> carve(unsigned char *raw, int warp, int capS, int nrc, int nal,
-                                           int D, bool fwd) {
-  const size_t per = (size_t)5 * capS + (size_t)nrc * capS * (fwd ? 1 : 2) + (size_t)nal * capS +
-                     (size_t)nal * 32 + (fwd ? (size_t)D * 32 : (size_t)3 * capS + D);
-  T *b = reinterpret_cast<T *>(raw) + per * warp;
+__host__ __device__ __forceinline__ size_t per_warp_elems(int capS, int nrc, int nal, int D,
+                                                          int nang, bool fwd) {
+  return fwd ? (size_t)5 * capS + (size_t)nrc * capS + (size_t)nal * capS + (size_t)nrc * 32 +
+                   (size_t)nal * 32
+             : (size_t)5 * capS + (size_t)2 * nrc * capS + (size_t)nal * capS +
+                   (size_t)nal * 32 + (size_t)3 * capS + D + (size_t)2 * nang;
+}
+
+template <typename T>
+__device__ __forceinline__ Layout<T> carve(unsigned char *raw, int warp, int capS, int nrc,
+                                           int nal, int D, int nang, bool fwd) {
+  T *b = reinterpret_cast<T *>(raw + kTableBytes(sizeof(SFT<T>))) +
+         per_warp_elems<T>(capS, nrc, nal, D, nang, fwd) * warp;
   Layout<T> L;
   L.dx = b;
   L.dy = L.dx + capS;
@@ -84,53 +111,98 @@ __device__ __forceinline__ Layout<T> carve(unsigned char *raw, int warp, int cap
   L.fc = L.w + capS;
   L.dfc = L.fc + (size_t)nrc * capS;
   L.ea = fwd ? L.dfc : L.dfc + (size_t)nrc * capS;
-  L.ec = L.ea + (size_t)nal * capS;
-  T *rest = L.ec + (size_t)nal * 32;
+  T *p = L.ea + (size_t)nal * capS;
   if (fwd) {
-    L.acc = rest;
-    L.gx = L.gy = L.gz = L.dg = nullptr;
+    L.Fp = p;
+    L.Ep = L.Fp + (size_t)nrc * 32;
+    L.gx = L.gy = L.gz = L.dg = L.cA = L.cB = nullptr;
   } else {
-    L.acc = nullptr;
-    L.gx = rest;
+    L.Fp = nullptr;
+    L.Ep = p;
+    L.gx = L.Ep + (size_t)nal * 32;
     L.gy = L.gx + capS;
     L.gz = L.gy + capS;
     L.dg = L.gz + capS;
+    L.cA = L.dg + D;
+    L.cB = L.cA + nang;
   }
   return L;
 }
 
-// Stage the slots of atom i and the per-slot cutoff / exponential tables.
 template <typename T>
-__device__ __forceinline__ int stage_slots(const Layout<T> &L, int i, int cap, int capS, int lane,
-                                           const int *__restrict__ cnt,
+__device__ __forceinline__ void load_table(unsigned char *raw, const SFT<T> *__restrict__ g) {
+  const int n = (int)(sizeof(SFT<T>) / 4);
+  for (int q = threadIdx.x; q < n; q += blockDim.x)
+    reinterpret_cast<int *>(raw)[q] = reinterpret_cast<const int *>(g)[q];
+  __syncthreads();
+}
+
+// Slot geometry: FP64 from the image positions, FP32 from the FP32 records
+// the neighbour kernel wrote (one rounding of the FP64 difference).
+__device__ __forceinline__ void slot_geom(int i, int q, int cap, const double4 &pi,
+                                          const double4 *__restrict__ xyzr,
+                                          const int *__restrict__ nj,
+                                          const double4 *__restrict__ apos,
+                                          const float4 *__restrict__ d32,
+                                          const float *__restrict__ w32, double *dx, double *dy,
+                                          double *dz, double *r, double *w) {
+  (void)d32;
+  (void)w32;
+  const double4 e = xyzr[(size_t)i * cap + q];
+  *dx = e.x - pi.x;  // deltaxj = -(pos(i) - xyz) (wacsf.f90:90)
+  *dy = e.y - pi.y;
+  *dz = e.z - pi.z;
+  *r = e.w;
+  *w = apos[nj[(size_t)i * cap + q]].w;
+}
+__device__ __forceinline__ void slot_geom(int i, int q, int cap, const double4 &pi,
+                                          const double4 *__restrict__ xyzr,
+                                          const int *__restrict__ nj,
+                                          const double4 *__restrict__ apos,
+                                          const float4 *__restrict__ d32,
+                                          const float *__restrict__ w32, float *dx, float *dy,
+                                          float *dz, float *r, float *w) {
+  (void)pi;
+  (void)xyzr;
+  (void)nj;
+  (void)apos;
+  const float4 e = d32[(size_t)i * cap + q];
+  *dx = e.x;
+  *dy = e.y;
+  *dz = e.z;
+  *r = e.w;
+  *w = w32[(size_t)i * cap + q];
+}
+
+template <typename T>
+__device__ __forceinline__ int stage_slots(const Layout<T> &L, const SFT<T> &sf, int i, int cap,
+                                           int capS, int lane, const int *__restrict__ cnt,
                                            const double4 *__restrict__ xyzr,
                                            const int *__restrict__ nj,
                                            const double4 *__restrict__ apos,
-                                           const SFDev *__restrict__ sf, bool want_dfc) {
+                                           const float4 *__restrict__ d32,
+                                           const float *__restrict__ w32, bool want_dfc) {
   const int P = min(cnt[i], capS);
-  const double4 pi = apos[i];
-  const T PI = (T)kPiRef;
-  const int nrc = sf->nrc, nal = sf->nalpha;
+  double4 pi = make_double4(0, 0, 0, 0);
+  if (sizeof(T) == 8) pi = apos[i];
+  const int nrc = sf.nrc, nal = sf.nalpha;
   for (int q = lane; q < P; q += 32) {
-    const double4 e = xyzr[(size_t)i * cap + q];
-    const int j = nj[(size_t)i * cap + q];
-    // deltaxj = -(pos(i) - xyz) (wacsf.f90:90)
-    L.dx[q] = (T)(e.x - pi.x);
-    L.dy[q] = (T)(e.y - pi.y);
-    L.dz[q] = (T)(e.z - pi.z);
-    const T r = (T)e.w;
+    T dx, dy, dz, r, w;
+    slot_geom(i, q, cap, pi, xyzr, nj, apos, d32, w32, &dx, &dy, &dz, &r, &w);
+    L.dx[q] = dx;
+    L.dy[q] = dy;
+    L.dz[q] = dz;
     L.r[q] = r;
-    L.w[q] = (T)apos[j].w;
+    L.w[q] = w;
     for (int g = 0; g < nrc; ++g) {
-      const T rc = (T)sf->rc_val[g];
       T fcv = (T)0, dfcv = (T)0;
-      if (r <= rc) {
-        const T x = PI * r / rc;
+      if (r <= sf.rc_val[g]) {
+        const T x = sf.pi_over_rc[g] * r;
         if (want_dfc) {
           T sn, cs;
           t_sincos(x, &sn, &cs);
           fcv = (T)0.5 * (cs + (T)1);
-          dfcv = (T)0.5 * (-sn) * (PI / rc);
+          dfcv = (T)-0.5 * sn * sf.pi_over_rc[g];
         } else {
           fcv = (T)0.5 * (t_cos(x) + (T)1);
         }
@@ -138,87 +210,111 @@ __device__ __forceinline__ int stage_slots(const Layout<T> &L, int i, int cap, i
       L.fc[(size_t)g * capS + q] = fcv;
       if (want_dfc) L.dfc[(size_t)g * capS + q] = dfcv;
     }
-    for (int a = 0; a < nal; ++a) L.ea[(size_t)a * capS + q] = t_exp(-(T)sf->alpha_val[a] * r * r);
+    for (int a = 0; a < nal; ++a) L.ea[(size_t)a * capS + q] = t_exp(-sf.alpha_val[a] * r * r);
   }
   return P;
 }
 
+// FP32: at least 4 blocks (16 warps) per SM; FP64 is FP64-pipe bound and
+// keeps its registers.
 template <typename T>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, sizeof(T) == 4 ? 4 : 1)
     k_wacsf_fwd(int N, int cap, int capS, const int *__restrict__ cnt,
                 const double4 *__restrict__ xyzr, const int *__restrict__ nj,
-                const double4 *__restrict__ apos, const SFDev *__restrict__ sf,
+                const double4 *__restrict__ apos, const float4 *__restrict__ d32,
+                const float *__restrict__ w32, const SFT<T> *__restrict__ sfg,
                 T *__restrict__ G) {
   extern __shared__ __align__(16) unsigned char smraw[];
+  load_table<T>(smraw, sfg);
+  const SFT<T> &sf = *reinterpret_cast<const SFT<T> *>(smraw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nrc = sf->nrc, nal = sf->nalpha, D = sf->D, nsf = sf->nsf;
-  const int nrad = sf->nrad, ngrp = sf->n_ang_grp;
-  const Layout<T> L = carve<T>(smraw, warp, capS, nrc, nal, D, true);
-  const T PI = (T)kPiRef;
-  const T maxrc = (T)sf->max_ang_rc;
+  const int nrc = sf.nrc, nal = sf.nalpha, D = sf.D, nsf = sf.nsf;
+  const int nrad = sf.nrad, nang = sf.nang, ngrp = sf.n_ang_grp;
+  const Layout<T> L = carve<T>(smraw, warp, capS, nrc, nal, D, nang, true);
+  const T maxrc = sf.max_ang_rc;
   for (int i = blockIdx.x * kWarpsPerBlock + warp; i < N; i += gridDim.x * kWarpsPerBlock) {
-    const int P = stage_slots<T>(L, i, cap, capS, lane, cnt, xyzr, nj, apos, sf, false);
-    for (int d = 0; d < D; ++d) L.acc[d * 32 + lane] = (T)0;
+    const int P = stage_slots<T>(L, sf, i, cap, capS, lane, cnt, xyzr, nj, apos, d32, w32, false);
     __syncwarp();
-    // radial terms: lanes own slots
-    for (int q = lane; q < P; q += 32) {
-      const T r = L.r[q], w = L.w[q];
-      for (int s = 0; s < nrad; ++s) {
-        const T f = L.fc[(size_t)sf->rad_rc[s] * capS + q];
-        if (r > (T)sf->rc_val[sf->rad_rc[s]]) continue;
-        const T u = r - (T)sf->rad_rs[s];
-        const T v = t_exp(-(T)sf->rad_alpha[s] * u * u) * f;
-        const int d = sf->rad_d[s];
-        L.acc[d * 32 + lane] += v;
-        L.acc[(d + nsf) * 32 + lane] += v * w;
+    T *Gi = G + (size_t)i * D;
+    // radial: one SF per lane, slots in the reference's order
+    for (int s = lane; s < nrad; s += 32) {
+      const int rci = sf.rad_rc[s];
+      const T alpha = sf.rad_alpha[s], rs = sf.rad_rs[s];
+      const T *fcr = L.fc + (size_t)rci * capS;
+      T acc = (T)0, accw = (T)0;
+      for (int q = 0; q < P; ++q) {
+        const T f = fcr[q];
+        if (f == (T)0) continue;  // beyond the cutoff (or exactly at it: a zero term)
+        const T u = L.r[q] - rs;
+        const T v = t_exp(-alpha * u * u) * f;
+        acc += v;
+        accw += v * L.w[q];
       }
+      const int d = sf.rad_d[s];
+      Gi[d] = acc;
+      Gi[d + nsf] = accw;
     }
-    // angular terms: lanes walk the upper triangle j < k with stride 32
-    if (sf->nang > 0 && P > 1) {
-      const int npair = P * (P - 1) / 2;
-      int j = 0, k = 1 + lane;
-      while (j < P - 1 && k >= P) { const int o = k - P; ++j; k = j + 1 + o; }
-      for (int p = lane; p < npair; p += 32) {
-        const T a = L.r[j], b = L.r[k];
-        if (a <= maxrc && b <= maxrc) {
-          const T cx = L.dx[j] - L.dx[k], cy = L.dy[j] - L.dy[k], cz = L.dz[j] - L.dz[k];
-          const T c2 = cx * cx + cy * cy + cz * cz;
-          const T c = t_sqrt(c2);
-          if (c <= maxrc) {
-            // costheta = f/g, f = rjk^2 - rij^2 - rik^2, g = -2 rij rik (wacsf.f90:271-273)
-            const T cosv = (c2 - a * a - b * b) / ((T)-2 * a * b);
-            for (int al = 0; al < nal; ++al) L.ec[al * 32 + lane] = t_exp(-(T)sf->alpha_val[al] * c2);
-            const T wjk = L.w[j] * L.w[k];
-            for (int g = 0; g < ngrp; ++g) {
-              const int rci = sf->ang_grp_rc[g];
-              const T rc = (T)sf->rc_val[rci];
-              if (a > rc || b > rc || c > rc) continue;
-              const T F = L.fc[(size_t)rci * capS + j] * L.fc[(size_t)rci * capS + k] *
-                          ((T)0.5 * (t_cos(PI * c / rc) + (T)1));
-              for (int s = sf->ang_grp_start[g]; s < sf->ang_grp_start[g + 1]; ++s) {
-                const int al = sf->ang_alpha[s];
+    // angular: chunks of kAngChunk SFs accumulated in registers
+    for (int c0 = 0; c0 < nang; c0 += kAngChunk) {
+      int code[kAngChunk];
+      T accA[kAngChunk], accW[kAngChunk];
+#pragma unroll
+      for (int s = 0; s < kAngChunk; ++s) {
+        code[s] = (c0 + s < nang) ? sf.ang_code[c0 + s] : -1;
+        accA[s] = accW[s] = (T)0;
+      }
+      if (P > 1) {
+        const int npair = P * (P - 1) / 2;
+        int j = 0, k = 1 + lane;
+        while (j < P - 1 && k >= P) { const int o = k - P; ++j; k = j + 1 + o; }
+        for (int p = lane; p < npair; p += 32) {
+          const T a = L.r[j], b = L.r[k];
+          if (a <= maxrc && b <= maxrc) {
+            const T cx = L.dx[j] - L.dx[k], cy = L.dy[j] - L.dy[k], cz = L.dz[j] - L.dz[k];
+            const T c2 = cx * cx + cy * cy + cz * cz;
+            const T c = t_sqrt(c2);
+            if (c <= maxrc) {
+              // costheta = f/g, f = rjk^2 - rij^2 - rik^2, g = -2 rij rik (wacsf.f90:271-273)
+              const T cosv = (c2 - a * a - b * b) / ((T)-2 * a * b);
+              for (int g = 0; g < ngrp; ++g) {
+                const int rci = sf.ang_grp_rc[g];
+                const T fcc = (c <= sf.rc_val[rci])
+                                  ? (T)0.5 * (t_cos(sf.pi_over_rc[rci] * c) + (T)1) : (T)0;
+                L.Fp[rci * 32 + lane] =
+                    L.fc[(size_t)rci * capS + j] * L.fc[(size_t)rci * capS + k] * fcc;
+              }
+              for (int al = 0; al < nal; ++al)
+                L.Ep[al * 32 + lane] = L.ea[(size_t)al * capS + j] * L.ea[(size_t)al * capS + k] *
+                                       t_exp(-sf.alpha_val[al] * c2);
+              const T wjk = L.w[j] * L.w[k];
+#pragma unroll
+              for (int s = 0; s < kAngChunk; ++s) {
+                if (code[s] < 0) continue;
+                const int rci = code[s] & 255, al = (code[s] >> 8) & 255;
+                const int iz = (code[s] >> 16) & 255;
+                const T base = (code[s] >> 24) ? (T)1 - cosv : (T)1 + cosv;
                 T A, dA;
-                ang_factor<T>((T)1 + (T)sf->ang_lambda[s] * cosv, sf->ang_izeta[s],
-                              (T)sf->ang_zeta[s], (T)sf->ang_pref[s], &A, &dA);
-                const T E = L.ea[(size_t)al * capS + j] * L.ea[(size_t)al * capS + k] *
-                            L.ec[al * 32 + lane];
-                const T v = A * E * F;
-                const int d = sf->ang_d[s];
-                L.acc[d * 32 + lane] += v;
-                L.acc[(d + nsf) * 32 + lane] += v * wjk;
+                ang_pow<T>(base, iz, iz ? (T)1 : sf.ang_zeta[c0 + s], &A, &dA);
+                const T v = A * L.Ep[al * 32 + lane] * L.Fp[rci * 32 + lane];
+                accA[s] += v;
+                accW[s] += v * wjk;
               }
             }
           }
+          k += 32;
+          while (j < P - 1 && k >= P) { const int o = k - P; ++j; k = j + 1 + o; }
         }
-        k += 32;
-        while (j < P - 1 && k >= P) { const int o = k - P; ++j; k = j + 1 + o; }
       }
-    }
-    __syncwarp();
-    for (int d = lane; d < D; d += 32) {
-      T s = (T)0;
-      for (int l = 0; l < 32; ++l) s += L.acc[d * 32 + l];
-      G[(size_t)i * D + d] = s;
+#pragma unroll
+      for (int s = 0; s < kAngChunk; ++s) {
+        if (c0 + s >= nang) continue;
+        const T x = warp_sum(accA[s]), y = warp_sum(accW[s]);
+        if (lane == 0) {
+          const int d = sf.ang_d[c0 + s];
+          Gi[d] = sf.ang_pref[c0 + s] * x;
+          Gi[d + nsf] = sf.ang_pref[c0 + s] * y;
+        }
+      }
     }
     __syncwarp();
   }
@@ -228,45 +324,53 @@ template <typename T>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     k_wacsf_bwd(int N, int cap, int capS, const int *__restrict__ cnt,
                 const double4 *__restrict__ xyzr, const int *__restrict__ nj,
-                const double4 *__restrict__ apos, const SFDev *__restrict__ sf,
+                const double4 *__restrict__ apos, const float4 *__restrict__ d32,
+                const float *__restrict__ w32, const SFT<T> *__restrict__ sfg,
                 const T *__restrict__ dedg, typename Vec4<T>::type *__restrict__ gslot,
                 double *__restrict__ wvir) {
   using V4 = typename Vec4<T>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
+  load_table<T>(smraw, sfg);
+  const SFT<T> &sf = *reinterpret_cast<const SFT<T> *>(smraw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nrc = sf->nrc, nal = sf->nalpha, D = sf->D, nsf = sf->nsf;
-  const int nrad = sf->nrad, ngrp = sf->n_ang_grp;
-  const Layout<T> L = carve<T>(smraw, warp, capS, nrc, nal, D, false);
-  const T PI = (T)kPiRef;
-  const T maxrc = (T)sf->max_ang_rc;
+  const int nrc = sf.nrc, nal = sf.nalpha, D = sf.D, nsf = sf.nsf;
+  const int nrad = sf.nrad, nang = sf.nang, ngrp = sf.n_ang_grp;
+  const Layout<T> L = carve<T>(smraw, warp, capS, nrc, nal, D, nang, false);
+  const T maxrc = sf.max_ang_rc;
   for (int i = blockIdx.x * kWarpsPerBlock + warp; i < N; i += gridDim.x * kWarpsPerBlock) {
-    const int P = stage_slots<T>(L, i, cap, capS, lane, cnt, xyzr, nj, apos, sf, true);
+    const int P = stage_slots<T>(L, sf, i, cap, capS, lane, cnt, xyzr, nj, apos, d32, w32, true);
     for (int d = lane; d < D; d += 32) L.dg[d] = dedg[(size_t)i * D + d];
     for (int q = lane; q < P; q += 32) L.gx[q] = L.gy[q] = L.gz[q] = (T)0;
     __syncwarp();
-    // radial terms
+    // per-atom angular coefficients: 2^(1-zeta) dE/dG of both copies
+    for (int s = lane; s < nang; s += 32) {
+      const int d = sf.ang_d[s];
+      L.cA[s] = sf.ang_pref[s] * L.dg[d];
+      L.cB[s] = sf.ang_pref[s] * L.dg[d + nsf];
+    }
+    // radial terms: lanes own slots
     for (int q = lane; q < P; q += 32) {
       const T r = L.r[q], w = L.w[q];
       T S = (T)0;
       for (int s = 0; s < nrad; ++s) {
-        const int rci = sf->rad_rc[s];
-        if (r > (T)sf->rc_val[rci]) continue;
+        const int rci = sf.rad_rc[s];
+        if (r > sf.rc_val[rci]) continue;
         const T f = L.fc[(size_t)rci * capS + q], df = L.dfc[(size_t)rci * capS + q];
-        const T alpha = (T)sf->rad_alpha[s];
-        const T u = r - (T)sf->rad_rs[s];
+        const T alpha = sf.rad_alpha[s];
+        const T u = r - sf.rad_rs[s];
         const T ex = t_exp(-alpha * u * u);
         const T dphi = (T)-2 * alpha * u * ex * f + ex * df;
-        const int d = sf->rad_d[s];
+        const int d = sf.rad_d[s];
         S += (L.dg[d] + L.dg[d + nsf] * w) * dphi;
       }
-      const T ir = (T)1 / r;
-      L.gx[q] += S * L.dx[q] * ir;
-      L.gy[q] += S * L.dy[q] * ir;
-      L.gz[q] += S * L.dz[q] * ir;
+      const T ir = S / r;
+      L.gx[q] += ir * L.dx[q];
+      L.gy[q] += ir * L.dy[q];
+      L.gz[q] += ir * L.dz[q];
     }
     __syncwarp();
     // angular terms in round-robin rounds (circle method over Pp slots)
-    if (sf->nang > 0 && P > 1) {
+    if (nang > 0 && P > 1) {
       const int Pp = P + (P & 1);
       const int half = Pp >> 1;
       for (int round = 0; round < Pp - 1; ++round) {
@@ -293,39 +397,38 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
           const T dcda = ib - cosv * ia;  // d cos / d r_ij
           const T dcdb = ia - cosv * ib;  // d cos / d r_ik
           const T dcdc = -c * ia * ib;    // d cos / d r_jk
-          for (int al = 0; al < nal; ++al) L.ec[al * 32 + lane] = t_exp(-(T)sf->alpha_val[al] * c2);
+          for (int al = 0; al < nal; ++al)
+            L.Ep[al * 32 + lane] = L.ea[(size_t)al * capS + j] * L.ea[(size_t)al * capS + k] *
+                                   t_exp(-sf.alpha_val[al] * c2);
           const T wjk = L.w[j] * L.w[k];
           T S1 = (T)0, S2 = (T)0, S3 = (T)0;
           for (int g = 0; g < ngrp; ++g) {
-            const int rci = sf->ang_grp_rc[g];
-            const T rc = (T)sf->rc_val[rci];
-            if (a > rc || b > rc || c > rc) continue;
+            const int rci = sf.ang_grp_rc[g];
+            if (a > sf.rc_val[rci] || b > sf.rc_val[rci] || c > sf.rc_val[rci]) continue;
             const T fa = L.fc[(size_t)rci * capS + j], fb = L.fc[(size_t)rci * capS + k];
             const T dfa = L.dfc[(size_t)rci * capS + j], dfb = L.dfc[(size_t)rci * capS + k];
             T sn, cs;
-            t_sincos(PI * c / rc, &sn, &cs);
+            t_sincos(sf.pi_over_rc[rci] * c, &sn, &cs);
             const T fcc = (T)0.5 * (cs + (T)1);
-            const T dfcc = (T)0.5 * (-sn) * (PI / rc);
+            const T dfcc = (T)-0.5 * sn * sf.pi_over_rc[rci];
             const T F = fa * fb * fcc;
-            for (int s = sf->ang_grp_start[g]; s < sf->ang_grp_start[g + 1]; ++s) {
-              const int al = sf->ang_alpha[s];
-              const T lam = (T)sf->ang_lambda[s];
+            T SP = (T)0, SQ = (T)0, SU = (T)0;
+            for (int s = sf.ang_grp_start[g]; s < sf.ang_grp_start[g + 1]; ++s) {
+              const int code = sf.ang_code[s];
+              const int al = (code >> 8) & 255, iz = (code >> 16) & 255;
+              const T lam = (code >> 24) ? (T)-1 : (T)1;
               T A, dA;
-              ang_factor<T>((T)1 + lam * cosv, sf->ang_izeta[s], (T)sf->ang_zeta[s],
-                            (T)sf->ang_pref[s], &A, &dA);
-              const T Ap = dA * lam;  // d A / d cos
-              const T E = L.ea[(size_t)al * capS + j] * L.ea[(size_t)al * capS + k] *
-                          L.ec[al * 32 + lane];
-              const T alpha = (T)sf->alpha_val[al];
-              const T AE = A * E;
-              const T EF = E * F;
-              const T m2a = (T)-2 * alpha * AE * F;
-              const int d = sf->ang_d[s];
-              const T cs_ = L.dg[d] + L.dg[d + nsf] * wjk;
-              S1 += cs_ * (Ap * dcda * EF + m2a * a + AE * dfa * fb * fcc);
-              S2 += cs_ * (Ap * dcdb * EF + m2a * b + AE * fa * dfb * fcc);
-              S3 += cs_ * (Ap * dcdc * EF + m2a * c + AE * fa * fb * dfcc);
+              ang_pow<T>((T)1 + lam * cosv, iz, iz ? (T)1 : sf.ang_zeta[s], &A, &dA);
+              const T X = (L.cA[s] + L.cB[s] * wjk) * L.Ep[al * 32 + lane];
+              const T XA = X * A;
+              SP += X * dA * lam;
+              SQ += XA;
+              SU += XA * sf.alpha_val[al];
             }
+            // dG/da = E [A' dcos/da F + A (-2 alpha a F + fc'(a) fc(b) fc(c))], etc.
+            S1 += F * (SP * dcda - (T)2 * SU * a) + SQ * (dfa * fb * fcc);
+            S2 += F * (SP * dcdb - (T)2 * SU * b) + SQ * (fa * dfb * fcc);
+            S3 += F * (SP * dcdc - (T)2 * SU * c) + SQ * (fa * fb * dfcc);
           }
           const T s1 = S1 * ia, s2 = S2 * ib, s3 = S3 * ic;
           L.gx[j] += s1 * djx + s3 * cx;
@@ -339,8 +442,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
       }
     }
     __syncwarp();
-    // write slot gradients and the per-atom virial (FP64 accumulation)
-    double W[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    // slot gradients and the per-atom virial (lanes in T, the warp sum in FP64)
+    T W[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int q = lane; q < P; q += 32) {
       const T gx = L.gx[q], gy = L.gy[q], gz = L.gz[q];
       V4 v;
@@ -349,21 +452,23 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
       v.z = gz;
       v.w = (T)0;
       gslot[(size_t)i * cap + q] = v;
-      const double d3[3] = {(double)L.dx[q], (double)L.dy[q], (double)L.dz[q]};
-      const double g3[3] = {(double)gx, (double)gy, (double)gz};
+      const T d3[3] = {L.dx[q], L.dy[q], L.dz[q]};
+      const T g3[3] = {gx, gy, gz};
 #pragma unroll
       for (int aa = 0; aa < 3; ++aa)
 #pragma unroll
         for (int bb = 0; bb < 3; ++bb) W[aa * 3 + bb] += d3[aa] * g3[bb];
     }
+    double Wd[9];
 #pragma unroll
-    for (int t = 0; t < 9; ++t) {
-      double v = W[t];
+    for (int t = 0; t < 9; ++t) Wd[t] = warp_sum<double>((double)W[t]);
+    if (lane < 9) {
+      double v = 0;
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-      W[t] = v;
+      for (int t = 0; t < 9; ++t)
+        if (lane == t) v = Wd[t];
+      wvir[(size_t)i * 9 + lane] = v;
     }
-    if (lane < 9) wvir[(size_t)i * 9 + lane] = W[lane];
     __syncwarp();
   }
 }
@@ -382,11 +487,18 @@ int warp_grid(int N, size_t smem_per_block, const void *fn) {
 }  // namespace
 
 size_t wacsf_smem_bytes(const SFDev &t, int capS, bool fwd, size_t elem) {
-  const size_t per = (size_t)5 * capS + (size_t)t.nrc * capS * (fwd ? 1 : 2) +
-                     (size_t)t.nalpha * capS + (size_t)t.nalpha * 32 +
-                     (fwd ? (size_t)t.D * 32 : (size_t)3 * capS + t.D);
-  return per * elem * kWarpsPerBlock;
+  const size_t table = elem == 8 ? kTableBytes(sizeof(SFT<double>)) : kTableBytes(sizeof(SFT<float>));
+  const size_t per = elem == 8 ? per_warp_elems<double>(capS, t.nrc, t.nalpha, t.D, t.nang, fwd)
+                               : per_warp_elems<float>(capS, t.nrc, t.nalpha, t.D, t.nang, fwd);
+  return table + per * elem * kWarpsPerBlock;
 }
+
+template <typename T>
+static const SFT<T> *sft_of(const gapgb_model *m);
+template <>
+const SFT<double> *sft_of<double>(const gapgb_model *m) { return m->d_sft64; }
+template <>
+const SFT<float> *sft_of<float>(const gapgb_model *m) { return m->d_sft32; }
 
 template <typename T>
 void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int capS,
@@ -394,9 +506,12 @@ void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
   const size_t smem = wacsf_smem_bytes(m->sfh, capS, true, sizeof(T));
   auto fn = k_wacsf_fwd<T>;
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (m->sfh.D > 2 * m->sfh.nsf || m->sfh.nrad + m->sfh.nang < m->sfh.nsf)
+    cudaMemsetAsync(ws.G, 0, sizeof(T) * (size_t)N * m->sfh.D, st);  // never-written entries
   const int grid = warp_grid(N, smem, (const void *)fn);
   fn<<<grid, 32 * kWarpsPerBlock, smem, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
-                                               ws.apos, m->d_sf, (T *)ws.G);
+                                               ws.apos, ws.nbr_d32, ws.nbr_w32, sft_of<T>(m),
+                                               (T *)ws.G);
 }
 
 template <typename T>
@@ -407,7 +522,8 @@ void launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const int grid = warp_grid(N, smem, (const void *)fn);
   fn<<<grid, 32 * kWarpsPerBlock, smem, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
-                                               ws.apos, m->d_sf, (const T *)ws.dedg,
+                                               ws.apos, ws.nbr_d32, ws.nbr_w32, sft_of<T>(m),
+                                               (const T *)ws.dedg,
                                                (typename Vec4<T>::type *)ws.gslot, ws.wvir);
 }
 
