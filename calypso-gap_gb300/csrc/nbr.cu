@@ -5,12 +5,15 @@
 // [-nabc, nabc] ascending, forms xyz = pos(j) + n1 a1 + n2 a2 + n3 a3,
 // dr = pos(i) - xyz, dis = sqrt(dr.dr) and keeps the image if dis <= rcut
 // (self image (0,0,0) skipped).  Here one warp owns atom i and its lanes own
-// consecutive j, so a warp prefix sum over per-lane counts writes the list in
-// exactly the reference order.  Each lane prunes its pair's image box with the
-// fractional-coordinate bound |f_a + n_a| <= rcut*|b_a|/(2 pi) (FP32 with a
-// margin, conservative), then applies the reference's FP64 distance test with
-// separately rounded operations in the reference's statement order, so the
-// kept set and every stored distance are bit-identical to the loop above.
+// consecutive j.  Each lane prunes its pair's image box with the
+// fractional-coordinate bound |f_a + n_a| <= rcut*|b_a|/(2 pi) and screens
+// the images in FP32 against rcut plus a rounding margin (both conservative).
+// The survivors go, in the reference order (lane = j, then n1, n2, n3),
+// through a per-warp shared queue, and the warp applies the reference's FP64
+// distance test 32 candidates at a time (separately rounded operations in the
+// reference's statement order), appending hits with a ballot prefix.  The
+// kept set, its order and every stored distance are bit-identical to the loop
+// above.
 #include <cfloat>
 
 #include "gapgb_internal.h"
@@ -134,15 +137,14 @@ __device__ __forceinline__ double ref_image(const double4 &pi, const double4 &pj
                               __dmul_rn(dr[2], dr[2])));
 }
 
-__device__ __forceinline__ void image_box(const StructInfo &si, const float4 &fi,
+__device__ __forceinline__ void image_box(const float ext[3], const int nabc[3], const float4 &fi,
                                           const float4 &fj, int lo[3], int hi[3]) {
   const float d[3] = {fj.x - fi.x, fj.y - fi.y, fj.z - fi.z};
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    float e = (float)si.ext[a];
-    float l = ceilf(-d[a] - e), h = floorf(-d[a] + e);
-    lo[a] = max(-si.nabc[a], (int)fmaxf(l, -1e6f));
-    hi[a] = min(si.nabc[a], (int)fminf(h, 1e6f));
+    const float l = ceilf(-d[a] - ext[a]), h = floorf(-d[a] + ext[a]);
+    lo[a] = max(-nabc[a], (int)fmaxf(l, -1e6f));
+    hi[a] = min(nabc[a], (int)fminf(h, 1e6f));
   }
 }
 
@@ -158,37 +160,7 @@ __device__ __forceinline__ float screen_r2(const float *L32, const float fd[3], 
   return x * x + y * y + z * z;
 }
 
-template <bool kWrite>
-__device__ __forceinline__ int scan_pair(const StructInfo &si, const double4 &pi, const double4 &pj,
-                                         bool self, const int lo[3], const int hi[3], double rcut,
-                                         const float *L32, const float fd[3], float r2max,
-                                         int j, int slot0, int cap, double4 *xyzr, int *nj,
-                                         int *ns, float4 *d32, float *w32) {
-  int c = 0;
-  for (int n1 = lo[0]; n1 <= hi[0]; ++n1)
-    for (int n2 = lo[1]; n2 <= hi[1]; ++n2)
-      for (int n3 = lo[2]; n3 <= hi[2]; ++n3) {
-        if (self && n1 == 0 && n2 == 0 && n3 == 0) continue;
-        if (screen_r2(L32, fd, n1, n2, n3) > r2max) continue;
-        double xyz[3];
-        double dis = ref_image(pi, pj, si.lat, n1, n2, n3, xyz);
-        if (dis > rcut) continue;
-        if (kWrite) {
-          int q = slot0 + c;
-          if (q < cap) {
-            xyzr[q] = make_double4(xyz[0], xyz[1], xyz[2], dis);
-            nj[q] = j;
-            ns[q] = ((n1 + 128) << 16) | ((n2 + 128) << 8) | (n3 + 128);
-            // deltaxj = -(pos(i) - xyz) (wacsf.f90:90), rounded once to FP32
-            d32[q] = make_float4((float)(xyz[0] - pi.x), (float)(xyz[1] - pi.y),
-                                 (float)(xyz[2] - pi.z), (float)dis);
-            w32[q] = (float)pj.w;
-          }
-        }
-        ++c;
-      }
-  return c;
-}
+constexpr int kQueue = 256;  // survivors per warp per exact-test round
 
 __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
                                                    const double4 *__restrict__ apos,
@@ -199,7 +171,10 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
                                                    int *__restrict__ nj, int *__restrict__ ns,
                                                    float4 *__restrict__ d32, float *__restrict__ w32,
                                                    int *__restrict__ flags) {
+  __shared__ int s_qj[kWarpsPerBlock][kQueue];
+  __shared__ int s_qs[kWarpsPerBlock][kQueue];
   const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int i = gw; i < N; i += nw) {
@@ -216,41 +191,95 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
     // FP32 screen bound: rcut plus the fractional rounding margin in Angstrom
     const float rs = (float)rcut + 2.5e-4f * lsum + 1e-3f;
     const float r2max = rs * rs;
+    const float ext[3] = {(float)si.ext[0], (float)si.ext[1], (float)si.ext[2]};
     double4 *oxyz = xyzr + (size_t)i * cap;
     int *oj = nj + (size_t)i * cap;
     int *os = ns + (size_t)i * cap;
     float4 *od = d32 + (size_t)i * cap;
     float *ow = w32 + (size_t)i * cap;
+    int *qj = s_qj[warp];
+    int *qs = s_qs[warp];
+    const unsigned lt_mask = (1u << lane) - 1u;
     int total = 0;
     for (int base = 0; base < si.na; base += 32) {
       const int jl = base + lane;
       const bool valid = jl < si.na;
       const int j = si.a0 + jl;
       int lo[3] = {0, 0, 0}, hi[3] = {-1, -1, -1};
-      double4 pj = pi;
       float fd[3] = {0.f, 0.f, 0.f};
       if (valid) {
-        pj = apos[j];
         const float4 fj = frac32[j];
         fd[0] = fj.x - fi.x;
         fd[1] = fj.y - fi.y;
         fd[2] = fj.z - fi.z;
-        image_box(si, fi, fj, lo, hi);
+        image_box(ext, si.nabc, fi, fj, lo, hi);
       }
-      int c = valid ? scan_pair<false>(si, pi, pj, j == i, lo, hi, rcut, L32, fd, r2max, j, 0, 0,
-                                       nullptr, nullptr, nullptr, nullptr, nullptr)
-                    : 0;
+      // FP32 screen: survivors of this lane's image box, in (n1, n2, n3) order
+      int c = 0;
+      if (valid)
+        for (int n1 = lo[0]; n1 <= hi[0]; ++n1)
+          for (int n2 = lo[1]; n2 <= hi[1]; ++n2)
+            for (int n3 = lo[2]; n3 <= hi[2]; ++n3) {
+              if (j == i && n1 == 0 && n2 == 0 && n3 == 0) continue;
+              if (screen_r2(L32, fd, n1, n2, n3) <= r2max) ++c;
+            }
       int incl = c;
 #pragma unroll
       for (int off = 1; off < 32; off <<= 1) {
-        int t = __shfl_up_sync(0xffffffffu, incl, off);
+        const int t = __shfl_up_sync(0xffffffffu, incl, off);
         if (lane >= off) incl += t;
       }
-      const int wtot = __shfl_sync(0xffffffffu, incl, 31);
-      if (c > 0 && total + incl - c < cap)
-        scan_pair<true>(si, pi, pj, j == i, lo, hi, rcut, L32, fd, r2max, j, total + incl - c, cap,
-                        oxyz, oj, os, od, ow);
-      total += wtot;
+      const int excl = incl - c;
+      const int T = __shfl_sync(0xffffffffu, incl, 31);
+      // survivors in canonical order (lane = j order, then shifts) through a
+      // per-warp queue; the exact FP64 test then runs 32 candidates at a time
+      for (int r0 = 0; r0 < T; r0 += kQueue) {
+        if (c > 0 && excl < r0 + kQueue && excl + c > r0) {
+          int idx = excl;
+          for (int n1 = lo[0]; n1 <= hi[0] && idx < r0 + kQueue; ++n1)
+            for (int n2 = lo[1]; n2 <= hi[1] && idx < r0 + kQueue; ++n2)
+              for (int n3 = lo[2]; n3 <= hi[2] && idx < r0 + kQueue; ++n3) {
+                if (j == i && n1 == 0 && n2 == 0 && n3 == 0) continue;
+                if (screen_r2(L32, fd, n1, n2, n3) > r2max) continue;
+                if (idx >= r0) {
+                  qj[idx - r0] = j;
+                  qs[idx - r0] = ((n1 + 128) << 16) | ((n2 + 128) << 8) | (n3 + 128);
+                }
+                ++idx;
+              }
+        }
+        __syncwarp();
+        const int nq = min(kQueue, T - r0);
+        for (int q0 = 0; q0 < nq; q0 += 32) {
+          const int t = q0 + lane;
+          bool hit = false;
+          double xyz[3] = {0, 0, 0};
+          double dis = 0;
+          int jj = 0, sh = 0;
+          double4 pj = pi;
+          if (t < nq) {
+            jj = qj[t];
+            sh = qs[t];
+            pj = apos[jj];
+            dis = ref_image(pi, pj, si.lat, ((sh >> 16) & 255) - 128, ((sh >> 8) & 255) - 128,
+                            (sh & 255) - 128, xyz);
+            hit = !(dis > rcut);
+          }
+          const unsigned m = __ballot_sync(0xffffffffu, hit);
+          const int q = total + __popc(m & lt_mask);
+          if (hit && q < cap) {
+            oxyz[q] = make_double4(xyz[0], xyz[1], xyz[2], dis);
+            oj[q] = jj;
+            os[q] = sh;
+            // deltaxj = -(pos(i) - xyz) (wacsf.f90:90), rounded once to FP32
+            od[q] = make_float4((float)(xyz[0] - pi.x), (float)(xyz[1] - pi.y),
+                                (float)(xyz[2] - pi.z), (float)dis);
+            ow[q] = (float)pj.w;
+          }
+          total += __popc(m);
+        }
+        __syncwarp();
+      }
     }
     if (lane == 0) {
       cnt[i] = min(total, cap);
@@ -312,12 +341,13 @@ __global__ void __launch_bounds__(128) k_min_bond(int N, double rcut,
     const StructInfo si = sinfo[atom_struct[i]];
     const double4 pi = apos[i];
     const float4 fi = frac32[i];
+    const float ext[3] = {(float)si.ext[0], (float)si.ext[1], (float)si.ext[2]};
     double best = 10.0;  // get_bond.f90:38
     for (int jl = lane; jl < si.na; jl += 32) {
       const int j = si.a0 + jl;
       const double4 pj = apos[j];
       int lo[3], hi[3];
-      image_box(si, fi, frac32[j], lo, hi);
+      image_box(ext, si.nabc, fi, frac32[j], lo, hi);
       for (int n1 = lo[0]; n1 <= hi[0]; ++n1)
         for (int n2 = lo[1]; n2 <= hi[1]; ++n2)
           for (int n3 = lo[2]; n3 <= hi[2]; ++n3) {

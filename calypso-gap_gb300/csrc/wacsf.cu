@@ -379,9 +379,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
           if (t == 0) {
             j = Pp - 1;
             k = round;
-          } else {
-            j = (round + t) % (Pp - 1);
-            k = (round - t + Pp - 1) % (Pp - 1);
+          } else {  // (round +- t) mod (Pp - 1) with 0 < t < Pp/2, round < Pp - 1
+            j = round + t;
+            if (j >= Pp - 1) j -= Pp - 1;
+            k = round - t;
+            if (k < 0) k += Pp - 1;
           }
           if (j >= P || k >= P) continue;
           const T a = L.r[j], b = L.r[k];
