@@ -63,6 +63,8 @@ void free_ws(Workspace &ws) {
   free_dev(ws.d_flags);
   free_dev(ws.orphans);
   free_dev(ws.gpr_scratch);
+  free_dev(ws.tc_scratch);
+  ws.tc_scratch_size = 0;
   if (ws.h_flags) cudaFreeHost(ws.h_flags);
   ws.h_flags = nullptr;
   ws.N = ws.S = ws.cap = ws.D = 0;
@@ -127,6 +129,11 @@ gapgb_status ensure_ws(gapgb_model *m, int N, int S, int cap) {
     }
   }
   ws.gpr_scratch_size = sc;
+  ws.tc_scratch_size = tc_atom_scratch_bytes(nN);
+  if (cudaMalloc(&ws.tc_scratch, ws.tc_scratch_size) != cudaSuccess) {
+    free_ws(ws);
+    return fail(GAPGB_ERR_ALLOC, "cudaMalloc failed for tensor-core scratch");
+  }
   if (cudaMallocHost((void **)&ws.h_flags, 8 * sizeof(int)) != cudaSuccess) {
     free_ws(ws);
     return fail(GAPGB_ERR_ALLOC, "cudaMallocHost failed");
@@ -238,7 +245,11 @@ gapgb_status enqueue_tail(gapgb_model *m, int S, int N, int cap, int capS, int l
   if (fp64) launch_wacsf_fwd<double>(m, ws, N, cap, capS, st);
   else launch_wacsf_fwd<float>(m, ws, N, cap, capS, st);
   if (prof) cudaEventRecord(m->ev[2], st);
-  if (m->precision == GAPGB_PREC_TC) launch_gpr_tc(m, ws, N, st);
+  if (m->precision == GAPGB_PREC_TC) {
+    gapgb_status s = build_tc_image(m);  // first call only (allocates)
+    if (s) return s;
+    launch_gpr_tc(m, ws, N, st);
+  }
   else if (fp64) launch_gpr<double, double>(m, ws, N, st);
   else if (m->precision == GAPGB_PREC_MIXED) launch_gpr<double, float>(m, ws, N, st);
   else launch_gpr<float, float>(m, ws, N, st);
@@ -266,6 +277,7 @@ gapgb_status flags_to_status(const int *f) {
   if (f[0] & kFlagImageLimit) return fail(GAPGB_ERR_CAP_EXCEEDED, "more than 127 periodic images per lattice direction");
   if (f[0] & kFlagNeighbourOverflow) return fail(GAPGB_ERR_NEIGHBOUR_OVERFLOW, "neighbour capacity exceeded (max count " + std::to_string(f[1]) + ")");
   if (f[0] & kFlagOrphanOverflow) return fail(GAPGB_ERR_CAP_EXCEEDED, "too many unpaired neighbour slots");
+  if (f[0] & kFlagTimeout) return fail(GAPGB_ERR_TIMEOUT, "a bounded device wait gave up");
   return GAPGB_OK;
 }
 
@@ -480,9 +492,11 @@ gapgb_status gapgb_set_option(gapgb_model *m, gapgb_option opt, int64_t value) {
   if (!m) return fail(GAPGB_ERR_ARG, "null model");
   switch (opt) {
     case GAPGB_OPT_PRECISION:
-      if (value == GAPGB_PREC_TC) return fail(GAPGB_ERR_ARG, "tensor-core GPR not built yet");
-      if (value != GAPGB_PREC_FP64 && value != GAPGB_PREC_FP32 && value != GAPGB_PREC_MIXED)
+      if (value != GAPGB_PREC_FP64 && value != GAPGB_PREC_FP32 && value != GAPGB_PREC_MIXED &&
+          value != GAPGB_PREC_TC)
         return fail(GAPGB_ERR_ARG, "unknown precision");
+      if (value == GAPGB_PREC_TC && m->host.D > 64)
+        return fail(GAPGB_ERR_CAP_EXCEEDED, "tensor-core GPR supports D <= 64");
       m->precision = (int)value;
       return GAPGB_OK;
     case GAPGB_OPT_NEIGHBOUR_CAP:

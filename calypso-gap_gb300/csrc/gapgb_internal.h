@@ -43,6 +43,7 @@ enum : int {
   kFlagUnknownSpecies = 2,
   kFlagImageLimit = 4,
   kFlagOrphanOverflow = 8,
+  kFlagTimeout = 16,
 };
 
 // Symmetry-function table as the kernels read it.  Angular SFs are grouped by
@@ -191,6 +192,8 @@ struct Workspace {
   int *h_flags = nullptr;     // pinned mirror of d_flags
   void *gpr_scratch = nullptr;  // split-K partial sums of the GPR
   size_t gpr_scratch_size = 0;
+  void *tc_scratch = nullptr;   // atom operand tiles of the tensor-core GPR
+  size_t tc_scratch_size = 0;
 };
 
 }  // namespace gapgb
@@ -209,6 +212,7 @@ struct gapgb_model {
   float *d_coeff32 = nullptr;
   void *d_tc = nullptr;                // tensor-core operand images (gpr_tc.cu)
   size_t tc_bytes = 0;
+  int tc_tiles = 0;
   int device = 0;
   int precision = GAPGB_PREC_FP64;
   int cap = 256;
@@ -251,6 +255,8 @@ void launch_min_bond(Workspace &ws, int N, double rcut, double *d_out, cudaStrea
 size_t wacsf_smem_bytes(const SFDev &t, int cap_smem, bool fwd, size_t elem);
 int gpr_nsplit(int N, int M);
 size_t gpr_scratch_bytes(int N, int M, int D, size_t elem);
+gapgb_status build_tc_image(gapgb_model *m);
+size_t tc_atom_scratch_bytes(int N);
 
 }  // namespace gapgb
 

@@ -1,9 +1,442 @@
-// gpr_tc.cu - tensor-core GPR (placeholder until the tcgen05 kernel lands;
-// GAPGB_PREC_TC is rejected by gapgb_set_option, so this is never reached).
+// gpr_tc.cu - the sparse-GPR contraction on the 5th-generation tensor cores.
+//
+// Same quantities as gpr.cu (GET_COV and the energy / dE/dG loops of
+// FGAP_CALC, gappy/libgap/gap_calc.f90:143-166, 268-288), computed as two
+// GEMMs with split-BF16 operands and FP32 accumulation in tensor memory:
+//
+//   centred, scaled descriptors  x'' = x/theta - mu,  m'' = m/theta - mu
+//   (mu = mean of the sparse points; differences are unchanged by centring)
+//   s_ik  = |x''_i|^2 + |m''_k|^2 - 2 x''_i . m''_k
+//   GEMM1 (N x M, K = D):  x''.m'' ~ xh.mh + xh.ml + xl.mh  (3-term BF16 split,
+//                          x'' = xh + xl, m'' = mh + ml, every product exact in FP32)
+//   w_ik  = c_k exp(-s_ik / 2),  e_i = sum_k w_ik  (compensated FP32)
+//   GEMM2 (N x D, K = M):  (W M'')_id ~ wh.mh + wh.ml + wl.mh
+//   dE/dG_id = -(1/theta_d) (x''_id e_i - (W M'')_id)
+//
+// One CTA (4 warps) owns 128 atoms.  For each tile of 128 sparse points: one
+// 1-D bulk copy brings the pre-arranged operand tiles into shared memory,
+// one thread issues GEMM1 (12 tcgen05.mma, M=128 N=128 K=16) into a TMEM
+// accumulator, the four warps read it back with tcgen05.ld (thread = atom
+// row), form w, accumulate e and write wh/wl into shared memory as GEMM2's A
+// operand, and one thread issues GEMM2 (24 tcgen05.mma, M=128 N=64 K=16)
+// accumulating over all sparse tiles in a second TMEM region.
+//
+// Operand tiles use the no-swizzle K-major canonical layout: 8-row x 16-byte
+// core matrices, K-adjacent cores 128 B apart (LBO), 8-row groups
+// (K/8)*128 B apart (SBO).  The model's tiles are built once on the host in
+// that layout, so a tile is a contiguous block and needs no tensor map.
+//
+// Every mbarrier wait is bounded; a wait that gives up sets an error flag,
+// the CTA skips the rest of its work, frees its tensor memory and returns.
+#include <cuda_bf16.h>
+
+#include <cstring>
+
 #include "gapgb_internal.h"
 
 namespace gapgb {
-void launch_gpr_tc(gapgb_model *m, Workspace &ws, int N, cudaStream_t st) {
-  (void)m; (void)ws; (void)N; (void)st;
+namespace {
+
+constexpr int kRows = 128;   // atoms per CTA (UMMA M)
+constexpr int kTileK = 128;  // sparse points per tile (GEMM1 N, GEMM2 K)
+constexpr int kDP = 64;      // padded descriptor length (GEMM1 K, GEMM2 N)
+constexpr int kTileBytes16 = kRows * kDP * 2;        // 128 x 64 bf16: 16 KB
+constexpr int kWBytes = kRows * kTileK * 2;          // 128 x 128 bf16: 32 KB
+// per sparse tile image: mh, ml (128 x 64), mhT, mlT (64 x 128), mn[128], c[128]
+constexpr int kImgTile = 4 * kTileBytes16 + 2 * kTileK * 4;  // 66 KB
+constexpr int kImgAtoms = 2 * kTileBytes16;                   // xh, xl per 128 atoms
+constexpr long kSpinLimit = 1L << 26;
+
+// shared memory map (bytes from the 1024-aligned base)
+constexpr int kOffXh = 0;
+constexpr int kOffXl = kOffXh + kTileBytes16;
+constexpr int kOffImg = kOffXl + kTileBytes16;           // one sparse tile image
+constexpr int kOffMh = kOffImg;
+constexpr int kOffMl = kOffMh + kTileBytes16;
+constexpr int kOffMhT = kOffMl + kTileBytes16;
+constexpr int kOffMlT = kOffMhT + kTileBytes16;
+constexpr int kOffMn = kOffMlT + kTileBytes16;
+constexpr int kOffC = kOffMn + kTileK * 4;
+constexpr int kOffWh = kOffImg + kImgTile;
+constexpr int kOffWl = kOffWh + kWBytes;
+constexpr int kOffBar = kOffWl + kWBytes;                 // 3 mbarriers + tmem base
+constexpr int kSmemBytes = kOffBar + 64 + 1024;           // + alignment slack
+
+// byte offset of element (r, k) of a K-major no-swizzle bf16 tile with
+// `kcores` K-cores per 8-row group
+__host__ __device__ __forceinline__ int kmajor_off(int r, int k, int kcores) {
+  return (r & 7) * 16 + (r >> 3) * (kcores * 128) + (k & 7) * 2 + (k >> 3) * 128;
 }
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// tcgen05 shared-memory matrix descriptor: no swizzle, version 1
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// instruction descriptor, kind::f16: BF16 x BF16 -> F32, both K-major
+__host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait: false (and the error flag) if the phase never completes
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *flags) {
+  for (long it = 0; it < kSpinLimit; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  atomicOr(flags, kFlagTimeout);
+  return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes,
+                                         uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                     uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+__global__ void __launch_bounds__(128, 1)
+    k_gpr_tc(int N, int ntiles, const unsigned char *__restrict__ img_model,
+             const unsigned char *__restrict__ img_atoms, const float *__restrict__ xs,
+             const float *__restrict__ xn, const float *__restrict__ invth, int D,
+             double *__restrict__ e_out, float *__restrict__ dedg, int *__restrict__ flags) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  unsigned char *sm = reinterpret_cast<unsigned char *>(
+      ((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t s_base = smem_u32(sm);
+  const uint32_t bar_load = s_base + kOffBar, bar_g1 = bar_load + 8, bar_g2 = bar_load + 16;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + kOffBar + 32);
+  int *abort_flag = reinterpret_cast<int *>(sm + kOffBar + 40);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
+                     smem_u32(tmem_slot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    mbar_init(bar_load, 1);
+    mbar_init(bar_g1, 1);
+    mbar_init(bar_g2, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t tC1 = tmem, tC2 = tmem + 128;
+  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;  // this warp's TMEM lanes
+  const int row = tid;                                      // atom row of this thread
+  const int i = blockIdx.x * kRows + row;
+  const float xnorm = (i < N) ? xn[i] : 0.f;
+  float ehi = 0.f, elo = 0.f;
+  const uint32_t id1 = instr_desc(kRows, kTileK), id2 = instr_desc(kRows, kDP);
+  uint32_t ph_load = 0, ph_g1 = 0, ph_g2 = 0;
+  bool ok = true;
+  const float *smn = reinterpret_cast<const float *>(sm + kOffMn);
+  const float *sc = reinterpret_cast<const float *>(sm + kOffC);
+  for (int t = 0; t < ntiles && ok; ++t) {
+    if (tid == 0) {
+      const uint32_t bytes = kImgTile + (t == 0 ? kImgAtoms : 0);
+      mbar_expect_tx(bar_load, bytes);
+      if (t == 0)
+        bulk_g2s(s_base + kOffXh, img_atoms + (size_t)blockIdx.x * kImgAtoms, kImgAtoms, bar_load);
+      bulk_g2s(s_base + kOffImg, img_model + (size_t)t * kImgTile, kImgTile, bar_load);
+    }
+    ok = mbar_wait(bar_load, ph_load, flags);
+    ph_load ^= 1;
+    if (!__syncthreads_and(ok)) break;
+    // GEMM1: C1[128 x 128] = xh.mh + xh.ml + xl.mh over K = 64 (4 steps of 16)
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a_off[3] = {kOffXh, kOffXh, kOffXl};
+      const uint32_t b_off[3] = {kOffMh, kOffMl, kOffMh};
+      for (int p = 0; p < 3; ++p)
+        for (int kk = 0; kk < kDP / 16; ++kk) {
+          const uint64_t ad = smem_desc(s_base + a_off[p] + kk * 256, 128, (kDP / 8) * 128);
+          const uint64_t bd = smem_desc(s_base + b_off[p] + kk * 256, 128, (kDP / 8) * 128);
+          umma(tC1, ad, bd, id1, (p > 0 || kk > 0) ? 1u : 0u);
+        }
+      umma_commit(bar_g1);
+    }
+    ok = mbar_wait(bar_g1, ph_g1, flags);
+    ph_g1 ^= 1;
+    if (!__syncthreads_and(ok)) break;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // epilogue 1: w = c exp(-s/2), e += w, W tile (bf16 hi / lo) for GEMM2
+    unsigned char *wh = sm + kOffWh, *wl = sm + kOffWl;
+#pragma unroll 1
+    for (int cc = 0; cc < kTileK / 32; ++cc) {
+      float v[32];
+      tmem_ld32(tC1 + lane_base + cc * 32, v);
+#pragma unroll
+      for (int g = 0; g < 4; ++g) {
+        uint32_t hpk[4], lpk[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          float w2[2];
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            const int k = cc * 32 + g * 8 + h * 2 + u;
+            const float s = xnorm + smn[k] - 2.f * v[g * 8 + h * 2 + u];
+            const float w = sc[k] * __expf(-0.5f * s);
+            const float tt = ehi + w;  // two-sum
+            const float bb = tt - ehi;
+            elo += (ehi - (tt - bb)) + (w - bb);
+            ehi = tt;
+            w2[u] = w;
+          }
+          const __nv_bfloat162 hi = __floats2bfloat162_rn(w2[0], w2[1]);
+          const float2 hf = __bfloat1622float2(hi);
+          hpk[h] = *reinterpret_cast<const uint32_t *>(&hi);
+          lpk[h] = pack_bf16(w2[0] - hf.x, w2[1] - hf.y);
+        }
+        const int k0 = cc * 32 + g * 8;
+        const int off = kmajor_off(row, k0, kTileK / 8);
+        *reinterpret_cast<uint4 *>(wh + off) = make_uint4(hpk[0], hpk[1], hpk[2], hpk[3]);
+        *reinterpret_cast<uint4 *>(wl + off) = make_uint4(lpk[0], lpk[1], lpk[2], lpk[3]);
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    // GEMM2: C2[128 x 64] += wh.mhT + wh.mlT + wl.mhT over K = 128 (8 steps of 16)
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a_off[3] = {kOffWh, kOffWh, kOffWl};
+      const uint32_t b_off[3] = {kOffMhT, kOffMlT, kOffMhT};
+      for (int p = 0; p < 3; ++p)
+        for (int kk = 0; kk < kTileK / 16; ++kk) {
+          const uint64_t ad = smem_desc(s_base + a_off[p] + kk * 256, 128, (kTileK / 8) * 128);
+          const uint64_t bd = smem_desc(s_base + b_off[p] + kk * 256, 128, (kTileK / 8) * 128);
+          umma(tC2, ad, bd, id2, (t > 0 || p > 0 || kk > 0) ? 1u : 0u);
+        }
+      umma_commit(bar_g2);
+    }
+    ok = mbar_wait(bar_g2, ph_g2, flags);  // operands are overwritten next tile
+    ph_g2 ^= 1;
+    ok = __syncthreads_and(ok);
+  }
+  if (ok) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const double e = (double)ehi + (double)elo;
+    float c2[64];
+    tmem_ld32(tC2 + lane_base, c2);
+    tmem_ld32(tC2 + lane_base + 32, c2 + 32);
+    if (i < N) {
+      e_out[i] = e;
+      const float ef = (float)e;
+#pragma unroll
+      for (int d = 0; d < kDP; ++d)
+        if (d < D) dedg[(size_t)i * D + d] = -invth[d] * (xs[(size_t)i * kDP + d] * ef - c2[d]);
+    }
+  } else if (tid == 0) {
+    // a wait gave up: give the outstanding copy / MMA phases one more bounded
+    // wait before the tensor memory and shared memory are released
+    mbar_wait(bar_load, ph_load, flags);
+    mbar_wait(bar_g1, ph_g1, flags);
+    mbar_wait(bar_g2, ph_g2, flags);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
+}
+
+// x'' = G / theta - mu (FP32, row-padded to 64), |x''|^2, and the xh/xl tiles
+__global__ void k_tc_prep_atoms(int N, int D, const float *__restrict__ G,
+                                const float *__restrict__ invth, const float *__restrict__ mu,
+                                float *__restrict__ xs, float *__restrict__ xn,
+                                unsigned char *__restrict__ img) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ntile_rows = ((N + kRows - 1) / kRows) * kRows;
+  if (i >= ntile_rows) return;
+  unsigned char *tile = img + (size_t)(i / kRows) * kImgAtoms;
+  const int r = i % kRows;
+  float nrm = 0.f;
+  for (int k0 = 0; k0 < kDP; k0 += 8) {
+    uint32_t hp[4], lp[4];
+    for (int h = 0; h < 4; ++h) {
+      float x2[2];
+      for (int u = 0; u < 2; ++u) {
+        const int d = k0 + h * 2 + u;
+        float x = 0.f;
+        if (i < N && d < D) x = G[(size_t)i * D + d] * invth[d] - mu[d];
+        if (i < N) xs[(size_t)i * kDP + d] = x;
+        nrm += x * x;
+        x2[u] = x;
+      }
+      const __nv_bfloat162 hi = __floats2bfloat162_rn(x2[0], x2[1]);
+      const float2 hf = __bfloat1622float2(hi);
+      hp[h] = *reinterpret_cast<const uint32_t *>(&hi);
+      lp[h] = pack_bf16(x2[0] - hf.x, x2[1] - hf.y);
+    }
+    const int off = kmajor_off(r, k0, kDP / 8);
+    *reinterpret_cast<uint4 *>(tile + off) = make_uint4(hp[0], hp[1], hp[2], hp[3]);
+    *reinterpret_cast<uint4 *>(tile + kTileBytes16 + off) = make_uint4(lp[0], lp[1], lp[2], lp[3]);
+  }
+  if (i < N) xn[i] = nrm;
+}
+
+// host-side bf16 (round to nearest even) for the model image
+uint16_t bf16_bits(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return (uint16_t)(u >> 16);  // inf / nan
+  const uint32_t lsb = (u >> 16) & 1u;
+  u += 0x7fffu + lsb;
+  return (uint16_t)(u >> 16);
+}
+float bf16_val(uint16_t b) {
+  const uint32_t u = (uint32_t)b << 16;
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+
+}  // namespace
+
+size_t tc_smem_bytes() { return kSmemBytes; }
+
+// Builds the model's tensor-core image: per sparse tile mh, ml (K-major over
+// D), mhT, mlT (K-major over the tile's points), |m''|^2 and c (FP32), plus mu.
+gapgb_status build_tc_image(gapgb_model *m) {
+  if (m->d_tc) return GAPGB_OK;
+  const HostModel &h = m->host;
+  const int M = h.M, D = h.D;
+  if (D > kDP) {
+    set_last_error("tensor-core GPR supports D <= 64");
+    return GAPGB_ERR_CAP_EXCEEDED;
+  }
+  const int nt = (M + kTileK - 1) / kTileK;
+  std::vector<double> mu(kDP, 0.0);
+  std::vector<double> mm2((size_t)M * kDP, 0.0);
+  for (int k = 0; k < M; ++k)
+    for (int d = 0; d < D; ++d) {
+      mm2[(size_t)k * kDP + d] = h.mm[(size_t)k * D + d] / h.theta[d];
+      mu[d] += mm2[(size_t)k * kDP + d] / M;
+    }
+  std::vector<unsigned char> img((size_t)nt * kImgTile, 0);
+  for (int t = 0; t < nt; ++t) {
+    unsigned char *T = img.data() + (size_t)t * kImgTile;
+    float *mn = reinterpret_cast<float *>(T + 4 * kTileBytes16);
+    float *cf = mn + kTileK;
+    for (int kk = 0; kk < kTileK; ++kk) {
+      const int k = t * kTileK + kk;
+      if (k >= M) continue;
+      double nrm = 0.0;
+      for (int d = 0; d < kDP; ++d) {
+        const double v = (d < D) ? mm2[(size_t)k * kDP + d] - mu[d] : 0.0;
+        nrm += v * v;
+        const uint16_t hb = bf16_bits((float)v);
+        const uint16_t lb = bf16_bits((float)(v - (double)bf16_val(hb)));
+        // GEMM1 B operand: rows = sparse points, K = descriptor components
+        std::memcpy(T + kmajor_off(kk, d, kDP / 8), &hb, 2);
+        std::memcpy(T + kTileBytes16 + kmajor_off(kk, d, kDP / 8), &lb, 2);
+        // GEMM2 B operand: rows = descriptor components, K = sparse points
+        std::memcpy(T + 2 * kTileBytes16 + kmajor_off(d, kk, kTileK / 8), &hb, 2);
+        std::memcpy(T + 3 * kTileBytes16 + kmajor_off(d, kk, kTileK / 8), &lb, 2);
+      }
+      mn[kk] = (float)nrm;
+      cf[kk] = (float)h.coeff[k];
+    }
+  }
+  std::vector<float> muf(kDP);
+  for (int d = 0; d < kDP; ++d) muf[d] = (float)mu[d];
+  const size_t bytes = img.size() + kDP * sizeof(float);
+  GAPGB_CUDA_TRY(cudaMalloc(&m->d_tc, bytes));
+  GAPGB_CUDA_TRY(cudaMemcpy(m->d_tc, img.data(), img.size(), cudaMemcpyHostToDevice));
+  GAPGB_CUDA_TRY(cudaMemcpy((unsigned char *)m->d_tc + img.size(), muf.data(), kDP * sizeof(float),
+                            cudaMemcpyHostToDevice));
+  m->tc_bytes = img.size();
+  m->tc_tiles = nt;
+  return GAPGB_OK;
+}
+
+size_t tc_atom_scratch_bytes(int N) {
+  const size_t tiles = (size_t)(N + kRows - 1) / kRows;
+  return tiles * kImgAtoms + (size_t)N * kDP * sizeof(float) + (size_t)N * sizeof(float) + 1024;
+}
+
+void launch_gpr_tc(gapgb_model *m, Workspace &ws, int N, cudaStream_t st) {
+  const int D = m->host.D;
+  const int tiles = (N + kRows - 1) / kRows;
+  unsigned char *img_atoms = reinterpret_cast<unsigned char *>(ws.tc_scratch);
+  float *xs = reinterpret_cast<float *>(img_atoms + (size_t)tiles * kImgAtoms);
+  float *xn = xs + (size_t)N * kDP;
+  const float *mu = reinterpret_cast<const float *>((const unsigned char *)m->d_tc + m->tc_bytes);
+  k_tc_prep_atoms<<<(tiles * kRows + 127) / 128, 128, 0, st>>>(N, D, (const float *)ws.G,
+                                                                m->d_invth32, mu, xs, xn, img_atoms);
+  cudaFuncSetAttribute(k_gpr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+  k_gpr_tc<<<tiles, 128, kSmemBytes, st>>>(N, m->tc_tiles, (const unsigned char *)m->d_tc,
+                                          img_atoms, xs, xn, m->d_invth32, D, ws.e,
+                                          (float *)ws.dedg, ws.d_flags);
+}
+
 }  // namespace gapgb

@@ -395,3 +395,51 @@ def test_min_bond_matches_oracle(gapgb_mod, oracle_mod, synth_pop):
     _, _, structs = synth_pop
     for lat, pos, _ in structs:
         assert gapgb_mod.min_bond(lat, pos, 6.0) == oracle_mod.min_bond(lat, pos, 6.0)
+
+
+# ---------------------------------------------------------------- tensor-core GPR
+
+def test_tc_si_vs_oracle(synth_si, oracle_mod):
+    """Split-BF16 tcgen05 GPR (FP32 descriptors) within the reduced-precision bar."""
+    import gapgb.synth as S
+    g, o = synth_si
+    g.set_precision("tc")
+    try:
+        structs = [S.si64(seed=s) for s in (41, 42, 43)]
+        off, sp, lat, pos = S.pack(structs)
+        E, F, St = g.eval_batch(off, sp, lat, pos)
+        for s, (l, p, z) in enumerate(structs):
+            oE, oF, oS, _ = oracle_mod.gap_calc(o, z, l, p, 6.0, True)
+            assert abs(E[s] - oE) / len(p) <= 1e-3
+            assert np.abs(F[off[s]:off[s + 1]] - oF).max() <= 20e-3
+    finally:
+        g.set_precision("fp64")
+
+
+def test_tc_matches_fp32_path_alloy(gapgb_mod, oracle_mod, tmp_path):
+    """TC and FP32 forms on the alloy workload (M = 600, many atom tiles)."""
+    import gapgb.synth as S
+    path = str(tmp_path / "gp")
+    synth_model_file(path, oracle_mod, [S.alloy512(seed=s) for s in range(2)], M=600,
+                     theta_scale=0.8, coeff_std=1e-2, seed=2)
+    m = gapgb_mod.GapModel.load(path)
+    structs = [S.alloy512(seed=s) for s in (50, 51)]
+    off, sp, lat, pos = S.pack(structs)
+    m.set_precision("fp32")
+    E32, F32, S32 = m.eval_batch(off, sp, lat, pos)
+    m.set_precision("tc")
+    Etc, Ftc, Stc = m.eval_batch(off, sp, lat, pos)
+    assert np.abs(Etc - E32).max() / 512 <= 1e-4
+    assert np.abs(Ftc - F32).max() <= 2e-3
+    o = oracle_mod.Model(path)
+    l, p, z = structs[1]
+    oE, oF, _, _ = oracle_mod.gap_calc(o, z, l, p, 6.0, True)
+    assert abs(Etc[1] - oE) / 512 <= 1e-3
+    assert np.abs(Ftc[512:] - oF).max() <= 20e-3
+    m.close()
+
+
+def test_tc_rejects_long_descriptors(golden_model, gapgb_mod):
+    with pytest.raises(gapgb_mod.GapError) as ei:
+        golden_model.set_precision("tc")
+    assert ei.value.status == 3
