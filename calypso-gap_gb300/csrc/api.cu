@@ -505,6 +505,9 @@ gapgb_status gapgb_set_option(gapgb_model *m, gapgb_option opt, int64_t value) {
       return GAPGB_OK;
     case GAPGB_OPT_DEVICE:
       return fail(GAPGB_ERR_ARG, "the device is fixed when the model is created");
+    case GAPGB_OPT_GENERIC_KERNELS:
+      m->generic_kernels = value != 0;
+      return GAPGB_OK;
   }
   return fail(GAPGB_ERR_ARG, "unknown option");
 }
@@ -515,6 +518,7 @@ gapgb_status gapgb_get_option(const gapgb_model *m, gapgb_option opt, int64_t *v
     case GAPGB_OPT_PRECISION: *value = m->precision; return GAPGB_OK;
     case GAPGB_OPT_NEIGHBOUR_CAP: *value = m->cap; return GAPGB_OK;
     case GAPGB_OPT_DEVICE: *value = m->device; return GAPGB_OK;
+    case GAPGB_OPT_GENERIC_KERNELS: *value = m->generic_kernels ? 1 : 0; return GAPGB_OK;
   }
   return fail(GAPGB_ERR_ARG, "unknown option");
 }

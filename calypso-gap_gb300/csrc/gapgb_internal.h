@@ -216,6 +216,7 @@ struct gapgb_model {
   int device = 0;
   int precision = GAPGB_PREC_FP64;
   int cap = 256;
+  bool generic_kernels = false;        // force the generic FP32 descriptor kernels
   cudaStream_t stream = nullptr;       // internal stream of the host-buffer calls
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   bool profile_stages = false;

@@ -55,7 +55,9 @@ typedef enum {
   GAPGB_OPT_PRECISION = 0,     /* gapgb_precision, default GAPGB_PREC_FP64 */
   GAPGB_OPT_NEIGHBOUR_CAP = 1, /* slots per atom, default 256; grown on overflow
                                   by the host-buffer calls */
-  GAPGB_OPT_DEVICE = 2         /* CUDA device ordinal, default 0 */
+  GAPGB_OPT_DEVICE = 2,        /* CUDA device ordinal, default 0 */
+  GAPGB_OPT_GENERIC_KERNELS = 3 /* 1: FP32 descriptor kernels take the generic
+                                   path even when the fast path applies */
 } gapgb_option;
 
 typedef struct gapgb_model gapgb_model;

@@ -443,3 +443,26 @@ def test_tc_rejects_long_descriptors(golden_model, gapgb_mod):
     with pytest.raises(gapgb_mod.GapError) as ei:
         golden_model.set_precision("tc")
     assert ei.value.status == 3
+
+
+def test_fp32_fast_and_generic_kernels_agree(synth_si, oracle_mod):
+    """The register/queue fast path and the generic FP32 descriptor kernels."""
+    import gapgb
+    import gapgb.synth as S
+    g, o = synth_si
+    structs = [S.si64(seed=s) for s in (61, 62)]
+    off, sp, lat, pos = S.pack(structs)
+    g.set_precision("fp32")
+    try:
+        load = gapgb.load()
+        load.gapgb_set_option(g.handle, 3, 1)
+        Eg, Fg, Sg = g.eval_batch(off, sp, lat, pos)
+        load.gapgb_set_option(g.handle, 3, 0)
+        Ef, Ff, Sf = g.eval_batch(off, sp, lat, pos)
+        assert np.abs(Ef - Eg).max() <= 1e-5 * np.abs(Eg).max()
+        assert np.abs(Ff - Fg).max() <= 1e-4 * max(1.0, np.abs(Fg).max())
+        assert np.abs(Sf - Sg).max() <= 1e-4 * max(1.0, np.abs(Sg).max())
+        oE, oF, _, _ = oracle_mod.gap_calc(o, structs[0][2], structs[0][0], structs[0][1], 6.0, True)
+        assert abs(Ef[0] - oE) / 64 <= 1e-3 and np.abs(Ff[:64] - oF).max() <= 20e-3
+    finally:
+        g.set_precision("fp64")
