@@ -186,6 +186,7 @@ gapgb_status upload_model(gapgb_model *m) {
   GAPGB_CUDA_TRY(cudaMemcpy(d_sf, &m->sfh, sizeof(SFDev), cudaMemcpyHostToDevice));
   const SFT<double> t64 = make_sft<double>(m->sfh);
   const SFT<float> t32 = make_sft<float>(m->sfh);
+  m->sft32h = t32;
   GAPGB_CUDA_TRY(cudaMalloc(&m->d_sft64, sizeof(t64)));
   GAPGB_CUDA_TRY(cudaMemcpy(m->d_sft64, &t64, sizeof(t64), cudaMemcpyHostToDevice));
   GAPGB_CUDA_TRY(cudaMalloc(&m->d_sft32, sizeof(t32)));

@@ -104,6 +104,16 @@ struct SFT {
   T ang_pref[kMaxSF];
   int ang_grp_rc[kMaxRC];
   int ang_grp_start[kMaxRC + 1];
+  // grouped form of the angular SFs: SF s = (alpha index q_s, combination c_s
+  // of lambda and integer zeta).  fast_nal / fast_nc are the padded grid sizes
+  // of the templated fast kernels (0 when the model does not qualify: more
+  // than one angular cutoff, more than 4 alphas, more than 8 combinations or
+  // a non-integer zeta).
+  int ncomb;
+  int comb_iz[8];
+  T comb_lam[8];
+  int ang_comb[kMaxSF];
+  int fast_nal, fast_nc;
 };
 
 template <typename T>
@@ -139,6 +149,33 @@ inline SFT<T> make_sft(const SFDev &s) {
   }
   for (int g = 0; g < s.n_ang_grp; ++g) t.ang_grp_rc[g] = s.ang_grp_rc[g];
   for (int g = 0; g <= s.n_ang_grp; ++g) t.ang_grp_start[g] = s.ang_grp_start[g];
+  // combinations of (lambda, integer zeta)
+  bool ok = s.n_ang_grp <= 1 && s.nalpha <= 4;
+  t.ncomb = 0;
+  for (int q = 0; q < s.nang && ok; ++q) {
+    if (s.ang_izeta[q] <= 0) { ok = false; break; }
+    int c = -1;
+    for (int k = 0; k < t.ncomb; ++k)
+      if (t.comb_iz[k] == s.ang_izeta[q] && t.comb_lam[k] == (T)s.ang_lambda[q]) c = k;
+    if (c < 0) {
+      if (t.ncomb == 8) { ok = false; break; }
+      c = t.ncomb++;
+      t.comb_iz[c] = s.ang_izeta[q];
+      t.comb_lam[c] = (T)s.ang_lambda[q];
+    }
+    t.ang_comb[q] = c;
+  }
+  t.fast_nal = t.fast_nc = 0;
+  if (ok) {
+    const int na = s.nalpha < 1 ? 1 : s.nalpha;
+    t.fast_nal = na <= 1 ? 1 : (na <= 2 ? 2 : 4);
+    const int nc = t.ncomb < 1 ? 1 : t.ncomb;
+    t.fast_nc = nc <= 2 ? 2 : (nc <= 4 ? 4 : (nc <= 6 ? 6 : 8));
+    for (int c = t.ncomb; c < 8; ++c) {  // padding combinations carry zero weight
+      t.comb_iz[c] = 1;
+      t.comb_lam[c] = (T)1;
+    }
+  }
   return t;
 }
 
@@ -204,6 +241,7 @@ struct gapgb_model {
   gapgb::SFDev *d_sf = nullptr;
   gapgb::SFT<double> *d_sft64 = nullptr;
   gapgb::SFT<float> *d_sft32 = nullptr;
+  gapgb::SFT<float> sft32h{};          // host copy (kernel selection)
   double *d_mmt = nullptr;             // M x D, mm / theta (FP64)
   float *d_mmt32 = nullptr;            // M x D, mm / theta (FP32)
   double *d_invth = nullptr;           // D, 1 / theta

@@ -477,300 +477,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
   }
 }
 
-// ---------------------------------------------------------------------------
-// FP32 fast path, taken when every angular SF shares one cutoff and there are
-// at most four angular alphas (the usual wACSF sets, including all synthetic
-// models here).  Per-SF parameters stay in registers, and the angular pairs
-// are first screened (r_jk <= cutoff) and compacted through a per-warp ring
-// queue with a ballot, so the SF arithmetic runs on 32 contributing pairs at a
-// time.  The gradient kernel accumulates slot gradients with shared-memory
-// FP32 atomics (summation order, hence the last bits, may vary run to run;
-// the FP64 path keeps the deterministic round-robin schedule).
-constexpr int kPairQ = 64;
-
-__device__ __forceinline__ float sel4(int al, float e0, float e1, float e2, float e3) {
-  return al == 0 ? e0 : (al == 1 ? e1 : (al == 2 ? e2 : e3));
-}
-
-// Walks the upper triangle of P slots, screens pairs and calls `work(j, k, c2)`
-// for every contributing pair with all lanes of the warp busy.
-template <typename Work>
-__device__ __forceinline__ void pair_stream(const Layout<float> &L, int P, float rc, int lane,
-                                            int *qjk, float *qc2, Work work) {
-  const int npair = P * (P - 1) / 2;
-  const float rc2 = rc * rc;
-  const unsigned lt = (1u << lane) - 1u;
-  int j = 0, k = 1 + lane;
-  while (j < P - 1 && k >= P) { const int o = k - P; ++j; k = j + 1 + o; }
-  int qh = 0, qn = 0;  // ring queue: entries [qh, qn) are pending
-  for (int base = 0; base < npair; base += 32) {
-    bool valid = false;
-    float c2 = 0.f;
-    if (base + lane < npair) {
-      const float a = L.r[j], b = L.r[k];
-      if (a <= rc && b <= rc) {
-        const float cx = L.dx[j] - L.dx[k], cy = L.dy[j] - L.dy[k], cz = L.dz[j] - L.dz[k];
-        c2 = cx * cx + cy * cy + cz * cz;
-        valid = c2 <= rc2;
-      }
-    }
-    const unsigned m = __ballot_sync(0xffffffffu, valid);
-    if (valid) {
-      const int e = (qn + __popc(m & lt)) & (kPairQ - 1);
-      qjk[e] = j | (k << 16);
-      qc2[e] = c2;
-    }
-    qn += __popc(m);
-    __syncwarp();
-    if (qn - qh >= 32) {
-      const int e = (qh + lane) & (kPairQ - 1);
-      const int jk = qjk[e];
-      const float cc = qc2[e];
-      __syncwarp();
-      work(jk & 0xffff, jk >> 16, cc);
-      qh += 32;
-    }
-    k += 32;
-    while (j < P - 1 && k >= P) { const int o = k - P; ++j; k = j + 1 + o; }
-  }
-  if (qn > qh) {
-    const int e = (qh + lane) & (kPairQ - 1);
-    const bool have = lane < qn - qh;
-    const int jk = have ? qjk[e] : 0;
-    const float cc = have ? qc2[e] : 0.f;
-    __syncwarp();
-    if (have) work(jk & 0xffff, jk >> 16, cc);
-  }
-  __syncwarp();
-}
-
-__global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
-    k_wacsf_fwd_fast(int N, int cap, int capS, const int *__restrict__ cnt,
-                     const double4 *__restrict__ xyzr, const int *__restrict__ nj,
-                     const double4 *__restrict__ apos, const float4 *__restrict__ d32,
-                     const float *__restrict__ w32, const SFT<float> *__restrict__ sfg,
-                     float *__restrict__ G) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ int s_qjk[kWarpsPerBlock][kPairQ];
-  __shared__ float s_qc2[kWarpsPerBlock][kPairQ];
-  load_table<float>(smraw, sfg);
-  const SFT<float> &sf = *reinterpret_cast<const SFT<float> *>(smraw);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nrc = sf.nrc, nal = sf.nalpha, D = sf.D, nsf = sf.nsf;
-  const int nrad = sf.nrad, nang = sf.nang;
-  const Layout<float> L = carve<float>(smraw, warp, capS, nrc, nal, D, nang, true);
-  const int rci = nang > 0 ? sf.ang_grp_rc[0] : 0;
-  const float rc = sf.rc_val[rci], pirc = sf.pi_over_rc[rci];
-  const float *fcr = L.fc + (size_t)rci * capS;
-  float alv[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) alv[q] = q < nal ? sf.alpha_val[q] : 0.f;
-  for (int i = blockIdx.x * kWarpsPerBlock + warp; i < N; i += gridDim.x * kWarpsPerBlock) {
-    const int P = stage_slots<float>(L, sf, i, cap, capS, lane, cnt, xyzr, nj, apos, d32, w32,
-                                     false);
-    __syncwarp();
-    float *Gi = G + (size_t)i * D;
-    for (int s = lane; s < nrad; s += 32) {
-      const int rr = sf.rad_rc[s];
-      const float alpha = sf.rad_alpha[s], rs = sf.rad_rs[s];
-      const float *f_ = L.fc + (size_t)rr * capS;
-      float acc = 0.f, accw = 0.f;
-      for (int q = 0; q < P; ++q) {
-        const float f = f_[q];
-        if (f == 0.f) continue;
-        const float u = L.r[q] - rs;
-        const float v = expf(-alpha * u * u) * f;
-        acc += v;
-        accw += v * L.w[q];
-      }
-      const int d = sf.rad_d[s];
-      Gi[d] = acc;
-      Gi[d + nsf] = accw;
-    }
-    for (int c0 = 0; c0 < nang; c0 += kAngChunk) {
-      int code[kAngChunk];
-      float accA[kAngChunk], accW[kAngChunk];
-#pragma unroll
-      for (int s = 0; s < kAngChunk; ++s) {
-        code[s] = (c0 + s < nang) ? sf.ang_code[c0 + s] : -1;
-        accA[s] = accW[s] = 0.f;
-      }
-      if (P > 1)
-        pair_stream(L, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2) {
-          const float a = L.r[j], b = L.r[k];
-          const float c = sqrtf(c2);
-          const float cosv = (c2 - a * a - b * b) / (-2.f * a * b);
-          const float F = fcr[j] * fcr[k] * (0.5f * (cosf(pirc * c) + 1.f));
-          float E[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q)
-            E[q] = q < nal ? L.ea[(size_t)q * capS + j] * L.ea[(size_t)q * capS + k] *
-                                 expf(-alv[q] * c2)
-                           : 0.f;
-          const float wjk = L.w[j] * L.w[k];
-#pragma unroll
-          for (int s = 0; s < kAngChunk; ++s) {
-            if (code[s] < 0) continue;
-            const int al = (code[s] >> 8) & 255, iz = (code[s] >> 16) & 255;
-            const float base = (code[s] >> 24) ? 1.f - cosv : 1.f + cosv;
-            float A, dA;
-            ang_pow<float>(base, iz, iz ? 1.f : sf.ang_zeta[c0 + s], &A, &dA);
-            const float v = A * sel4(al, E[0], E[1], E[2], E[3]) * F;
-            accA[s] += v;
-            accW[s] += v * wjk;
-          }
-        });
-#pragma unroll
-      for (int s = 0; s < kAngChunk; ++s) {
-        if (c0 + s >= nang) continue;
-        const float x = warp_sum(accA[s]), y = warp_sum(accW[s]);
-        if (lane == 0) {
-          const int d = sf.ang_d[c0 + s];
-          Gi[d] = sf.ang_pref[c0 + s] * x;
-          Gi[d + nsf] = sf.ang_pref[c0 + s] * y;
-        }
-      }
-    }
-    __syncwarp();
-  }
-}
-
-__global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
-    k_wacsf_bwd_fast(int N, int cap, int capS, const int *__restrict__ cnt,
-                     const double4 *__restrict__ xyzr, const int *__restrict__ nj,
-                     const double4 *__restrict__ apos, const float4 *__restrict__ d32,
-                     const float *__restrict__ w32, const SFT<float> *__restrict__ sfg,
-                     const float *__restrict__ dedg, float4 *__restrict__ gslot,
-                     double *__restrict__ wvir) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ int s_qjk[kWarpsPerBlock][kPairQ];
-  __shared__ float s_qc2[kWarpsPerBlock][kPairQ];
-  load_table<float>(smraw, sfg);
-  const SFT<float> &sf = *reinterpret_cast<const SFT<float> *>(smraw);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nrc = sf.nrc, nal = sf.nalpha, D = sf.D, nsf = sf.nsf;
-  const int nrad = sf.nrad, nang = sf.nang;
-  const Layout<float> L = carve<float>(smraw, warp, capS, nrc, nal, D, nang, false);
-  const int rci = nang > 0 ? sf.ang_grp_rc[0] : 0;
-  const float rc = sf.rc_val[rci], pirc = sf.pi_over_rc[rci];
-  const float *fcr = L.fc + (size_t)rci * capS;
-  const float *dfcr = L.dfc + (size_t)rci * capS;
-  float alv[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) alv[q] = q < nal ? sf.alpha_val[q] : 0.f;
-  for (int i = blockIdx.x * kWarpsPerBlock + warp; i < N; i += gridDim.x * kWarpsPerBlock) {
-    const int P = stage_slots<float>(L, sf, i, cap, capS, lane, cnt, xyzr, nj, apos, d32, w32,
-                                     true);
-    for (int d = lane; d < D; d += 32) L.dg[d] = dedg[(size_t)i * D + d];
-    for (int q = lane; q < P; q += 32) L.gx[q] = L.gy[q] = L.gz[q] = 0.f;
-    __syncwarp();
-    for (int q = lane; q < P; q += 32) {
-      const float r = L.r[q], w = L.w[q];
-      float S = 0.f;
-      for (int s = 0; s < nrad; ++s) {
-        const int rr = sf.rad_rc[s];
-        if (r > sf.rc_val[rr]) continue;
-        const float f = L.fc[(size_t)rr * capS + q], df = L.dfc[(size_t)rr * capS + q];
-        const float alpha = sf.rad_alpha[s];
-        const float u = r - sf.rad_rs[s];
-        const float ex = expf(-alpha * u * u);
-        const int d = sf.rad_d[s];
-        S += (L.dg[d] + L.dg[d + nsf] * w) * (-2.f * alpha * u * ex * f + ex * df);
-      }
-      const float ir = S / r;
-      L.gx[q] += ir * L.dx[q];
-      L.gy[q] += ir * L.dy[q];
-      L.gz[q] += ir * L.dz[q];
-    }
-    __syncwarp();
-    for (int c0 = 0; c0 < nang; c0 += kAngChunk) {
-      int code[kAngChunk];
-      float cA[kAngChunk], cB[kAngChunk], alS[kAngChunk];
-#pragma unroll
-      for (int s = 0; s < kAngChunk; ++s) {
-        const bool on = c0 + s < nang;
-        code[s] = on ? sf.ang_code[c0 + s] : -1;
-        const int d = on ? sf.ang_d[c0 + s] : 0;
-        const float pref = on ? sf.ang_pref[c0 + s] : 0.f;
-        cA[s] = pref * L.dg[d];
-        cB[s] = pref * L.dg[d + nsf];
-        alS[s] = on ? sel4((code[s] >> 8) & 255, alv[0], alv[1], alv[2], alv[3]) : 0.f;
-      }
-      if (P > 1)
-        pair_stream(L, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2) {
-          const float a = L.r[j], b = L.r[k];
-          const float c = sqrtf(c2);
-          const float ia = 1.f / a, ib = 1.f / b, ic = 1.f / c;
-          const float cosv = (c2 - a * a - b * b) / (-2.f * a * b);
-          const float dcda = ib - cosv * ia, dcdb = ia - cosv * ib, dcdc = -c * ia * ib;
-          float sn, cs;
-          sincosf(pirc * c, &sn, &cs);
-          const float fcc = 0.5f * (cs + 1.f), dfcc = -0.5f * sn * pirc;
-          const float fa = fcr[j], fb = fcr[k], dfa = dfcr[j], dfb = dfcr[k];
-          const float F = fa * fb * fcc;
-          float E[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q)
-            E[q] = q < nal ? L.ea[(size_t)q * capS + j] * L.ea[(size_t)q * capS + k] *
-                                 expf(-alv[q] * c2)
-                           : 0.f;
-          const float wjk = L.w[j] * L.w[k];
-          float SP = 0.f, SQ = 0.f, SU = 0.f;
-#pragma unroll
-          for (int s = 0; s < kAngChunk; ++s) {
-            if (code[s] < 0) continue;
-            const int al = (code[s] >> 8) & 255, iz = (code[s] >> 16) & 255;
-            const float lam = (code[s] >> 24) ? -1.f : 1.f;
-            float A, dA;
-            ang_pow<float>(1.f + lam * cosv, iz, iz ? 1.f : sf.ang_zeta[c0 + s], &A, &dA);
-            const float X = (cA[s] + cB[s] * wjk) * sel4(al, E[0], E[1], E[2], E[3]);
-            const float XA = X * A;
-            SP += X * dA * lam;
-            SQ += XA;
-            SU += XA * alS[s];
-          }
-          const float S1 = F * (SP * dcda - 2.f * SU * a) + SQ * (dfa * fb * fcc);
-          const float S2 = F * (SP * dcdb - 2.f * SU * b) + SQ * (fa * dfb * fcc);
-          const float S3 = F * (SP * dcdc - 2.f * SU * c) + SQ * (fa * fb * dfcc);
-          const float s1 = S1 * ia, s2 = S2 * ib, s3 = S3 * ic;
-          const float cx = L.dx[j] - L.dx[k], cy = L.dy[j] - L.dy[k], cz = L.dz[j] - L.dz[k];
-          atomicAdd(&L.gx[j], s1 * L.dx[j] + s3 * cx);
-          atomicAdd(&L.gy[j], s1 * L.dy[j] + s3 * cy);
-          atomicAdd(&L.gz[j], s1 * L.dz[j] + s3 * cz);
-          atomicAdd(&L.gx[k], s2 * L.dx[k] - s3 * cx);
-          atomicAdd(&L.gy[k], s2 * L.dy[k] - s3 * cy);
-          atomicAdd(&L.gz[k], s2 * L.dz[k] - s3 * cz);
-        });
-      __syncwarp();
-    }
-    float W[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int q = lane; q < P; q += 32) {
-      const float gx = L.gx[q], gy = L.gy[q], gz = L.gz[q];
-      gslot[(size_t)i * cap + q] = make_float4(gx, gy, gz, 0.f);
-      const float d3[3] = {L.dx[q], L.dy[q], L.dz[q]};
-      const float g3[3] = {gx, gy, gz};
-#pragma unroll
-      for (int aa = 0; aa < 3; ++aa)
-#pragma unroll
-        for (int bb = 0; bb < 3; ++bb) W[aa * 3 + bb] += d3[aa] * g3[bb];
-    }
-    double Wd[9];
-#pragma unroll
-    for (int t = 0; t < 9; ++t) Wd[t] = warp_sum<double>((double)W[t]);
-    if (lane < 9) {
-      double v = 0;
-#pragma unroll
-      for (int t = 0; t < 9; ++t)
-        if (lane == t) v = Wd[t];
-      wvir[(size_t)i * 9 + lane] = v;
-    }
-    __syncwarp();
-  }
-}
-
-bool fast_ok(const SFDev &t) {
-  return (t.nang == 0 || t.n_ang_grp == 1) && t.nalpha <= 4 && t.nang <= 2 * kAngChunk;
-}
+#include "wacsf_grouped.cuh"
 
 int warp_grid(int N, size_t smem_per_block, const void *fn) {
   int dev = 0, sms = 148, per_sm = 1;
@@ -806,11 +513,12 @@ void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
   if (m->sfh.D > 2 * m->sfh.nsf || m->sfh.nrad + m->sfh.nang < m->sfh.nsf)
     cudaMemsetAsync(ws.G, 0, sizeof(T) * (size_t)N * m->sfh.D, st);  // never-written entries
   if constexpr (std::is_same<T, float>::value) {
-    if (fast_ok(m->sfh) && !m->generic_kernels) {
-      auto fn = k_wacsf_fwd_fast;
-      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      const int grid = warp_grid(N, smem, (const void *)fn);
-      fn<<<grid, 32 * kWarpsPerBlock, smem, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
+    GrpFwd gf;
+    GrpBwd gb;
+    if (!m->generic_kernels && grouped_kernels(m->sft32h, &gf, &gb)) {
+      cudaFuncSetAttribute(gf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      const int grid = warp_grid(N, smem, (const void *)gf);
+      gf<<<grid, 32 * kWarpsPerBlock, smem, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
                                                    ws.apos, ws.nbr_d32, ws.nbr_w32, m->d_sft32,
                                                    (float *)ws.G);
       return;
@@ -829,11 +537,12 @@ void launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
                       cudaStream_t st) {
   const size_t smem = wacsf_smem_bytes(m->sfh, capS, false, sizeof(T));
   if constexpr (std::is_same<T, float>::value) {
-    if (fast_ok(m->sfh) && !m->generic_kernels) {
-      auto fn = k_wacsf_bwd_fast;
-      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      const int grid = warp_grid(N, smem, (const void *)fn);
-      fn<<<grid, 32 * kWarpsPerBlock, smem, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
+    GrpFwd gf;
+    GrpBwd gb;
+    if (!m->generic_kernels && grouped_kernels(m->sft32h, &gf, &gb)) {
+      cudaFuncSetAttribute(gb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      const int grid = warp_grid(N, smem, (const void *)gb);
+      gb<<<grid, 32 * kWarpsPerBlock, smem, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
                                                    ws.apos, ws.nbr_d32, ws.nbr_w32, m->d_sft32,
                                                    (const float *)ws.dedg, (float4 *)ws.gslot,
                                                    ws.wvir);

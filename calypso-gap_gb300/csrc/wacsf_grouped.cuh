@@ -1,0 +1,366 @@
+// wacsf_grouped.cuh - FP32 descriptor kernels for grouped angular SF sets
+// (included by wacsf.cu inside its anonymous namespace).
+//
+// Taken when every angular SF shares one cutoff, there are at most 4
+// angular alphas and at most 8 combinations of (lambda, integer zeta) - the
+// usual wACSF sets, including every synthetic model here.  An angular SF s is
+// then the pair (alpha q_s, combination c_s), and for a triplet
+//   G_s term = 2^(1-zeta) A_c(cos) E_q F,   A_c = (1 + lambda_c cos)^zeta_c,
+//   E_q = exp(-alpha_q (rij^2 + rik^2 + rjk^2)),  F = fc(rij) fc(rik) fc(rjk),
+// so per pair only NAL exponentials and NC powers are distinct:
+//  - forward: the pair adds A_c E_q F (and its w_j w_k weighted copy) to a
+//    NAL x NC register grid; every SF reads its cell at the end;
+//  - gradient: dE/dG is contracted first into per-atom NAL x NC matrices
+//    UA = sum_s 2^(1-zeta) dE/dG_s, UB = the same for the weighted copies,
+//    so the pair's chain-rule scalars need NAL x NC multiply-adds in total.
+// Pairs beyond the cutoff are dropped by a per-warp ballot queue before the
+// arithmetic, so all lanes work on contributing pairs.  The gradient kernel
+// accumulates slot gradients with shared-memory FP32 atomics (summation
+// order, hence the last bits, may vary between runs; the FP64 path keeps the
+// deterministic round-robin schedule).
+
+constexpr int kPairQ = 64;
+
+// Walks the upper triangle of P slots, screens pairs (r_jk <= rc) and calls
+// `work(j, k, rjk^2)` for every contributing pair, 32 at a time.
+template <typename Work>
+__device__ __forceinline__ void pair_stream(const Layout<float> &L, int P, float rc, int lane,
+                                            int *qjk, float *qc2, Work work) {
+  const int npair = P * (P - 1) / 2;
+  const float rc2 = rc * rc;
+  const unsigned lt = (1u << lane) - 1u;
+  int j = 0, k = 1 + lane;
+  while (j < P - 1 && k >= P) { const int o = k - P; ++j; k = j + 1 + o; }
+  int qh = 0, qn = 0;  // ring queue: entries [qh, qn) are pending
+  for (int base = 0; base < npair; base += 32) {
+    bool valid = false;
+    float c2 = 0.f;
+    if (base + lane < npair) {
+      const float a = L.r[j], b = L.r[k];
+      if (a <= rc && b <= rc) {
+        const float cx = L.dx[j] - L.dx[k], cy = L.dy[j] - L.dy[k], cz = L.dz[j] - L.dz[k];
+        c2 = cx * cx + cy * cy + cz * cz;
+        valid = c2 <= rc2;
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, valid);
+    if (valid) {
+      const int e = (qn + __popc(m & lt)) & (kPairQ - 1);
+      qjk[e] = j | (k << 16);
+      qc2[e] = c2;
+    }
+    qn += __popc(m);
+    __syncwarp();
+    if (qn - qh >= 32) {
+      const int e = (qh + lane) & (kPairQ - 1);
+      const int jk = qjk[e];
+      const float cc = qc2[e];
+      __syncwarp();
+      work(jk & 0xffff, jk >> 16, cc);
+      qh += 32;
+    }
+    k += 32;
+    while (j < P - 1 && k >= P) { const int o = k - P; ++j; k = j + 1 + o; }
+  }
+  if (qn > qh) {
+    const int e = (qh + lane) & (kPairQ - 1);
+    const bool have = lane < qn - qh;
+    const int jk = have ? qjk[e] : 0;
+    const float cc = have ? qc2[e] : 0.f;
+    __syncwarp();
+    if (have) work(jk & 0xffff, jk >> 16, cc);
+  }
+  __syncwarp();
+}
+
+// radial part shared by both grouped kernels (one SF per lane, slot order)
+__device__ __forceinline__ void radial_fwd(const Layout<float> &L, const SFT<float> &sf, int P,
+                                           int capS, int lane, float *Gi) {
+  for (int s = lane; s < sf.nrad; s += 32) {
+    const int rr = sf.rad_rc[s];
+    const float alpha = sf.rad_alpha[s], rs = sf.rad_rs[s];
+    const float *f_ = L.fc + rr * capS;
+    float acc = 0.f, accw = 0.f;
+    for (int q = 0; q < P; ++q) {
+      const float f = f_[q];
+      if (f == 0.f) continue;
+      const float u = L.r[q] - rs;
+      const float v = __expf(-alpha * u * u) * f;
+      acc += v;
+      accw += v * L.w[q];
+    }
+    const int d = sf.rad_d[s];
+    Gi[d] = acc;
+    Gi[d + sf.nsf] = accw;
+  }
+}
+
+template <int NAL, int NC>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
+    k_wacsf_fwd_grp(int N, int cap, int capS, const int *__restrict__ cnt,
+                    const double4 *__restrict__ xyzr, const int *__restrict__ nj,
+                    const double4 *__restrict__ apos, const float4 *__restrict__ d32,
+                    const float *__restrict__ w32, const SFT<float> *__restrict__ sfg,
+                    float *__restrict__ G) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ int s_qjk[kWarpsPerBlock][kPairQ];
+  __shared__ float s_qc2[kWarpsPerBlock][kPairQ];
+  __shared__ float s_acc[kWarpsPerBlock][2 * NAL * NC];
+  load_table<float>(smraw, sfg);
+  const SFT<float> &sf = *reinterpret_cast<const SFT<float> *>(smraw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nal = sf.nalpha, D = sf.D, nsf = sf.nsf, nang = sf.nang;
+  const Layout<float> L = carve<float>(smraw, warp, capS, sf.nrc, nal, D, nang, true);
+  const int rci = nang > 0 ? sf.ang_grp_rc[0] : 0;
+  const float rc = sf.rc_val[rci], pirc = sf.pi_over_rc[rci];
+  const float *fcr = L.fc + rci * capS;
+  float alv[NAL], clam[NC];
+  int ciz[NC];
+#pragma unroll
+  for (int q = 0; q < NAL; ++q) alv[q] = q < nal ? sf.alpha_val[q] : 0.f;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    clam[c] = sf.comb_lam[c];
+    ciz[c] = sf.comb_iz[c];
+  }
+  for (int i = blockIdx.x * kWarpsPerBlock + warp; i < N; i += gridDim.x * kWarpsPerBlock) {
+    const int P = stage_slots<float>(L, sf, i, cap, capS, lane, cnt, xyzr, nj, apos, d32, w32,
+                                     false);
+    __syncwarp();
+    float *Gi = G + (size_t)i * D;
+    radial_fwd(L, sf, P, capS, lane, Gi);
+    if (nang == 0) continue;
+    float acc[NAL][NC], accw[NAL][NC];
+#pragma unroll
+    for (int q = 0; q < NAL; ++q)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) acc[q][c] = accw[q][c] = 0.f;
+    if (P > 1)
+      pair_stream(L, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2) {
+        const float a = L.r[j], b = L.r[k];
+        const float c = sqrtf(c2);
+        const float cosv = (c2 - a * a - b * b) / (-2.f * a * b);
+        const float F = fcr[j] * fcr[k] * (0.5f * (__cosf(pirc * c) + 1.f));
+        const float wjk = L.w[j] * L.w[k];
+        float EF[NAL];
+#pragma unroll
+        for (int q = 0; q < NAL; ++q)
+          EF[q] = q < nal ? L.ea[q * capS + j] * L.ea[q * capS + k] * __expf(-alv[q] * c2) * F
+                          : 0.f;
+#pragma unroll
+        for (int cc = 0; cc < NC; ++cc) {
+          const float base = 1.f + clam[cc] * cosv;
+          float A = base;
+          for (int t = 1; t < ciz[cc]; ++t) A *= base;
+#pragma unroll
+          for (int q = 0; q < NAL; ++q) {
+            const float v = A * EF[q];
+            acc[q][cc] += v;
+            accw[q][cc] += v * wjk;
+          }
+        }
+      });
+#pragma unroll
+    for (int q = 0; q < NAL; ++q)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        const float x = warp_sum(acc[q][c]), y = warp_sum(accw[q][c]);
+        if (lane == 0) {
+          s_acc[warp][q * NC + c] = x;
+          s_acc[warp][NAL * NC + q * NC + c] = y;
+        }
+      }
+    __syncwarp();
+    for (int s = lane; s < nang; s += 32) {
+      const int cell = ((sf.ang_code[s] >> 8) & 255) * NC + sf.ang_comb[s];
+      const int d = sf.ang_d[s];
+      Gi[d] = sf.ang_pref[s] * s_acc[warp][cell];
+      Gi[d + nsf] = sf.ang_pref[s] * s_acc[warp][NAL * NC + cell];
+    }
+    __syncwarp();
+  }
+}
+
+template <int NAL, int NC>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
+    k_wacsf_bwd_grp(int N, int cap, int capS, const int *__restrict__ cnt,
+                    const double4 *__restrict__ xyzr, const int *__restrict__ nj,
+                    const double4 *__restrict__ apos, const float4 *__restrict__ d32,
+                    const float *__restrict__ w32, const SFT<float> *__restrict__ sfg,
+                    const float *__restrict__ dedg, float4 *__restrict__ gslot,
+                    double *__restrict__ wvir) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ int s_qjk[kWarpsPerBlock][kPairQ];
+  __shared__ float s_qc2[kWarpsPerBlock][kPairQ];
+  __shared__ float s_u[kWarpsPerBlock][2 * NAL * NC];
+  load_table<float>(smraw, sfg);
+  const SFT<float> &sf = *reinterpret_cast<const SFT<float> *>(smraw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nal = sf.nalpha, D = sf.D, nsf = sf.nsf, nrad = sf.nrad, nang = sf.nang;
+  const Layout<float> L = carve<float>(smraw, warp, capS, sf.nrc, nal, D, nang, false);
+  const int rci = nang > 0 ? sf.ang_grp_rc[0] : 0;
+  const float rc = sf.rc_val[rci], pirc = sf.pi_over_rc[rci];
+  const float *fcr = L.fc + rci * capS;
+  const float *dfcr = L.dfc + rci * capS;
+  float alv[NAL], clam[NC];
+  int ciz[NC];
+#pragma unroll
+  for (int q = 0; q < NAL; ++q) alv[q] = q < nal ? sf.alpha_val[q] : 0.f;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    clam[c] = sf.comb_lam[c];
+    ciz[c] = sf.comb_iz[c];
+  }
+  for (int i = blockIdx.x * kWarpsPerBlock + warp; i < N; i += gridDim.x * kWarpsPerBlock) {
+    const int P = stage_slots<float>(L, sf, i, cap, capS, lane, cnt, xyzr, nj, apos, d32, w32,
+                                     true);
+    for (int d = lane; d < D; d += 32) L.dg[d] = dedg[(size_t)i * D + d];
+    for (int q = lane; q < P; q += 32) L.gx[q] = L.gy[q] = L.gz[q] = 0.f;
+    if (lane < 2 * NAL * NC) s_u[warp][lane] = 0.f;
+    __syncwarp();
+    // radial terms: lanes own slots
+    for (int q = lane; q < P; q += 32) {
+      const float r = L.r[q], w = L.w[q];
+      float S = 0.f;
+      for (int s = 0; s < nrad; ++s) {
+        const int rr = sf.rad_rc[s];
+        if (r > sf.rc_val[rr]) continue;
+        const float f = L.fc[rr * capS + q], df = L.dfc[rr * capS + q];
+        const float alpha = sf.rad_alpha[s];
+        const float u = r - sf.rad_rs[s];
+        const float ex = __expf(-alpha * u * u);
+        const int d = sf.rad_d[s];
+        S += (L.dg[d] + L.dg[d + nsf] * w) * (-2.f * alpha * u * ex * f + ex * df);
+      }
+      const float ir = S / r;
+      L.gx[q] += ir * L.dx[q];
+      L.gy[q] += ir * L.dy[q];
+      L.gz[q] += ir * L.dz[q];
+    }
+    if (nang > 0) {
+      // dE/dG contracted onto the (alpha, combination) grid (one lane, fixed order)
+      if (lane == 0)
+        for (int s = 0; s < nang; ++s) {
+          const int cell = ((sf.ang_code[s] >> 8) & 255) * NC + sf.ang_comb[s];
+          const int d = sf.ang_d[s];
+          s_u[warp][cell] += sf.ang_pref[s] * L.dg[d];
+          s_u[warp][NAL * NC + cell] += sf.ang_pref[s] * L.dg[d + nsf];
+        }
+      __syncwarp();
+      float UA[NAL][NC], UB[NAL][NC];
+#pragma unroll
+      for (int q = 0; q < NAL; ++q)
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          UA[q][c] = s_u[warp][q * NC + c];
+          UB[q][c] = s_u[warp][NAL * NC + q * NC + c];
+        }
+      if (P > 1)
+        pair_stream(L, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2) {
+          const float a = L.r[j], b = L.r[k];
+          const float c = sqrtf(c2);
+          const float ia = 1.f / a, ib = 1.f / b, ic = 1.f / c;
+          const float cosv = (c2 - a * a - b * b) / (-2.f * a * b);
+          const float dcda = ib - cosv * ia, dcdb = ia - cosv * ib, dcdc = -c * ia * ib;
+          float sn, cs;
+          __sincosf(pirc * c, &sn, &cs);
+          const float fcc = 0.5f * (cs + 1.f), dfcc = -0.5f * sn * pirc;
+          const float fa = fcr[j], fb = fcr[k], dfa = dfcr[j], dfb = dfcr[k];
+          const float F = fa * fb * fcc;
+          const float wjk = L.w[j] * L.w[k];
+          float A[NC], dAl[NC];
+#pragma unroll
+          for (int cc = 0; cc < NC; ++cc) {
+            const float base = 1.f + clam[cc] * cosv;
+            float p = 1.f;
+            for (int t = 1; t < ciz[cc]; ++t) p *= base;  // base^(zeta-1)
+            A[cc] = p * base;
+            dAl[cc] = (float)ciz[cc] * p * clam[cc];  // d A / d cos
+          }
+          float SP = 0.f, SQ = 0.f, SU = 0.f;
+#pragma unroll
+          for (int q = 0; q < NAL; ++q) {
+            const float E = q < nal ? L.ea[q * capS + j] * L.ea[q * capS + k] *
+                                          __expf(-alv[q] * c2)
+                                    : 0.f;
+            float sp = 0.f, sq = 0.f;
+#pragma unroll
+            for (int cc = 0; cc < NC; ++cc) {
+              const float V = UA[q][cc] + wjk * UB[q][cc];
+              sp += dAl[cc] * V;
+              sq += A[cc] * V;
+            }
+            SP += E * sp;
+            SQ += E * sq;
+            SU += alv[q] * E * sq;
+          }
+          // dG/da = E [A' dcos/da F + A (-2 alpha a F + fc'(a) fc(b) fc(c))], etc.
+          const float S1 = F * (SP * dcda - 2.f * SU * a) + SQ * (dfa * fb * fcc);
+          const float S2 = F * (SP * dcdb - 2.f * SU * b) + SQ * (fa * dfb * fcc);
+          const float S3 = F * (SP * dcdc - 2.f * SU * c) + SQ * (fa * fb * dfcc);
+          const float s1 = S1 * ia, s2 = S2 * ib, s3 = S3 * ic;
+          const float cx = L.dx[j] - L.dx[k], cy = L.dy[j] - L.dy[k], cz = L.dz[j] - L.dz[k];
+          atomicAdd(&L.gx[j], s1 * L.dx[j] + s3 * cx);
+          atomicAdd(&L.gy[j], s1 * L.dy[j] + s3 * cy);
+          atomicAdd(&L.gz[j], s1 * L.dz[j] + s3 * cz);
+          atomicAdd(&L.gx[k], s2 * L.dx[k] - s3 * cx);
+          atomicAdd(&L.gy[k], s2 * L.dy[k] - s3 * cy);
+          atomicAdd(&L.gz[k], s2 * L.dz[k] - s3 * cz);
+        });
+    }
+    __syncwarp();
+    float W[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int q = lane; q < P; q += 32) {
+      const float gx = L.gx[q], gy = L.gy[q], gz = L.gz[q];
+      gslot[(size_t)i * cap + q] = make_float4(gx, gy, gz, 0.f);
+      const float d3[3] = {L.dx[q], L.dy[q], L.dz[q]};
+      const float g3[3] = {gx, gy, gz};
+#pragma unroll
+      for (int aa = 0; aa < 3; ++aa)
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb) W[aa * 3 + bb] += d3[aa] * g3[bb];
+    }
+    double Wd[9];
+#pragma unroll
+    for (int t = 0; t < 9; ++t) Wd[t] = warp_sum<double>((double)W[t]);
+    if (lane < 9) {
+      double v = 0;
+#pragma unroll
+      for (int t = 0; t < 9; ++t)
+        if (lane == t) v = Wd[t];
+      wvir[(size_t)i * 9 + lane] = v;
+    }
+    __syncwarp();
+  }
+}
+
+// Kernel pointers of every (NAL, NC) instantiation.
+template <int NAL, int NC>
+struct GrpPair {
+  static constexpr auto fwd = k_wacsf_fwd_grp<NAL, NC>;
+  static constexpr auto bwd = k_wacsf_bwd_grp<NAL, NC>;
+};
+
+using GrpFwd = decltype(&k_wacsf_fwd_grp<1, 2>);
+using GrpBwd = decltype(&k_wacsf_bwd_grp<1, 2>);
+
+template <int NAL>
+__host__ inline void pick_nc(int nc, GrpFwd *f, GrpBwd *b) {
+  switch (nc) {
+    case 2: *f = GrpPair<NAL, 2>::fwd; *b = GrpPair<NAL, 2>::bwd; break;
+    case 4: *f = GrpPair<NAL, 4>::fwd; *b = GrpPair<NAL, 4>::bwd; break;
+    case 6: *f = GrpPair<NAL, 6>::fwd; *b = GrpPair<NAL, 6>::bwd; break;
+    default: *f = GrpPair<NAL, 8>::fwd; *b = GrpPair<NAL, 8>::bwd; break;
+  }
+}
+
+// The grouped kernels for a model, or false when it does not qualify.
+__host__ inline bool grouped_kernels(const SFT<float> &t, GrpFwd *f, GrpBwd *b) {
+  if (t.fast_nal == 0 || t.fast_nc == 0) return false;
+  switch (t.fast_nal) {
+    case 1: pick_nc<1>(t.fast_nc, f, b); break;
+    case 2: pick_nc<2>(t.fast_nc, f, b); break;
+    default: pick_nc<4>(t.fast_nc, f, b); break;
+  }
+  return true;
+}
