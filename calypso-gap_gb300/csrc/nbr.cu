@@ -114,22 +114,42 @@ __global__ void k_prep_atoms(int N, int S, const int *__restrict__ atom_off,
   const double *inv = sinfo[lo].linv;
   frac32[i] = make_float4((float)(x * inv[0] + y * inv[3] + zc * inv[6]),
                           (float)(x * inv[1] + y * inv[4] + zc * inv[7]),
-                          (float)(x * inv[2] + y * inv[5] + zc * inv[8]), 0.f);
+                          (float)(x * inv[2] + y * inv[5] + zc * inv[8]), (float)w);
 }
 
 // Reference distance of image (n1,n2,n3) of atom j from atom i, with the
 // reference's operation order and no contraction (gap_calc.f90:98-100).
+// IEEE double -> float with round-to-nearest-even, in integer arithmetic so
+// that it stays off the narrow FP64 pipe.  For finite |v| below 2^128;
+// results below the float normal range become a signed zero (distances and
+// relative vectors here are either zero or far above 1e-38).
+__device__ __forceinline__ float d2f_rn(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7ff) - 1023 + 127;
+  if (e <= 0) return __uint_as_float(sign);
+  const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+  const unsigned m = (unsigned)(mant >> 29);
+  const unsigned long long rem = mant & 0x1FFFFFFFull;
+  unsigned r = ((unsigned)e << 23) | m;
+  if (rem > 0x10000000ull || (rem == 0x10000000ull && (m & 1u))) r += 1u;  // carry is exact
+  return __uint_as_float(sign | r);
+}
+
+// `dn` holds the image indices as doubles (exactly (double)n; read from a
+// table instead of converted, since int-to-double conversion occupies the
+// narrow FP64 pipe).
 __device__ __forceinline__ double ref_image(const double4 &pi, const double4 &pj,
-                                            const double *L, int n1, int n2, int n3,
+                                            const double *L, double dn1, double dn2, double dn3,
                                             double *xyz) {
   const double p[3] = {pj.x, pj.y, pj.z};
   const double c[3] = {pi.x, pi.y, pi.z};
   double dr[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    double v = __dadd_rn(p[k], __dmul_rn((double)n1, L[k]));
-    v = __dadd_rn(v, __dmul_rn((double)n2, L[3 + k]));
-    v = __dadd_rn(v, __dmul_rn((double)n3, L[6 + k]));
+    double v = __dadd_rn(p[k], __dmul_rn(dn1, L[k]));
+    v = __dadd_rn(v, __dmul_rn(dn2, L[3 + k]));
+    v = __dadd_rn(v, __dmul_rn(dn3, L[6 + k]));
     xyz[k] = v;
     dr[k] = __dsub_rn(c[k], v);
   }
@@ -173,6 +193,9 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
                                                    int *__restrict__ flags) {
   __shared__ int s_qj[kWarpsPerBlock][kQueue];
   __shared__ int s_qs[kWarpsPerBlock][kQueue];
+  __shared__ double s_dn[2 * kMaxImage + 1];  // s_dn[n + kMaxImage] = (double)n
+  for (int t = threadIdx.x; t < 2 * kMaxImage + 1; t += blockDim.x) s_dn[t] = (double)(t - kMaxImage);
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -256,13 +279,16 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
           double xyz[3] = {0, 0, 0};
           double dis = 0;
           int jj = 0, sh = 0;
-          double4 pj = pi;
+          int n1 = 0, n2 = 0, n3 = 0;
           if (t < nq) {
             jj = qj[t];
             sh = qs[t];
-            pj = apos[jj];
-            dis = ref_image(pi, pj, si.lat, ((sh >> 16) & 255) - 128, ((sh >> 8) & 255) - 128,
-                            (sh & 255) - 128, xyz);
+            n1 = ((sh >> 16) & 255) - 128;
+            n2 = ((sh >> 8) & 255) - 128;
+            n3 = (sh & 255) - 128;
+            const double4 pj = apos[jj];
+            dis = ref_image(pi, pj, si.lat, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
+                            s_dn[n3 + kMaxImage], xyz);
             hit = !(dis > rcut);
           }
           const unsigned m = __ballot_sync(0xffffffffu, hit);
@@ -271,10 +297,11 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
             oxyz[q] = make_double4(xyz[0], xyz[1], xyz[2], dis);
             oj[q] = jj;
             os[q] = sh;
-            // deltaxj = -(pos(i) - xyz) (wacsf.f90:90), rounded once to FP32
-            od[q] = make_float4((float)(xyz[0] - pi.x), (float)(xyz[1] - pi.y),
-                                (float)(xyz[2] - pi.z), (float)dis);
-            ow[q] = (float)pj.w;
+            // FP32 record for the FP32 kernels: deltaxj = xyz - pos(i)
+            // (wacsf.f90:90) in FP64, rounded once to FP32
+            od[q] = make_float4(d2f_rn(xyz[0] - pi.x), d2f_rn(xyz[1] - pi.y),
+                                d2f_rn(xyz[2] - pi.z), d2f_rn(dis));
+            ow[q] = frac32[jj].w;
           }
           total += __popc(m);
         }
@@ -353,7 +380,7 @@ __global__ void __launch_bounds__(128) k_min_bond(int N, double rcut,
           for (int n3 = lo[2]; n3 <= hi[2]; ++n3) {
             if (j == i && n1 == 0 && n2 == 0 && n3 == 0) continue;
             double xyz[3];
-            double dis = ref_image(pi, pj, si.lat, n1, n2, n3, xyz);
+            double dis = ref_image(pi, pj, si.lat, (double)n1, (double)n2, (double)n3, xyz);
             if (dis > rcut) continue;
             if (dis < best) best = dis;
           }
