@@ -224,6 +224,43 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
     int *qs = s_qs[warp];
     const unsigned lt_mask = (1u << lane) - 1u;
     int total = 0;
+    int qh = 0, qt = 0;  // ring queue: candidates [qh, qt) are pending
+    // exact FP64 test of queued candidates, 32 at a time (all of them when
+    // `all`), hits appended in queue order = the reference order
+    auto drain = [&](bool all) {
+      while (qt - qh >= 32 || (all && qt > qh)) {
+        const int t = qh + lane;
+        bool hit = false;
+        double xyz[3] = {0, 0, 0};
+        double dis = 0;
+        int jj = 0, sh = 0;
+        if (t < qt) {
+          const int e = t & (kQueue - 1);
+          jj = qj[e];
+          sh = qs[e];
+          const int n1 = ((sh >> 16) & 255) - 128, n2 = ((sh >> 8) & 255) - 128,
+                    n3 = (sh & 255) - 128;
+          dis = ref_image(pi, apos[jj], si.lat, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
+                          s_dn[n3 + kMaxImage], xyz);
+          hit = !(dis > rcut);
+        }
+        __syncwarp();
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        const int q = total + __popc(m & lt_mask);
+        if (hit && q < cap) {
+          oxyz[q] = make_double4(xyz[0], xyz[1], xyz[2], dis);
+          oj[q] = jj;
+          os[q] = sh;
+          // FP32 record for the FP32 kernels: deltaxj = xyz - pos(i)
+          // (wacsf.f90:90) in FP64, rounded once to FP32
+          od[q] = make_float4(d2f_rn(xyz[0] - pi.x), d2f_rn(xyz[1] - pi.y),
+                              d2f_rn(xyz[2] - pi.z), d2f_rn(dis));
+          ow[q] = frac32[jj].w;
+        }
+        total += __popc(m);
+        qh += min(32, qt - qh);
+      }
+    };
     for (int base = 0; base < si.na; base += 32) {
       const int jl = base + lane;
       const bool valid = jl < si.na;
@@ -254,60 +291,32 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
       }
       const int excl = incl - c;
       const int T = __shfl_sync(0xffffffffu, incl, 31);
-      // survivors in canonical order (lane = j order, then shifts) through a
-      // per-warp queue; the exact FP64 test then runs 32 candidates at a time
-      for (int r0 = 0; r0 < T; r0 += kQueue) {
-        if (c > 0 && excl < r0 + kQueue && excl + c > r0) {
+      // survivors in canonical order (lane = j order, then shifts) enter a
+      // per-warp ring queue that spans chunks; the exact FP64 test runs on
+      // 32 queued candidates at a time
+      for (int r0 = 0; r0 < T; r0 += kQueue - 32) {
+        const int take = min(kQueue - 32, T - r0);
+        if (c > 0 && excl < r0 + take && excl + c > r0) {
           int idx = excl;
-          for (int n1 = lo[0]; n1 <= hi[0] && idx < r0 + kQueue; ++n1)
-            for (int n2 = lo[1]; n2 <= hi[1] && idx < r0 + kQueue; ++n2)
-              for (int n3 = lo[2]; n3 <= hi[2] && idx < r0 + kQueue; ++n3) {
+          for (int n1 = lo[0]; n1 <= hi[0] && idx < r0 + take; ++n1)
+            for (int n2 = lo[1]; n2 <= hi[1] && idx < r0 + take; ++n2)
+              for (int n3 = lo[2]; n3 <= hi[2] && idx < r0 + take; ++n3) {
                 if (j == i && n1 == 0 && n2 == 0 && n3 == 0) continue;
                 if (screen_r2(L32, fd, n1, n2, n3) > r2max) continue;
                 if (idx >= r0) {
-                  qj[idx - r0] = j;
-                  qs[idx - r0] = ((n1 + 128) << 16) | ((n2 + 128) << 8) | (n3 + 128);
+                  const int e = (qt + idx - r0) & (kQueue - 1);
+                  qj[e] = j;
+                  qs[e] = ((n1 + 128) << 16) | ((n2 + 128) << 8) | (n3 + 128);
                 }
                 ++idx;
               }
         }
+        qt += take;
         __syncwarp();
-        const int nq = min(kQueue, T - r0);
-        for (int q0 = 0; q0 < nq; q0 += 32) {
-          const int t = q0 + lane;
-          bool hit = false;
-          double xyz[3] = {0, 0, 0};
-          double dis = 0;
-          int jj = 0, sh = 0;
-          int n1 = 0, n2 = 0, n3 = 0;
-          if (t < nq) {
-            jj = qj[t];
-            sh = qs[t];
-            n1 = ((sh >> 16) & 255) - 128;
-            n2 = ((sh >> 8) & 255) - 128;
-            n3 = (sh & 255) - 128;
-            const double4 pj = apos[jj];
-            dis = ref_image(pi, pj, si.lat, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
-                            s_dn[n3 + kMaxImage], xyz);
-            hit = !(dis > rcut);
-          }
-          const unsigned m = __ballot_sync(0xffffffffu, hit);
-          const int q = total + __popc(m & lt_mask);
-          if (hit && q < cap) {
-            oxyz[q] = make_double4(xyz[0], xyz[1], xyz[2], dis);
-            oj[q] = jj;
-            os[q] = sh;
-            // FP32 record for the FP32 kernels: deltaxj = xyz - pos(i)
-            // (wacsf.f90:90) in FP64, rounded once to FP32
-            od[q] = make_float4(d2f_rn(xyz[0] - pi.x), d2f_rn(xyz[1] - pi.y),
-                                d2f_rn(xyz[2] - pi.z), d2f_rn(dis));
-            ow[q] = frac32[jj].w;
-          }
-          total += __popc(m);
-        }
-        __syncwarp();
+        drain(false);
       }
     }
+    drain(true);
     if (lane == 0) {
       cnt[i] = min(total, cap);
       atomicMax(flags + 1, total);
