@@ -87,15 +87,15 @@ __host__ __device__ constexpr size_t kTableBytes(size_t s) { return (s + 15) / 1
 
 template <typename T>
 struct Layout {
-  T *dx, *dy, *dz, *r, *w, *fc, *dfc, *ea, *Fp, *Ep, *gx, *gy, *gz, *dg, *cA, *cB;
+  T *dx, *dy, *dz, *r, *w, *ir, *fc, *dfc, *ea, *Fp, *Ep, *gx, *gy, *gz, *dg, *cA, *cB;
 };
 
 template <typename T>
 __host__ __device__ __forceinline__ size_t per_warp_elems(int capS, int nrc, int nal, int D,
                                                           int nang, bool fwd) {
-  return fwd ? (size_t)5 * capS + (size_t)nrc * capS + (size_t)nal * capS + (size_t)nrc * 32 +
+  return fwd ? (size_t)6 * capS + (size_t)nrc * capS + (size_t)nal * capS + (size_t)nrc * 32 +
                    (size_t)nal * 32
-             : (size_t)5 * capS + (size_t)2 * nrc * capS + (size_t)nal * capS +
+             : (size_t)6 * capS + (size_t)2 * nrc * capS + (size_t)nal * capS +
                    (size_t)nal * 32 + (size_t)3 * capS + D + (size_t)2 * nang;
 }
 
@@ -110,7 +110,8 @@ __device__ __forceinline__ Layout<T> carve(unsigned char *raw, int warp, int cap
   L.dz = L.dy + capS;
   L.r = L.dz + capS;
   L.w = L.r + capS;
-  L.fc = L.w + capS;
+  L.ir = L.w + capS;
+  L.fc = L.ir + capS;
   L.dfc = L.fc + (size_t)nrc * capS;
   L.ea = fwd ? L.dfc : L.dfc + (size_t)nrc * capS;
   T *p = L.ea + (size_t)nal * capS;
@@ -196,6 +197,7 @@ __device__ __forceinline__ int stage_slots(const Layout<T> &L, const SFT<T> &sf,
     L.dz[q] = dz;
     L.r[q] = r;
     L.w[q] = w;
+    L.ir[q] = (T)1 / r;
     for (int g = 0; g < nrc; ++g) {
       T fcv = (T)0, dfcv = (T)0;
       if (r <= sf.rc_val[g]) {

@@ -21,6 +21,20 @@
 
 constexpr int kPairQ = 64;
 
+// b^iz and b^(iz-1) for integer zeta >= 1 (branch-free up to 4)
+__device__ __forceinline__ float pow_iz(float b, int iz, float *pm1) {
+  const float b2 = b * b;
+  float p;
+  if (iz <= 4) {
+    p = iz == 1 ? 1.f : (iz == 2 ? b : (iz == 3 ? b2 : b2 * b));
+  } else {
+    p = b2 * b2;
+    for (int t = 5; t < iz; ++t) p *= b;
+  }
+  *pm1 = p;
+  return p * b;
+}
+
 // Walks the upper triangle of P slots, screens pairs (r_jk <= rc) and calls
 // `work(j, k, rjk^2)` for every contributing pair, 32 at a time.
 template <typename Work>
@@ -139,7 +153,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
       pair_stream(L, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2) {
         const float a = L.r[j], b = L.r[k];
         const float c = sqrtf(c2);
-        const float cosv = (c2 - a * a - b * b) / (-2.f * a * b);
+        // costheta = (rij^2 + rik^2 - rjk^2) / (2 rij rik) (wacsf.f90:271-273)
+        const float cosv = (a * a + b * b - c2) * 0.5f * L.ir[j] * L.ir[k];
         const float F = fcr[j] * fcr[k] * (0.5f * (__cosf(pirc * c) + 1.f));
         const float wjk = L.w[j] * L.w[k];
         float EF[NAL];
@@ -149,9 +164,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
                           : 0.f;
 #pragma unroll
         for (int cc = 0; cc < NC; ++cc) {
-          const float base = 1.f + clam[cc] * cosv;
-          float A = base;
-          for (int t = 1; t < ciz[cc]; ++t) A *= base;
+          float pm1;
+          const float A = pow_iz(1.f + clam[cc] * cosv, ciz[cc], &pm1);
 #pragma unroll
           for (int q = 0; q < NAL; ++q) {
             const float v = A * EF[q];
@@ -259,8 +273,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
         pair_stream(L, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2) {
           const float a = L.r[j], b = L.r[k];
           const float c = sqrtf(c2);
-          const float ia = 1.f / a, ib = 1.f / b, ic = 1.f / c;
-          const float cosv = (c2 - a * a - b * b) / (-2.f * a * b);
+          const float ia = L.ir[j], ib = L.ir[k], ic = 1.f / c;
+          const float cosv = (a * a + b * b - c2) * 0.5f * ia * ib;
           const float dcda = ib - cosv * ia, dcdb = ia - cosv * ib, dcdc = -c * ia * ib;
           float sn, cs;
           __sincosf(pirc * c, &sn, &cs);
@@ -271,10 +285,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
           float A[NC], dAl[NC];
 #pragma unroll
           for (int cc = 0; cc < NC; ++cc) {
-            const float base = 1.f + clam[cc] * cosv;
-            float p = 1.f;
-            for (int t = 1; t < ciz[cc]; ++t) p *= base;  // base^(zeta-1)
-            A[cc] = p * base;
+            float p;  // base^(zeta-1)
+            A[cc] = pow_iz(1.f + clam[cc] * cosv, ciz[cc], &p);
             dAl[cc] = (float)ciz[cc] * p * clam[cc];  // d A / d cos
           }
           float SP = 0.f, SQ = 0.f, SU = 0.f;
