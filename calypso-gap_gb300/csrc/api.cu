@@ -576,6 +576,65 @@ gapgb_status gapgb_eval_batch_device(gapgb_model *m, int nstruct, int natoms, in
                       d_atom_energy, s);
 }
 
+struct gapgb_graph {
+  gapgb_model *model = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+gapgb_status gapgb_graph_create(gapgb_model *m, int nstruct, int natoms, int max_atoms,
+                                const int *d_atom_off, const int *d_species, const double *d_lat,
+                                const double *d_pos, int lgrad, double *d_energy, double *d_force,
+                                double *d_stress, double *d_atom_energy, gapgb_graph **out) {
+  if (!m || !out) return fail(GAPGB_ERR_ARG, "null argument");
+  *out = nullptr;
+  // warm-up outside capture: workspace, tensor-core image, device flags
+  gapgb_status st = gapgb_eval_batch_device(m, nstruct, natoms, max_atoms, d_atom_off, d_species,
+                                            d_lat, d_pos, lgrad, d_energy, d_force, d_stress,
+                                            d_atom_energy, m->stream);
+  if (st) return st;
+  GAPGB_CUDA_TRY(cudaStreamSynchronize(m->stream));
+  st = gapgb_check_device_status(m);
+  if (st) return st;
+  gapgb_graph *g = new gapgb_graph();
+  g->model = m;
+  cudaError_t e = cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    delete g;
+    return fail(GAPGB_ERR_CUDA, std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(e));
+  }
+  st = gapgb_eval_batch_device(m, nstruct, natoms, max_atoms, d_atom_off, d_species, d_lat, d_pos,
+                               lgrad, d_energy, d_force, d_stress, d_atom_energy, m->stream);
+  e = cudaStreamEndCapture(m->stream, &g->graph);
+  if (st || e != cudaSuccess) {
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    if (st) return st;
+    return fail(GAPGB_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+  }
+  e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g->graph);
+    delete g;
+    return fail(GAPGB_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  }
+  *out = g;
+  return GAPGB_OK;
+}
+
+gapgb_status gapgb_graph_launch(gapgb_graph *g, void *stream) {
+  if (!g || !g->exec) return fail(GAPGB_ERR_ARG, "null graph");
+  GAPGB_CUDA_TRY(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+  return GAPGB_OK;
+}
+
+void gapgb_graph_free(gapgb_graph *g) {
+  if (!g) return;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
+}
+
 gapgb_status gapgb_check_device_status(gapgb_model *m) {
   if (!m) return fail(GAPGB_ERR_ARG, "null model");
   if (!m->ws.d_flags) return GAPGB_OK;

@@ -41,6 +41,9 @@ SYMBOLS = [
     ("gapgb_eval_batch", _I, [_P, _I, _P, _P, _P, _P, _I, _P, _P, _P, _P]),
     ("gapgb_eval_batch_device", _I, [_P, _I, _I, _I, _P, _P, _P, _P, _I, _P, _P, _P, _P, _P]),
     ("gapgb_check_device_status", _I, [_P]),
+    ("gapgb_graph_create", _I, [_P, _I, _I, _I, _P, _P, _P, _P, _I, _P, _P, _P, _P, C.POINTER(_P)]),
+    ("gapgb_graph_launch", _I, [_P, _P]),
+    ("gapgb_graph_free", None, [_P]),
     ("gapgb_stage_times", _I, [_P, _P]),
     ("gapgb_descriptors", _I, [_P, _I, _P, _P, _P, _P, _P]),
     ("gapgb_neighbors", _I, [_P, _I, _P, _P, _P, _I, _P, _P]),
@@ -234,6 +237,16 @@ class GapModel:
         _check(load().gapgb_eval_batch(self._h, nstruct, atom_off, species, lat, pos, int(lgrad),
                                        energy, force, stress, None), "gapgb_eval_batch")
 
+    def graph(self, nstruct, natoms, max_atoms, atom_off, species, lat, pos, lgrad, energy, force,
+              stress, atom_energy=0):
+        """Capture the device-buffer evaluation on these device pointers into a
+        CUDA graph (see gapgb_graph_create); returns a Graph."""
+        h = C.c_void_p()
+        _check(load().gapgb_graph_create(self._h, nstruct, natoms, max_atoms, atom_off, species, lat,
+                                         pos, int(lgrad), energy, force, stress,
+                                         atom_energy or None, C.byref(h)), "gapgb_graph_create")
+        return Graph(h, self)
+
     def check_device_status(self):
         _check(load().gapgb_check_device_status(self._h), "gapgb_check_device_status")
 
@@ -260,6 +273,28 @@ class GapModel:
         _check(load().gapgb_neighbors(self._h, n, _ptr(_i32(species)), _ptr(_f64(lat, (3, 3))),
                                       _ptr(pos), cap, _ptr(cnt), _ptr(nb)), "gapgb_neighbors")
         return cnt, nb
+
+
+class Graph:
+    """A captured evaluation (gapgb_graph); launch() replays it on a stream."""
+
+    def __init__(self, handle, model):
+        self._h = handle
+        self.model = model  # keeps the model alive
+
+    def launch(self, stream=0):
+        _check(load().gapgb_graph_launch(self._h, stream or None), "gapgb_graph_launch")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().gapgb_graph_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def min_bond(lat, pos, rcut=6.0):

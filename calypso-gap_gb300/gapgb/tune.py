@@ -1,0 +1,132 @@
+"""Autotuner for the evaluation configuration of a model on a workload.
+
+For a calibration batch it evaluates every candidate configuration:
+  - precision form: "tc" (tensor-core GPR, D <= 64), "fp32", "mixed";
+  - descriptor kernel family: grouped register-grid kernels or the generic
+    ones (GAPGB_OPT_GENERIC_KERNELS);
+  - neighbour capacity: the tight bound (the largest count rounded up to 8)
+    or 25 % headroom.  The capacity sets the per-warp shared-memory tiles of
+    the descriptor kernels, hence their occupancy.
+It keeps the candidates whose energies and forces lie within `tol_e`
+eV/atom and `tol_f` eV/A of the plain FP64 path (the drop-in parity path),
+times them on the device-buffer path, and applies the fastest to the model.
+Results are cached in a JSON file keyed by the model's arrays, the GPU name
+and the batch shape, so a later run reuses the decision without re-timing.
+"""
+import hashlib
+import json
+import os
+import time
+
+import numpy as np
+
+from . import GapModel, OPT_NEIGHBOUR_CAP, load
+
+OPT_GENERIC_KERNELS = 3
+
+
+def _signature(model, off, device_name):
+    th, mm, co = model.arrays()
+    h = hashlib.sha1()
+    for a in (th, mm, co):
+        h.update(np.ascontiguousarray(a).tobytes())
+    h.update(("%s|%d|%d" % (device_name, len(off) - 1, int(off[-1]))).encode())
+    return h.hexdigest()[:24]
+
+
+def _max_count(model, off, species, lat, pos):
+    """Largest neighbour count of the batch (one FP64 pass of the list)."""
+    mx = 0
+    for s in range(len(off) - 1):
+        a, b = int(off[s]), int(off[s + 1])
+        cnt, _ = model.neighbors(species[a:b], lat[s], pos[a:b], cap=1024)
+        mx = max(mx, int(cnt.max()))
+    return mx
+
+
+def autotune(model, off, species, lat, pos, tol_e=1e-3, tol_f=20e-3, reps=5, cache=None,
+             verbose=False):
+    """Choose and apply the fastest configuration within tolerance.
+
+    Returns a dict with the choice, its errors against FP64 and its time."""
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device())
+    name = torch.cuda.get_device_name(dev)
+    off = np.ascontiguousarray(off, np.int32)
+    S, N = len(off) - 1, int(off[-1])
+    sig = _signature(model, off, name)
+    if cache and os.path.exists(cache):
+        db = json.load(open(cache))
+        if sig in db:
+            best = db[sig]
+            _apply(model, best)
+            return dict(best, cached=True)
+    # reference: the plain FP64 path
+    model.set_precision("fp64")
+    E64, F64, _ = model.eval_batch(off, species, lat, pos)
+    natoms = np.diff(off)
+    mx = _max_count(model, off, species, lat, pos)
+    caps = sorted({((mx + 7) // 8) * 8, ((int(mx * 1.25) + 7) // 8) * 8})
+    forms = (["tc"] if model.des_len <= 64 else []) + ["fp32", "mixed"]
+    t_off = torch.from_numpy(off).to(dev)
+    t_sp = torch.from_numpy(np.ascontiguousarray(species, np.int32)).to(dev)
+    t_lat = torch.from_numpy(np.ascontiguousarray(lat, np.float64)).to(dev)
+    t_pos = torch.from_numpy(np.ascontiguousarray(pos, np.float64)).to(dev)
+    t_E = torch.zeros(S, dtype=torch.float64, device=dev)
+    t_F = torch.zeros(N, 3, dtype=torch.float64, device=dev)
+    t_S = torch.zeros(S, 6, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    results = []
+    for form in forms:
+        for generic in (0, 1):
+            for cap in caps:
+                cfg = {"precision": form, "generic_kernels": generic, "cap": cap}
+                _apply(model, cfg)
+                E, F, _ = model.eval_batch(off, species, lat, pos)
+                de = float(np.max(np.abs(E - E64) / natoms))
+                df = float(np.max(np.abs(F - F64)))
+                cfg.update(dE_per_atom=de, dF=df)
+                if de > tol_e or df > tol_f:
+                    cfg["ms"] = None
+                    results.append(cfg)
+                    continue
+
+                def run():
+                    model.eval_batch_ptrs(S, N, int(natoms.max()), t_off.data_ptr(),
+                                          t_sp.data_ptr(), t_lat.data_ptr(), t_pos.data_ptr(), 1,
+                                          t_E.data_ptr(), t_F.data_ptr(), t_S.data_ptr(), 0,
+                                          stream.cuda_stream)
+                run()
+                model.check_device_status()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                for _ in range(reps):
+                    run()
+                b.record(stream)
+                torch.cuda.synchronize()
+                model.check_device_status()
+                cfg["ms"] = a.elapsed_time(b) / reps
+                results.append(cfg)
+                if verbose:
+                    print("autotune", cfg)
+    ok = [r for r in results if r["ms"] is not None]
+    if not ok:
+        best = {"precision": "fp64", "generic_kernels": 0, "cap": caps[-1], "dE_per_atom": 0.0,
+                "dF": 0.0, "ms": None}
+    else:
+        best = min(ok, key=lambda r: r["ms"])
+    _apply(model, best)
+    best = dict(best, candidates=results)
+    if cache:
+        db = json.load(open(cache)) if os.path.exists(cache) else {}
+        db[sig] = {k: v for k, v in best.items() if k != "candidates"}
+        tmp = cache + ".tmp"
+        json.dump(db, open(tmp, "w"), indent=1)
+        os.replace(tmp, cache)
+    return best
+
+
+def _apply(model, cfg):
+    model.set_precision(cfg["precision"])
+    load().gapgb_set_option(model.handle, OPT_GENERIC_KERNELS, int(cfg.get("generic_kernels", 0)))
+    model.set_neighbour_cap(int(cfg["cap"]))

@@ -156,6 +156,25 @@ gapgb_status gapgb_eval_batch_device(gapgb_model *model, int nstruct,
  * evaluation (synchronises the model's device). */
 gapgb_status gapgb_check_device_status(gapgb_model *model);
 
+/* A device-buffer evaluation captured once into a CUDA graph and replayed.
+ * gapgb_graph_create runs one warm-up evaluation (which sizes the workspace,
+ * builds the tensor-core image and checks the device flags), then captures
+ * the same launch sequence; the graph stays bound to these buffers, so the
+ * caller refills d_pos / d_lat (same sizes) between launches.  Structure
+ * search evaluates a whole ragged population with one graph launch; MD
+ * replays it every step.  The model must not be reconfigured (precision,
+ * capacity) while a graph built from it is alive. */
+typedef struct gapgb_graph gapgb_graph;
+gapgb_status gapgb_graph_create(gapgb_model *model, int nstruct, int natoms,
+                                int max_atoms, const int *d_atom_off,
+                                const int *d_species, const double *d_lat,
+                                const double *d_pos, int lgrad,
+                                double *d_energy, double *d_force,
+                                double *d_stress, double *d_atom_energy,
+                                gapgb_graph **out);
+gapgb_status gapgb_graph_launch(gapgb_graph *graph, void *stream);
+void gapgb_graph_free(gapgb_graph *graph);
+
 /* Device time of each stage of the last evaluation, in milliseconds:
  * t[0] neighbours, t[1] descriptors, t[2] GPR, t[3] chain rule + reduction.
  * Only filled when GAPGB_PROFILE_STAGES is set in the environment. */

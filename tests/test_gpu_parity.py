@@ -466,3 +466,69 @@ def test_fp32_fast_and_generic_kernels_agree(synth_si, oracle_mod):
         assert abs(Ef[0] - oE) / 64 <= 1e-3 and np.abs(Ff[:64] - oF).max() <= 20e-3
     finally:
         g.set_precision("fp64")
+
+
+# ---------------------------------------------------------------- graphs and tuning
+
+def _dev_batch(batch):
+    import torch
+    import gapgb.synth as S
+    off, sp, lat, pos = S.pack(batch)
+    dev = torch.device("cuda:0")
+    t = dict(off=torch.from_numpy(off).to(dev), sp=torch.from_numpy(sp).to(dev),
+             lat=torch.from_numpy(lat).to(dev), pos=torch.from_numpy(pos).to(dev))
+    S_, N = len(batch), int(off[-1])
+    t["E"] = torch.zeros(S_, dtype=torch.float64, device=dev)
+    t["F"] = torch.zeros(N, 3, dtype=torch.float64, device=dev)
+    t["S"] = torch.zeros(S_, 6, dtype=torch.float64, device=dev)
+    return (off, sp, lat, pos), t
+
+
+def test_graph_replay_matches_direct(synth_pop):
+    """A captured graph replays the evaluation bit for bit and follows new
+    positions written into its bound buffers."""
+    import torch
+    import gapgb.synth as S
+    g, _, _ = synth_pop
+    g.set_precision("fp64")
+    rng = np.random.default_rng(12)
+    batch = [S.random_structure(rng, n, species_pool=(3, 8, 14, 26)) for n in (9, 30, 21)]
+    (off, sp, lat, pos), t = _dev_batch(batch)
+    nmax = int(np.diff(off).max())
+    gr = g.graph(len(batch), int(off[-1]), nmax, t["off"].data_ptr(), t["sp"].data_ptr(),
+                 t["lat"].data_ptr(), t["pos"].data_ptr(), 1, t["E"].data_ptr(),
+                 t["F"].data_ptr(), t["S"].data_ptr())
+    stream = torch.cuda.current_stream().cuda_stream
+    gr.launch(stream)
+    torch.cuda.synchronize()
+    g.check_device_status()
+    E0, F0, S0 = g.eval_batch(off, sp, lat, pos)
+    assert np.array_equal(t["E"].cpu().numpy(), E0)
+    assert np.array_equal(t["F"].cpu().numpy(), F0)
+    pos2 = pos + rng.normal(0, 0.02, pos.shape)
+    t["pos"].copy_(torch.from_numpy(pos2))
+    gr.launch(stream)
+    torch.cuda.synchronize()
+    g.check_device_status()
+    E2, F2, _ = g.eval_batch(off, sp, lat, pos2)
+    assert np.array_equal(t["E"].cpu().numpy(), E2)
+    assert np.array_equal(t["F"].cpu().numpy(), F2)
+    gr.close()
+
+
+def test_autotune_choice_within_tolerance(synth_si):
+    import gapgb.synth as S
+    from gapgb import tune
+    g, _ = synth_si
+    batch = [S.si64(seed=s) for s in (71, 72, 73, 74)]
+    off, sp, lat, pos = S.pack(batch)
+    best = tune.autotune(g, off, sp, lat, pos, reps=2)
+    assert best["precision"] in ("tc", "fp32", "mixed")
+    assert best["dE_per_atom"] <= 1e-3 and best["dF"] <= 20e-3
+    E, F, _ = g.eval_batch(off, sp, lat, pos)
+    g.set_precision("fp64")
+    E64, F64, _ = g.eval_batch(off, sp, lat, pos)
+    assert np.max(np.abs(E - E64)) / 64 <= 1e-3 and np.abs(F - F64).max() <= 20e-3
+    g.set_neighbour_cap(256)
+    gapgb_load = __import__("gapgb").load()
+    gapgb_load.gapgb_set_option(g.handle, 3, 0)
