@@ -44,6 +44,7 @@ SYMBOLS = [
     ("gapgb_graph_create", _I, [_P, _I, _I, _I, _P, _P, _P, _P, _I, _P, _P, _P, _P, C.POINTER(_P)]),
     ("gapgb_graph_launch", _I, [_P, _P]),
     ("gapgb_graph_free", None, [_P]),
+    ("gapgb_gpr_noalloc", _I, [_P, _I, _P, _P, _P, _P]),
     ("gapgb_stage_times", _I, [_P, _P]),
     ("gapgb_descriptors", _I, [_P, _I, _P, _P, _P, _P, _P]),
     ("gapgb_neighbors", _I, [_P, _I, _P, _P, _P, _I, _P, _P]),

@@ -180,6 +180,27 @@ void gapgb_graph_free(gapgb_graph *graph);
  * Only filled when GAPGB_PROFILE_STAGES is set in the environment. */
 gapgb_status gapgb_stage_times(gapgb_model *model, float t[4]);
 
+/* ---- GPR step without device allocation ---------------------------------- */
+
+/* Atomic energies e[natoms] and dE/dG[natoms*D] (FP64, row-major) from FP64
+ * descriptors d_G[natoms*D] already in device memory, enqueued on `stream`
+ * with no device allocation of any kind.  No counterpart in the reference:
+ * it serves callers that cannot allocate when they need the GPR - code inside
+ * a CUDA stream capture (an allocation would invalidate the capture), hosts
+ * that reserve all device memory up front in their own pool, and loops that
+ * cannot take the device-wide synchronisation an allocation may cause.
+ * Working memory is one fixed 8 MiB array in device memory per GPU, held
+ * until the process exits; calls with natoms * (D + 1) > 1048576 (16131 atoms
+ * at D = 64) return GAPGB_ERR_CAP_EXCEEDED.  The model must already be
+ * resident on the device (any evaluation uploads it; this call never does).
+ * The first call on a device looks up the array's device address, so make
+ * one call before capturing it in a graph.  All calls share the array: calls
+ * that overlap on the GPU (other streams, other host threads) race and must
+ * be serialised by the caller. */
+gapgb_status gapgb_gpr_noalloc(gapgb_model *model, int natoms,
+                               const double *d_G, double *d_e, double *d_dedg,
+                               void *stream);
+
 /* ---- descriptor export and utilities ------------------------------------ */
 
 /* wACSF descriptors XX (D per atom, the reference layout of
