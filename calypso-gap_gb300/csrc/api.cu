@@ -235,9 +235,33 @@ gapgb_status check_batch_host(int nstruct, const int *atom_off, const double *la
 }
 
 // Everything after the neighbour list, enqueued on `st`.
+// Fallback buffers of the surrogate form for N atoms (allocates; runs before
+// any capture, so a captured evaluation finds them sized).
+gapgb_status ensure_surrogate(gapgb_model *m, int N) {
+  if (!m->surrogate) return fail(GAPGB_ERR_ARG, "no surrogate attached to the model");
+  gapgb_status st = surrogate_prepare(m->surrogate, N);
+  if (st) return st;
+  if (N <= m->surr_cap) return GAPGB_OK;
+  free_dev(m->surr_std);
+  free_dev(m->fb_rows);
+  free_dev(m->fb_count);
+  free_dev(m->fb_scratch);
+  m->surr_cap = 0;
+  const int n = N + N / 8;
+  if (cudaMalloc(&m->surr_std, sizeof(float) * n) != cudaSuccess ||
+      cudaMalloc(&m->fb_rows, sizeof(int) * n) != cudaSuccess ||
+      cudaMalloc(&m->fb_count, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&m->fb_scratch, gpr_rows_scratch_bytes(n, m->host.D)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(GAPGB_ERR_ALLOC, "cudaMalloc failed for the surrogate fallback buffers");
+  }
+  m->surr_cap = n;
+  return GAPGB_OK;
+}
+
 gapgb_status enqueue_tail(gapgb_model *m, int S, int N, int cap, int capS, int lgrad,
-                          double *d_energy, double *d_force, double *d_stress, double *d_atom_e,
-                          cudaStream_t st) {
+                          const int *d_species, double *d_energy, double *d_force,
+                          double *d_stress, double *d_atom_e, cudaStream_t st) {
   Workspace &ws = m->ws;
   const bool prof = m->profile_stages;
   launch_reverse(ws, N, cap, st);
@@ -246,7 +270,15 @@ gapgb_status enqueue_tail(gapgb_model *m, int S, int N, int cap, int capS, int l
   if (fp64) launch_wacsf_fwd<double>(m, ws, N, cap, capS, st);
   else launch_wacsf_fwd<float>(m, ws, N, cap, capS, st);
   if (prof) cudaEventRecord(m->ev[2], st);
-  if (m->precision == GAPGB_PREC_TC) {
+  if (m->precision == GAPGB_PREC_SURROGATE) {
+    // committee for every atom, then the exact GPR for the atoms it flags
+    surrogate_enqueue(m->surrogate, N, d_species, (const float *)ws.G, ws.e, m->surr_std,
+                      (float *)ws.dedg, ws.d_flags, st);
+    surrogate_select_fallback(N, m->surr_std, (float)m->surr_threshold, m->fb_rows, m->fb_count,
+                              st);
+    launch_gpr_rows(m, ws, m->surr_cap, m->fb_rows, m->fb_count, m->fb_scratch, st);
+  }
+  else if (m->precision == GAPGB_PREC_TC) {
     gapgb_status s = build_tc_image(m);  // first call only (allocates)
     if (s) return s;
     launch_gpr_tc(m, ws, N, st);
@@ -271,6 +303,11 @@ gapgb_status enqueue_tail(gapgb_model *m, int S, int N, int cap, int capS, int l
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(GAPGB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
   return GAPGB_OK;
+}
+
+__global__ void k_d2f(size_t n, const double *__restrict__ a, float *__restrict__ b) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
 }
 
 gapgb_status flags_to_status(const int *f) {
@@ -336,7 +373,12 @@ gapgb_status eval_host(gapgb_model *m, int S, const int *atom_off, const int *sp
       GAPGB_CUDA_TRY(cudaStreamSynchronize(s));
       return GAPGB_OK;
     }
-    st = enqueue_tail(m, S, N, cap, capS, lgrad, ws.d_energy, ws.d_force, ws.d_stress, ws.d_atom_e, s);
+    if (m->precision == GAPGB_PREC_SURROGATE) {
+      st = ensure_surrogate(m, N);
+      if (st) return st;
+    }
+    st = enqueue_tail(m, S, N, cap, capS, lgrad, ws.d_species, ws.d_energy, ws.d_force,
+                      ws.d_stress, ws.d_atom_e, s);
     if (st) return st;
     GAPGB_CUDA_TRY(cudaMemcpyAsync(energy, ws.d_energy, sizeof(double) * S, cudaMemcpyDeviceToHost, s));
     if (force) GAPGB_CUDA_TRY(cudaMemcpyAsync(force, ws.d_force, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s));
@@ -449,6 +491,10 @@ void gapgb_model_free(gapgb_model *m) {
   free_dev(m->d_invth32);
   free_dev(m->d_coeff);
   free_dev(m->d_coeff32);
+  free_dev(m->surr_std);
+  free_dev(m->fb_rows);
+  free_dev(m->fb_count);
+  free_dev(m->fb_scratch);
   if (m->d_tc) cudaFree(m->d_tc);
   for (auto &e : m->ev)
     if (e) cudaEventDestroy(e);
@@ -494,8 +540,10 @@ gapgb_status gapgb_set_option(gapgb_model *m, gapgb_option opt, int64_t value) {
   switch (opt) {
     case GAPGB_OPT_PRECISION:
       if (value != GAPGB_PREC_FP64 && value != GAPGB_PREC_FP32 && value != GAPGB_PREC_MIXED &&
-          value != GAPGB_PREC_TC)
+          value != GAPGB_PREC_TC && value != GAPGB_PREC_SURROGATE)
         return fail(GAPGB_ERR_ARG, "unknown precision");
+      if (value == GAPGB_PREC_SURROGATE && !m->surrogate)
+        return fail(GAPGB_ERR_ARG, "attach a surrogate (gapgb_model_set_surrogate) first");
       if (value == GAPGB_PREC_TC && m->host.D > 64)
         return fail(GAPGB_ERR_CAP_EXCEEDED, "tensor-core GPR supports D <= 64");
       m->precision = (int)value;
@@ -563,6 +611,10 @@ gapgb_status gapgb_eval_batch_device(gapgb_model *m, int nstruct, int natoms, in
   GAPGB_CUDA_TRY(cudaSetDevice(m->device));
   st = ensure_ws(m, natoms, nstruct, m->cap);
   if (st) return st;
+  if (m->precision == GAPGB_PREC_SURROGATE) {
+    st = ensure_surrogate(m, natoms);
+    if (st) return st;
+  }
   Workspace &ws = m->ws;
   cudaStream_t s = (cudaStream_t)stream;
   const int cap = m->cap;
@@ -572,8 +624,8 @@ gapgb_status gapgb_eval_batch_device(gapgb_model *m, int nstruct, int natoms, in
   launch_neighbors(ws, natoms, cap, m->host.rcut, s);
   double *d_stress_use = d_stress ? d_stress : ws.d_stress;
   double *d_force_use = d_force ? d_force : ws.d_force;
-  return enqueue_tail(m, nstruct, natoms, cap, cap, lgrad, d_energy, d_force_use, d_stress_use,
-                      d_atom_energy, s);
+  return enqueue_tail(m, nstruct, natoms, cap, cap, lgrad, d_species, d_energy, d_force_use,
+                      d_stress_use, d_atom_energy, s);
 }
 
 struct gapgb_graph {
@@ -650,6 +702,65 @@ gapgb_status gapgb_check_device_status(gapgb_model *m) {
 gapgb_status gapgb_stage_times(gapgb_model *m, float t[4]) {
   if (!m || !t) return fail(GAPGB_ERR_ARG, "null argument");
   for (int q = 0; q < 4; ++q) t[q] = m->stage_ms[q];
+  return GAPGB_OK;
+}
+
+gapgb_status gapgb_model_set_surrogate(gapgb_model *m, gapgb_surrogate *s, double threshold_ev) {
+  if (!m) return fail(GAPGB_ERR_ARG, "null model");
+  if (!s) {
+    m->surrogate = nullptr;
+    if (m->precision == GAPGB_PREC_SURROGATE) m->precision = GAPGB_PREC_MIXED;
+    return GAPGB_OK;
+  }
+  if (!(threshold_ev >= 0.0)) return fail(GAPGB_ERR_ARG, "threshold must be >= 0");
+  if (surrogate_des_len(s) != m->host.D)
+    return fail(GAPGB_ERR_ARG, "surrogate des_len differs from the model's D");
+  if (surrogate_device(s) != m->device)
+    return fail(GAPGB_ERR_ARG, "surrogate and model live on different devices");
+  for (int z : m->host.species_z)
+    if (!surrogate_has_species(s, z))
+      return fail(GAPGB_ERR_UNKNOWN_SPECIES, "surrogate lacks species Z=" + std::to_string(z));
+  m->surrogate = s;
+  m->surr_threshold = threshold_ev;
+  return GAPGB_OK;
+}
+
+gapgb_status gapgb_surrogate_fallback_count(gapgb_model *m, int *count) {
+  if (!m || !count) return fail(GAPGB_ERR_ARG, "null argument");
+  *count = 0;
+  if (!m->fb_count) return GAPGB_OK;
+  GAPGB_CUDA_TRY(cudaSetDevice(m->device));
+  GAPGB_CUDA_TRY(cudaDeviceSynchronize());
+  GAPGB_CUDA_TRY(cudaMemcpy(count, m->fb_count, sizeof(int), cudaMemcpyDeviceToHost));
+  return GAPGB_OK;
+}
+
+gapgb_status gapgb_gpr_labels(gapgb_model *m, int nstruct, const int *atom_off, const int *species,
+                              const double *lat, const double *pos, float *d_G, double *d_e,
+                              float *d_dedg) {
+  if (!m || !atom_off || !species || !lat || !pos || !d_G || !d_e || !d_dedg)
+    return fail(GAPGB_ERR_ARG, "null argument");
+  if (m->precision == GAPGB_PREC_SURROGATE)
+    return fail(GAPGB_ERR_ARG, "labels come from the GPR: choose a GPR precision");
+  gapgb_status st = check_batch_host(nstruct, atom_off, lat, pos);
+  if (st) return st;
+  std::vector<double> energy(nstruct);
+  st = eval_host(m, nstruct, atom_off, species, lat, pos, 0, energy.data(), nullptr, nullptr,
+                 nullptr, nullptr);
+  if (st) return st;
+  const Workspace &ws = m->ws;
+  const size_t n = (size_t)atom_off[nstruct], nd = n * m->host.D;
+  cudaStream_t s = m->stream;
+  if (m->precision == GAPGB_PREC_FP64) {
+    k_d2f<<<(unsigned)((nd + 255) / 256), 256, 0, s>>>(nd, (const double *)ws.G, d_G);
+    k_d2f<<<(unsigned)((nd + 255) / 256), 256, 0, s>>>(nd, (const double *)ws.dedg, d_dedg);
+  } else {
+    GAPGB_CUDA_TRY(cudaMemcpyAsync(d_G, ws.G, nd * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    GAPGB_CUDA_TRY(cudaMemcpyAsync(d_dedg, ws.dedg, nd * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  }
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(d_e, ws.e, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  GAPGB_CUDA_TRY(cudaGetLastError());
+  GAPGB_CUDA_TRY(cudaStreamSynchronize(s));
   return GAPGB_OK;
 }
 

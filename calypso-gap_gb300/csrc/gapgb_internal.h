@@ -260,6 +260,14 @@ struct gapgb_model {
   bool profile_stages = false;
   float stage_ms[4] = {0, 0, 0, 0};
   gapgb::Workspace ws;
+  // learned surrogate (not owned) and its fallback buffers
+  gapgb_surrogate *surrogate = nullptr;
+  double surr_threshold = 0.005;
+  int surr_cap = 0;
+  float *surr_std = nullptr;   // committee std per atom (eV)
+  int *fb_rows = nullptr;      // atoms that take the GPR
+  int *fb_count = nullptr;
+  void *fb_scratch = nullptr;  // partial sums of the fallback GPR
 };
 
 namespace gapgb {
@@ -296,6 +304,19 @@ int gpr_nsplit(int N, int M);
 size_t gpr_scratch_bytes(int N, int M, int D, size_t elem);
 gapgb_status build_tc_image(gapgb_model *m);
 size_t tc_atom_scratch_bytes(int N);
+void launch_gpr_rows(const gapgb_model *m, Workspace &ws, int cap, const int *d_rows,
+                     const int *d_count, void *scratch, cudaStream_t st);
+size_t gpr_rows_scratch_bytes(int cap, int D);
+
+// mlp.cu (learned surrogate)
+gapgb_status surrogate_prepare(gapgb_surrogate *s, int N);
+void surrogate_enqueue(gapgb_surrogate *s, int N, const int *d_Z, const float *d_G, double *d_e,
+                       float *d_std, float *d_dedg, int *d_err, cudaStream_t st);
+void surrogate_select_fallback(int N, const float *d_std, float threshold, int *d_rows,
+                               int *d_count, cudaStream_t st);
+int surrogate_device(const gapgb_surrogate *s);
+int surrogate_des_len(const gapgb_surrogate *s);
+bool surrogate_has_species(const gapgb_surrogate *s, int z);
 
 }  // namespace gapgb
 

@@ -33,25 +33,27 @@ constexpr int kBK = 64;
 __device__ __forceinline__ double g_exp(double x) { return exp(x); }
 __device__ __forceinline__ float g_exp(float x) { return expf(x); }
 
+// One work item: atoms [i0, i0 + 64) of a list of N rows (row i is atom
+// rows[i], or atom i when rows is null) against sparse points [kbeg, kend);
+// partial results go to e_out[base + i] and dedg_out[(base + i) * D + d].
 template <typename T, typename TG, int NB>
-__global__ void __launch_bounds__(256)
-    k_gpr(int N, int M, int D, int klen, const TG *__restrict__ G, const T *__restrict__ mmt,
-          const T *__restrict__ invth, const double *__restrict__ coeff,
-          const float *__restrict__ coeff32,
-          double *__restrict__ e_out, T *__restrict__ dedg_out) {
+__device__ __forceinline__ void gpr_tile(int N, int D, int i0, int kbeg, int kend, size_t base0,
+                                         const int *__restrict__ rows, const TG *__restrict__ G,
+                                         const T *__restrict__ mmt, const T *__restrict__ invth,
+                                         const double *__restrict__ coeff,
+                                         const float *__restrict__ coeff32,
+                                         double *__restrict__ e_out, T *__restrict__ dedg_out) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int ld = D + 1;
   T *xs = reinterpret_cast<T *>(smraw);  // [kBM][D+1]
   T *ms = xs + kBM * ld;                 // [kBK][D+1]
   T *ws = ms + kBK * ld;                 // [kBM][kBK+1]
   const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
-  const int i0 = blockIdx.x * kBM;
-  const int kbeg = blockIdx.y * klen;
-  const int kend = min(M, kbeg + klen);
   for (int q = t; q < kBM * D; q += 256) {
     const int r = q / D, d = q - r * D;
     const int i = i0 + r;
-    xs[r * ld + d] = (i < N) ? (T)G[(size_t)i * D + d] * invth[d] : (T)0;
+    const size_t a = rows ? (size_t)(i < N ? rows[i] : 0) : (size_t)i;
+    xs[r * ld + d] = (i < N) ? (T)G[a * D + d] * invth[d] : (T)0;
   }
   __syncthreads();
   T xr[4][NB];
@@ -153,7 +155,7 @@ __global__ void __launch_bounds__(256)
   for (int a = 0; a < 4; ++a) {
     const int i = i0 + ty + 16 * a;
     if (i >= N) continue;
-    const size_t base = (size_t)blockIdx.y * N + i;
+    const size_t base = base0 + i;
     if (tx == 0) e_out[base] = epart[a];
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
@@ -161,6 +163,76 @@ __global__ void __launch_bounds__(256)
       if (d < D) dedg_out[base * D + d] = -acc[a][b] * invth[d];
     }
   }
+}
+
+template <typename T, typename TG, int NB>
+__global__ void __launch_bounds__(256)
+    k_gpr(int N, int M, int D, int klen, const TG *__restrict__ G, const T *__restrict__ mmt,
+          const T *__restrict__ invth, const double *__restrict__ coeff,
+          const float *__restrict__ coeff32,
+          double *__restrict__ e_out, T *__restrict__ dedg_out) {
+  const int kbeg = blockIdx.y * klen;
+  gpr_tile<T, TG, NB>(N, D, blockIdx.x * kBM, kbeg, min(M, kbeg + klen), (size_t)blockIdx.y * N,
+                      nullptr, G, mmt, invth, coeff, coeff32, e_out, dedg_out);
+}
+
+// Split of a device-counted row list over `nblocks` persistent blocks: enough
+// sparse-point splits that the (row tile, split) items fill the blocks.
+struct RowSplit {
+  int ntiles, nsp, klen;
+};
+__host__ __device__ inline RowSplit row_split(int count, int M, int nblocks) {
+  RowSplit r;
+  r.ntiles = (count + kBM - 1) / kBM;
+  const int kt = (M + kBK - 1) / kBK;
+  int ns = r.ntiles > 0 ? (nblocks + r.ntiles - 1) / r.ntiles : 1;
+  ns = ns < 1 ? 1 : (ns > kt ? kt : ns);
+  r.klen = ((kt + ns - 1) / ns) * kBK;
+  r.nsp = (M + r.klen - 1) / r.klen;
+  return r;
+}
+
+// The GPR over the atoms listed in rows[0 .. *count): persistent blocks walk
+// the (row tile, sparse split) items, so the launch shape is independent of
+// the count (CUDA-graph friendly).  Partials: split p of row i at p * count + i.
+template <typename T, typename TG, int NB>
+__global__ void __launch_bounds__(256)
+    k_gpr_rows(const int *__restrict__ count, const int *__restrict__ rows, int M, int D,
+               const TG *__restrict__ G, const T *__restrict__ mmt, const T *__restrict__ invth,
+               const double *__restrict__ coeff, const float *__restrict__ coeff32,
+               double *__restrict__ e_out, T *__restrict__ dedg_out) {
+  const int n = *count;
+  const RowSplit rs = row_split(n, M, gridDim.x);
+  for (int w = blockIdx.x; w < rs.ntiles * rs.nsp; w += gridDim.x) {
+    const int tile = w / rs.nsp, p = w - tile * rs.nsp;
+    const int kbeg = p * rs.klen;
+    __syncthreads();  // the previous item's last reads of the shared tiles
+    gpr_tile<T, TG, NB>(n, D, tile * kBM, kbeg, min(M, kbeg + rs.klen), (size_t)p * n, rows, G,
+                        mmt, invth, coeff, coeff32, e_out, dedg_out);
+  }
+}
+
+template <typename T, typename TG>
+__global__ void k_gpr_reduce_rows(int cap, int D, int M, int nblocks, const int *__restrict__ count,
+                                  const int *__restrict__ rows, const double *__restrict__ e_part,
+                                  const T *__restrict__ dedg_part, double *__restrict__ e,
+                                  TG *__restrict__ dedg) {
+  const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = *count;
+  const RowSplit rs = row_split(n, M, nblocks);
+  const size_t nd = (size_t)n * D;
+  if (tid < nd) {
+    T s = (T)0;
+    for (int p = 0; p < rs.nsp; ++p) s += dedg_part[(size_t)p * nd + tid];
+    const size_t i = tid / D;
+    dedg[(size_t)rows[i] * D + (tid - i * D)] = (TG)s;
+  }
+  if (tid < (size_t)n) {
+    double s = 0.0;
+    for (int p = 0; p < rs.nsp; ++p) s += e_part[(size_t)p * n + tid];
+    e[rows[tid]] = s;
+  }
+  (void)cap;
 }
 
 template <typename T, typename TG>
@@ -227,6 +299,45 @@ void launch_gpr(const gapgb_model *m, Workspace &ws, int N, cudaStream_t st) {
   const size_t nd = (size_t)N * D;
   k_gpr_reduce<T, TG><<<(unsigned)((nd + 255) / 256), 256, 0, st>>>(N, D, nsp, e_part, d_part,
                                                                      ws.e, (TG *)ws.dedg);
+}
+
+constexpr int kRowBlocksPerSm = 2;
+
+int gpr_rows_blocks() {
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return kRowBlocksPerSm * sms;
+}
+
+size_t gpr_rows_scratch_bytes(int cap, int D) {
+  // rows of partials: nsp * count <= max(cap, (nblocks + ntiles) * 64)
+  const size_t rows = (size_t)cap + (size_t)(gpr_rows_blocks() + 1) * kBM + (size_t)cap / kBM + kBM;
+  return rows * sizeof(double) * (size_t)(D + 1);
+}
+
+// FP64 GPR (FP32 descriptors, FP32 dE/dG out: the mixed form) of the atoms
+// d_rows[0 .. *d_count), d_count <= cap, written into ws.e / ws.dedg at
+// those atoms.  The scratch holds gpr_rows_scratch_bytes(cap, D).
+void launch_gpr_rows(const gapgb_model *m, Workspace &ws, int cap, const int *d_rows,
+                     const int *d_count, void *scratch, cudaStream_t st) {
+  const int M = m->host.M, D = m->host.D;
+  const int nb = gpr_rows_blocks();
+  const size_t smem = ((size_t)(kBM + kBK) * (D + 1) + (size_t)kBM * (kBK + 1)) * sizeof(double);
+  const size_t prow = gpr_rows_scratch_bytes(cap, D) / (sizeof(double) * (D + 1));
+  double *e_part = reinterpret_cast<double *>(scratch);
+  double *d_part = e_part + prow;
+  const float *G = (const float *)ws.G;
+  auto run = [&](auto fn) {
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    fn<<<nb, 256, smem, st>>>(d_count, d_rows, M, D, G, m->d_mmt, m->d_invth, m->d_coeff,
+                              m->d_coeff32, e_part, d_part);
+  };
+  if (D <= 64) run(k_gpr_rows<double, float, 4>);
+  else run(k_gpr_rows<double, float, 8>);
+  const size_t nd = (size_t)cap * D;
+  k_gpr_reduce_rows<double, float><<<(unsigned)((nd + 255) / 256), 256, 0, st>>>(
+      cap, D, M, nb, d_count, d_rows, e_part, d_part, ws.e, (float *)ws.dedg);
 }
 
 template void launch_gpr<double, double>(const gapgb_model *, Workspace &, int, cudaStream_t);

@@ -11,9 +11,10 @@ import numpy as np
 
 from . import build as _build
 
-PREC_FP64, PREC_FP32, PREC_TC, PREC_MIXED = 0, 1, 2, 3
+PREC_FP64, PREC_FP32, PREC_TC, PREC_MIXED, PREC_SURROGATE = 0, 1, 2, 3, 4
 OPT_PRECISION, OPT_NEIGHBOUR_CAP, OPT_DEVICE = 0, 1, 2
-PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "tc": PREC_TC, "mixed": PREC_MIXED}
+PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "tc": PREC_TC, "mixed": PREC_MIXED,
+              "surrogate": PREC_SURROGATE}
 
 STATUS = {
     0: "OK", 1: "ERR_FILE", 2: "ERR_PARSE", 3: "ERR_CAP_EXCEEDED", 4: "ERR_UNKNOWN_SPECIES",
@@ -46,6 +47,16 @@ SYMBOLS = [
     ("gapgb_graph_free", None, [_P]),
     ("gapgb_gpr_noalloc", _I, [_P, _I, _P, _P, _P, _P]),
     ("gapgb_stage_times", _I, [_P, _P]),
+    ("gapgb_surrogate_create", _I, [_I, _P, _I, _I, _I, C.c_ulonglong, C.POINTER(_P)]),
+    ("gapgb_surrogate_free", None, [_P]),
+    ("gapgb_surrogate_info", _I, [_P, _P, _P, _P, _P, _P]),
+    ("gapgb_surrogate_set_norm", _I, [_P, _P, _P, _P, _D]),
+    ("gapgb_surrogate_params", _I, [_P, _P, _P]),
+    ("gapgb_surrogate_train_step", _I, [_P, _I, _P, _P, _P, _P, C.c_float, C.c_float, _I, _P, _P]),
+    ("gapgb_surrogate_predict", _I, [_P, _I, _P, _P, _P, _P, _P, _P]),
+    ("gapgb_model_set_surrogate", _I, [_P, _P, _D]),
+    ("gapgb_surrogate_fallback_count", _I, [_P, _P]),
+    ("gapgb_gpr_labels", _I, [_P, _I, _P, _P, _P, _P, _P, _P, _P]),
     ("gapgb_descriptors", _I, [_P, _I, _P, _P, _P, _P, _P]),
     ("gapgb_neighbors", _I, [_P, _I, _P, _P, _P, _I, _P, _P]),
     ("gapgb_min_bond", _I, [_I, _P, _P, _D, _P]),
@@ -247,6 +258,20 @@ class GapModel:
                                          pos, int(lgrad), energy, force, stress,
                                          atom_energy or None, C.byref(h)), "gapgb_graph_create")
         return Graph(h, self)
+
+    def attach_surrogate(self, sur, threshold=0.005):
+        """Use a trained gapgb.surrogate.Surrogate at precision "surrogate";
+        atoms whose committee std exceeds `threshold` (eV) take the GPR."""
+        _check(load().gapgb_model_set_surrogate(self._h, sur.handle if sur is not None else None,
+                                                float(threshold)), "gapgb_model_set_surrogate")
+        self._surrogate = sur  # keeps it alive while attached
+
+    def fallback_count(self):
+        """Atoms sent to the GPR by the last surrogate evaluation."""
+        n = C.c_int()
+        _check(load().gapgb_surrogate_fallback_count(self._h, C.byref(n)),
+               "gapgb_surrogate_fallback_count")
+        return n.value
 
     def check_device_status(self):
         _check(load().gapgb_check_device_status(self._h), "gapgb_check_device_status")

@@ -11,6 +11,10 @@ workloads the evaluator is measured on:
   population  structures of 8-256 atoms, 1-4 species from {3, 8, 14, 26},
             12-20 A^3/atom, triclinic angles 60-120 deg, min distance 1.6 A
   sige      Si/Ge 50/50 diamond 16x16x16 (32768 atoms), a = 5.54 A, jitter 0.1
+  surrogate the alloy512 generator with a smooth alloy GAP (theta = 4 std):
+            the narrow theta = 0.8 std GAP is a sum of 4000 sharp bumps that a
+            64-128-128-1 network cannot represent, so the learned surrogate is
+            trained and judged on the smooth one
 
 SF set (used by all synthetic models): 20 type-1 radial functions with alpha
 log-spaced 0.003..2.0 A^-2, cutoff 6 A; 12 angular functions = zeta {1,2,4}
@@ -178,3 +182,22 @@ def species_table(zs):
     """Atomic-number weights (the wACSF weights of the synthetic models)."""
     z = np.array(sorted(set(int(v) for v in zs)), np.int32)
     return z, z.astype(np.float64)
+
+
+def alloy_model(M=4000, theta_scale=0.8, coeff_std=1e-3, seed=0, ncells=8):
+    """Arrays (species_z, species_w, sf_type, sf_alpha, sf_cutoff, sf_zeta,
+    theta, mm, coeff) of the synthetic ternary-alloy GAP: its sparse points
+    are descriptors of `ncells` seeded alloy512 cells computed by the library
+    itself (needs the GPU)."""
+    from . import GapModel
+    ty, al, rc, ze = sf_table()
+    zt = np.array([13, 28, 40], np.int32)
+    wt = zt.astype(np.float64)
+    D = 2 * len(ty)
+    probe = GapModel.create(zt, wt, ty, al, rc, np.ones(D), np.zeros((1, D)), np.zeros(1),
+                            sf_zeta=ze)
+    off, sp, lat, pos = pack([alloy512(seed=s) for s in range(ncells)])
+    X = probe.descriptors(off, sp, lat, pos)
+    probe.close()
+    theta, mm, coeff = model_arrays(X, M, theta_scale=theta_scale, coeff_std=coeff_std, seed=seed)
+    return zt, wt, ty, al, rc, ze, theta, mm, coeff

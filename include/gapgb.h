@@ -47,8 +47,12 @@ typedef enum {
   GAPGB_PREC_FP32 = 1, /* FP32 descriptors and GPR, FP64 energy/virial sums */
   GAPGB_PREC_TC = 2,   /* FP32 descriptors, tensor-core GPR (split BF16, FP32
                           accumulate), FP64 energy/virial sums */
-  GAPGB_PREC_MIXED = 3 /* FP32 descriptors and gradients, FP64 GPR (for models
+  GAPGB_PREC_MIXED = 3, /* FP32 descriptors and gradients, FP64 GPR (for models
                           whose coefficients cancel strongly) */
+  GAPGB_PREC_SURROGATE = 4 /* FP32 descriptors, the attached learned surrogate
+                              for e and dE/dG, FP64 GPR (the mixed form) for
+                              the atoms whose committee disagrees; needs
+                              gapgb_model_set_surrogate first */
 } gapgb_precision;
 
 typedef enum {
@@ -200,6 +204,90 @@ gapgb_status gapgb_stage_times(gapgb_model *model, float t[4]);
 gapgb_status gapgb_gpr_noalloc(gapgb_model *model, int natoms,
                                const double *d_G, double *d_e, double *d_dedg,
                                void *stream);
+
+/* ---- learned surrogate with GPR fallback --------------------------------- */
+
+/* No counterpart in the reference, which evaluates the GPR only.  A committee
+ * of `members` per-species networks D -> H -> H -> 1 (SiLU) maps a descriptor
+ * to an atomic energy; its input gradient replaces dE/dG, so forces and
+ * stress follow through the same chain rule.  Trained on the GAP's own
+ * atomic energies and dE/dG (per atom: forces are the fixed linear map
+ * F = -J^T dE/dG of them) with the library's own forward, backward and Adam
+ * kernels: BF16 weights and row operands, FP32 accumulation, FP32 master
+ * weights.  In an evaluation at GAPGB_PREC_SURROGATE, atoms whose committee
+ * standard deviation exceeds the threshold take the exact GPR instead. */
+typedef struct gapgb_surrogate gapgb_surrogate;
+
+/* Random initialisation from `seed` on the current CUDA device. */
+gapgb_status gapgb_surrogate_create(int nspecies, const int *species_z,
+                                    int des_len, int hidden, int members,
+                                    unsigned long long seed,
+                                    gapgb_surrogate **out);
+void gapgb_surrogate_free(gapgb_surrogate *s);
+gapgb_status gapgb_surrogate_info(const gapgb_surrogate *s, int *nspecies,
+                                  int *des_len, int *hidden, int *members,
+                                  size_t *params_per_block);
+
+/* Input standardisation (mean, std per descriptor component; components with
+ * std <= 1e-12 pass through) and the energy normalisation e = e_scale * y +
+ * e_shift[species]. */
+gapgb_status gapgb_surrogate_set_norm(gapgb_surrogate *s, const double *g_mean,
+                                      const double *g_std,
+                                      const double *e_shift, double e_scale);
+
+/* FP32 master weights, members * nspecies blocks of params_per_block floats
+ * in the order block (q * nspecies + s) = {W1[H][D], b1[H], W2[H][H], b2[H],
+ * w3[H], b3}.  `get` copies them out, `set` replaces them (and resets Adam);
+ * either may be NULL. */
+gapgb_status gapgb_surrogate_params(gapgb_surrogate *s, float *get,
+                                    const float *set);
+
+/* One training step of every (member, species) block at once.  d_rows holds
+ * members * nspecies * rows_per_species atom indices (device; block order as
+ * above, each block's rows of that species) into the label arrays: FP32
+ * descriptors d_G[n*D], atomic energies d_e[n] (eV), dE/dG d_dedg[n*D].
+ * rows_per_species is a multiple of 64.  Loss per block: mean over its rows
+ * of (y - y*)^2 + lambda |dy/dx - t*|^2 in normalised units.  With update,
+ * one Adam step (lr, beta 0.9 / 0.999, eps 1e-8).  loss (host, nullable)
+ * receives the members * nspecies block losses (this call then waits for the
+ * step); d_grad (device, nullable) the weight gradient in the params layout.
+ * The step runs on the surrogate's own stream: the caller makes d_rows and
+ * the labels complete on the device before the call. */
+gapgb_status gapgb_surrogate_train_step(gapgb_surrogate *s, int rows_per_species,
+                                        const int *d_rows, const float *d_G,
+                                        const double *d_e, const float *d_dedg,
+                                        float lambda, float lr, int update,
+                                        double *loss, float *d_grad);
+
+/* Committee prediction for natoms atoms (atomic numbers d_species, FP32
+ * descriptors d_G, device): mean atomic energy d_e (eV), committee standard
+ * deviation d_std (eV) and mean dE/dG d_dedg[natoms*D].  Waits for the
+ * stream (NULL: the surrogate's own stream). */
+gapgb_status gapgb_surrogate_predict(gapgb_surrogate *s, int natoms,
+                                     const int *d_species, const float *d_G,
+                                     double *d_e, float *d_std, float *d_dedg,
+                                     void *stream);
+
+/* Attach a surrogate (not owned; NULL detaches) and the fallback threshold
+ * on the committee standard deviation, in eV.  Its des_len must be the
+ * model's D and its species must include every species of the model.
+ * Detaching while the precision is GAPGB_PREC_SURROGATE sets it to
+ * GAPGB_PREC_MIXED. */
+gapgb_status gapgb_model_set_surrogate(gapgb_model *model, gapgb_surrogate *s,
+                                       double threshold_ev);
+
+/* Number of atoms that took the GPR fallback in the model's last
+ * GAPGB_PREC_SURROGATE evaluation (synchronises the model's device). */
+gapgb_status gapgb_surrogate_fallback_count(gapgb_model *model, int *count);
+
+/* Training labels: FP32 descriptors d_G[n*D], atomic energies d_e[n] and
+ * dE/dG d_dedg[n*D] (device) of a packed batch (host inputs as in
+ * gapgb_eval_batch), from the model's GPR at its current precision (any but
+ * GAPGB_PREC_SURROGATE). */
+gapgb_status gapgb_gpr_labels(gapgb_model *model, int nstruct,
+                              const int *atom_off, const int *species,
+                              const double *lat, const double *pos,
+                              float *d_G, double *d_e, float *d_dedg);
 
 /* ---- descriptor export and utilities ------------------------------------ */
 
