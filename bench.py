@@ -49,10 +49,18 @@ def parse():
     p.add_argument("--batch", type=int, default=64, help="structures per step per GPU")
     p.add_argument("--precision", default="tc", choices=["fp32", "tc", "fp64", "mixed"])
     p.add_argument("--no-oracle", action="store_true", help="skip the oracle error check")
-    p.add_argument("--workload", default="alloy", choices=["alloy", "population"],
+    p.add_argument("--workload", default="alloy", choices=["alloy", "population", "surrogate"],
                    help="alloy: 512-atom ternary fcc cells (the headline metric); population: "
-                        "a ragged structure-search population evaluated by one CUDA graph")
-    p.add_argument("--count", type=int, default=8192, help="population size")
+                        "a ragged structure-search population evaluated by one CUDA graph; "
+                        "surrogate: the learned surrogate with GPR fallback on held-out alloy "
+                        "cells, after training on GAP labels")
+    p.add_argument("--count", type=int, default=8192,
+                   help="population size / held-out structures of the surrogate workload")
+    p.add_argument("--train-structs", type=int, default=20000,
+                   help="surrogate workload: training structures (512 atoms each)")
+    p.add_argument("--epochs", type=int, default=4, help="surrogate workload: training epochs")
+    p.add_argument("--threshold", type=float, default=0.005,
+                   help="surrogate workload: committee std (eV) above which an atom takes the GPR")
     return p.parse_args()
 
 
@@ -379,10 +387,247 @@ def run_population(args):
     m.close()
 
 
+def _alloy_chunk(args):
+    seed0, count = args
+    import gapgb.synth as S
+    return S.pack([S.alloy512(seed=seed0 + s) for s in range(count)])
+
+
+def build_alloy_set(count, seed0, workers=None):
+    """`count` seeded alloy512 cells (seeds seed0 ..), packed, generated by a
+    spawn-started process pool."""
+    import multiprocessing as mp
+    workers = workers or max(1, min(16, len(os.sched_getaffinity(0))))
+    chunk = (count + workers - 1) // workers
+    jobs = [(seed0 + w * chunk, min(chunk, count - w * chunk)) for w in range(workers)
+            if count - w * chunk > 0]
+    with mp.get_context("spawn").Pool(len(jobs)) as pool:
+        parts = pool.map(_alloy_chunk, jobs)
+    offs, sps, lats, poss = [], [], [], []
+    base = 0
+    for off, sp, lat, pos in parts:
+        offs.append(off[:-1] + base)
+        base += int(off[-1])
+        sps.append(sp), lats.append(lat), poss.append(pos)
+    off = np.concatenate(offs + [np.array([base])]).astype(np.int32)
+    return off, np.concatenate(sps), np.concatenate(lats), np.concatenate(poss)
+
+
+def run_surrogate(args):
+    """The learned surrogate with GPR fallback (ternary alloy cells, the smooth
+    alloy GAP: M = 4000, theta = 4 std).  Labels: the tensor-core GPR path on
+    `train_structs` seeded cells; training: the library's own kernels; timed:
+    the surrogate-with-fallback evaluation of `count` held-out cells in chunks
+    of 512 cells (device buffers, CUDA events), beside the plain FP64 path and
+    the tensor-core GPR path on the same chunks.  Errors are against the FP64
+    path on every held-out atom and against the CPU oracle on two cells."""
+    train_set = build_alloy_set(args.train_structs, 1_000_000)
+    held = build_alloy_set(args.count, 9_000_000)
+    import torch
+    import gapgb
+    import gapgb.synth as S
+    import gapgb.surrogate as SU
+    dev = torch.device("cuda", 0)
+    arrays = S.alloy_model(M=M_SPARSE, theta_scale=4.0, coeff_std=1e-3, seed=0, ncells=8)
+    zt, wt, ty, al, rc, ze, theta, mm, coeff = arrays
+
+    def new_model(prec):
+        m = gapgb.GapModel.create(zt, wt, ty, al, rc, theta, mm, coeff, sf_zeta=ze)
+        m.set_neighbour_cap(96)
+        m.set_precision(prec)
+        return m
+
+    # labels and training
+    t0 = time.perf_counter()
+    lab = new_model("tc")
+    off, sp, lat, pos = train_set
+    G, e, t = SU.gpr_labels(lab, off, sp, lat, pos)
+    lab.close()
+    torch.cuda.synchronize()
+    t_label = time.perf_counter() - t0
+    Zd = torch.from_numpy(sp).to(dev)
+    sur = SU.Surrogate(zt, G.shape[1], 128, 4, seed=0)
+    SU.fit_norm(sur, G, e, Zd)
+    t0 = time.perf_counter()
+    hist = SU.train(sur, G, e, t, Zd, epochs=args.epochs, rows_per_species=1024, lam=1.0,
+                    lr=2e-3, lr_final=2e-5, seed=0)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    n_train = int(off[-1])
+    del G, e, t, Zd
+    torch.cuda.empty_cache()
+
+    # held-out evaluation in chunks of 512 cells
+    off, sp, lat, pos = held
+    Sh, Nh = len(off) - 1, int(off[-1])
+    CH = 512
+    chunks = []
+    for c0 in range(0, Sh, CH):
+        c1 = min(Sh, c0 + CH)
+        a0, a1 = int(off[c0]), int(off[c1])
+        chunks.append(dict(S=c1 - c0, N=a1 - a0, a0=a0, c0=c0,
+                           off=torch.from_numpy(off[c0:c1 + 1] - a0).to(dev),
+                           sp=torch.from_numpy(sp[a0:a1]).to(dev),
+                           lat=torch.from_numpy(np.ascontiguousarray(lat[c0:c1])).to(dev),
+                           pos=torch.from_numpy(np.ascontiguousarray(pos[a0:a1])).to(dev)))
+    nmax = max(c["N"] for c in chunks)
+    smax = max(c["S"] for c in chunks)
+    d_E = torch.zeros(smax, dtype=torch.float64, device=dev)
+    d_F = torch.zeros(nmax, 3, dtype=torch.float64, device=dev)
+    d_St = torch.zeros(smax, 6, dtype=torch.float64, device=dev)
+    d_ae = torch.zeros(nmax, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def step(m, c):
+        m.eval_batch_ptrs(c["S"], c["N"], ATOMS, c["off"].data_ptr(), c["sp"].data_ptr(),
+                          c["lat"].data_ptr(), c["pos"].data_ptr(), 1, d_E.data_ptr(),
+                          d_F.data_ptr(), d_St.data_ptr(), d_ae.data_ptr(), stream.cuda_stream)
+
+    def timed(m, cs, sampler=False):
+        for _ in range(max(3, args.warmup)):
+            step(m, cs[0])
+        torch.cuda.synchronize()
+        m.check_device_status()
+        stop, lines, th = threading.Event(), [], None
+        if sampler:
+            th = threading.Thread(target=clocks_sampler, args=(stop, lines), daemon=True)
+            th.start()
+            time.sleep(0.3)
+        evs = []
+        for c in cs:
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step(m, c)
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        if th:
+            stop.set()
+            th.join()
+        m.check_device_status()
+        ms = sum(a.elapsed_time(b) for a, b in evs)
+        return sum(c["N"] for c in cs) / (ms * 1e-3), ms, summarize_clocks(lines)
+
+    def outputs(m, cs):
+        ae, F, E = [], [], []
+        for c in cs:
+            step(m, c)
+            torch.cuda.synchronize()
+            m.check_device_status()
+            ae.append(d_ae[:c["N"]].cpu().numpy().copy())
+            F.append(d_F[:c["N"]].cpu().numpy().copy())
+            E.append(d_E[:c["S"]].cpu().numpy().copy())
+        return np.concatenate(ae), np.concatenate(F), np.concatenate(E)
+
+    m_s = new_model("mixed")
+    m_s.attach_surrogate(sur, threshold=args.threshold)
+    m_s.set_precision("surrogate")
+    value, ms_total, clocks = timed(m_s, chunks, sampler=True)
+    ae_s, F_s, E_s = [], [], []
+    nfb = 0
+    for c in chunks:
+        step(m_s, c)
+        torch.cuda.synchronize()
+        m_s.check_device_status()
+        nfb += m_s.fallback_count()
+        ae_s.append(d_ae[:c["N"]].cpu().numpy().copy())
+        F_s.append(d_F[:c["N"]].cpu().numpy().copy())
+        E_s.append(d_E[:c["S"]].cpu().numpy().copy())
+    ae_s, F_s, E_s = np.concatenate(ae_s), np.concatenate(F_s), np.concatenate(E_s)
+    # stage times of the surrogate form on one chunk
+    os.environ["GAPGB_PROFILE_STAGES"] = "1"
+    prof = new_model("mixed")
+    prof.attach_surrogate(sur, threshold=args.threshold)
+    prof.set_precision("surrogate")
+    stages = np.zeros(4)
+    for it in range(6):
+        flush.zero_()
+        step(prof, chunks[0])
+        prof.check_device_status()
+        if it >= 3:
+            stages += np.array(prof.stage_times())
+    stages /= 3
+    prof.close()
+    os.environ["GAPGB_PROFILE_STAGES"] = "0"
+    m_tc = new_model("tc")
+    tc_value, _, _ = timed(m_tc, chunks)
+    m_tc.close()
+    m_p = new_model("fp64")
+    plain_value, _, _ = timed(m_p, chunks[:2])
+    ae_p, F_p, E_p = outputs(m_p, chunks)
+    m_p.close()
+    de = ae_s - ae_p
+    dF = F_s - F_p
+    dE = (E_s - E_p) / np.diff(off)
+    # two held-out cells against the CPU oracle (FP64 restatement of the reference)
+    oracle_err = None
+    try:
+        import tempfile
+        from oracle import oracle
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from helpers import write_model_file
+        oracle.build()
+        with tempfile.TemporaryDirectory() as d:
+            om = oracle.Model(write_model_file(os.path.join(d, "gp"), zt, wt, ty, al, rc, theta,
+                                               mm, coeff, ze))
+            errs = []
+            for s in range(2):
+                a0, a1 = int(off[s]), int(off[s + 1])
+                eo, fo, _, _ = oracle.gap_calc(om, sp[a0:a1], lat[s], pos[a0:a1], 6.0, True)
+                errs.append((abs(E_s[s] - eo) / (a1 - a0), float(np.abs(F_s[a0:a1] - fo).max())))
+            oracle_err = {"dE_per_atom_max": max(x[0] for x in errs),
+                          "dF_max": max(x[1] for x in errs), "structures": 2}
+    except Exception as ex:  # the oracle is a checker; its absence does not stop the bench
+        oracle_err = {"unavailable": str(ex)[:200]}
+    # kernels per surrogate evaluation: prep x2, neighbours, reverse, descriptors,
+    # surrogate (count, segments, scatter, gather, 4 GEMMs, 2 bias, output, dsilu,
+    # committee), fallback select, row-list GPR + reduce, slot gradients,
+    # forces, orphans, structure reduce
+    launches_per_eval = 25
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
+            "steps": len(chunks), "warmup": max(3, args.warmup),
+            "ms_per_step": ms_total / len(chunks), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16/f32 surrogate + f64 GPR fallback",
+            "data": "synthetic",
+            "config": {"workload": "surrogate: %d held-out alloy512 cells" % Sh,
+                       "atoms": Nh, "step": "one chunk of %d cells" % CH,
+                       "model": "alloy GAP M=4000 theta=4 std, D=64",
+                       "network": "per-species 64-128-128-1 SiLU, 4-member committee",
+                       "threshold_eV": args.threshold,
+                       "l2": "flushed between steps (512 MB write)"},
+            "train": {"structures": args.train_structs, "atoms": n_train, "epochs": args.epochs,
+                      "rows_per_species": 1024, "label_s": t_label, "train_s": t_train,
+                      "loss_first_last": [hist[0], hist[-1]]},
+            "fallback": {"atoms": int(nfb), "fraction": nfb / Nh},
+            "errors_vs_fp64": {"e_atom_rms": float(np.sqrt(np.mean(de ** 2))),
+                               "e_atom_p999": float(np.quantile(np.abs(de), 0.999)),
+                               "e_atom_max": float(np.abs(de).max()),
+                               "F_p999": float(np.quantile(np.abs(dF), 0.999)),
+                               "E_per_atom_max": float(np.abs(dE).max()),
+                               "F_rms": float(np.sqrt(np.mean(dF ** 2))),
+                               "F_max": float(np.abs(dF).max()), "atoms": Nh},
+            "errors_vs_oracle": oracle_err,
+            "plain_fp64": {"value": plain_value, "unit": UNIT},
+            "tc_gpr": {"value": tc_value, "unit": UNIT},
+            "speedup_vs_plain": value / plain_value,
+            "stage_ms_chunk": {"neighbours": stages[0], "descriptors": stages[1],
+                               "surrogate_and_fallback": stages[2], "chain_rule": stages[3]},
+            "gpu_launches": launches_per_eval * len(chunks),
+            "clocks": clocks}
+    print(json.dumps(line), flush=True)
+    m_s.close()
+    sur.close()
+
+
 def main():
     args = parse()
     if args.workload == "population" and args.impl != "reference":
         run_population(args)
+        return
+    if args.workload == "surrogate" and args.impl != "reference":
+        run_surrogate(args)
         return
     if args.impl == "reference":
         run_reference(args)
