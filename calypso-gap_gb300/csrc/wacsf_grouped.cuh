@@ -36,7 +36,10 @@ __device__ __forceinline__ float pow_iz(float b, int iz, float *pm1) {
 }
 
 // Walks the upper triangle of P slots, screens pairs (r_jk <= rc) and calls
-// `work(j, k, rjk^2)` for every contributing pair, 32 at a time.
+// `work(j, k, rjk^2, valid)` on all 32 lanes for every batch of up to 32
+// contributing pairs (valid is false on the idle lanes of the last batch).
+// Within a batch the pairs are in enumeration order: j is non-decreasing
+// across the valid lanes, which sit below the invalid ones.
 template <typename Work>
 __device__ __forceinline__ void pair_stream(const Layout<float> &L, int P, float rc, int lane,
                                             int *qjk, float *qc2, Work work) {
@@ -70,7 +73,7 @@ __device__ __forceinline__ void pair_stream(const Layout<float> &L, int P, float
       const int jk = qjk[e];
       const float cc = qc2[e];
       __syncwarp();
-      work(jk & 0xffff, jk >> 16, cc);
+      work(jk & 0xffff, jk >> 16, cc, true);
       qh += 32;
     }
     k += 32;
@@ -79,10 +82,10 @@ __device__ __forceinline__ void pair_stream(const Layout<float> &L, int P, float
   if (qn > qh) {
     const int e = (qh + lane) & (kPairQ - 1);
     const bool have = lane < qn - qh;
-    const int jk = have ? qjk[e] : 0;
-    const float cc = have ? qc2[e] : 0.f;
+    const int jk = have ? qjk[e] : (0 | (1 << 16));
+    const float cc = have ? qc2[e] : 1.f;
     __syncwarp();
-    if (have) work(jk & 0xffff, jk >> 16, cc);
+    work(jk & 0xffff, jk >> 16, cc, have);
   }
   __syncwarp();
 }
@@ -150,7 +153,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
 #pragma unroll
       for (int c = 0; c < NC; ++c) acc[q][c] = accw[q][c] = 0.f;
     if (P > 1)
-      pair_stream(L, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2) {
+      pair_stream(L, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
+        if (!ok) return;
         const float a = L.r[j], b = L.r[k];
         const float c = sqrtf(c2);
         // costheta = (rij^2 + rik^2 - rjk^2) / (2 rij rik) (wacsf.f90:271-273)
@@ -270,7 +274,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
           UB[q][c] = s_u[warp][NAL * NC + q * NC + c];
         }
       if (P > 1)
-        pair_stream(L, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2) {
+        pair_stream(L, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
           const float a = L.r[j], b = L.r[k];
           const float c = sqrtf(c2);
           const float ia = L.ir[j], ib = L.ir[k], ic = 1.f / c;
@@ -312,12 +316,36 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
           const float S3 = F * (SP * dcdc - 2.f * SU * c) + SQ * (fa * fb * dfcc);
           const float s1 = S1 * ia, s2 = S2 * ib, s3 = S3 * ic;
           const float cx = L.dx[j] - L.dx[k], cy = L.dy[j] - L.dy[k], cz = L.dz[j] - L.dz[k];
-          atomicAdd(&L.gx[j], s1 * L.dx[j] + s3 * cx);
-          atomicAdd(&L.gy[j], s1 * L.dy[j] + s3 * cy);
-          atomicAdd(&L.gz[j], s1 * L.dz[j] + s3 * cz);
-          atomicAdd(&L.gx[k], s2 * L.dx[k] - s3 * cx);
-          atomicAdd(&L.gy[k], s2 * L.dy[k] - s3 * cy);
-          atomicAdd(&L.gz[k], s2 * L.dz[k] - s3 * cz);
+          float vx = ok ? s1 * L.dx[j] + s3 * cx : 0.f;
+          float vy = ok ? s1 * L.dy[j] + s3 * cy : 0.f;
+          float vz = ok ? s1 * L.dz[j] + s3 * cz : 0.f;
+          // slot j: the batch's pairs share few j values (enumeration order),
+          // so sum each run of equal j across lanes first (segmented scan)
+          // and let the run's last lane add it: one shared atomic per run
+          const int key = ok ? j : 0x10000 + lane;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const float tx = __shfl_up_sync(0xffffffffu, vx, o);
+            const float ty = __shfl_up_sync(0xffffffffu, vy, o);
+            const float tz = __shfl_up_sync(0xffffffffu, vz, o);
+            const int kk = __shfl_up_sync(0xffffffffu, key, o);
+            if (lane >= o && kk == key) {
+              vx += tx;
+              vy += ty;
+              vz += tz;
+            }
+          }
+          const int knext = __shfl_down_sync(0xffffffffu, key, 1);
+          if (ok && (lane == 31 || knext != key)) {
+            atomicAdd(&L.gx[j], vx);
+            atomicAdd(&L.gy[j], vy);
+            atomicAdd(&L.gz[j], vz);
+          }
+          if (ok) {
+            atomicAdd(&L.gx[k], s2 * L.dx[k] - s3 * cx);
+            atomicAdd(&L.gy[k], s2 * L.dy[k] - s3 * cy);
+            atomicAdd(&L.gz[k], s2 * L.dz[k] - s3 * cz);
+          }
         });
     }
     __syncwarp();
