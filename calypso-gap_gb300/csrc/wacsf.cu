@@ -519,6 +519,8 @@ void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
     GrpBwd gb;
     if (!m->generic_kernels && grouped_kernels(m->sft32h, &gf, &gb)) {
       cudaFuncSetAttribute(gf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(gf, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           cudaSharedmemCarveoutMaxShared);
       const int grid = warp_grid(N, smem, (const void *)gf);
       gf<<<grid, 32 * kWarpsPerBlock, smem, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
                                                    ws.apos, ws.nbr_d32, ws.nbr_w32, m->d_sft32,
@@ -543,6 +545,8 @@ void launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
     GrpBwd gb;
     if (!m->generic_kernels && grouped_kernels(m->sft32h, &gf, &gb)) {
       cudaFuncSetAttribute(gb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(gb, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           cudaSharedmemCarveoutMaxShared);
       const int grid = warp_grid(N, smem, (const void *)gb);
       gb<<<grid, 32 * kWarpsPerBlock, smem, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
                                                    ws.apos, ws.nbr_d32, ws.nbr_w32, m->d_sft32,

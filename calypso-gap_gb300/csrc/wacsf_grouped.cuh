@@ -20,6 +20,10 @@
 // deterministic round-robin schedule).
 
 constexpr int kPairQ = 64;
+// resident blocks per SM the grouped kernels are compiled for (80 registers
+// a thread); their launchers ask for the largest shared-memory carve-out so
+// that the per-warp slot tables of 6 blocks fit
+constexpr int kGrpMinBlocks = 6;
 
 // b^iz and b^(iz-1) for integer zeta >= 1 (branch-free up to 4)
 __device__ __forceinline__ float pow_iz(float b, int iz, float *pm1) {
@@ -113,7 +117,7 @@ __device__ __forceinline__ void radial_fwd(const Layout<float> &L, const SFT<flo
 }
 
 template <int NAL, int NC>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
     k_wacsf_fwd_grp(int N, int cap, int capS, const int *__restrict__ cnt,
                     const double4 *__restrict__ xyzr, const int *__restrict__ nj,
                     const double4 *__restrict__ apos, const float4 *__restrict__ d32,
@@ -200,7 +204,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
 }
 
 template <int NAL, int NC>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock, 4)
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
     k_wacsf_bwd_grp(int N, int cap, int capS, const int *__restrict__ cnt,
                     const double4 *__restrict__ xyzr, const int *__restrict__ nj,
                     const double4 *__restrict__ apos, const float4 *__restrict__ d32,
