@@ -324,23 +324,22 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
           float vy = ok ? s1 * L.dy[j] + s3 * cy : 0.f;
           float vz = ok ? s1 * L.dz[j] + s3 * cz : 0.f;
           // slot j: the batch's pairs share few j values (enumeration order),
-          // so sum each run of equal j across lanes first (segmented scan)
-          // and let the run's last lane add it: one shared atomic per run
-          const int key = ok ? j : 0x10000 + lane;
+          // so each run of equal j (contiguous lanes) is summed by a
+          // segmented scan and its last lane adds it: one atomic per run
+          const unsigned run = __match_any_sync(0xffffffffu, ok ? j : 0x10000 + lane);
+          const int first = __ffs(run) - 1, last = 31 - __clz(run);
 #pragma unroll
           for (int o = 1; o < 32; o <<= 1) {
             const float tx = __shfl_up_sync(0xffffffffu, vx, o);
             const float ty = __shfl_up_sync(0xffffffffu, vy, o);
             const float tz = __shfl_up_sync(0xffffffffu, vz, o);
-            const int kk = __shfl_up_sync(0xffffffffu, key, o);
-            if (lane >= o && kk == key) {
+            if (lane - o >= first) {
               vx += tx;
               vy += ty;
               vz += tz;
             }
           }
-          const int knext = __shfl_down_sync(0xffffffffu, key, 1);
-          if (ok && (lane == 31 || knext != key)) {
+          if (ok && lane == last) {
             atomicAdd(&L.gx[j], vx);
             atomicAdd(&L.gy[j], vy);
             atomicAdd(&L.gz[j], vz);
@@ -364,15 +363,16 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
 #pragma unroll
         for (int bb = 0; bb < 3; ++bb) W[aa * 3 + bb] += d3[aa] * g3[bb];
     }
-    double Wd[9];
+    // per-atom virial in FP32 (a sum over its own slots); the sums over
+    // atoms are FP64 (k_struct_reduce)
 #pragma unroll
-    for (int t = 0; t < 9; ++t) Wd[t] = warp_sum<double>((double)W[t]);
+    for (int t = 0; t < 9; ++t) W[t] = warp_sum<float>(W[t]);
     if (lane < 9) {
-      double v = 0;
+      float v = 0.f;
 #pragma unroll
       for (int t = 0; t < 9; ++t)
-        if (lane == t) v = Wd[t];
-      wvir[(size_t)i * 9 + lane] = v;
+        if (lane == t) v = W[t];
+      wvir[(size_t)i * 9 + lane] = (double)v;
     }
     __syncwarp();
   }
