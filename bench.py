@@ -49,16 +49,18 @@ def parse():
     p.add_argument("--batch", type=int, default=64, help="structures per step per GPU")
     p.add_argument("--precision", default="tc", choices=["fp32", "tc", "fp64", "mixed"])
     p.add_argument("--no-oracle", action="store_true", help="skip the oracle error check")
-    p.add_argument("--workload", default="alloy", choices=["alloy", "population", "surrogate"],
+    p.add_argument("--workload", default="alloy", choices=["alloy", "population", "surrogate", "md"],
                    help="alloy: 512-atom ternary fcc cells (the headline metric); population: "
                         "a ragged structure-search population evaluated by one CUDA graph; "
                         "surrogate: the learned surrogate with GPR fallback on held-out alloy "
-                        "cells, after training on GAP labels")
+                        "cells, after training on GAP labels; md: 32768-atom Si/Ge NVE "
+                        "velocity Verlet, tensor-core form against the plain FP64 path")
     p.add_argument("--count", type=int, default=8192,
                    help="population size / held-out structures of the surrogate workload")
     p.add_argument("--train-structs", type=int, default=20000,
                    help="surrogate workload: training structures (512 atoms each)")
     p.add_argument("--epochs", type=int, default=4, help="surrogate workload: training epochs")
+    p.add_argument("--md-steps", type=int, default=100, help="md workload: velocity-Verlet steps")
     p.add_argument("--threshold", type=float, default=0.005,
                    help="surrogate workload: committee std (eV) above which an atom takes the GPR")
     return p.parse_args()
@@ -621,8 +623,107 @@ def run_surrogate(args):
     sur.close()
 
 
+def run_md(args):
+    """Config 5: 32768-atom Si/Ge (50/50) diamond cell, a = 5.54 A, jitter
+    0.1 A; GAP with M = 8000 sparse points (library descriptors of a second
+    seeded cell, theta = 1 std, coeff ~ N(0, 1e-3)); Maxwell-Boltzmann
+    velocities at 600 K; NVE velocity Verlet, dt = 1 fs, neighbour rebuild
+    (skin 0.5 A) every 10 steps, each step one graph launch.  The tensor-core
+    form and the plain FP64 path run the same trajectory start; reported:
+    atom-steps/s of each, NVE energy drift, and force / stress differences on
+    identical configurations (t = 0 and the FP64 run's last step)."""
+    import torch
+    import gapgb
+    import gapgb.synth as S
+    from gapgb.md import MD, masses_of, maxwell_boltzmann
+    L = gapgb.load()
+    dev = torch.device("cuda", 0)
+    lat, pos, z = S.sige(seed=0)
+    arrays = S.model_from_cells([S.sige(seed=1)], [14, 32], 8000, theta_scale=1.0,
+                                coeff_std=1e-3, seed=0)
+    zt, wt, ty, al, rc, ze, theta, mm, coeff = arrays
+    N = len(z)
+    masses = masses_of(z)
+    vel = maxwell_boltzmann([0, N], masses, 600.0, seed=0)
+    # a dedicated stream: the MD steps and the timing events share it (a null
+    # handle would select the MD object's own stream instead)
+    stream = torch.cuda.Stream(dev)
+    res = {}
+    for prec in ("tc", "fp64"):
+        m = gapgb.GapModel.create(zt, wt, ty, al, rc, theta, mm, coeff, sf_zeta=ze)
+        m.set_precision(prec)
+        m.set_neighbour_cap(64)
+        md = MD(m, [0, N], z, lat[None], pos, vel, masses, dt=1.0, skin=0.5, rebuild_every=10)
+        E0, F0, S0, K0 = md.outputs()
+        ep = torch.zeros((args.md_steps, 1), dtype=torch.float64, device=dev)
+        ek = torch.zeros((args.md_steps, 1), dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        stop, lines, th = threading.Event(), [], None
+        if prec == "tc":
+            th = threading.Thread(target=clocks_sampler, args=(stop, lines), daemon=True)
+            th.start()
+            time.sleep(0.3)
+        a.record(stream)
+        st = L.gapgb_md_run(md.handle, args.md_steps, ep.data_ptr(), ek.data_ptr(),
+                            stream.cuda_stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        if th:
+            stop.set()
+            th.join()
+        if st != 0:
+            raise gapgb.GapError(st, "gapgb_md_run")
+        md.check()
+        ms = a.elapsed_time(b)
+        et = (ep + ek).cpu().numpy()[:, 0]
+        e_init = E0[0] + K0[0]
+        res[prec] = dict(ms=ms, value=N * args.md_steps / (ms * 1e-3), E0=E0, F0=F0, S0=S0,
+                         drift=float(np.abs(et - e_init).max() / N),
+                         drift_end=float((et[-1] - e_init) / N),
+                         final=md.positions(), out=md.outputs(), clocks=summarize_clocks(lines))
+        md.close()
+        m.close()
+    # the FP64 run's last configuration evaluated in the tensor-core form
+    m = gapgb.GapModel.create(zt, wt, ty, al, rc, theta, mm, coeff, sf_zeta=ze)
+    m.set_precision("tc")
+    Et, Ft, St = m.eval_batch([0, N], z, lat[None], res["fp64"]["final"])
+    m.close()
+    Ep, Fp, Sp, _ = res["fp64"]["out"]
+    tc, fp = res["tc"], res["fp64"]
+    line = {"metric": METRIC, "value": tc["value"], "unit": "atom-steps/s", "n_gpus": 1,
+            "steps": args.md_steps, "warmup": 0, "ms_per_step": tc["ms"] / args.md_steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16x3/f32 (tensor-core form)", "data": "synthetic",
+            "config": {"workload": "md: Si/Ge 50/50 diamond 16^3 (32768 atoms), a=5.54, jitter 0.1",
+                       "model": "M=8000, D=64, theta=1 std", "integrator":
+                       "NVE velocity Verlet dt=1 fs, 600 K MB start, rebuild every 10 (skin 0.5 A)",
+                       "step": "one CUDA graph launch"},
+            "plain_fp64": {"value": fp["value"], "unit": "atom-steps/s",
+                           "ms_per_step": fp["ms"] / args.md_steps},
+            "speedup_vs_plain": tc["value"] / fp["value"],
+            "nve_drift_per_atom_eV": {"tc_max": tc["drift"], "fp64_max": fp["drift"],
+                                      "tc_end": tc["drift_end"], "fp64_end": fp["drift_end"]},
+            "tc_vs_fp64_same_config": {
+                "t0": {"dE_per_atom": float(abs(tc["E0"][0] - fp["E0"][0]) / N),
+                       "dF_max": float(np.abs(tc["F0"] - fp["F0"]).max()),
+                       "dF_rms": float(np.sqrt(np.mean((tc["F0"] - fp["F0"]) ** 2))),
+                       "dstress_max_GPa": float(np.abs(tc["S0"] - fp["S0"]).max())},
+                "t_end": {"dE_per_atom": float(abs(Et[0] - Ep[0]) / N),
+                          "dF_max": float(np.abs(Ft - Fp).max()),
+                          "dstress_max_GPa": float(np.abs(St - Sp).max())}},
+            # per step: kick+drift, wrap or skin check, prep x2, build or refresh,
+            # reverse, descriptors, tensor-core GPR (prep + kernel), slot gradients,
+            # forces, orphans, structure reduce, kick, kinetic energy
+            "gpu_launches": 15 * args.md_steps, "clocks": tc["clocks"]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "md" and args.impl != "reference":
+        run_md(args)
+        return
     if args.workload == "population" and args.impl != "reference":
         run_population(args)
         return

@@ -316,6 +316,8 @@ gapgb_status flags_to_status(const int *f) {
   if (f[0] & kFlagNeighbourOverflow) return fail(GAPGB_ERR_NEIGHBOUR_OVERFLOW, "neighbour capacity exceeded (max count " + std::to_string(f[1]) + ")");
   if (f[0] & kFlagOrphanOverflow) return fail(GAPGB_ERR_CAP_EXCEEDED, "too many unpaired neighbour slots");
   if (f[0] & kFlagTimeout) return fail(GAPGB_ERR_TIMEOUT, "a bounded device wait gave up");
+  if (f[0] & kFlagSkinExceeded)
+    return fail(GAPGB_ERR_CAP_EXCEEDED, "an atom moved more than half the Verlet skin between rebuilds");
   return GAPGB_OK;
 }
 
@@ -393,6 +395,49 @@ gapgb_status eval_host(gapgb_model *m, int S, const int *atom_off, const int *sp
 }
 
 }  // namespace
+
+// ---- molecular dynamics support (md.cu) ------------------------------------
+
+gapgb_status md_prepare(gapgb_model *m, int N, int S) {
+  gapgb_status st = upload_model(m);
+  if (st) return st;
+  GAPGB_CUDA_TRY(cudaSetDevice(m->device));
+  st = ensure_ws(m, N, S, m->cap);
+  if (st) return st;
+  if (m->precision == GAPGB_PREC_SURROGATE) return ensure_surrogate(m, N);
+  return GAPGB_OK;
+}
+
+// One evaluation of an MD step: the neighbour list is built with cutoff
+// rcut + skin (rebuild) or refreshed from the current positions (otherwise).
+// Error bits accumulate in flags[0] across steps; the per-pass counters are
+// reset here.  Never synchronises or allocates (md_prepare sized everything).
+gapgb_status md_eval_enqueue(gapgb_model *m, int S, int N, const int *d_atom_off,
+                             const int *d_species, const double *d_lat, const double *d_pos,
+                             bool rebuild, double skin, double *d_energy, double *d_force,
+                             double *d_stress, cudaStream_t s) {
+  Workspace &ws = m->ws;
+  const double rb = m->host.rcut + skin;
+  GAPGB_CUDA_TRY(cudaMemsetAsync(ws.d_flags + 1, 0, 2 * sizeof(int), s));
+  launch_prep(m, ws, S, N, d_atom_off, d_species, d_lat, d_pos, rb, s);
+  if (rebuild) launch_neighbors(ws, N, m->cap, rb, s);
+  else launch_refresh(ws, N, m->cap, s);
+  return enqueue_tail(m, S, N, m->cap, m->cap, 1, d_species, d_energy, d_force, d_stress, nullptr,
+                      s);
+}
+
+gapgb_status md_read_flags(gapgb_model *m, int *max_count) {
+  Workspace &ws = m->ws;
+  GAPGB_CUDA_TRY(cudaMemcpy(ws.h_flags, ws.d_flags, 8 * sizeof(int), cudaMemcpyDeviceToHost));
+  if (max_count) *max_count = ws.h_flags[1];
+  return flags_to_status(ws.h_flags);
+}
+
+gapgb_status md_clear_flags(gapgb_model *m) {
+  GAPGB_CUDA_TRY(cudaMemset(m->ws.d_flags, 0, 8 * sizeof(int)));
+  return GAPGB_OK;
+}
+
 }  // namespace gapgb
 
 using namespace gapgb;

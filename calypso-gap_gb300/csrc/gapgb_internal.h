@@ -44,6 +44,7 @@ enum : int {
   kFlagImageLimit = 4,
   kFlagOrphanOverflow = 8,
   kFlagTimeout = 16,
+  kFlagSkinExceeded = 32,  // MD: an atom moved more than half the skin since the last rebuild
 };
 
 // Symmetry-function table as the kernels read it.  Angular SFs are grouped by
@@ -285,6 +286,7 @@ void launch_prep(const gapgb_model *m, Workspace &ws, int S, int N, const int *d
                  double rcut, cudaStream_t st);
 void launch_neighbors(Workspace &ws, int N, int cap, double rcut, cudaStream_t st);
 void launch_reverse(Workspace &ws, int N, int cap, cudaStream_t st);
+void launch_refresh(Workspace &ws, int N, int cap, cudaStream_t st);
 template <typename T>
 void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int cap_smem,
                       cudaStream_t st);
@@ -307,6 +309,15 @@ size_t tc_atom_scratch_bytes(int N);
 void launch_gpr_rows(const gapgb_model *m, Workspace &ws, int cap, const int *d_rows,
                      const int *d_count, void *scratch, cudaStream_t st);
 size_t gpr_rows_scratch_bytes(int cap, int D);
+
+// api.cu, for md.cu
+gapgb_status md_prepare(gapgb_model *m, int N, int S);
+gapgb_status md_eval_enqueue(gapgb_model *m, int S, int N, const int *d_atom_off,
+                             const int *d_species, const double *d_lat, const double *d_pos,
+                             bool rebuild, double skin, double *d_energy, double *d_force,
+                             double *d_stress, cudaStream_t s);
+gapgb_status md_read_flags(gapgb_model *m, int *max_count);
+gapgb_status md_clear_flags(gapgb_model *m);
 
 // mlp.cu (learned surrogate)
 gapgb_status surrogate_prepare(gapgb_surrogate *s, int N);

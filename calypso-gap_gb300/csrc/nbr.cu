@@ -14,6 +14,7 @@
 // reference's statement order), appending hits with a ballot prefix.  The
 // kept set, its order and every stored distance are bit-identical to the loop
 // above.
+#include <algorithm>
 #include <cfloat>
 
 #include "gapgb_internal.h"
@@ -363,6 +364,39 @@ __global__ void k_nbr_reverse(int N, int cap, const int *__restrict__ cnt,
   }
 }
 
+// Verlet-list refresh: the slots of a list built with a larger cutoff keep
+// their (partner, image shift); their image positions, distances and FP32
+// records are recomputed from the current positions with the build's exact
+// formula.  Slots now beyond an SF cutoff contribute exactly zero in every
+// descriptor kernel, so the result equals a fresh build's up to summation
+// order.  One thread per slot.
+__global__ void k_nbr_refresh(int N, int cap, const int *__restrict__ cnt,
+                              const int *__restrict__ nj, const int *__restrict__ ns,
+                              const double4 *__restrict__ apos,
+                              const int *__restrict__ atom_struct,
+                              const StructInfo *__restrict__ sinfo, double4 *__restrict__ xyzr,
+                              float4 *__restrict__ d32) {
+  __shared__ double s_dn[2 * kMaxImage + 1];
+  for (int t = threadIdx.x; t < 2 * kMaxImage + 1; t += blockDim.x) s_dn[t] = (double)(t - kMaxImage);
+  __syncthreads();
+  const size_t total = (size_t)N * cap;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / cap), q = (int)(idx - (size_t)i * cap);
+    if (q >= cnt[i]) continue;
+    const int j = nj[idx], sh = ns[idx];
+    const int n1 = ((sh >> 16) & 255) - 128, n2 = ((sh >> 8) & 255) - 128, n3 = (sh & 255) - 128;
+    const double4 pi = apos[i];
+    const double *L = sinfo[atom_struct[i]].lat;
+    double xyz[3];
+    const double dis = ref_image(pi, apos[j], L, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
+                                 s_dn[n3 + kMaxImage], xyz);
+    xyzr[idx] = make_double4(xyz[0], xyz[1], xyz[2], dis);
+    d32[idx] = make_float4(d2f_rn(xyz[0] - pi.x), d2f_rn(xyz[1] - pi.y), d2f_rn(xyz[2] - pi.z),
+                           d2f_rn(dis));
+  }
+}
+
 // FGET_BOND (gappy/libgap/get_bond.f90:47-78): minimum over all kept images.
 __global__ void __launch_bounds__(128) k_min_bond(int N, double rcut,
                                                   const double4 *__restrict__ apos,
@@ -425,6 +459,17 @@ void launch_neighbors(Workspace &ws, int N, int cap, double rcut, cudaStream_t s
   k_nbr_build<<<grid_for_warps(N), 32 * kWarpsPerBlock, 0, st>>>(
       N, cap, rcut, ws.apos, ws.frac32, ws.atom_struct, ws.sinfo, ws.nbr_cnt, ws.nbr_xyz,
       ws.nbr_j, ws.nbr_s, ws.nbr_d32, ws.nbr_w32, ws.d_flags);
+}
+
+void launch_refresh(Workspace &ws, int N, int cap, cudaStream_t st) {
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t total = (size_t)N * cap;
+  const size_t want = (total + 255) / 256;
+  const int grid = (int)std::min<size_t>(want > 0 ? want : 1, (size_t)sms * 8);
+  k_nbr_refresh<<<grid, 256, 0, st>>>(N, cap, ws.nbr_cnt, ws.nbr_j, ws.nbr_s, ws.apos,
+                                      ws.atom_struct, ws.sinfo, ws.nbr_xyz, ws.nbr_d32);
 }
 
 void launch_reverse(Workspace &ws, int N, int cap, cudaStream_t st) {

@@ -57,6 +57,11 @@ SYMBOLS = [
     ("gapgb_model_set_surrogate", _I, [_P, _P, _D]),
     ("gapgb_surrogate_fallback_count", _I, [_P, _P]),
     ("gapgb_gpr_labels", _I, [_P, _I, _P, _P, _P, _P, _P, _P, _P]),
+    ("gapgb_md_create", _I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _D, _D, _I, C.POINTER(_P)]),
+    ("gapgb_md_run", _I, [_P, _I, _P, _P, _P]),
+    ("gapgb_md_outputs", _I, [_P, _P, _P, _P, _P]),
+    ("gapgb_md_check", _I, [_P]),
+    ("gapgb_md_free", None, [_P]),
     ("gapgb_descriptors", _I, [_P, _I, _P, _P, _P, _P, _P]),
     ("gapgb_neighbors", _I, [_P, _I, _P, _P, _P, _I, _P, _P]),
     ("gapgb_min_bond", _I, [_I, _P, _P, _D, _P]),

@@ -201,3 +201,20 @@ def alloy_model(M=4000, theta_scale=0.8, coeff_std=1e-3, seed=0, ncells=8):
     probe.close()
     theta, mm, coeff = model_arrays(X, M, theta_scale=theta_scale, coeff_std=coeff_std, seed=seed)
     return zt, wt, ty, al, rc, ze, theta, mm, coeff
+
+
+def model_from_cells(cells, species_z, M, theta_scale=1.0, coeff_std=1e-3, seed=0):
+    """Arrays of a synthetic GAP (atomic-number weights, the standard SF set)
+    whose M sparse points are library descriptors of `cells` (needs the GPU)."""
+    from . import GapModel
+    ty, al, rc, ze = sf_table()
+    zt = np.asarray(species_z, np.int32)
+    wt = zt.astype(np.float64)
+    D = 2 * len(ty)
+    probe = GapModel.create(zt, wt, ty, al, rc, np.ones(D), np.zeros((1, D)), np.zeros(1),
+                            sf_zeta=ze)
+    off, sp, lat, pos = pack(cells)
+    X = probe.descriptors(off, sp, lat, pos)
+    probe.close()
+    theta, mm, coeff = model_arrays(X, M, theta_scale=theta_scale, coeff_std=coeff_std, seed=seed)
+    return zt, wt, ty, al, rc, ze, theta, mm, coeff

@@ -289,6 +289,43 @@ gapgb_status gapgb_gpr_labels(gapgb_model *model, int nstruct,
                               const double *lat, const double *pos,
                               float *d_G, double *d_e, float *d_dedg);
 
+/* ---- molecular dynamics --------------------------------------------------- */
+
+/* NVE velocity-Verlet MD of a packed batch of fixed cells on the device.  No
+ * counterpart in the reference's hot path: gappy runs MD through ASE with
+ * one FGAP_CALC per step (gappy/example/ASE-GAPPY/run_md.py:10-27).  Units:
+ * Angstrom, fs, amu (d_mass[natoms]), eV; d_pos[natoms*3] and d_vel[natoms*3]
+ * (Angstrom/fs) are device arrays the object advances in place.  The
+ * neighbour list is built with cutoff rcut + skin every rebuild_every steps
+ * (atoms wrapped into their cells first) and refreshed from the current
+ * positions in between; slots beyond the cutoff contribute exactly zero, so
+ * a refreshed step equals a fresh build up to summation order.  An atom that
+ * moves more than skin/2 between rebuilds is reported by gapgb_md_check.
+ * Each step is one CUDA graph launch.  gapgb_md_create evaluates the forces
+ * at t = 0 (growing the neighbour capacity with 25 % headroom) and captures
+ * the two step graphs; the model is dedicated to the MD object while it
+ * lives (its workspace holds the list) and must not be reconfigured. */
+typedef struct gapgb_md gapgb_md;
+gapgb_status gapgb_md_create(gapgb_model *model, int nstruct, int natoms,
+                             const int *d_atom_off, const int *d_species,
+                             const double *d_lat, double *d_pos, double *d_vel,
+                             const double *d_mass, double dt_fs, double skin,
+                             int rebuild_every, gapgb_md **out);
+/* nsteps steps on `stream` (NULL: the object's stream); per step, the
+ * potential energy of each structure is appended to d_epot[k*nstruct + s]
+ * and the kinetic energy to d_ekin (device, either may be NULL). */
+gapgb_status gapgb_md_run(gapgb_md *md, int nsteps, double *d_epot,
+                          double *d_ekin, void *stream);
+/* Device pointers of the latest step's energy[nstruct], force[natoms*3],
+ * stress[nstruct*6] (GPa, reference order) and kinetic energy[nstruct]. */
+gapgb_status gapgb_md_outputs(const gapgb_md *md, const double **d_energy,
+                              const double **d_force, const double **d_stress,
+                              const double **d_ekin);
+/* Synchronises and reports the device flags raised since the last check
+ * (neighbour overflow, skin exceeded, unknown species). */
+gapgb_status gapgb_md_check(gapgb_md *md);
+void gapgb_md_free(gapgb_md *md);
+
 /* ---- descriptor export and utilities ------------------------------------ */
 
 /* wACSF descriptors XX (D per atom, the reference layout of
