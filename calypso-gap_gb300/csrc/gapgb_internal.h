@@ -18,6 +18,7 @@
 //   wvir[N*9]        per-atom virial sum_q (p_q - r_i)_a gslot_q,b (double)
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -326,6 +327,17 @@ void surrogate_enqueue(gapgb_surrogate *s, int N, const int *d_Z, const float *d
 void surrogate_select_fallback(int N, const float *d_std, float threshold, int *d_rows,
                                int *d_count, cudaStream_t st);
 int surrogate_device(const gapgb_surrogate *s);
+// mlp_tc.cu (surrogate inference on the tensor cores)
+bool mlp_tc_eligible(int D, int H);
+size_t mlp_tc_w_image_bytes(int nblk);
+size_t mlp_tc_x_image_bytes(int Mpad);
+void launch_mlp_w_image(int nblk, int D, size_t P, size_t offW1, size_t offW2,
+                        const __nv_bfloat16 *w16, unsigned char *img, cudaStream_t st);
+void launch_mlp_tc(int members, int nsp, int D, int Mpad, size_t P, size_t offb1, size_t offb2,
+                   size_t offw3, size_t offb3, const float *w, const unsigned char *wimg,
+                   unsigned char *ximg, const int *idx, const float *G, const float *mu,
+                   const float *isig, const int *tile_sp64, float *y, float *gx, int *flags,
+                   cudaStream_t st);
 int surrogate_des_len(const gapgb_surrogate *s);
 bool surrogate_has_species(const gapgb_surrogate *s, int z);
 

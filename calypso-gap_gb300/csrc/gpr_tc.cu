@@ -33,9 +33,12 @@
 #include <cstring>
 
 #include "gapgb_internal.h"
+#include "tc_util.cuh"
 
 namespace gapgb {
 namespace {
+
+using namespace tc;
 
 constexpr int kRows = 128;   // atoms per CTA (UMMA M)
 constexpr int kTileK = 128;  // sparse points per tile (GEMM1 N, GEMM2 K)
@@ -45,7 +48,6 @@ constexpr int kWBytes = kRows * kTileK * 2;          // 128 x 128 bf16: 32 KB
 // per sparse tile image: mh, ml (128 x 64), mhT, mlT (64 x 128), mn[128], c[128]
 constexpr int kImgTile = 4 * kTileBytes16 + 2 * kTileK * 4;  // 66 KB
 constexpr int kImgAtoms = 2 * kTileBytes16;                   // xh, xl per 128 atoms
-constexpr long kSpinLimit = 1L << 26;
 
 // shared memory map (bytes from the 1024-aligned base)
 constexpr int kOffXh = 0;
@@ -61,104 +63,6 @@ constexpr int kOffWh = kOffImg + kImgTile;
 constexpr int kOffWl = kOffWh + kWBytes;
 constexpr int kOffBar = kOffWl + kWBytes;                 // 3 mbarriers + tmem base
 constexpr int kSmemBytes = kOffBar + 64 + 1024;           // + alignment slack
-
-// byte offset of element (r, k) of a K-major no-swizzle bf16 tile with
-// `kcores` K-cores per 8-row group
-__host__ __device__ __forceinline__ int kmajor_off(int r, int k, int kcores) {
-  return (r & 7) * 16 + (r >> 3) * (kcores * 128) + (k & 7) * 2 + (k >> 3) * 128;
-}
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-// tcgen05 shared-memory matrix descriptor: no swizzle, version 1
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr >> 4) & 0x3FFF);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
-  d |= (uint64_t)1 << 46;
-  return d;
-}
-
-// instruction descriptor, kind::f16: BF16 x BF16 -> F32, both K-major
-__host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
-         ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// bounded wait: false (and the error flag) if the phase never completes
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *flags) {
-  for (long it = 0; it < kSpinLimit; ++it)
-    if (mbar_try_wait(bar, parity)) return true;
-  atomicOr(flags, kFlagTimeout);
-  return false;
-}
-
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes,
-                                         uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          dst),
-      "l"(src), "r"(bytes), "r"(bar)
-      : "memory");
-}
-
-__device__ __forceinline__ void umma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                     uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-}
-
-__device__ __forceinline__ void umma_commit(uint32_t bar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-      : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
-      "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
-}
-
-__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
-  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-  return *reinterpret_cast<const uint32_t *>(&h);
-}
 
 __global__ void __launch_bounds__(128, 1)
     k_gpr_tc(int N, int ntiles, const unsigned char *__restrict__ img_model,

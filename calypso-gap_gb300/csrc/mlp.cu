@@ -54,7 +54,8 @@
 namespace gapgb {
 namespace {
 
-constexpr int kTile = 64;      // rows per GEMM tile and species-segment padding
+constexpr int kTile = 64;      // rows per SIMT GEMM tile
+constexpr int kSeg = 128;      // species segments are padded to the tensor-core tile
 constexpr int kMaxSurrSpecies = 16;
 
 __device__ __forceinline__ float ldf(const float *p, size_t i) { return p[i]; }
@@ -340,7 +341,7 @@ __global__ void k_mlp_segments(int nsp, int ntiles, const int *__restrict__ cnt,
   __shared__ int off[kMaxSurrSpecies + 1];
   if (threadIdx.x == 0) {
     off[0] = 0;
-    for (int s = 0; s < nsp; ++s) off[s + 1] = off[s] + (cnt[s] + kTile - 1) / kTile * kTile;
+    for (int s = 0; s < nsp; ++s) off[s + 1] = off[s] + (cnt[s] + kSeg - 1) / kSeg * kSeg;
     for (int s = 0; s <= nsp; ++s) seg[s] = off[s];
   }
   __syncthreads();
@@ -435,6 +436,8 @@ struct gapgb_surrogate {
   double *lrows = nullptr;
   // prediction partition (sized for `cap_atoms`)
   int cap_atoms = 0, cap_tiles = 0;
+  unsigned char *w_img = nullptr;  // tensor-core weight images
+  unsigned char *x_img = nullptr;  // tensor-core row tiles (cap_tiles * 64 rows)
   int *p_cnt = nullptr, *p_sp = nullptr, *p_slot = nullptr, *p_seg = nullptr, *p_tile = nullptr,
       *p_err = nullptr;
   cudaStream_t stream = nullptr;
@@ -494,7 +497,10 @@ gapgb_status ensure_rows(gapgb_surrogate *s, size_t rows) {
   return GAPGB_OK;
 }
 
-int pad_tiles(int N, int nsp) { return (N + nsp * (kTile - 1) + kTile - 1) / kTile; }
+// 64-row tiles of the species-sorted rows (segments padded to 128 rows)
+int pad_tiles(int N, int nsp) {
+  return (N + nsp * (kSeg - 1) + kSeg - 1) / kSeg * (kSeg / kTile);
+}
 
 gapgb_status ensure_atoms(gapgb_surrogate *s, int N) {
   const int tiles = pad_tiles(N, s->nsp);
@@ -502,10 +508,14 @@ gapgb_status ensure_atoms(gapgb_surrogate *s, int N) {
   int *ps[] = {s->p_cnt, s->p_sp, s->p_slot, s->p_seg, s->p_tile, s->p_err};
   for (int *p : ps)
     if (p) cudaFree(p);
+  if (s->x_img) cudaFree(s->x_img);
   s->p_cnt = s->p_sp = s->p_slot = s->p_seg = s->p_tile = s->p_err = nullptr;
+  s->x_img = nullptr;
   s->cap_atoms = s->cap_tiles = 0;
+  const bool tcx = mlp_tc_eligible(s->D, s->H);
   if (!(dalloc(&s->p_cnt, kMaxSurrSpecies) && dalloc(&s->p_sp, N) && dalloc(&s->p_slot, N) &&
-        dalloc(&s->p_seg, kMaxSurrSpecies + 1) && dalloc(&s->p_tile, tiles) && dalloc(&s->p_err, 1))) {
+        dalloc(&s->p_seg, kMaxSurrSpecies + 1) && dalloc(&s->p_tile, tiles) && dalloc(&s->p_err, 1) &&
+        (!tcx || dalloc(&s->x_img, mlp_tc_x_image_bytes(tiles * kTile))))) {
     cudaGetLastError();
     return sfail(GAPGB_ERR_ALLOC, "surrogate partition buffers");
   }
@@ -545,6 +555,11 @@ namespace gapgb {
 gapgb_status surrogate_prepare(gapgb_surrogate *s, int N) {
   gapgb_status st = ensure_atoms(s, N);
   if (st) return st;
+  if (mlp_tc_eligible(s->D, s->H) && !s->w_img &&
+      !dalloc(&s->w_img, mlp_tc_w_image_bytes(s->members * s->nsp))) {
+    cudaGetLastError();
+    return sfail(GAPGB_ERR_ALLOC, "surrogate weight images");
+  }
   return ensure_rows(s, (size_t)s->cap_tiles * kTile * s->members);
 }
 
@@ -560,8 +575,18 @@ void surrogate_enqueue(gapgb_surrogate *s, int N, const int *d_Z, const float *d
   k_mlp_count<<<nblk(N), 256, 0, st>>>(N, d_Z, s->nsp, s->zt, s->p_cnt, s->p_sp, s->p_slot);
   k_mlp_segments<<<1, 256, 0, st>>>(s->nsp, tiles, s->p_cnt, s->p_seg, s->p_tile);
   k_mlp_scatter<<<nblk(N), 256, 0, st>>>(N, s->p_sp, s->p_slot, s->p_seg, s->idx, d_err);
-  k_mlp_gather<<<nblk((size_t)Mpad * s->D), 256, 0, st>>>(Mpad, s->D, s->idx, d_G, s->mu, s->isig, s->X);
-  forward(s, st, Mpad, s->p_tile, 0, true);
+  if (mlp_tc_eligible(s->D, s->H)) {
+    // tensor cores: BF16 weight images from the current weights, then the
+    // fused forward + input gradient of every member
+    launch_mlp_w_image(s->members * s->nsp, s->D, s->P, s->W1, s->W2, s->w16, s->w_img, st);
+    launch_mlp_tc(s->members, s->nsp, s->D, Mpad, s->P, s->b1, s->b2, s->w3, s->b3, s->w,
+                  s->w_img, s->x_img, s->idx, d_G, s->mu, s->isig, s->p_tile, s->y, s->Gx, d_err,
+                  st);
+  } else {
+    k_mlp_gather<<<nblk((size_t)Mpad * s->D), 256, 0, st>>>(Mpad, s->D, s->idx, d_G, s->mu,
+                                                          s->isig, s->X);
+    forward(s, st, Mpad, s->p_tile, 0, true);
+  }
   k_mlp_committee<<<nblk((size_t)Mpad * 32), 256, 0, st>>>(Mpad, s->D, s->members, s->idx, s->p_tile,
                                                           s->y, s->Gx, s->isig, s->e_shift,
                                                           s->e_scale, d_e, d_std, d_dedg);
@@ -653,7 +678,8 @@ void gapgb_surrogate_free(gapgb_surrogate *s) {
   if (!s) return;
   free_rows(s);
   void *ps[] = {s->w, s->m, s->v, s->grad, s->w16, s->mu, s->isig, s->sd, s->e_shift, s->zt,
-                s->t_tile_sp, s->p_cnt, s->p_sp, s->p_slot, s->p_seg, s->p_tile, s->p_err};
+                s->t_tile_sp, s->p_cnt, s->p_sp, s->p_slot, s->p_seg, s->p_tile, s->p_err,
+                s->w_img, s->x_img};
   for (void *p : ps)
     if (p) cudaFree(p);
   if (s->stream) cudaStreamDestroy(s->stream);

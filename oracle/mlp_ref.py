@@ -68,9 +68,12 @@ def d2silu(z):
     return s * (1.0 - s) * (2.0 + z * (1.0 - 2.0 * s))
 
 
-def forward(p, x, D, H, emulate_bf16=False):
-    """y[B] and g = dy/dx [B, D] for standardised inputs x [B, D]."""
+def forward(p, x, D, H, emulate_bf16=False, tc=False):
+    """y[B] and g = dy/dx [B, D] for standardised inputs x [B, D].  tc adds
+    the rounding points of the tensor-core inference kernel (d2 and d1 are
+    BF16 GEMM operands there, FP32 in the SIMT kernels)."""
     r = bf16 if emulate_bf16 else _id
+    rt = r if tc else _id
     W1, b1, W2, b2, w3, b3 = unpack(p, D, H)
     W1h, W2h = r(W1), r(W2)
     x = r(x)
@@ -79,8 +82,8 @@ def forward(p, x, D, H, emulate_bf16=False):
     z2 = a1 @ W2h.T + b2
     y = silu(z2) @ w3 + b3
     d2 = w3 * dsilu(z2)
-    d1 = dsilu(z1) * (d2 @ W2h)
-    g = d1 @ W1h
+    d1 = dsilu(z1) * (rt(d2) @ W2h)
+    g = rt(d1) @ W1h
     return dict(x=x, z1=z1, a1=a1, z2=z2, y=y, d2=d2, d1=d1, g=g, W1h=W1h, W2h=W2h, w3=w3)
 
 
@@ -134,12 +137,12 @@ def numeric_grad(p, x, y_lab, t_lab, lam, D, H, h=1e-6):
     return out
 
 
-def committee(blocks, x, D, H, e_scale, e_shift, sd, emulate_bf16=False):
+def committee(blocks, x, D, H, e_scale, e_shift, sd, emulate_bf16=False, tc=False):
     """Committee mean energy (eV), std (eV, ddof 1) and mean dE/dG for the
     rows x of one species, from that species' parameter blocks."""
     ys, gs = [], []
     for p in blocks:
-        f = forward(p, x, D, H, emulate_bf16)
+        f = forward(p, x, D, H, emulate_bf16, tc)
         ys.append(f["y"])
         gs.append(f["g"])
     ys = np.array(ys)

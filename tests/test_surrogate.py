@@ -172,8 +172,9 @@ def test_predict_matches_cpu_oracle(gapgb_mod):
     for k, z in enumerate(species):
         sel = np.nonzero(Z == z)[0]
         x = _std_x(G[sel], mean, std)
+        # D <= 64 and H = 128: prediction runs on the tensor cores
         e_r, s_r, g_r = MR.committee([w[q, k] for q in range(Q)], x, D, H, scale, shift[k],
-                                     1.0 / isig32.astype(np.float64), emulate_bf16=True)
+                                     1.0 / isig32.astype(np.float64), emulate_bf16=True, tc=True)
         assert np.abs(e_g[sel] - e_r).max() <= PRED_ABS * scale
         assert np.abs(s_g[sel] - s_r).max() <= PRED_ABS * scale
         # gradients compared in normalised units (dy/dx)
