@@ -331,10 +331,10 @@ int surrogate_device(const gapgb_surrogate *s);
 bool mlp_tc_eligible(int D, int H);
 size_t mlp_tc_w_image_bytes(int nblk);
 size_t mlp_tc_x_image_bytes(int Mpad);
-void launch_mlp_w_image(int nblk, int D, size_t P, size_t offW1, size_t offW2,
-                        const __nv_bfloat16 *w16, unsigned char *img, cudaStream_t st);
-void launch_mlp_tc(int members, int nsp, int D, int Mpad, size_t P, size_t offb1, size_t offb2,
-                   size_t offw3, size_t offb3, const float *w, const unsigned char *wimg,
+void launch_mlp_w_image(int nblk, int D, size_t P, size_t offW1, size_t offW2, size_t offb1,
+                        size_t offb2, size_t offw3, size_t offb3, const __nv_bfloat16 *w16,
+                        const float *w32, unsigned char *img, cudaStream_t st);
+void launch_mlp_tc(int members, int nsp, int D, int Mpad, const unsigned char *wimg,
                    unsigned char *ximg, const int *idx, const float *G, const float *mu,
                    const float *isig, const int *tile_sp64, float *y, float *gx, int *flags,
                    cudaStream_t st);

@@ -578,10 +578,10 @@ void surrogate_enqueue(gapgb_surrogate *s, int N, const int *d_Z, const float *d
   if (mlp_tc_eligible(s->D, s->H)) {
     // tensor cores: BF16 weight images from the current weights, then the
     // fused forward + input gradient of every member
-    launch_mlp_w_image(s->members * s->nsp, s->D, s->P, s->W1, s->W2, s->w16, s->w_img, st);
-    launch_mlp_tc(s->members, s->nsp, s->D, Mpad, s->P, s->b1, s->b2, s->w3, s->b3, s->w,
-                  s->w_img, s->x_img, s->idx, d_G, s->mu, s->isig, s->p_tile, s->y, s->Gx, d_err,
-                  st);
+    launch_mlp_w_image(s->members * s->nsp, s->D, s->P, s->W1, s->W2, s->b1, s->b2, s->w3,
+                       s->b3, s->w16, s->w, s->w_img, st);
+    launch_mlp_tc(s->members, s->nsp, s->D, Mpad, s->w_img, s->x_img, s->idx, d_G, s->mu,
+                  s->isig, s->p_tile, s->y, s->Gx, d_err, st);
   } else {
     k_mlp_gather<<<nblk((size_t)Mpad * s->D), 256, 0, st>>>(Mpad, s->D, s->idx, d_G, s->mu,
                                                           s->isig, s->X);

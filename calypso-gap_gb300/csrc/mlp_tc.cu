@@ -15,6 +15,9 @@
 //   epi 3  d1 = silu'(z1 + b1) o U -> BF16
 //   GEMM4  G = d1 W1            (B = W1^T image, M 128, N 64, K 128)
 //   epi 4  y and dy/dx rows to global memory (member-major, as mlp.cu)
+// Eight warps: warps w and w + 4 read the same TMEM lanes (rows) and split
+// the columns; b1, b2, w3, b3 travel in the weight image; the next tile's X
+// is prefetched into a second buffer while the current tile is processed.
 // The operands d2 and d1 are BF16 here (FP32 in the SIMT forward of
 // mlp.cu): 2^-9 relative rounding of each element, far below the network's
 // own error.  One thread issues the MMAs; every mbarrier wait is bounded
@@ -35,33 +38,43 @@ using namespace tc;
 constexpr int kR = 128;   // rows per tile (UMMA M)
 constexpr int kDp = 64;   // padded descriptor length
 constexpr int kHid = 128; // hidden units
+constexpr int kThreads = 256;  // 8 warps: warps w and w + 4 share TMEM lanes, split columns
 constexpr int kXBytes = kR * kDp * 2;        // 16 KB
 constexpr int kW1Bytes = kHid * kDp * 2;     // 16 KB
 constexpr int kW2Bytes = kHid * kHid * 2;    // 32 KB
-constexpr int kWImg = 2 * kW1Bytes + 2 * kW2Bytes;  // W1, W2, W2T, W1T: 96 KB
+constexpr int kVecBytes = (3 * kHid + 4) * 4;                   // b1, b2, w3, b3 (FP32)
+constexpr int kWImg = 2 * kW1Bytes + 2 * kW2Bytes + kVecBytes;  // one (member, species) image
+constexpr int kOffVec = 2 * kW1Bytes + 2 * kW2Bytes;            // within the image
 // shared memory map (from the 1024-aligned base)
-constexpr int kOffX = 0;
-constexpr int kOffW1 = kOffX + kXBytes;
+constexpr int kOffX0 = 0;                    // X tiles, double-buffered
+constexpr int kOffX1 = kOffX0 + kXBytes;
+constexpr int kOffW1 = kOffX1 + kXBytes;     // weight image: W1, W2, W2T, W1T, vectors
 constexpr int kOffW2 = kOffW1 + kW1Bytes;
 constexpr int kOffW2T = kOffW2 + kW2Bytes;
 constexpr int kOffW1T = kOffW2T + kW2Bytes;
-constexpr int kOffA = kOffW1T + kW1Bytes;     // a1, then d1 (128 x 128)
-constexpr int kOffDd = kOffA + kW2Bytes;      // d2 (128 x 128)
-constexpr int kOffBar = kOffDd + kW2Bytes;
+constexpr int kOffA = (kOffW1 + kWImg + 1023) / 1024 * 1024;  // a1, then d1 (128 x 128)
+constexpr int kOffDd = kOffA + kW2Bytes;                       // d2 (128 x 128)
+constexpr int kOffY = kOffDd + kW2Bytes;                       // partial y [2][128]
+constexpr int kOffBar = kOffY + 2 * kR * 4;
 constexpr int kMlpSmem = kOffBar + 64 + 1024;
+static_assert(kWImg % 16 == 0, "bulk copies move multiples of 16 bytes");
 
 __device__ __forceinline__ float sig(float z) { return 1.f / (1.f + __expf(-z)); }
 
 // weight image of every (member, species) block: W1 [h][d], W2 [i][j],
-// W2^T [j][i], W1^T [d][h], each a K-major canonical tile (rows = UMMA N)
-__global__ void k_mlp_w_image(int nblk, int D, size_t P, size_t offW1, size_t offW2,
-                              const __nv_bfloat16 *__restrict__ w16, unsigned char *__restrict__ img) {
+// W2^T [j][i], W1^T [d][h] as K-major canonical BF16 tiles (rows = UMMA N),
+// then b1, b2, w3, b3 in FP32
+__global__ void k_mlp_w_image(int nblk, int D, size_t P, size_t offW1, size_t offW2, size_t offb1,
+                              size_t offb2, size_t offw3, size_t offb3,
+                              const __nv_bfloat16 *__restrict__ w16, const float *__restrict__ w32,
+                              unsigned char *__restrict__ img) {
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const size_t per = (size_t)kHid * kDp + (size_t)kHid * kHid;  // elements of W1 and W2
+  const size_t per = (size_t)kHid * kDp + (size_t)kHid * kHid + kHid;  // W1, W2 elements, vectors
   if (t >= per * nblk) return;
   const int b = (int)(t / per);
   const size_t e = t - (size_t)b * per;
   const __nv_bfloat16 *w = w16 + (size_t)b * P;
+  const float *wf = w32 + (size_t)b * P;
   unsigned char *o = img + (size_t)b * kWImg;
   const __nv_bfloat16 zero = __float2bfloat16(0.f);
   if (e < (size_t)kHid * kDp) {
@@ -70,13 +83,20 @@ __global__ void k_mlp_w_image(int nblk, int D, size_t P, size_t offW1, size_t of
     *reinterpret_cast<__nv_bfloat16 *>(o + kmajor_off(h, d, kDp / 8)) = v;  // W1 (N = h, K = d)
     *reinterpret_cast<__nv_bfloat16 *>(o + kW1Bytes + 2 * kW2Bytes + kmajor_off(d, h, kHid / 8)) =
         v;  // W1^T (N = d, K = h)
-  } else {
+  } else if (e < (size_t)kHid * kDp + (size_t)kHid * kHid) {
     const size_t f = e - (size_t)kHid * kDp;
     const int i = (int)(f / kHid), j = (int)(f % kHid);
     const __nv_bfloat16 v = w[offW2 + (size_t)i * kHid + j];
     *reinterpret_cast<__nv_bfloat16 *>(o + kW1Bytes + kmajor_off(i, j, kHid / 8)) = v;  // W2
     *reinterpret_cast<__nv_bfloat16 *>(o + kW1Bytes + kW2Bytes + kmajor_off(j, i, kHid / 8)) =
         v;  // W2^T (N = j, K = i)
+  } else {
+    const int h = (int)(e - (size_t)kHid * kDp - (size_t)kHid * kHid);
+    float *vec = reinterpret_cast<float *>(o + kOffVec);
+    vec[h] = wf[offb1 + h];
+    vec[kHid + h] = wf[offb2 + h];
+    vec[2 * kHid + h] = wf[offw3 + h];
+    if (h < 4) vec[3 * kHid + h] = h == 0 ? wf[offb3] : 0.f;
   }
 }
 
@@ -107,8 +127,6 @@ __global__ void k_mlp_x_image(int Mpad, int D, const int *__restrict__ idx,
 
 struct MlpTcArgs {
   int ntiles, Mpad, D, nsp;
-  size_t P, offb1, offb2, offw3, offb3;
-  const float *w;                // FP32 parameters (biases, w3, b3)
   const unsigned char *wimg;     // weight images [members * nsp]
   const unsigned char *ximg;     // X tiles [ntiles]
   const int *tile_sp64;          // species of each 64-row tile (-1: beyond the rows)
@@ -116,15 +134,21 @@ struct MlpTcArgs {
   int *flags;
 };
 
-__global__ void __launch_bounds__(128, 1) k_mlp_tc(MlpTcArgs a) {
+__global__ void __launch_bounds__(kThreads, 1) k_mlp_tc(MlpTcArgs a) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   unsigned char *sm =
       reinterpret_cast<unsigned char *>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int quad = warp & 3, half = warp >> 2;  // TMEM lane quadrant, column half
+  const int r = quad * 32 + lane;                // row of the tile
   const int q = blockIdx.y;
   const uint32_t s_base = smem_u32(sm);
-  const uint32_t bar_load = s_base + kOffBar, bar_mma = bar_load + 8;
+  const uint32_t bar_x0 = s_base + kOffBar, bar_x1 = bar_x0 + 8, bar_w = bar_x0 + 16,
+                 bar_mma = bar_x0 + 24;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + kOffBar + 32);
+  float *ypart = reinterpret_cast<float *>(sm + kOffY);
+  const float *vb1 = reinterpret_cast<const float *>(sm + kOffW1 + kOffVec);
+  const float *vb2 = vb1 + kHid, *vw3 = vb1 + 2 * kHid, *vb3 = vb1 + 3 * kHid;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
                      smem_u32(tmem_slot))
@@ -132,7 +156,9 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(MlpTcArgs a) {
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    mbar_init(bar_load, 1);
+    mbar_init(bar_x0, 1);
+    mbar_init(bar_x1, 1);
+    mbar_init(bar_w, 1);
     mbar_init(bar_mma, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -141,11 +167,22 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(MlpTcArgs a) {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
   const uint32_t tZ1 = tmem, tZ2 = tmem + 128, tG = tmem + 256;
-  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+  const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
   const uint32_t id128 = instr_desc(kR, 128), id64 = instr_desc(kR, 64);
-  uint32_t ph_load = 0, ph_mma = 0;
+  uint32_t ph_x[2] = {0, 0}, ph_w = 0, ph_mma = 0;
   bool ok = true;
-  int loaded = -1;
+  int loaded = -1, buf = 0;
+  bool pending[2] = {false, false};  // X copies in flight, per buffer
+  bool pending_w = false, pending_mma = false;
+  auto valid_tile = [&](int t) { return t < a.ntiles && a.tile_sp64[2 * t] >= 0; };
+  auto load_x = [&](int t, int b) {
+    if (tid == 0) {
+      const uint32_t bar = b ? bar_x1 : bar_x0;
+      mbar_expect_tx(bar, kXBytes);
+      bulk_g2s(s_base + (b ? kOffX1 : kOffX0), a.ximg + (size_t)t * kXBytes, kXBytes, bar);
+    }
+    pending[b] = true;
+  };
   // MMA issue (one thread) and the bounded wait on its completion
   auto gemm = [&](uint32_t dt, int offA, int offB, int kcores, int ksteps, uint32_t idesc) {
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -159,33 +196,48 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(MlpTcArgs a) {
       }
       umma_commit(bar_mma);
     }
+    pending_mma = true;
     ok = mbar_wait(bar_mma, ph_mma, a.flags);
-    ph_mma ^= 1;
+    if (ok) {
+      ph_mma ^= 1;
+      pending_mma = false;
+    }
     ok = __syncthreads_and(ok);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   };
+  if (valid_tile(blockIdx.x)) load_x(blockIdx.x, 0);
   for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
     const int sp = a.tile_sp64[2 * t];
     if (sp < 0) break;  // padding tiles come last
-    const bool reload = sp != loaded;
-    if (tid == 0) {
-      mbar_expect_tx(bar_load, kXBytes + (reload ? kWImg : 0));
-      bulk_g2s(s_base + kOffX, a.ximg + (size_t)t * kXBytes, kXBytes, bar_load);
-      if (reload)
-        bulk_g2s(s_base + kOffW1, a.wimg + (size_t)(q * a.nsp + sp) * kWImg, kWImg, bar_load);
+    if (sp != loaded) {
+      // every MMA reading the previous weights has completed (waited below)
+      if (tid == 0) {
+        mbar_expect_tx(bar_w, kWImg);
+        bulk_g2s(s_base + kOffW1, a.wimg + (size_t)(q * a.nsp + sp) * kWImg, kWImg, bar_w);
+      }
+      loaded = sp;
+      pending_w = true;
+      ok = mbar_wait(bar_w, ph_w, a.flags);
+      if (ok) {
+        ph_w ^= 1;
+        pending_w = false;
+      }
+      if (!__syncthreads_and(ok)) break;
     }
-    loaded = sp;
-    ok = mbar_wait(bar_load, ph_load, a.flags);
-    ph_load ^= 1;
+    ok = mbar_wait(buf ? bar_x1 : bar_x0, ph_x[buf], a.flags);
+    if (ok) {
+      ph_x[buf] ^= 1;
+      pending[buf] = false;
+    }
     if (!__syncthreads_and(ok)) break;
-    const float *blk = a.w + (size_t)(q * a.nsp + sp) * a.P;
-    const float *b1 = blk + a.offb1, *b2 = blk + a.offb2, *w3 = blk + a.offw3;
-    const int row = t * kR + tid;
-    // GEMM1 and epilogue 1: a1 = silu(z1 + b1)
-    gemm(tZ1, kOffX, kOffW1, kDp / 8, kDp / 16, id128);
+    const int row = t * kR + r;
+    // GEMM1; its X buffer is then free, so the next tile's X is prefetched
+    gemm(tZ1, buf ? kOffX1 : kOffX0, kOffW1, kDp / 8, kDp / 16, id128);
     if (!ok) break;
+    if (valid_tile(t + gridDim.x)) load_x(t + gridDim.x, buf ^ 1);
+    // epilogue 1: a1 = silu(z1 + b1), this thread's 64 columns
 #pragma unroll 1
-    for (int cc = 0; cc < 4; ++cc) {
+    for (int cc = 2 * half; cc < 2 * half + 2; ++cc) {
       float v[32];
       tmem_ld32(tZ1 + lane_base + cc * 32, v);
 #pragma unroll
@@ -194,20 +246,20 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(MlpTcArgs a) {
 #pragma unroll
         for (int h = 0; h < 4; ++h) {
           const int c0 = cc * 32 + g * 8 + 2 * h;
-          const float z0 = v[g * 8 + 2 * h] + b1[c0], z1 = v[g * 8 + 2 * h + 1] + b1[c0 + 1];
+          const float z0 = v[g * 8 + 2 * h] + vb1[c0], z1 = v[g * 8 + 2 * h + 1] + vb1[c0 + 1];
           pk[h] = pack_bf16(z0 * sig(z0), z1 * sig(z1));
         }
-        *reinterpret_cast<uint4 *>(sm + kOffA + kmajor_off(tid, cc * 32 + g * 8, kHid / 8)) =
+        *reinterpret_cast<uint4 *>(sm + kOffA + kmajor_off(r, cc * 32 + g * 8, kHid / 8)) =
             make_uint4(pk[0], pk[1], pk[2], pk[3]);
       }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    // GEMM2 and epilogue 2: y, d2
+    // GEMM2 and epilogue 2: partial y, d2
     gemm(tZ2, kOffA, kOffW2, kHid / 8, kHid / 16, id128);
     if (!ok) break;
     float ysum = 0.f;
 #pragma unroll 1
-    for (int cc = 0; cc < 4; ++cc) {
+    for (int cc = 2 * half; cc < 2 * half + 2; ++cc) {
       float v[32];
       tmem_ld32(tZ2 + lane_base + cc * 32, v);
 #pragma unroll
@@ -219,24 +271,26 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(MlpTcArgs a) {
 #pragma unroll
           for (int u = 0; u < 2; ++u) {
             const int c = cc * 32 + g * 8 + 2 * h + u;
-            const float z = v[g * 8 + 2 * h + u] + b2[c];
+            const float z = v[g * 8 + 2 * h + u] + vb2[c];
             const float s = sig(z);
-            ysum = fmaf(z * s, w3[c], ysum);
-            d2v[u] = w3[c] * s * (1.f + z * (1.f - s));
+            ysum = fmaf(z * s, vw3[c], ysum);
+            d2v[u] = vw3[c] * s * (1.f + z * (1.f - s));
           }
           pk[h] = pack_bf16(d2v[0], d2v[1]);
         }
-        *reinterpret_cast<uint4 *>(sm + kOffDd + kmajor_off(tid, cc * 32 + g * 8, kHid / 8)) =
+        *reinterpret_cast<uint4 *>(sm + kOffDd + kmajor_off(r, cc * 32 + g * 8, kHid / 8)) =
             make_uint4(pk[0], pk[1], pk[2], pk[3]);
       }
     }
-    if (row < a.Mpad) a.y[(size_t)q * a.Mpad + row] = ysum + blk[a.offb3];
+    ypart[half * kR + r] = ysum;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    // GEMM3 (into the Z2 columns) and epilogue 3: d1 = silu'(z1 + b1) o U
+    // GEMM3 (into the Z2 columns); the partial y are complete after its sync
     gemm(tZ2, kOffDd, kOffW2T, kHid / 8, kHid / 16, id128);
     if (!ok) break;
+    if (half == 0 && row < a.Mpad) a.y[(size_t)q * a.Mpad + row] = ypart[r] + ypart[kR + r] + vb3[0];
+    // epilogue 3: d1 = silu'(z1 + b1) o U
 #pragma unroll 1
-    for (int cc = 0; cc < 4; ++cc) {
+    for (int cc = 2 * half; cc < 2 * half + 2; ++cc) {
       float u[32], z[32];
       tmem_ld32(tZ2 + lane_base + cc * 32, u);
       tmem_ld32(tZ1 + lane_base + cc * 32, z);
@@ -249,35 +303,37 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(MlpTcArgs a) {
 #pragma unroll
           for (int w = 0; w < 2; ++w) {
             const int k = g * 8 + 2 * h + w;
-            const float zz = z[k] + b1[cc * 32 + k];
+            const float zz = z[k] + vb1[cc * 32 + k];
             const float s = sig(zz);
             dv[w] = s * (1.f + zz * (1.f - s)) * u[k];
           }
           pk[h] = pack_bf16(dv[0], dv[1]);
         }
-        *reinterpret_cast<uint4 *>(sm + kOffA + kmajor_off(tid, cc * 32 + g * 8, kHid / 8)) =
+        *reinterpret_cast<uint4 *>(sm + kOffA + kmajor_off(r, cc * 32 + g * 8, kHid / 8)) =
             make_uint4(pk[0], pk[1], pk[2], pk[3]);
       }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    // GEMM4 and epilogue 4: dy/dx rows
+    // GEMM4 and epilogue 4: dy/dx, this thread's 32 components
     gemm(tG, kOffA, kOffW1T, kHid / 8, kHid / 16, id64);
     if (!ok) break;
-    float gv[64];
-    tmem_ld32(tG + lane_base, gv);
-    tmem_ld32(tG + lane_base + 32, gv + 32);
+    float gv[32];
+    tmem_ld32(tG + lane_base + half * 32, gv);
     if (row < a.Mpad) {
-      float *o = a.gx + ((size_t)q * a.Mpad + row) * a.D;
+      float *o = a.gx + ((size_t)q * a.Mpad + row) * a.D + half * 32;
 #pragma unroll
-      for (int d = 0; d < kDp; ++d)
-        if (d < a.D) o[d] = gv[d];
+      for (int d = 0; d < 32; ++d)
+        if (half * 32 + d < a.D) o[d] = gv[d];
     }
+    buf ^= 1;
   }
   if (!ok && tid == 0) {
-    // a wait gave up: one more bounded wait for the outstanding phases
-    // before the tensor memory and shared memory are released
-    mbar_wait(bar_load, ph_load, a.flags);
-    mbar_wait(bar_mma, ph_mma, a.flags);
+    // a wait gave up: one more bounded wait for every phase that may still be
+    // outstanding before the tensor and shared memory are released
+    if (pending[0]) mbar_wait(bar_x0, ph_x[0], a.flags);
+    if (pending[1]) mbar_wait(bar_x1, ph_x[1], a.flags);
+    if (pending_w) mbar_wait(bar_w, ph_w, a.flags);
+    if (pending_mma) mbar_wait(bar_mma, ph_mma, a.flags);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -291,14 +347,15 @@ size_t mlp_tc_w_image_bytes(int nblk) { return (size_t)nblk * kWImg; }
 size_t mlp_tc_x_image_bytes(int Mpad) { return (size_t)((Mpad + kR - 1) / kR) * kXBytes; }
 bool mlp_tc_eligible(int D, int H) { return D <= kDp && H == kHid; }
 
-void launch_mlp_w_image(int nblk, int D, size_t P, size_t offW1, size_t offW2,
-                        const __nv_bfloat16 *w16, unsigned char *img, cudaStream_t st) {
-  const size_t n = ((size_t)kHid * kDp + (size_t)kHid * kHid) * nblk;
-  k_mlp_w_image<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(nblk, D, P, offW1, offW2, w16, img);
+void launch_mlp_w_image(int nblk, int D, size_t P, size_t offW1, size_t offW2, size_t offb1,
+                        size_t offb2, size_t offw3, size_t offb3, const __nv_bfloat16 *w16,
+                        const float *w32, unsigned char *img, cudaStream_t st) {
+  const size_t n = ((size_t)kHid * kDp + (size_t)kHid * kHid + kHid) * nblk;
+  k_mlp_w_image<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(nblk, D, P, offW1, offW2, offb1,
+                                                             offb2, offw3, offb3, w16, w32, img);
 }
 
-void launch_mlp_tc(int members, int nsp, int D, int Mpad, size_t P, size_t offb1, size_t offb2,
-                   size_t offw3, size_t offb3, const float *w, const unsigned char *wimg,
+void launch_mlp_tc(int members, int nsp, int D, int Mpad, const unsigned char *wimg,
                    unsigned char *ximg, const int *idx, const float *G, const float *mu,
                    const float *isig, const int *tile_sp64, float *y, float *gx, int *flags,
                    cudaStream_t st) {
@@ -309,10 +366,9 @@ void launch_mlp_tc(int members, int nsp, int D, int Mpad, size_t P, size_t offb1
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int ntiles = Mpad / kR;
   const int per_member = std::max(1, std::min(ntiles, (sms + members - 1) / members));
-  MlpTcArgs a{ntiles, Mpad, D, nsp, P, offb1, offb2, offw3, offb3, w, wimg, ximg, tile_sp64,
-              y, gx, flags};
+  MlpTcArgs a{ntiles, Mpad, D, nsp, wimg, ximg, tile_sp64, y, gx, flags};
   cudaFuncSetAttribute(k_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kMlpSmem);
-  k_mlp_tc<<<dim3(per_member, members), 128, kMlpSmem, st>>>(a);
+  k_mlp_tc<<<dim3(per_member, members), kThreads, kMlpSmem, st>>>(a);
 }
 
 }  // namespace gapgb
