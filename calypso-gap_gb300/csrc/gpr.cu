@@ -20,6 +20,7 @@
 // 16 difference-square-adds).  Phase B: the same thread accumulates dE/dG of
 // atoms ty+16a and descriptor components tx+16b.  Small batches split the
 // sparse points over blockIdx.y; a fixed-order reduction sums the partials.
+#include <algorithm>
 #include <type_traits>
 
 #include "gapgb_internal.h"
@@ -217,20 +218,21 @@ __global__ void k_gpr_reduce_rows(int cap, int D, int M, int nblocks, const int 
                                   const int *__restrict__ rows, const double *__restrict__ e_part,
                                   const T *__restrict__ dedg_part, double *__restrict__ e,
                                   TG *__restrict__ dedg) {
-  const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int n = *count;
   const RowSplit rs = row_split(n, M, nblocks);
   const size_t nd = (size_t)n * D;
-  if (tid < nd) {
+  // grid-stride over the listed rows only (the grid does not depend on n)
+  for (size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x; tid < nd;
+       tid += (size_t)gridDim.x * blockDim.x) {
     T s = (T)0;
     for (int p = 0; p < rs.nsp; ++p) s += dedg_part[(size_t)p * nd + tid];
     const size_t i = tid / D;
     dedg[(size_t)rows[i] * D + (tid - i * D)] = (TG)s;
-  }
-  if (tid < (size_t)n) {
-    double s = 0.0;
-    for (int p = 0; p < rs.nsp; ++p) s += e_part[(size_t)p * n + tid];
-    e[rows[tid]] = s;
+    if (tid - i * D == 0) {
+      double se = 0.0;
+      for (int p = 0; p < rs.nsp; ++p) se += e_part[(size_t)p * n + i];
+      e[rows[i]] = se;
+    }
   }
   (void)cap;
 }
@@ -336,7 +338,8 @@ void launch_gpr_rows(const gapgb_model *m, Workspace &ws, int cap, const int *d_
   if (D <= 64) run(k_gpr_rows<double, float, 4>);
   else run(k_gpr_rows<double, float, 8>);
   const size_t nd = (size_t)cap * D;
-  k_gpr_reduce_rows<double, float><<<(unsigned)((nd + 255) / 256), 256, 0, st>>>(
+  const unsigned rb = (unsigned)std::min<size_t>((nd + 255) / 256, (size_t)nb * 4);
+  k_gpr_reduce_rows<double, float><<<rb > 0 ? rb : 1, 256, 0, st>>>(
       cap, D, M, nb, d_count, d_rows, e_part, d_part, ws.e, (float *)ws.dedg);
 }
 

@@ -125,7 +125,9 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-__device__ __forceinline__ float sigm(float z) { return 1.f / (1.f + __expf(-z)); }
+// logistic function with the fast reciprocal (2-ulp division): the values
+// feed BF16 operands or FP32 sums where that error is far below the rest
+__device__ __forceinline__ float sigm(float z) { return __fdividef(1.f, 1.f + __expf(-z)); }
 __device__ __forceinline__ float silu(float z) { return z * sigm(z); }
 __device__ __forceinline__ float dsilu(float z) {
   const float s = sigm(z);
@@ -385,16 +387,17 @@ __global__ void k_mlp_committee(int Mpad, int D, int members, const int *__restr
     dedg_out[(size_t)a * D + d] = s * sc * isig[d];
   }
   if (lane == 0) {
-    double mean = 0.0;
+    // FP32 statistics (the FP64 pipe is narrow); the energy itself in FP64
+    float mean = 0.f;
     for (int q = 0; q < members; ++q) mean += y[(size_t)q * Mpad + row];
-    mean /= members;
-    double var = 0.0;
+    mean = __fdividef(mean, (float)members);
+    float var = 0.f;
     for (int q = 0; q < members; ++q) {
-      const double dv = y[(size_t)q * Mpad + row] - mean;
-      var += dv * dv;
+      const float dv = y[(size_t)q * Mpad + row] - mean;
+      var = fmaf(dv, dv, var);
     }
-    e_out[a] = (double)e_scale * mean + (double)e_shift[sp];
-    std_out[a] = (float)((double)e_scale * sqrt(var / (members > 1 ? members - 1 : 1)));
+    e_out[a] = (double)e_scale * (double)mean + (double)e_shift[sp];
+    std_out[a] = e_scale * sqrtf(__fdividef(var, (float)(members > 1 ? members - 1 : 1)));
   }
 }
 

@@ -59,7 +59,9 @@ constexpr int kOffBar = kOffY + 2 * kR * 4;
 constexpr int kMlpSmem = kOffBar + 64 + 1024;
 static_assert(kWImg % 16 == 0, "bulk copies move multiples of 16 bytes");
 
-__device__ __forceinline__ float sig(float z) { return 1.f / (1.f + __expf(-z)); }
+// logistic function with the fast reciprocal (2-ulp division; the results
+// become BF16 operands or FP32 sums)
+__device__ __forceinline__ float sig(float z) { return __fdividef(1.f, 1.f + __expf(-z)); }
 
 // weight image of every (member, species) block: W1 [h][d], W2 [i][j],
 // W2^T [j][i], W1^T [d][h] as K-major canonical BF16 tiles (rows = UMMA N),
@@ -169,10 +171,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_tc(MlpTcArgs a) {
   const uint32_t tZ1 = tmem, tZ2 = tmem + 128, tG = tmem + 256;
   const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
   const uint32_t id128 = instr_desc(kR, 128), id64 = instr_desc(kR, 64);
-  uint32_t ph_x[2] = {0, 0}, ph_w = 0, ph_mma = 0;
+  uint32_t ph_x0 = 0, ph_x1 = 0, ph_w = 0, ph_mma = 0;
   bool ok = true;
   int loaded = -1, buf = 0;
-  bool pending[2] = {false, false};  // X copies in flight, per buffer
+  bool pend0 = false, pend1 = false;  // X copies in flight, per buffer
   bool pending_w = false, pending_mma = false;
   auto valid_tile = [&](int t) { return t < a.ntiles && a.tile_sp64[2 * t] >= 0; };
   auto load_x = [&](int t, int b) {
@@ -181,7 +183,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_tc(MlpTcArgs a) {
       mbar_expect_tx(bar, kXBytes);
       bulk_g2s(s_base + (b ? kOffX1 : kOffX0), a.ximg + (size_t)t * kXBytes, kXBytes, bar);
     }
-    pending[b] = true;
+    if (b) pend1 = true; else pend0 = true;
   };
   // MMA issue (one thread) and the bounded wait on its completion
   auto gemm = [&](uint32_t dt, int offA, int offB, int kcores, int ksteps, uint32_t idesc) {
@@ -224,10 +226,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_tc(MlpTcArgs a) {
       }
       if (!__syncthreads_and(ok)) break;
     }
-    ok = mbar_wait(buf ? bar_x1 : bar_x0, ph_x[buf], a.flags);
+    ok = mbar_wait(buf ? bar_x1 : bar_x0, buf ? ph_x1 : ph_x0, a.flags);
     if (ok) {
-      ph_x[buf] ^= 1;
-      pending[buf] = false;
+      if (buf) { ph_x1 ^= 1; pend1 = false; } else { ph_x0 ^= 1; pend0 = false; }
     }
     if (!__syncthreads_and(ok)) break;
     const int row = t * kR + r;
@@ -317,21 +318,33 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_tc(MlpTcArgs a) {
     // GEMM4 and epilogue 4: dy/dx, this thread's 32 components
     gemm(tG, kOffA, kOffW1T, kHid / 8, kHid / 16, id64);
     if (!ok) break;
+    // the tile's dy/dx rows go through shared memory (the Dd tile is free
+    // after GEMM3) and leave as contiguous 16-byte stores
     float gv[32];
     tmem_ld32(tG + lane_base + half * 32, gv);
-    if (row < a.Mpad) {
-      float *o = a.gx + ((size_t)q * a.Mpad + row) * a.D + half * 32;
+    float *stage = reinterpret_cast<float *>(sm + kOffDd);  // [128][a.D] row-major
 #pragma unroll
-      for (int d = 0; d < 32; ++d)
-        if (half * 32 + d < a.D) o[d] = gv[d];
+    for (int d = 0; d < 32; ++d)
+      if (half * 32 + d < a.D) stage[r * a.D + half * 32 + d] = gv[d];
+    __syncthreads();
+    {
+      const size_t base = ((size_t)q * a.Mpad + (size_t)t * kR) * a.D;
+      const int n = kR * a.D;  // floats of the tile (rows t*128 .. t*128 + 127)
+      if ((a.D & 3) == 0) {
+        const float4 *src = reinterpret_cast<const float4 *>(stage);
+        float4 *dst = reinterpret_cast<float4 *>(a.gx + base);
+        for (int k = tid; k < n / 4; k += kThreads) dst[k] = src[k];
+      } else {
+        for (int k = tid; k < n; k += kThreads) a.gx[base + k] = stage[k];
+      }
     }
     buf ^= 1;
   }
   if (!ok && tid == 0) {
     // a wait gave up: one more bounded wait for every phase that may still be
     // outstanding before the tensor and shared memory are released
-    if (pending[0]) mbar_wait(bar_x0, ph_x[0], a.flags);
-    if (pending[1]) mbar_wait(bar_x1, ph_x[1], a.flags);
+    if (pend0) mbar_wait(bar_x0, ph_x0, a.flags);
+    if (pend1) mbar_wait(bar_x1, ph_x1, a.flags);
     if (pending_w) mbar_wait(bar_w, ph_w, a.flags);
     if (pending_mma) mbar_wait(bar_mma, ph_mma, a.flags);
   }
