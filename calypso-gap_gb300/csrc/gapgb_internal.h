@@ -116,6 +116,10 @@ struct SFT {
   T comb_lam[8];
   int ang_comb[kMaxSF];
   int fast_nal, fast_nc;
+  // 1 when the combinations are exactly zeta {1, 2, 4} x lambda {+1, -1},
+  // renumbered c = 2 log2(zeta) + (lambda < 0): the powers then have a
+  // closed form (fast kernels' STD variant)
+  int std6;
 };
 
 template <typename T>
@@ -168,6 +172,32 @@ inline SFT<T> make_sft(const SFDev &s) {
     t.ang_comb[q] = c;
   }
   t.fast_nal = t.fast_nc = 0;
+  t.std6 = 0;
+  if (ok && t.ncomb == 6) {
+    bool seen[6] = {false, false, false, false, false, false};
+    bool std = true;
+    for (int c = 0; c < 6 && std; ++c) {
+      const int iz = t.comb_iz[c];
+      const int lg = iz == 1 ? 0 : (iz == 2 ? 1 : (iz == 4 ? 2 : -1));
+      if (lg < 0) { std = false; break; }
+      const int k = 2 * lg + (t.comb_lam[c] < (T)0 ? 1 : 0);
+      if (seen[k]) std = false;
+      seen[k] = true;
+    }
+    if (std) {
+      int remap[8];
+      for (int c = 0; c < 6; ++c) {
+        const int iz = t.comb_iz[c];
+        remap[c] = 2 * (iz == 1 ? 0 : (iz == 2 ? 1 : 2)) + (t.comb_lam[c] < (T)0 ? 1 : 0);
+      }
+      for (int q = 0; q < s.nang; ++q) t.ang_comb[q] = remap[t.ang_comb[q]];
+      for (int k = 0; k < 6; ++k) {
+        t.comb_iz[k] = 1 << (k / 2);
+        t.comb_lam[k] = (k & 1) ? (T)-1 : (T)1;
+      }
+      t.std6 = 1;
+    }
+  }
   if (ok) {
     const int na = s.nalpha < 1 ? 1 : s.nalpha;
     t.fast_nal = na <= 1 ? 1 : (na <= 2 ? 2 : 4);

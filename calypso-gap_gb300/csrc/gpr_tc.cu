@@ -62,9 +62,11 @@ constexpr int kOffC = kOffMn + kTileK * 4;
 constexpr int kOffWh = kOffImg + kImgTile;
 constexpr int kOffWl = kOffWh + kWBytes;
 constexpr int kOffBar = kOffWl + kWBytes;                 // 3 mbarriers + tmem base
-constexpr int kSmemBytes = kOffBar + 64 + 1024;           // + alignment slack
+constexpr int kOffEp = kOffBar + 64;                      // partial energies [128] (FP64)
+constexpr int kSmemBytes = kOffEp + kRows * 8 + 1024;     // + alignment slack
+constexpr int kGprThreads = 256;  // warps w and w + 4 share TMEM lanes and split the columns
 
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(kGprThreads, 1)
     k_gpr_tc(int N, int ntiles, const unsigned char *__restrict__ img_model,
              const unsigned char *__restrict__ img_atoms, const float *__restrict__ xs,
              const float *__restrict__ xn, const float *__restrict__ invth, int D,
@@ -72,7 +74,8 @@ __global__ void __launch_bounds__(128, 1)
   extern __shared__ __align__(1024) unsigned char smraw[];
   unsigned char *sm = reinterpret_cast<unsigned char *>(
       ((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int quad = warp & 3, half = warp >> 2;  // TMEM lane quadrant, column half
   const uint32_t s_base = smem_u32(sm);
   const uint32_t bar_load = s_base + kOffBar, bar_g1 = bar_load + 8, bar_g2 = bar_load + 16;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + kOffBar + 32);
@@ -95,8 +98,8 @@ __global__ void __launch_bounds__(128, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
   const uint32_t tC1 = tmem, tC2 = tmem + 128;
-  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;  // this warp's TMEM lanes
-  const int row = tid;                                      // atom row of this thread
+  const uint32_t lane_base = (uint32_t)(quad * 32) << 16;  // this warp's TMEM lanes
+  const int row = quad * 32 + lane;                         // atom row of this thread
   const int i = blockIdx.x * kRows + row;
   const float xnorm = (i < N) ? xn[i] : 0.f;
   float ehi = 0.f, elo = 0.f;
@@ -136,7 +139,7 @@ __global__ void __launch_bounds__(128, 1)
     // epilogue 1: w = c exp(-s/2), e += w, W tile (bf16 hi / lo) for GEMM2
     unsigned char *wh = sm + kOffWh, *wl = sm + kOffWl;
 #pragma unroll 1
-    for (int cc = 0; cc < kTileK / 32; ++cc) {
+    for (int cc = 2 * half; cc < 2 * half + 2; ++cc) {
       float v[32];
       tmem_ld32(tC1 + lane_base + cc * 32, v);
 #pragma unroll
@@ -189,16 +192,23 @@ __global__ void __launch_bounds__(128, 1)
   }
   if (ok) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const double e = (double)ehi + (double)elo;
-    float c2[64];
-    tmem_ld32(tC2 + lane_base, c2);
-    tmem_ld32(tC2 + lane_base + 32, c2 + 32);
+    // the two column halves' partial energies, summed in a fixed order
+    double *ep = reinterpret_cast<double *>(sm + kOffEp);
+    if (half == 1) ep[row] = (double)ehi + (double)elo;
+    __syncthreads();
+    if (half == 0) ep[row] = ((double)ehi + (double)elo) + ep[row];
+    __syncthreads();
+    const double etot = ep[row];
+    float c2[32];
+    tmem_ld32(tC2 + lane_base + half * 32, c2);
     if (i < N) {
-      e_out[i] = e;
-      const float ef = (float)e;
+      if (half == 0) e_out[i] = etot;
+      const float ef = (float)etot;
 #pragma unroll
-      for (int d = 0; d < kDP; ++d)
-        if (d < D) dedg[(size_t)i * D + d] = -invth[d] * (xs[(size_t)i * kDP + d] * ef - c2[d]);
+      for (int k = 0; k < 32; ++k) {
+        const int d = half * 32 + k;
+        if (d < D) dedg[(size_t)i * D + d] = -invth[d] * (xs[(size_t)i * kDP + d] * ef - c2[k]);
+      }
     }
   } else if (tid == 0) {
     // a wait gave up: give the outstanding copy / MMA phases one more bounded
@@ -338,7 +348,7 @@ void launch_gpr_tc(gapgb_model *m, Workspace &ws, int N, cudaStream_t st) {
   k_tc_prep_atoms<<<(tiles * kRows + 127) / 128, 128, 0, st>>>(N, D, (const float *)ws.G,
                                                                 m->d_invth32, mu, xs, xn, img_atoms);
   cudaFuncSetAttribute(k_gpr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-  k_gpr_tc<<<tiles, 128, kSmemBytes, st>>>(N, m->tc_tiles, (const unsigned char *)m->d_tc,
+  k_gpr_tc<<<tiles, kGprThreads, kSmemBytes, st>>>(N, m->tc_tiles, (const unsigned char *)m->d_tc,
                                           img_atoms, xs, xn, m->d_invth32, D, ws.e,
                                           (float *)ws.dedg, ws.d_flags);
 }

@@ -39,6 +39,39 @@ __device__ __forceinline__ float pow_iz(float b, int iz, float *pm1) {
   return p * b;
 }
 
+// A_c = (1 + lambda_c cos)^zeta_c and dA_c/dcos for the combinations of a
+// pair: closed form for the standard set (STD: c = 2 log2(zeta) + (lambda < 0)),
+// integer powers otherwise
+template <int NC, bool STD>
+__device__ __forceinline__ void ang_powers(float cosv, const float *clam, const int *ciz,
+                                           float *A, float *dAl) {
+  if constexpr (STD && NC == 6) {
+    const float bp = 1.f + cosv, bm = 1.f - cosv;
+    const float bp2 = bp * bp, bm2 = bm * bm;
+    A[0] = bp;
+    A[1] = bm;
+    A[2] = bp2;
+    A[3] = bm2;
+    A[4] = bp2 * bp2;
+    A[5] = bm2 * bm2;
+    if (dAl) {
+      dAl[0] = 1.f;
+      dAl[1] = -1.f;
+      dAl[2] = 2.f * bp;
+      dAl[3] = -2.f * bm;
+      dAl[4] = 4.f * bp * bp2;
+      dAl[5] = -4.f * bm * bm2;
+    }
+  } else {
+#pragma unroll
+    for (int cc = 0; cc < NC; ++cc) {
+      float p;  // base^(zeta-1)
+      A[cc] = pow_iz(1.f + clam[cc] * cosv, ciz[cc], &p);
+      if (dAl) dAl[cc] = (float)ciz[cc] * p * clam[cc];  // d A / d cos
+    }
+  }
+}
+
 // Walks the upper triangle of P slots, screens pairs (r_jk <= rc) and calls
 // `work(j, k, rjk^2, valid)` on all 32 lanes for every batch of up to 32
 // contributing pairs (valid is false on the idle lanes of the last batch).
@@ -116,7 +149,7 @@ __device__ __forceinline__ void radial_fwd(const Layout<float> &L, const SFT<flo
   }
 }
 
-template <int NAL, int NC>
+template <int NAL, int NC, bool STD>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
     k_wacsf_fwd_grp(int N, int cap, int capS, const int *__restrict__ cnt,
                     const double4 *__restrict__ xyzr, const int *__restrict__ nj,
@@ -160,7 +193,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
       pair_stream(L, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
         if (!ok) return;
         const float a = L.r[j], b = L.r[k];
-        const float c = sqrtf(c2);
+        const float c = c2 > 0.f ? c2 * rsqrtf(c2) : 0.f;
         // costheta = (rij^2 + rik^2 - rjk^2) / (2 rij rik) (wacsf.f90:271-273)
         const float cosv = (a * a + b * b - c2) * 0.5f * L.ir[j] * L.ir[k];
         const float F = fcr[j] * fcr[k] * (0.5f * (__cosf(pirc * c) + 1.f));
@@ -170,13 +203,13 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
         for (int q = 0; q < NAL; ++q)
           EF[q] = q < nal ? L.ea[q * capS + j] * L.ea[q * capS + k] * __expf(-alv[q] * c2) * F
                           : 0.f;
+        float Ac[NC];
+        ang_powers<NC, STD>(cosv, clam, ciz, Ac, nullptr);
 #pragma unroll
         for (int cc = 0; cc < NC; ++cc) {
-          float pm1;
-          const float A = pow_iz(1.f + clam[cc] * cosv, ciz[cc], &pm1);
 #pragma unroll
           for (int q = 0; q < NAL; ++q) {
-            const float v = A * EF[q];
+            const float v = Ac[cc] * EF[q];
             acc[q][cc] += v;
             accw[q][cc] += v * wjk;
           }
@@ -203,7 +236,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
   }
 }
 
-template <int NAL, int NC>
+template <int NAL, int NC, bool STD>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
     k_wacsf_bwd_grp(int N, int cap, int capS, const int *__restrict__ cnt,
                     const double4 *__restrict__ xyzr, const int *__restrict__ nj,
@@ -280,8 +313,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
       if (P > 1)
         pair_stream(L, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
           const float a = L.r[j], b = L.r[k];
-          const float c = sqrtf(c2);
-          const float ia = L.ir[j], ib = L.ir[k], ic = 1.f / c;
+          const float ic = c2 > 0.f ? rsqrtf(c2) : 0.f, c = c2 * ic;
+          const float ia = L.ir[j], ib = L.ir[k];
           const float cosv = (a * a + b * b - c2) * 0.5f * ia * ib;
           const float dcda = ib - cosv * ia, dcdb = ia - cosv * ib, dcdc = -c * ia * ib;
           float sn, cs;
@@ -291,12 +324,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
           const float F = fa * fb * fcc;
           const float wjk = L.w[j] * L.w[k];
           float A[NC], dAl[NC];
-#pragma unroll
-          for (int cc = 0; cc < NC; ++cc) {
-            float p;  // base^(zeta-1)
-            A[cc] = pow_iz(1.f + clam[cc] * cosv, ciz[cc], &p);
-            dAl[cc] = (float)ciz[cc] * p * clam[cc];  // d A / d cos
-          }
+          ang_powers<NC, STD>(cosv, clam, ciz, A, dAl);
           float SP = 0.f, SQ = 0.f, SU = 0.f;
 #pragma unroll
           for (int q = 0; q < NAL; ++q) {
@@ -379,21 +407,24 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
 }
 
 // Kernel pointers of every (NAL, NC) instantiation.
-template <int NAL, int NC>
+template <int NAL, int NC, bool STD = false>
 struct GrpPair {
-  static constexpr auto fwd = k_wacsf_fwd_grp<NAL, NC>;
-  static constexpr auto bwd = k_wacsf_bwd_grp<NAL, NC>;
+  static constexpr auto fwd = k_wacsf_fwd_grp<NAL, NC, STD>;
+  static constexpr auto bwd = k_wacsf_bwd_grp<NAL, NC, STD>;
 };
 
-using GrpFwd = decltype(&k_wacsf_fwd_grp<1, 2>);
-using GrpBwd = decltype(&k_wacsf_bwd_grp<1, 2>);
+using GrpFwd = decltype(&k_wacsf_fwd_grp<1, 2, false>);
+using GrpBwd = decltype(&k_wacsf_bwd_grp<1, 2, false>);
 
 template <int NAL>
-__host__ inline void pick_nc(int nc, GrpFwd *f, GrpBwd *b) {
+__host__ inline void pick_nc(int nc, bool std6, GrpFwd *f, GrpBwd *b) {
   switch (nc) {
     case 2: *f = GrpPair<NAL, 2>::fwd; *b = GrpPair<NAL, 2>::bwd; break;
     case 4: *f = GrpPair<NAL, 4>::fwd; *b = GrpPair<NAL, 4>::bwd; break;
-    case 6: *f = GrpPair<NAL, 6>::fwd; *b = GrpPair<NAL, 6>::bwd; break;
+    case 6:
+      if (std6) { *f = GrpPair<NAL, 6, true>::fwd; *b = GrpPair<NAL, 6, true>::bwd; }
+      else { *f = GrpPair<NAL, 6>::fwd; *b = GrpPair<NAL, 6>::bwd; }
+      break;
     default: *f = GrpPair<NAL, 8>::fwd; *b = GrpPair<NAL, 8>::bwd; break;
   }
 }
@@ -401,10 +432,11 @@ __host__ inline void pick_nc(int nc, GrpFwd *f, GrpBwd *b) {
 // The grouped kernels for a model, or false when it does not qualify.
 __host__ inline bool grouped_kernels(const SFT<float> &t, GrpFwd *f, GrpBwd *b) {
   if (t.fast_nal == 0 || t.fast_nc == 0) return false;
+  const bool std6 = t.std6 && t.fast_nc == 6;
   switch (t.fast_nal) {
-    case 1: pick_nc<1>(t.fast_nc, f, b); break;
-    case 2: pick_nc<2>(t.fast_nc, f, b); break;
-    default: pick_nc<4>(t.fast_nc, f, b); break;
+    case 1: pick_nc<1>(t.fast_nc, std6, f, b); break;
+    case 2: pick_nc<2>(t.fast_nc, std6, f, b); break;
+    default: pick_nc<4>(t.fast_nc, std6, f, b); break;
   }
   return true;
 }
