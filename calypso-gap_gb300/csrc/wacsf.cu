@@ -518,11 +518,14 @@ void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
     GrpFwd gf;
     GrpBwd gb;
     if (!m->generic_kernels && grouped_kernels(m->sft32h, &gf, &gb)) {
-      cudaFuncSetAttribute(gf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      const size_t smg = kTableBytes(sizeof(SFT<float>)) +
+                         (size_t)kWarpsPerBlock * 4 *
+                             grp_warp_floats(capS, m->sfh.nrc, m->sfh.D, true);
+      cudaFuncSetAttribute(gf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smg);
       cudaFuncSetAttribute(gf, cudaFuncAttributePreferredSharedMemoryCarveout,
                            cudaSharedmemCarveoutMaxShared);
-      const int grid = warp_grid(N, smem, (const void *)gf);
-      gf<<<grid, 32 * kWarpsPerBlock, smem, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
+      const int grid = warp_grid(N, smg, (const void *)gf);
+      gf<<<grid, 32 * kWarpsPerBlock, smg, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
                                                    ws.apos, ws.nbr_d32, ws.nbr_w32, m->d_sft32,
                                                    (float *)ws.G);
       return;
@@ -544,11 +547,14 @@ void launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
     GrpFwd gf;
     GrpBwd gb;
     if (!m->generic_kernels && grouped_kernels(m->sft32h, &gf, &gb)) {
-      cudaFuncSetAttribute(gb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      const size_t smg = kTableBytes(sizeof(SFT<float>)) +
+                         (size_t)kWarpsPerBlock * 4 *
+                             grp_warp_floats(capS, m->sfh.nrc, m->sfh.D, false);
+      cudaFuncSetAttribute(gb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smg);
       cudaFuncSetAttribute(gb, cudaFuncAttributePreferredSharedMemoryCarveout,
                            cudaSharedmemCarveoutMaxShared);
-      const int grid = warp_grid(N, smem, (const void *)gb);
-      gb<<<grid, 32 * kWarpsPerBlock, smem, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
+      const int grid = warp_grid(N, smg, (const void *)gb);
+      gb<<<grid, 32 * kWarpsPerBlock, smg, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
                                                    ws.apos, ws.nbr_d32, ws.nbr_w32, m->d_sft32,
                                                    (const float *)ws.dedg, (float4 *)ws.gslot,
                                                    ws.wvir);

@@ -25,6 +25,86 @@ constexpr int kPairQ = 64;
 // that the per-warp slot tables of 6 blocks fit
 constexpr int kGrpMinBlocks = 6;
 
+// Per-warp shared-memory layout of the grouped kernels: packed slot records
+// (a pair reads its two slots with six 128-bit loads) and the per-cutoff
+// tables of the radial terms.
+//   a[q] = (dx, dy, dz, r)        b[q] = (1/r, w, fc, fc') at the angular cutoff
+//   e[q] = exp(-alpha_t r^2), t < 4
+//   fc[g][q], dfc[g][q]           cutoff function of every cutoff group g
+//   gx, gy, gz [q], dg[D]         slot gradients and dE/dG (gradient kernel)
+struct GLay {
+  float4 *a, *b, *e;
+  float *fc, *dfc, *gx, *gy, *gz, *dg;
+};
+
+__host__ __device__ inline size_t grp_warp_floats(int capS, int nrc, int D, bool fwd) {
+  const size_t n = (size_t)12 * capS + (size_t)nrc * capS * (fwd ? 1 : 2) +
+                   (fwd ? 0 : (size_t)3 * capS + D);
+  return (n + 3) / 4 * 4;  // keeps every warp's records 16-byte aligned
+}
+
+__device__ __forceinline__ GLay grp_carve(unsigned char *raw, int warp, int capS, int nrc, int D,
+                                          bool fwd) {
+  float *base = reinterpret_cast<float *>(raw + kTableBytes(sizeof(SFT<float>))) +
+                grp_warp_floats(capS, nrc, D, fwd) * warp;
+  GLay L;
+  L.a = reinterpret_cast<float4 *>(base);
+  L.b = L.a + capS;
+  L.e = L.b + capS;
+  L.fc = reinterpret_cast<float *>(L.e + capS);
+  L.dfc = fwd ? nullptr : L.fc + (size_t)nrc * capS;
+  L.gx = fwd ? nullptr : L.dfc + (size_t)nrc * capS;
+  L.gy = fwd ? nullptr : L.gx + capS;
+  L.gz = fwd ? nullptr : L.gy + capS;
+  L.dg = fwd ? nullptr : L.gz + capS;
+  return L;
+}
+
+// Stages atom i's slots from the FP32 records of the neighbour kernel.
+__device__ __forceinline__ int grp_stage(const GLay &L, const SFT<float> &sf, int i, int cap,
+                                         int capS, int lane, int rci, const int *__restrict__ cnt,
+                                         const float4 *__restrict__ d32,
+                                         const float *__restrict__ w32, bool want_dfc) {
+  const int P = min(cnt[i], capS);
+  const int nrc = sf.nrc, nal = sf.nalpha;
+  for (int q = lane; q < P; q += 32) {
+    const float4 g = d32[(size_t)i * cap + q];
+    const float r = g.w, w = w32[(size_t)i * cap + q];
+    float fa = 0.f, dfa = 0.f;
+    for (int gr = 0; gr < nrc; ++gr) {
+      float fcv = 0.f, dfcv = 0.f;
+      if (r <= sf.rc_val[gr]) {
+        const float x = sf.pi_over_rc[gr] * r;
+        if (want_dfc) {
+          float sn, cs;
+          sincosf(x, &sn, &cs);
+          fcv = 0.5f * (cs + 1.f);
+          dfcv = -0.5f * sn * sf.pi_over_rc[gr];
+        } else {
+          fcv = 0.5f * (cosf(x) + 1.f);
+        }
+      }
+      L.fc[(size_t)gr * capS + q] = fcv;
+      if (want_dfc) L.dfc[(size_t)gr * capS + q] = dfcv;
+      if (gr == rci) {
+        fa = fcv;
+        dfa = dfcv;
+      }
+    }
+    float ev[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) ev[t] = t < nal ? expf(-sf.alpha_val[t] * r * r) : 0.f;
+    L.a[q] = g;
+    L.b[q] = make_float4(1.f / r, w, fa, dfa);
+    L.e[q] = make_float4(ev[0], ev[1], ev[2], ev[3]);
+  }
+  return P;
+}
+
+__device__ __forceinline__ float f4get(const float4 &v, int t) {
+  return t == 0 ? v.x : (t == 1 ? v.y : (t == 2 ? v.z : v.w));
+}
+
 // b^iz and b^(iz-1) for integer zeta >= 1 (branch-free up to 4)
 __device__ __forceinline__ float pow_iz(float b, int iz, float *pm1) {
   const float b2 = b * b;
@@ -78,7 +158,7 @@ __device__ __forceinline__ void ang_powers(float cosv, const float *clam, const 
 // Within a batch the pairs are in enumeration order: j is non-decreasing
 // across the valid lanes, which sit below the invalid ones.
 template <typename Work>
-__device__ __forceinline__ void pair_stream(const Layout<float> &L, int P, float rc, int lane,
+__device__ __forceinline__ void pair_stream(const float4 *__restrict__ A, int P, float rc, int lane,
                                             int *qjk, float *qc2, Work work) {
   const int npair = P * (P - 1) / 2;
   const float rc2 = rc * rc;
@@ -90,9 +170,9 @@ __device__ __forceinline__ void pair_stream(const Layout<float> &L, int P, float
     bool valid = false;
     float c2 = 0.f;
     if (base + lane < npair) {
-      const float a = L.r[j], b = L.r[k];
-      if (a <= rc && b <= rc) {
-        const float cx = L.dx[j] - L.dx[k], cy = L.dy[j] - L.dy[k], cz = L.dz[j] - L.dz[k];
+      const float4 aj = A[j], ak = A[k];
+      if (aj.w <= rc && ak.w <= rc) {
+        const float cx = aj.x - ak.x, cy = aj.y - ak.y, cz = aj.z - ak.z;
         c2 = cx * cx + cy * cy + cz * cz;
         valid = c2 <= rc2;
       }
@@ -128,8 +208,8 @@ __device__ __forceinline__ void pair_stream(const Layout<float> &L, int P, float
 }
 
 // radial part shared by both grouped kernels (one SF per lane, slot order)
-__device__ __forceinline__ void radial_fwd(const Layout<float> &L, const SFT<float> &sf, int P,
-                                           int capS, int lane, float *Gi) {
+__device__ __forceinline__ void radial_fwd(const GLay &L, const SFT<float> &sf, int P, int capS,
+                                           int lane, float *Gi) {
   for (int s = lane; s < sf.nrad; s += 32) {
     const int rr = sf.rad_rc[s];
     const float alpha = sf.rad_alpha[s], rs = sf.rad_rs[s];
@@ -138,10 +218,10 @@ __device__ __forceinline__ void radial_fwd(const Layout<float> &L, const SFT<flo
     for (int q = 0; q < P; ++q) {
       const float f = f_[q];
       if (f == 0.f) continue;
-      const float u = L.r[q] - rs;
+      const float u = L.a[q].w - rs;
       const float v = __expf(-alpha * u * u) * f;
       acc += v;
-      accw += v * L.w[q];
+      accw += v * L.b[q].y;
     }
     const int d = sf.rad_d[s];
     Gi[d] = acc;
@@ -156,6 +236,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
                     const double4 *__restrict__ apos, const float4 *__restrict__ d32,
                     const float *__restrict__ w32, const SFT<float> *__restrict__ sfg,
                     float *__restrict__ G) {
+  (void)xyzr;
+  (void)nj;
+  (void)apos;
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ int s_qjk[kWarpsPerBlock][kPairQ];
   __shared__ float s_qc2[kWarpsPerBlock][kPairQ];
@@ -164,10 +247,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
   const SFT<float> &sf = *reinterpret_cast<const SFT<float> *>(smraw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nal = sf.nalpha, D = sf.D, nsf = sf.nsf, nang = sf.nang;
-  const Layout<float> L = carve<float>(smraw, warp, capS, sf.nrc, nal, D, nang, true);
+  const GLay L = grp_carve(smraw, warp, capS, sf.nrc, D, true);
   const int rci = nang > 0 ? sf.ang_grp_rc[0] : 0;
   const float rc = sf.rc_val[rci], pirc = sf.pi_over_rc[rci];
-  const float *fcr = L.fc + rci * capS;
   float alv[NAL], clam[NC];
   int ciz[NC];
 #pragma unroll
@@ -178,8 +260,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
     ciz[c] = sf.comb_iz[c];
   }
   for (int i = blockIdx.x * kWarpsPerBlock + warp; i < N; i += gridDim.x * kWarpsPerBlock) {
-    const int P = stage_slots<float>(L, sf, i, cap, capS, lane, cnt, xyzr, nj, apos, d32, w32,
-                                     false);
+    const int P = grp_stage(L, sf, i, cap, capS, lane, rci, cnt, d32, w32, false);
     __syncwarp();
     float *Gi = G + (size_t)i * D;
     radial_fwd(L, sf, P, capS, lane, Gi);
@@ -190,19 +271,19 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
 #pragma unroll
       for (int c = 0; c < NC; ++c) acc[q][c] = accw[q][c] = 0.f;
     if (P > 1)
-      pair_stream(L, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
+      pair_stream(L.a, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
         if (!ok) return;
-        const float a = L.r[j], b = L.r[k];
+        const float a = L.a[j].w, b = L.a[k].w;
+        const float4 Bj = L.b[j], Bk = L.b[k], Ej = L.e[j], Ek = L.e[k];
         const float c = c2 > 0.f ? c2 * rsqrtf(c2) : 0.f;
         // costheta = (rij^2 + rik^2 - rjk^2) / (2 rij rik) (wacsf.f90:271-273)
-        const float cosv = (a * a + b * b - c2) * 0.5f * L.ir[j] * L.ir[k];
-        const float F = fcr[j] * fcr[k] * (0.5f * (__cosf(pirc * c) + 1.f));
-        const float wjk = L.w[j] * L.w[k];
+        const float cosv = (a * a + b * b - c2) * 0.5f * Bj.x * Bk.x;
+        const float F = Bj.z * Bk.z * (0.5f * (__cosf(pirc * c) + 1.f));
+        const float wjk = Bj.y * Bk.y;
         float EF[NAL];
 #pragma unroll
         for (int q = 0; q < NAL; ++q)
-          EF[q] = q < nal ? L.ea[q * capS + j] * L.ea[q * capS + k] * __expf(-alv[q] * c2) * F
-                          : 0.f;
+          EF[q] = q < nal ? f4get(Ej, q) * f4get(Ek, q) * __expf(-alv[q] * c2) * F : 0.f;
         float Ac[NC];
         ang_powers<NC, STD>(cosv, clam, ciz, Ac, nullptr);
 #pragma unroll
@@ -244,6 +325,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
                     const float *__restrict__ w32, const SFT<float> *__restrict__ sfg,
                     const float *__restrict__ dedg, float4 *__restrict__ gslot,
                     double *__restrict__ wvir) {
+  (void)xyzr;
+  (void)nj;
+  (void)apos;
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ int s_qjk[kWarpsPerBlock][kPairQ];
   __shared__ float s_qc2[kWarpsPerBlock][kPairQ];
@@ -252,11 +336,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
   const SFT<float> &sf = *reinterpret_cast<const SFT<float> *>(smraw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nal = sf.nalpha, D = sf.D, nsf = sf.nsf, nrad = sf.nrad, nang = sf.nang;
-  const Layout<float> L = carve<float>(smraw, warp, capS, sf.nrc, nal, D, nang, false);
+  const GLay L = grp_carve(smraw, warp, capS, sf.nrc, D, false);
   const int rci = nang > 0 ? sf.ang_grp_rc[0] : 0;
   const float rc = sf.rc_val[rci], pirc = sf.pi_over_rc[rci];
-  const float *fcr = L.fc + rci * capS;
-  const float *dfcr = L.dfc + rci * capS;
   float alv[NAL], clam[NC];
   int ciz[NC];
 #pragma unroll
@@ -267,15 +349,15 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
     ciz[c] = sf.comb_iz[c];
   }
   for (int i = blockIdx.x * kWarpsPerBlock + warp; i < N; i += gridDim.x * kWarpsPerBlock) {
-    const int P = stage_slots<float>(L, sf, i, cap, capS, lane, cnt, xyzr, nj, apos, d32, w32,
-                                     true);
+    const int P = grp_stage(L, sf, i, cap, capS, lane, rci, cnt, d32, w32, true);
     for (int d = lane; d < D; d += 32) L.dg[d] = dedg[(size_t)i * D + d];
     for (int q = lane; q < P; q += 32) L.gx[q] = L.gy[q] = L.gz[q] = 0.f;
     if (lane < 2 * NAL * NC) s_u[warp][lane] = 0.f;
     __syncwarp();
     // radial terms: lanes own slots
     for (int q = lane; q < P; q += 32) {
-      const float r = L.r[q], w = L.w[q];
+      const float4 aq = L.a[q];
+      const float r = aq.w, w = L.b[q].y;
       float S = 0.f;
       for (int s = 0; s < nrad; ++s) {
         const int rr = sf.rad_rc[s];
@@ -288,9 +370,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
         S += (L.dg[d] + L.dg[d + nsf] * w) * (-2.f * alpha * u * ex * f + ex * df);
       }
       const float ir = S / r;
-      L.gx[q] += ir * L.dx[q];
-      L.gy[q] += ir * L.dy[q];
-      L.gz[q] += ir * L.dz[q];
+      L.gx[q] += ir * aq.x;
+      L.gy[q] += ir * aq.y;
+      L.gz[q] += ir * aq.z;
     }
     if (nang > 0) {
       // dE/dG contracted onto the (alpha, combination) grid (one lane, fixed order)
@@ -311,26 +393,26 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
           UB[q][c] = s_u[warp][NAL * NC + q * NC + c];
         }
       if (P > 1)
-        pair_stream(L, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
-          const float a = L.r[j], b = L.r[k];
+        pair_stream(L.a, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
+          const float4 Aj = L.a[j], Ak = L.a[k], Bj = L.b[j], Bk = L.b[k];
+          const float4 Ej = L.e[j], Ek = L.e[k];
+          const float a = Aj.w, b = Ak.w;
           const float ic = c2 > 0.f ? rsqrtf(c2) : 0.f, c = c2 * ic;
-          const float ia = L.ir[j], ib = L.ir[k];
+          const float ia = Bj.x, ib = Bk.x;
           const float cosv = (a * a + b * b - c2) * 0.5f * ia * ib;
           const float dcda = ib - cosv * ia, dcdb = ia - cosv * ib, dcdc = -c * ia * ib;
           float sn, cs;
           __sincosf(pirc * c, &sn, &cs);
           const float fcc = 0.5f * (cs + 1.f), dfcc = -0.5f * sn * pirc;
-          const float fa = fcr[j], fb = fcr[k], dfa = dfcr[j], dfb = dfcr[k];
+          const float fa = Bj.z, fb = Bk.z, dfa = Bj.w, dfb = Bk.w;
           const float F = fa * fb * fcc;
-          const float wjk = L.w[j] * L.w[k];
+          const float wjk = Bj.y * Bk.y;
           float A[NC], dAl[NC];
           ang_powers<NC, STD>(cosv, clam, ciz, A, dAl);
           float SP = 0.f, SQ = 0.f, SU = 0.f;
 #pragma unroll
           for (int q = 0; q < NAL; ++q) {
-            const float E = q < nal ? L.ea[q * capS + j] * L.ea[q * capS + k] *
-                                          __expf(-alv[q] * c2)
-                                    : 0.f;
+            const float E = q < nal ? f4get(Ej, q) * f4get(Ek, q) * __expf(-alv[q] * c2) : 0.f;
             float sp = 0.f, sq = 0.f;
 #pragma unroll
             for (int cc = 0; cc < NC; ++cc) {
@@ -347,10 +429,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
           const float S2 = F * (SP * dcdb - 2.f * SU * b) + SQ * (fa * dfb * fcc);
           const float S3 = F * (SP * dcdc - 2.f * SU * c) + SQ * (fa * fb * dfcc);
           const float s1 = S1 * ia, s2 = S2 * ib, s3 = S3 * ic;
-          const float cx = L.dx[j] - L.dx[k], cy = L.dy[j] - L.dy[k], cz = L.dz[j] - L.dz[k];
-          float vx = ok ? s1 * L.dx[j] + s3 * cx : 0.f;
-          float vy = ok ? s1 * L.dy[j] + s3 * cy : 0.f;
-          float vz = ok ? s1 * L.dz[j] + s3 * cz : 0.f;
+          const float cx = Aj.x - Ak.x, cy = Aj.y - Ak.y, cz = Aj.z - Ak.z;
+          float vx = ok ? s1 * Aj.x + s3 * cx : 0.f;
+          float vy = ok ? s1 * Aj.y + s3 * cy : 0.f;
+          float vz = ok ? s1 * Aj.z + s3 * cz : 0.f;
           // slot j: the batch's pairs share few j values (enumeration order),
           // so each run of equal j (contiguous lanes) is summed by a
           // segmented scan and its last lane adds it: one atomic per run
@@ -373,9 +455,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
             atomicAdd(&L.gz[j], vz);
           }
           if (ok) {
-            atomicAdd(&L.gx[k], s2 * L.dx[k] - s3 * cx);
-            atomicAdd(&L.gy[k], s2 * L.dy[k] - s3 * cy);
-            atomicAdd(&L.gz[k], s2 * L.dz[k] - s3 * cz);
+            atomicAdd(&L.gx[k], s2 * Ak.x - s3 * cx);
+            atomicAdd(&L.gy[k], s2 * Ak.y - s3 * cy);
+            atomicAdd(&L.gz[k], s2 * Ak.z - s3 * cz);
           }
         });
     }
@@ -384,7 +466,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
     for (int q = lane; q < P; q += 32) {
       const float gx = L.gx[q], gy = L.gy[q], gz = L.gz[q];
       gslot[(size_t)i * cap + q] = make_float4(gx, gy, gz, 0.f);
-      const float d3[3] = {L.dx[q], L.dy[q], L.dz[q]};
+      const float4 aq = L.a[q];
+      const float d3[3] = {aq.x, aq.y, aq.z};
       const float g3[3] = {gx, gy, gz};
 #pragma unroll
       for (int aa = 0; aa < 3; ++aa)
