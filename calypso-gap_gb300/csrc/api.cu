@@ -60,6 +60,13 @@ void free_ws(Workspace &ws) {
   free_dev(ws.gslot);
   free_dev(ws.e);
   free_dev(ws.wvir);
+  free_dev(ws.red_part);
+  free_dev(ws.bin_count);
+  free_dev(ws.bin_start);
+  free_dev(ws.bin_atoms);
+  free_dev(ws.atom_bin);
+  free_dev(ws.atom_slot);
+  free_dev(ws.atom_m);
   free_dev(ws.d_flags);
   free_dev(ws.orphans);
   free_dev(ws.gpr_scratch);
@@ -117,6 +124,13 @@ gapgb_status ensure_ws(gapgb_model *m, int N, int S, int cap) {
   WS_ALLOC(*(double4 **)&ws.gslot, nslots);
   WS_ALLOC(ws.e, nN);
   WS_ALLOC(ws.wvir, (size_t)nN * 9);
+  WS_ALLOC(ws.red_part, (size_t)nS * 64 * 7);
+  WS_ALLOC(ws.bin_count, (size_t)nN + 1);
+  WS_ALLOC(ws.bin_start, (size_t)nN + 2);
+  WS_ALLOC(ws.bin_atoms, nN);
+  WS_ALLOC(ws.atom_bin, nN);
+  WS_ALLOC(ws.atom_slot, nN);
+  WS_ALLOC(ws.atom_m, nN);
   WS_ALLOC(ws.d_flags, 8);
   ws.orphan_cap = 1 << 16;
   WS_ALLOC(ws.orphans, ws.orphan_cap);
@@ -209,6 +223,12 @@ gapgb_status upload_model(gapgb_model *m) {
   m->profile_stages = prof && prof[0] && prof[0] != '0';
   m->d_sf = d_sf;  // marks the model as uploaded
   return GAPGB_OK;
+}
+
+int max_struct_atoms(int S, const int *atom_off) {
+  int mx = 0;
+  for (int s = 0; s < S; ++s) mx = std::max(mx, atom_off[s + 1] - atom_off[s]);
+  return mx;
 }
 
 bool finite_all(const double *p, size_t n) {
@@ -349,8 +369,10 @@ gapgb_status eval_host(gapgb_model *m, int S, const int *atom_off, const int *sp
     const int cap = m->cap;
     GAPGB_CUDA_TRY(cudaMemsetAsync(ws.d_flags, 0, 8 * sizeof(int), s));
     if (m->profile_stages) cudaEventRecord(m->ev[0], s);
-    launch_prep(m, ws, S, N, ws.d_atom_off, ws.d_species, ws.d_lat, ws.d_pos, m->host.rcut, s);
-    launch_neighbors(ws, N, cap, m->host.rcut, s);
+    const int maxa = max_struct_atoms(S, atom_off);
+    launch_prep(m, ws, S, N, ws.d_atom_off, ws.d_species, ws.d_lat, ws.d_pos, m->host.rcut, s,
+                maxa >= kBinMinAtoms);
+    launch_neighbors(ws, S, N, maxa, cap, m->host.rcut, s);
     GAPGB_CUDA_TRY(cudaGetLastError());
     GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.h_flags, ws.d_flags, 8 * sizeof(int), cudaMemcpyDeviceToHost, s));
     GAPGB_CUDA_TRY(cudaStreamSynchronize(s));
@@ -419,8 +441,8 @@ gapgb_status md_eval_enqueue(gapgb_model *m, int S, int N, const int *d_atom_off
   Workspace &ws = m->ws;
   const double rb = m->host.rcut + skin;
   GAPGB_CUDA_TRY(cudaMemsetAsync(ws.d_flags + 1, 0, 2 * sizeof(int), s));
-  launch_prep(m, ws, S, N, d_atom_off, d_species, d_lat, d_pos, rb, s);
-  if (rebuild) launch_neighbors(ws, N, m->cap, rb, s);
+  launch_prep(m, ws, S, N, d_atom_off, d_species, d_lat, d_pos, rb, s, rebuild && N >= kBinMinAtoms);
+  if (rebuild) launch_neighbors(ws, S, N, N, m->cap, rb, s);
   else launch_refresh(ws, N, m->cap, s);
   return enqueue_tail(m, S, N, m->cap, m->cap, 1, d_species, d_energy, d_force, d_stress, nullptr,
                       s);
@@ -646,7 +668,6 @@ gapgb_status gapgb_eval_batch_device(gapgb_model *m, int nstruct, int natoms, in
                                      const double *d_lat, const double *d_pos, int lgrad,
                                      double *d_energy, double *d_force, double *d_stress,
                                      double *d_atom_energy, void *stream) {
-  (void)max_atoms;
   if (!m || !d_atom_off || !d_species || !d_lat || !d_pos || !d_energy)
     return fail(GAPGB_ERR_ARG, "null argument");
   if (nstruct <= 0 || natoms <= 0) return fail(GAPGB_ERR_ARG, "sizes must be positive");
@@ -665,8 +686,10 @@ gapgb_status gapgb_eval_batch_device(gapgb_model *m, int nstruct, int natoms, in
   const int cap = m->cap;
   GAPGB_CUDA_TRY(cudaMemsetAsync(ws.d_flags, 0, 8 * sizeof(int), s));
   if (m->profile_stages) cudaEventRecord(m->ev[0], s);
-  launch_prep(m, ws, nstruct, natoms, d_atom_off, d_species, d_lat, d_pos, m->host.rcut, s);
-  launch_neighbors(ws, natoms, cap, m->host.rcut, s);
+  const int maxa = max_atoms > 0 ? max_atoms : natoms;
+  launch_prep(m, ws, nstruct, natoms, d_atom_off, d_species, d_lat, d_pos, m->host.rcut, s,
+              maxa >= kBinMinAtoms);
+  launch_neighbors(ws, nstruct, natoms, maxa, cap, m->host.rcut, s);
   double *d_stress_use = d_stress ? d_stress : ws.d_stress;
   double *d_force_use = d_force ? d_force : ws.d_force;
   return enqueue_tail(m, nstruct, natoms, cap, cap, lgrad, d_species, d_energy, d_force_use,
@@ -844,8 +867,9 @@ gapgb_status gapgb_neighbors(gapgb_model *m, int natoms, const int *species, con
   GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_lat, lat, sizeof(double) * 9, cudaMemcpyHostToDevice, s));
   GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_pos, pos, sizeof(double) * 3 * natoms, cudaMemcpyHostToDevice, s));
   GAPGB_CUDA_TRY(cudaMemsetAsync(ws.d_flags, 0, 8 * sizeof(int), s));
-  launch_prep(m, ws, 1, natoms, ws.d_atom_off, ws.d_species, ws.d_lat, ws.d_pos, m->host.rcut, s);
-  launch_neighbors(ws, natoms, cap, m->host.rcut, s);
+  launch_prep(m, ws, 1, natoms, ws.d_atom_off, ws.d_species, ws.d_lat, ws.d_pos, m->host.rcut, s,
+              natoms >= kBinMinAtoms);
+  launch_neighbors(ws, 1, natoms, natoms, cap, m->host.rcut, s);
   GAPGB_CUDA_TRY(cudaGetLastError());
   std::vector<double4> xyz((size_t)natoms * cap);
   std::vector<int> nj((size_t)natoms * cap);

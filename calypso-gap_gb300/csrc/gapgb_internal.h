@@ -218,7 +218,13 @@ struct StructInfo {
   double volume;   // |det(lat)| (gap_calc.f90:201)
   int nabc[3];     // gap_calc.f90:85-88
   int a0, na;
+  // spatial bins of a large cell (nb[0] == 0: not binned): nb[a] bins of
+  // fractional width >= ext[a] per axis, global bin ids bin0 .. bin0 + nb0 nb1 nb2 - 1
+  int nb[3];
+  int bin0;
 };
+
+constexpr int kBinMinAtoms = 2048;  // cells smaller than this use the O(na) scan
 
 template <typename T> struct Vec4;
 template <> struct Vec4<double> { using type = double4; };
@@ -255,6 +261,10 @@ struct Workspace {
   float *nbr_w32 = nullptr;   // FP32 weight of every slot's atom
   void *G = nullptr, *dedg = nullptr, *gslot = nullptr;
   double *e = nullptr, *wvir = nullptr;
+  double *red_part = nullptr;  // per-structure partial sums [S][64][7]
+  // spatial bins of large cells (neighbour build)
+  int *bin_count = nullptr, *bin_start = nullptr, *bin_atoms = nullptr;
+  int *atom_bin = nullptr, *atom_slot = nullptr, *atom_m = nullptr;
   int *d_flags = nullptr;     // [0] error bits, [1] max neighbour count, [2] orphan count
   int *orphans = nullptr;     // orphan slot list
   int orphan_cap = 0;
@@ -314,8 +324,9 @@ void set_last_error(const std::string &s);
 // kernel launchers (nbr.cu, wacsf.cu, gpr.cu, reduce.cu)
 void launch_prep(const gapgb_model *m, Workspace &ws, int S, int N, const int *d_atom_off,
                  const int *d_species, const double *d_lat, const double *d_pos,
-                 double rcut, cudaStream_t st);
-void launch_neighbors(Workspace &ws, int N, int cap, double rcut, cudaStream_t st);
+                 double rcut, cudaStream_t st, bool allow_bins = false);
+void launch_neighbors(Workspace &ws, int S, int N, int max_atoms, int cap, double rcut,
+                      cudaStream_t st);
 void launch_reverse(Workspace &ws, int N, int cap, cudaStream_t st);
 void launch_refresh(Workspace &ws, int N, int cap, cudaStream_t st);
 template <typename T>

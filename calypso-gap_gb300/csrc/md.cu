@@ -9,6 +9,7 @@
 // positions (k_nbr_refresh); a step takes the first every `rebuild_every`
 // steps.  Units: Angstrom, fs, amu, eV; a = F / m * 9.648533212e-3 A/fs^2
 // per eV/(A amu), KE = 1/2 m v^2 * 103.642697 eV per amu A^2/fs^2.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -79,16 +80,22 @@ __global__ void k_md_wrap(int N, int S, const int *__restrict__ atom_off,
   for (int c = 0; c < 3; ++c) x[c] = f[0] * L[c] + f[1] * L[3 + c] + f[2] * L[6 + c];
 }
 
-// kinetic energy per structure (one block per structure, fixed-order tree)
-__global__ void k_md_kinetic(int S, const int *__restrict__ atom_off, const double *__restrict__ vel,
-                             const double *__restrict__ mass, double *__restrict__ ekin) {
+// kinetic energy per structure in two fixed-order stages (parts of up to
+// 64 blocks per structure, then one thread per structure)
+constexpr int kKinParts = 64;
+
+__global__ void k_md_kin_partial(int parts, const int *__restrict__ atom_off,
+                                 const double *__restrict__ vel, const double *__restrict__ mass,
+                                 double *__restrict__ part) {
   __shared__ double red[256];
-  const int s = blockIdx.x;
-  if (s >= S) return;
+  const int s = blockIdx.y, p = blockIdx.x;
+  const int a0 = atom_off[s], na = atom_off[s + 1] - a0;
+  const int len = (na + parts - 1) / parts;
+  const int beg = p * len, end = min(na, beg + len);
   double acc = 0.0;
-  for (int i = atom_off[s] + threadIdx.x; i < atom_off[s + 1]; i += blockDim.x) {
-    const double *v = vel + 3 * (size_t)i;
-    acc += mass[i] * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  for (int q = beg + threadIdx.x; q < end; q += blockDim.x) {
+    const double *v = vel + 3 * (size_t)(a0 + q);
+    acc += mass[a0 + q] * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
   }
   red[threadIdx.x] = acc;
   __syncthreads();
@@ -96,7 +103,16 @@ __global__ void k_md_kinetic(int S, const int *__restrict__ atom_off, const doub
     if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) ekin[s] = 0.5 * kKinetic * red[0];
+  if (threadIdx.x == 0) part[(size_t)s * parts + p] = red[0];
+}
+
+__global__ void k_md_kin_final(int S, int parts, const double *__restrict__ part,
+                               double *__restrict__ ekin) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S) return;
+  double t = 0.0;
+  for (int p = 0; p < parts; ++p) t += part[(size_t)s * parts + p];
+  ekin[s] = 0.5 * kKinetic * t;
 }
 
 // displacement since the last rebuild above half the skin: flag it (the
@@ -135,12 +151,20 @@ struct gapgb_md {
   double *d_pos = nullptr, *d_vel = nullptr;
   double *accf = nullptr, *energy = nullptr, *force = nullptr, *stress = nullptr, *ekin = nullptr;
   double *pos_ref = nullptr;  // positions at the last rebuild
+  double *kin_part = nullptr;  // kinetic-energy partial sums [S][parts]
+  int kin_parts = 1;
   cudaStream_t stream = nullptr;
   cudaGraphExec_t g_rebuild = nullptr, g_refresh = nullptr;
   long step = 0;
 };
 
 namespace {
+
+void kinetic(gapgb_md *md, cudaStream_t s) {
+  k_md_kin_partial<<<dim3(md->kin_parts, md->S), 256, 0, s>>>(md->kin_parts, md->d_atom_off,
+                                                               md->d_vel, md->d_mass, md->kin_part);
+  k_md_kin_final<<<(md->S + 127) / 128, 128, 0, s>>>(md->S, md->kin_parts, md->kin_part, md->ekin);
+}
 
 // the launch sequence of one step (captured, never run directly)
 gapgb_status md_step_enqueue(gapgb_md *md, bool rebuild, cudaStream_t s) {
@@ -159,7 +183,7 @@ gapgb_status md_step_enqueue(gapgb_md *md, bool rebuild, cudaStream_t s) {
                                     md->stress, s);
   if (st) return st;
   k_vv_kick<<<b, 256, 0, s>>>(md->N, md->d_vel, md->force, md->accf, md->dt);
-  k_md_kinetic<<<md->S, 256, 0, s>>>(md->S, md->d_atom_off, md->d_vel, md->d_mass, md->ekin);
+  kinetic(md, s);
   GAPGB_CUDA_TRY(cudaGetLastError());
   return GAPGB_OK;
 }
@@ -188,7 +212,7 @@ void gapgb_md_free(gapgb_md *md) {
   if (!md) return;
   if (md->g_rebuild) cudaGraphExecDestroy(md->g_rebuild);
   if (md->g_refresh) cudaGraphExecDestroy(md->g_refresh);
-  void *ps[] = {md->accf, md->energy, md->force, md->stress, md->ekin, md->pos_ref};
+  void *ps[] = {md->accf, md->energy, md->force, md->stress, md->ekin, md->pos_ref, md->kin_part};
   for (void *p : ps)
     if (p) cudaFree(p);
   if (md->stream) cudaStreamDestroy(md->stream);
@@ -218,6 +242,7 @@ gapgb_status gapgb_md_create(gapgb_model *m, int nstruct, int natoms, const int 
   md->d_pos = d_pos;
   md->d_vel = d_vel;
   md->d_mass = d_mass;
+  md->kin_parts = std::max(1, std::min(kKinParts, natoms / nstruct / 2048));
   gapgb_status st = md_prepare(m, natoms, nstruct);
   if (st) {
     gapgb_md_free(md);
@@ -229,6 +254,7 @@ gapgb_status gapgb_md_create(gapgb_model *m, int nstruct, int natoms, const int 
       cudaMalloc(&md->stress, sizeof(double) * 6 * (size_t)nstruct) != cudaSuccess ||
       cudaMalloc(&md->ekin, sizeof(double) * nstruct) != cudaSuccess ||
       cudaMalloc(&md->pos_ref, sizeof(double) * 3 * (size_t)natoms) != cudaSuccess ||
+      cudaMalloc(&md->kin_part, sizeof(double) * kKinParts * (size_t)nstruct) != cudaSuccess ||
       cudaStreamCreateWithFlags(&md->stream, cudaStreamNonBlocking) != cudaSuccess) {
     cudaGetLastError();
     gapgb_md_free(md);
@@ -262,7 +288,7 @@ gapgb_status gapgb_md_create(gapgb_model *m, int nstruct, int natoms, const int 
     break;
   }
   if (!st) {
-    k_md_kinetic<<<nstruct, 256, 0, md->stream>>>(nstruct, d_atom_off, d_vel, d_mass, md->ekin);
+    kinetic(md, md->stream);
     st = capture(md, true, &md->g_rebuild);
   }
   if (!st) st = capture(md, false, &md->g_refresh);

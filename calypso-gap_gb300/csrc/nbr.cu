@@ -32,7 +32,7 @@ __device__ __forceinline__ void crossp_rn(const double *a, const double *b, doub
 // recipvector/volume/crossp of :240-266, same operation order), volume
 // (det, :201 and :290-299) and the inverse lattice for pruning.
 __global__ void k_prep_struct(int S, const int *__restrict__ atom_off,
-                              const double *__restrict__ lat_all, double rcut,
+                              const double *__restrict__ lat_all, double rcut, int allow_bins,
                               StructInfo *__restrict__ out, int *__restrict__ flags) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= S) return;
@@ -87,7 +87,98 @@ __global__ void k_prep_struct(int S, const int *__restrict__ atom_off,
   }
   si.a0 = atom_off[s];
   si.na = atom_off[s + 1] - atom_off[s];
+  // bins of fractional width >= ext (+ 1e-3 for the FP32 coordinates of the
+  // binning) when the cell is at least 3 bins wide on every axis
+  si.nb[0] = si.nb[1] = si.nb[2] = 0;
+  si.bin0 = 0;
+  if (allow_bins && si.na >= kBinMinAtoms) {
+    int nb[3];
+    bool ok = true;
+    long prod = 1;
+    for (int a = 0; a < 3; ++a) {
+      nb[a] = (int)floor(1.0 / (si.ext[a] + 1e-3));
+      if (nb[a] > 64) nb[a] = 64;
+      if (nb[a] < 3) ok = false;
+      prod *= nb[a];
+    }
+    if (ok && prod <= si.na)
+      for (int a = 0; a < 3; ++a) si.nb[a] = nb[a];
+  }
   out[s] = si;
+}
+
+// ---- spatial bins of large cells -------------------------------------------
+
+// bin offsets of every binned structure and the total (one thread)
+__global__ void k_bin_offsets(int S, StructInfo *__restrict__ sinfo, int *__restrict__ total) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int t = 0;
+  for (int s = 0; s < S; ++s) {
+    sinfo[s].bin0 = t;
+    t += sinfo[s].nb[0] * sinfo[s].nb[1] * sinfo[s].nb[2];
+  }
+  *total = t;
+}
+
+// bin of every atom of a binned structure (from its wrapped FP32 fractional
+// coordinates), its slot in the bin and its wrap shift m = floor(f)
+__global__ void k_bin_count(int N, const float4 *__restrict__ frac32,
+                            const int *__restrict__ atom_struct,
+                            const StructInfo *__restrict__ sinfo, int *__restrict__ count,
+                            int *__restrict__ atom_bin, int *__restrict__ atom_slot,
+                            int *__restrict__ atom_m) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const StructInfo &si = sinfo[atom_struct[i]];
+  if (si.nb[0] == 0) return;
+  const float4 f = frac32[i];
+  const float fv[3] = {f.x, f.y, f.z};
+  int b[3], m[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float fl = floorf(fv[a]);
+    m[a] = (int)fl;
+    int bb = (int)((fv[a] - fl) * (float)si.nb[a]);
+    b[a] = bb < 0 ? 0 : (bb >= si.nb[a] ? si.nb[a] - 1 : bb);
+  }
+  const int gid = si.bin0 + (b[0] * si.nb[1] + b[1]) * si.nb[2] + b[2];
+  atom_bin[i] = gid;
+  atom_slot[i] = atomicAdd(&count[gid], 1);
+  atom_m[i] = ((m[0] + 128) << 16) | ((m[1] + 128) << 8) | (m[2] + 128);
+}
+
+// exclusive scan of the bin counts (one block)
+__global__ void k_bin_scan(const int *__restrict__ total, const int *__restrict__ count,
+                           int *__restrict__ start) {
+  __shared__ int part[1024];
+  const int T = *total;
+  int carry = 0;
+  for (int base = 0; base < T; base += 1024) {
+    const int t = base + threadIdx.x;
+    const int v = t < T ? count[t] : 0;
+    part[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+      const int add = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
+      __syncthreads();
+      part[threadIdx.x] += add;
+      __syncthreads();
+    }
+    if (t < T) start[t] = carry + part[threadIdx.x] - v;
+    carry += part[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) start[T] = carry;
+}
+
+__global__ void k_bin_fill(int N, const int *__restrict__ atom_struct,
+                           const StructInfo *__restrict__ sinfo, const int *__restrict__ atom_bin,
+                           const int *__restrict__ atom_slot, const int *__restrict__ start,
+                           int *__restrict__ bin_atoms) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  if (sinfo[atom_struct[i]].nb[0] == 0) return;
+  bin_atoms[start[atom_bin[i]] + atom_slot[i]] = i;
 }
 
 // One thread per atom: structure index, species weight, fractional coords.
@@ -203,6 +294,7 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int i = gw; i < N; i += nw) {
     const StructInfo si = sinfo[atom_struct[i]];
+    if (si.nb[0] != 0) continue;  // large cells: k_nbr_build_binned
     const double4 pi = apos[i];
     const float4 fi = frac32[i];
     float L32[9];
@@ -323,6 +415,153 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
       atomicMax(flags + 1, total);
       if (total > cap) atomicOr(flags, kFlagNeighbourOverflow);
     }
+  }
+}
+
+// Neighbour list of an atom of a binned cell: candidates from the 27 bins
+// around its own, the same FP32 screen and exact FP64 test as k_nbr_build,
+// hits collected in shared memory and sorted by (j, n1, n2, n3) - the
+// reference's order - before they are written, so the list is identical to
+// the O(na) scan's.  The image of candidate j is n = s - m_j + m_i, with s the
+// bin-wrap shift and m the atoms' own wrap shifts.
+__global__ void __launch_bounds__(128) k_nbr_build_binned(
+    int N, int cap, int hit_cap, double rcut, const double4 *__restrict__ apos,
+    const float4 *__restrict__ frac32, const int *__restrict__ atom_struct,
+    const StructInfo *__restrict__ sinfo, const int *__restrict__ bin_start,
+    const int *__restrict__ bin_atoms, const int *__restrict__ atom_bin,
+    const int *__restrict__ atom_m, int *__restrict__ cnt, double4 *__restrict__ xyzr,
+    int *__restrict__ nj, int *__restrict__ ns, float4 *__restrict__ d32, float *__restrict__ w32,
+    int *__restrict__ flags) {
+  extern __shared__ __align__(16) unsigned char smb[];
+  __shared__ double s_dn[2 * kMaxImage + 1];
+  for (int t = threadIdx.x; t < 2 * kMaxImage + 1; t += blockDim.x) s_dn[t] = (double)(t - kMaxImage);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // per warp: hit_cap keys (8 B), records (32 B)
+  unsigned long long *keys =
+      reinterpret_cast<unsigned long long *>(smb) + (size_t)warp * hit_cap;
+  double4 *recs = reinterpret_cast<double4 *>(smb + (size_t)kWarpsPerBlock * hit_cap * 8) +
+                  (size_t)warp * hit_cap;
+  int *order = reinterpret_cast<int *>(smb + (size_t)kWarpsPerBlock * hit_cap * 40) +
+               (size_t)warp * hit_cap;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int i = gw; i < N; i += nw) {
+    const StructInfo si = sinfo[atom_struct[i]];
+    if (si.nb[0] == 0) continue;
+    const double4 pi = apos[i];
+    const float4 fi = frac32[i];
+    float L32[9];
+    float lsum = 0.f;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      L32[q] = (float)si.lat[q];
+      lsum += fabsf(L32[q]);
+    }
+    const float rs = (float)rcut + 2.5e-4f * lsum + 1e-3f;
+    const float r2max = rs * rs;
+    const int mi = atom_m[i];
+    const int mi3[3] = {((mi >> 16) & 255) - 128, ((mi >> 8) & 255) - 128, (mi & 255) - 128};
+    const int local = atom_bin[i] - si.bin0;
+    const int bi[3] = {local / (si.nb[1] * si.nb[2]), (local / si.nb[2]) % si.nb[1],
+                       local % si.nb[2]};
+    int total = 0;
+    for (int d = 0; d < 27; ++d) {
+      int c[3], sh[3];
+      const int dd[3] = {d / 9 - 1, (d / 3) % 3 - 1, d % 3 - 1};
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        c[a] = bi[a] + dd[a];
+        sh[a] = c[a] < 0 ? -1 : (c[a] >= si.nb[a] ? 1 : 0);
+        c[a] -= sh[a] * si.nb[a];
+      }
+      const int gid = si.bin0 + (c[0] * si.nb[1] + c[1]) * si.nb[2] + c[2];
+      const int b0 = bin_start[gid], b1 = bin_start[gid + 1];
+      for (int t0 = b0; t0 < b1; t0 += 32) {
+        const int t = t0 + lane;
+        bool hit = false;
+        unsigned long long key = 0;
+        double4 rec = make_double4(0, 0, 0, 0);
+        if (t < b1) {
+          const int j = bin_atoms[t];
+          const int mj = atom_m[j];
+          const int n1 = sh[0] - (((mj >> 16) & 255) - 128) + mi3[0];
+          const int n2 = sh[1] - (((mj >> 8) & 255) - 128) + mi3[1];
+          const int n3 = sh[2] - ((mj & 255) - 128) + mi3[2];
+          const bool self = j == i && n1 == 0 && n2 == 0 && n3 == 0;
+          const bool inrange = n1 >= -kMaxImage && n1 <= kMaxImage && n2 >= -kMaxImage &&
+                               n2 <= kMaxImage && n3 >= -kMaxImage && n3 <= kMaxImage;
+          if (!self && inrange) {
+            const float4 fj = frac32[j];
+            const float fd[3] = {fj.x - fi.x, fj.y - fi.y, fj.z - fi.z};
+            if (screen_r2(L32, fd, n1, n2, n3) <= r2max) {
+              double xyz[3];
+              const double dis = ref_image(pi, apos[j], si.lat, s_dn[n1 + kMaxImage],
+                                           s_dn[n2 + kMaxImage], s_dn[n3 + kMaxImage], xyz);
+              hit = !(dis > rcut);
+              rec = make_double4(xyz[0], xyz[1], xyz[2], dis);
+              key = ((unsigned long long)j << 24) |
+                    (unsigned long long)(((n1 + 128) << 16) | ((n2 + 128) << 8) | (n3 + 128));
+            }
+          }
+        }
+        const unsigned mball = __ballot_sync(0xffffffffu, hit);
+        const int q = total + __popc(mball & lt_mask);
+        if (hit && q < hit_cap) {
+          keys[q] = key;
+          recs[q] = rec;
+        }
+        total += __popc(mball);
+      }
+    }
+    __syncwarp();
+    const int nh = min(total, hit_cap);
+    // bitonic sort of the hit keys (with their positions) in shared memory
+    int n2p = 1;
+    while (n2p < nh) n2p <<= 1;
+    for (int t = lane; t < n2p; t += 32) {
+      order[t] = t;
+      if (t >= nh) keys[t] = ~0ull;
+    }
+    __syncwarp();
+    for (int k = 2; k <= n2p; k <<= 1)
+      for (int jj = k >> 1; jj > 0; jj >>= 1) {
+        for (int t = lane; t < n2p; t += 32) {
+          const int p = t ^ jj;
+          if (p > t) {
+            const bool up = (t & k) == 0;
+            const unsigned long long a = keys[t], b = keys[p];
+            if ((a > b) == up) {
+              keys[t] = b;
+              keys[p] = a;
+              const int o = order[t];
+              order[t] = order[p];
+              order[p] = o;
+            }
+          }
+        }
+        __syncwarp();
+      }
+    const int nout = min(total, min(cap, hit_cap));
+    double4 *oxyz = xyzr + (size_t)i * cap;
+    for (int q = lane; q < nout; q += 32) {
+      const unsigned long long key = keys[q];
+      const double4 rec = recs[order[q]];
+      const int j = (int)(key >> 24);
+      oxyz[q] = rec;
+      nj[(size_t)i * cap + q] = j;
+      ns[(size_t)i * cap + q] = (int)(key & 0xFFFFFFull);
+      d32[(size_t)i * cap + q] = make_float4(d2f_rn(rec.x - pi.x), d2f_rn(rec.y - pi.y),
+                                             d2f_rn(rec.z - pi.z), d2f_rn(rec.w));
+      w32[(size_t)i * cap + q] = frac32[j].w;
+    }
+    if (lane == 0) {
+      cnt[i] = nout;
+      atomicMax(flags + 1, total);
+      if (total > cap || total > hit_cap) atomicOr(flags, kFlagNeighbourOverflow);
+    }
+    __syncwarp();
   }
 }
 
@@ -448,17 +687,39 @@ int grid_for_warps(int nwarps_needed) {
 
 void launch_prep(const gapgb_model *m, Workspace &ws, int S, int N, const int *d_atom_off,
                  const int *d_species, const double *d_lat, const double *d_pos, double rcut,
-                 cudaStream_t st) {
-  k_prep_struct<<<(S + 127) / 128, 128, 0, st>>>(S, d_atom_off, d_lat, rcut, ws.sinfo, ws.d_flags);
+                 cudaStream_t st, bool allow_bins) {
+  k_prep_struct<<<(S + 127) / 128, 128, 0, st>>>(S, d_atom_off, d_lat, rcut, allow_bins ? 1 : 0,
+                                                 ws.sinfo, ws.d_flags);
   k_prep_atoms<<<(N + 255) / 256, 256, 0, st>>>(N, S, d_atom_off, d_species, d_pos, m->d_sf,
                                                  ws.sinfo, ws.atom_struct, ws.apos, ws.frac32,
                                                  ws.d_flags);
 }
 
-void launch_neighbors(Workspace &ws, int N, int cap, double rcut, cudaStream_t st) {
+void launch_neighbors(Workspace &ws, int S, int N, int max_atoms, int cap, double rcut,
+                      cudaStream_t st) {
   k_nbr_build<<<grid_for_warps(N), 32 * kWarpsPerBlock, 0, st>>>(
       N, cap, rcut, ws.apos, ws.frac32, ws.atom_struct, ws.sinfo, ws.nbr_cnt, ws.nbr_xyz,
       ws.nbr_j, ws.nbr_s, ws.nbr_d32, ws.nbr_w32, ws.d_flags);
+  if (max_atoms < kBinMinAtoms) return;  // no structure was binned (launch_prep)
+  int *total = ws.bin_count + N;  // last entry of the count array holds the bin total
+  cudaMemsetAsync(ws.bin_count, 0, sizeof(int) * (size_t)(N + 1), st);
+  k_bin_offsets<<<1, 32, 0, st>>>(S, ws.sinfo, total);
+  k_bin_count<<<(N + 255) / 256, 256, 0, st>>>(N, ws.frac32, ws.atom_struct, ws.sinfo,
+                                               ws.bin_count, ws.atom_bin, ws.atom_slot,
+                                               ws.atom_m);
+  k_bin_scan<<<1, 1024, 0, st>>>(total, ws.bin_count, ws.bin_start);
+  k_bin_fill<<<(N + 255) / 256, 256, 0, st>>>(N, ws.atom_struct, ws.sinfo, ws.atom_bin,
+                                              ws.atom_slot, ws.bin_start, ws.bin_atoms);
+  // hits beyond the capacity are counted (overflow) but not stored; the
+  // per-warp sort buffer is a power of two (the bitonic network's size)
+  int hit_cap = 32;
+  while (hit_cap < cap && hit_cap < 1024) hit_cap <<= 1;
+  const size_t smem = (size_t)kWarpsPerBlock * hit_cap * (8 + 32 + 4);
+  cudaFuncSetAttribute(k_nbr_build_binned, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_nbr_build_binned<<<grid_for_warps(N), 32 * kWarpsPerBlock, smem, st>>>(
+      N, cap, hit_cap, rcut, ws.apos, ws.frac32, ws.atom_struct, ws.sinfo, ws.bin_start,
+      ws.bin_atoms, ws.atom_bin, ws.atom_m, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j, ws.nbr_s,
+      ws.nbr_d32, ws.nbr_w32, ws.d_flags);
 }
 
 void launch_refresh(Workspace &ws, int N, int cap, cudaStream_t st) {

@@ -12,6 +12,8 @@
 // sum_q gslot[partner(j,q)][rev(j,q)].  Slots whose reverse pair did not
 // survive the cutoff test (a last-bit difference of the two distances at
 // exactly r = rcut) are listed as orphans and added afterwards.
+#include <algorithm>
+
 #include "gapgb_internal.h"
 
 namespace gapgb {
@@ -72,20 +74,25 @@ __global__ void k_orphans(int cap, const int *__restrict__ flags, const int *__r
   }
 }
 
-// One block per structure: fixed-order reductions of e_i and the virial.
+// Per-structure sums of e_i and the virial in two fixed-order stages: block
+// (p, s) reduces part p of structure s's atoms (parts chosen from the batch
+// shape, so that a single large cell spreads over many SMs; FP64 adds are
+// slow on this part), then one thread per structure adds its parts in order.
+constexpr int kMaxParts = 64;
+
 __global__ void __launch_bounds__(128)
-    k_struct_reduce(int S, int lgrad, const StructInfo *__restrict__ sinfo,
-                    const double *__restrict__ e, const double *__restrict__ wvir,
-                    double *__restrict__ energy, double *__restrict__ stress,
-                    double *__restrict__ atom_e) {
+    k_struct_partial(int parts, int lgrad, const StructInfo *__restrict__ sinfo,
+                     const double *__restrict__ e, const double *__restrict__ wvir,
+                     double *__restrict__ atom_e, double *__restrict__ part) {
   __shared__ double red[7][128];
-  const int s = blockIdx.x;
-  if (s >= S) return;
+  const int s = blockIdx.y, p = blockIdx.x;
   const int a0 = sinfo[s].a0, na = sinfo[s].na;
+  const int len = (na + parts - 1) / parts;
+  const int beg = p * len, end = min(na, beg + len);
   double acc[7] = {0, 0, 0, 0, 0, 0, 0};
   // upper triangle (a <= b) in the reference's k1 order: 11 12 13 22 23 33
   const int comp[6] = {0, 1, 2, 4, 5, 8};
-  for (int q = threadIdx.x; q < na; q += blockDim.x) {
+  for (int q = beg + threadIdx.x; q < end; q += blockDim.x) {
     const int i = a0 + q;
     acc[0] += e[i];
     if (atom_e) atom_e[i] = e[i];
@@ -99,19 +106,28 @@ __global__ void __launch_bounds__(128)
       for (int c = 0; c < 7; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    energy[s] = red[0][0];
-    double sc[6];
-    const double vol = sinfo[s].volume;
-    for (int c = 0; c < 6; ++c) sc[c] = lgrad ? -red[1 + c][0] * (1.0 / kGPa2eVPang) / vol : 0.0;
-    double *o = stress + (size_t)s * 6;
-    o[0] = sc[0];  // XX
-    o[1] = sc[3];  // YY
-    o[2] = sc[5];  // ZZ
-    o[3] = sc[1];  // XY
-    o[4] = sc[4];  // YZ
-    o[5] = sc[2];  // ZX
-  }
+  if (threadIdx.x < 7) part[((size_t)s * parts + p) * 7 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void k_struct_final(int S, int parts, int lgrad, const StructInfo *__restrict__ sinfo,
+                               const double *__restrict__ part, double *__restrict__ energy,
+                               double *__restrict__ stress) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S) return;
+  double v[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int p = 0; p < parts; ++p)
+    for (int c = 0; c < 7; ++c) v[c] += part[((size_t)s * parts + p) * 7 + c];
+  energy[s] = v[0];
+  double sc[6];
+  const double vol = sinfo[s].volume;
+  for (int c = 0; c < 6; ++c) sc[c] = lgrad ? -v[1 + c] * (1.0 / kGPa2eVPang) / vol : 0.0;
+  double *o = stress + (size_t)s * 6;
+  o[0] = sc[0];  // XX
+  o[1] = sc[3];  // YY
+  o[2] = sc[5];  // ZZ
+  o[3] = sc[1];  // XY
+  o[4] = sc[4];  // YZ
+  o[5] = sc[2];  // ZX
 }
 
 }  // namespace
@@ -133,9 +149,13 @@ void launch_forces(Workspace &ws, int N, int cap, double *d_force, cudaStream_t 
 
 void launch_struct_reduce(Workspace &ws, int S, int lgrad, double *d_energy, double *d_stress,
                           double *d_atom_e, int N, cudaStream_t st) {
-  (void)N;
-  k_struct_reduce<<<S, 128, 0, st>>>(S, lgrad, ws.sinfo, ws.e, ws.wvir, d_energy, d_stress,
-                                      d_atom_e);
+  // about 2048 atoms per part for the mean structure size, at most kMaxParts
+  const long per = S > 0 ? (long)N / S : 0;
+  const int parts = (int)std::max(1L, std::min((long)kMaxParts, per / 2048));
+  k_struct_partial<<<dim3(parts, S), 128, 0, st>>>(parts, lgrad, ws.sinfo, ws.e, ws.wvir,
+                                                    d_atom_e, ws.red_part);
+  k_struct_final<<<(S + 127) / 128, 128, 0, st>>>(S, parts, lgrad, ws.sinfo, ws.red_part,
+                                                   d_energy, d_stress);
 }
 
 template void launch_forces<double>(Workspace &, int, int, double *, cudaStream_t);

@@ -97,6 +97,24 @@ def test_neighbours_bit_exact_alloy512(gapgb_mod, oracle_mod, synth_pop):
     m.close()
 
 
+def test_neighbours_bit_exact_binned_cell(gapgb_mod, oracle_mod):
+    """A cell of >= 2048 atoms takes the binned build (27 bins around each
+    atom, hits sorted into the reference's order); its list must equal the
+    oracle's O(N^2) scan bit for bit, including atoms jittered out of the cell."""
+    import gapgb.synth as S
+    lat, pos, z = S.sige(seed=2, reps=8, jitter=0.3)
+    pos = pos.copy()
+    pos[:5] -= lat[0] * 0.02  # a few atoms outside the cell
+    zt, wt = S.species_table(z)
+    m = gapgb_mod.GapModel.create(zt, wt, [1], [0.5], [6.0], np.ones(2), np.zeros((1, 2)),
+                                  np.zeros(1))
+    gcnt, gnb = m.neighbors(z, lat, pos, cap=128)
+    w = dict(zip(zt.tolist(), wt.tolist()))
+    ocnt, onb = oracle_mod.neighbors(lat, pos, np.array([w[v] for v in z]), 6.0, 128)
+    _assert_nbr_equal(gcnt, gnb, ocnt, onb)
+    m.close()
+
+
 # ---------------------------------------------------------------- descriptors
 
 def test_descriptors_match_oracle(synth_si, oracle_mod):
