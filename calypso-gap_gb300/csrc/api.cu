@@ -372,7 +372,8 @@ gapgb_status eval_host(gapgb_model *m, int S, const int *atom_off, const int *sp
     const int maxa = max_struct_atoms(S, atom_off);
     launch_prep(m, ws, S, N, ws.d_atom_off, ws.d_species, ws.d_lat, ws.d_pos, m->host.rcut, s,
                 maxa >= kBinMinAtoms);
-    launch_neighbors(ws, S, N, maxa, cap, m->host.rcut, s);
+    launch_neighbors(ws, S, N, maxa, cap, m->host.rcut, s,
+                     m->precision == GAPGB_PREC_FP64 || d_G_out != nullptr);
     GAPGB_CUDA_TRY(cudaGetLastError());
     GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.h_flags, ws.d_flags, 8 * sizeof(int), cudaMemcpyDeviceToHost, s));
     GAPGB_CUDA_TRY(cudaStreamSynchronize(s));
@@ -442,8 +443,8 @@ gapgb_status md_eval_enqueue(gapgb_model *m, int S, int N, const int *d_atom_off
   const double rb = m->host.rcut + skin;
   GAPGB_CUDA_TRY(cudaMemsetAsync(ws.d_flags + 1, 0, 2 * sizeof(int), s));
   launch_prep(m, ws, S, N, d_atom_off, d_species, d_lat, d_pos, rb, s, rebuild && N >= kBinMinAtoms);
-  if (rebuild) launch_neighbors(ws, S, N, N, m->cap, rb, s);
-  else launch_refresh(ws, N, m->cap, s);
+  if (rebuild) launch_neighbors(ws, S, N, N, m->cap, rb, s, m->precision == GAPGB_PREC_FP64);
+  else launch_refresh(ws, N, m->cap, s, m->precision == GAPGB_PREC_FP64);
   return enqueue_tail(m, S, N, m->cap, m->cap, 1, d_species, d_energy, d_force, d_stress, nullptr,
                       s);
 }
@@ -689,7 +690,8 @@ gapgb_status gapgb_eval_batch_device(gapgb_model *m, int nstruct, int natoms, in
   const int maxa = max_atoms > 0 ? max_atoms : natoms;
   launch_prep(m, ws, nstruct, natoms, d_atom_off, d_species, d_lat, d_pos, m->host.rcut, s,
               maxa >= kBinMinAtoms);
-  launch_neighbors(ws, nstruct, natoms, maxa, cap, m->host.rcut, s);
+  launch_neighbors(ws, nstruct, natoms, maxa, cap, m->host.rcut, s,
+                   m->precision == GAPGB_PREC_FP64);
   double *d_stress_use = d_stress ? d_stress : ws.d_stress;
   double *d_force_use = d_force ? d_force : ws.d_force;
   return enqueue_tail(m, nstruct, natoms, cap, cap, lgrad, d_species, d_energy, d_force_use,

@@ -325,10 +325,13 @@ void set_last_error(const std::string &s);
 void launch_prep(const gapgb_model *m, Workspace &ws, int S, int N, const int *d_atom_off,
                  const int *d_species, const double *d_lat, const double *d_pos,
                  double rcut, cudaStream_t st, bool allow_bins = false);
+// exact: the reference's bit-identical list (FP64 path, neighbour export);
+// otherwise the FP32 forms' cheaper geometry (same pairs up to last-bit
+// decisions at r = rcut, where every term vanishes)
 void launch_neighbors(Workspace &ws, int S, int N, int max_atoms, int cap, double rcut,
-                      cudaStream_t st);
+                      cudaStream_t st, bool exact = true);
 void launch_reverse(Workspace &ws, int N, int cap, cudaStream_t st);
-void launch_refresh(Workspace &ws, int N, int cap, cudaStream_t st);
+void launch_refresh(Workspace &ws, int N, int cap, cudaStream_t st, bool exact = true);
 template <typename T>
 void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int cap_smem,
                       cudaStream_t st);

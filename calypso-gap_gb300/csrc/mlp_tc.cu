@@ -54,6 +54,8 @@ constexpr int kOffW2T = kOffW2 + kW2Bytes;
 constexpr int kOffW1T = kOffW2T + kW2Bytes;
 constexpr int kOffA = (kOffW1 + kWImg + 1023) / 1024 * 1024;  // a1, then d1 (128 x 128)
 constexpr int kOffDd = kOffA + kW2Bytes;                       // d2 (128 x 128)
+constexpr int kPitch = kDp + 1;                                // dy/dx staging pitch (floats)
+static_assert(kR * kPitch * 4 <= 2 * kW2Bytes, "dy/dx staging fits the A and Dd tiles");
 constexpr int kOffY = kOffDd + kW2Bytes;                       // partial y [2][128]
 constexpr int kOffBar = kOffY + 2 * kR * 4;
 constexpr int kMlpSmem = kOffBar + 64 + 1024;
@@ -318,24 +320,21 @@ __global__ void __launch_bounds__(kThreads, 1) k_mlp_tc(MlpTcArgs a) {
     // GEMM4 and epilogue 4: dy/dx, this thread's 32 components
     gemm(tG, kOffA, kOffW1T, kHid / 8, kHid / 16, id64);
     if (!ok) break;
-    // the tile's dy/dx rows go through shared memory (the Dd tile is free
-    // after GEMM3) and leave as contiguous 16-byte stores
+    // the tile's dy/dx rows go through shared memory (the A and Dd tiles are
+    // free after GEMM4) with a row pitch of 65 floats, so the row-per-lane
+    // writes and the coalesced read-out are both free of bank conflicts
     float gv[32];
     tmem_ld32(tG + lane_base + half * 32, gv);
-    float *stage = reinterpret_cast<float *>(sm + kOffDd);  // [128][a.D] row-major
+    float *stage = reinterpret_cast<float *>(sm + kOffA);  // [128][kPitch]
 #pragma unroll
-    for (int d = 0; d < 32; ++d)
-      if (half * 32 + d < a.D) stage[r * a.D + half * 32 + d] = gv[d];
+    for (int d = 0; d < 32; ++d) stage[r * kPitch + half * 32 + d] = gv[d];
     __syncthreads();
     {
       const size_t base = ((size_t)q * a.Mpad + (size_t)t * kR) * a.D;
       const int n = kR * a.D;  // floats of the tile (rows t*128 .. t*128 + 127)
-      if ((a.D & 3) == 0) {
-        const float4 *src = reinterpret_cast<const float4 *>(stage);
-        float4 *dst = reinterpret_cast<float4 *>(a.gx + base);
-        for (int k = tid; k < n / 4; k += kThreads) dst[k] = src[k];
-      } else {
-        for (int k = tid; k < n; k += kThreads) a.gx[base + k] = stage[k];
+      for (int k = tid; k < n; k += kThreads) {
+        const int rr = k / a.D, d = k - rr * a.D;
+        a.gx[base + k] = stage[rr * kPitch + d];
       }
     }
     buf ^= 1;

@@ -249,6 +249,21 @@ __device__ __forceinline__ double ref_image(const double4 &pi, const double4 &pj
                               __dmul_rn(dr[2], dr[2])));
 }
 
+// FP32 forms of the evaluation: relative vector d = (p_j - p_i) + n L with
+// FP64 fused multiply-adds (12 FP64 operations instead of the reference
+// formula's ~40 with the square root), rounded once to FP32; the cutoff test
+// runs on the FP32 squared length.  The reverse pair's vector is the exact
+// negation, so both members of a pair agree.  Only where bit-identical
+// lists are not required (fc and fc' vanish at the cutoff).
+__device__ __forceinline__ float4 fast_rel(const double4 &pi, const double4 &pj, const double *L,
+                                           double dn1, double dn2, double dn3) {
+  const double p[3] = {pj.x - pi.x, pj.y - pi.y, pj.z - pi.z};
+  float d[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) d[k] = d2f_rn(fma(dn1, L[k], fma(dn2, L[3 + k], fma(dn3, L[6 + k], p[k]))));
+  return make_float4(d[0], d[1], d[2], d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+}
+
 __device__ __forceinline__ void image_box(const float ext[3], const int nabc[3], const float4 &fi,
                                           const float4 &fj, int lo[3], int hi[3]) {
   const float d[3] = {fj.x - fi.x, fj.y - fi.y, fj.z - fi.z};
@@ -274,6 +289,7 @@ __device__ __forceinline__ float screen_r2(const float *L32, const float fd[3], 
 
 constexpr int kQueue = 256;  // survivors per warp per exact-test round
 
+template <bool EXACT>
 __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
                                                    const double4 *__restrict__ apos,
                                                    const float4 *__restrict__ frac32,
@@ -307,6 +323,7 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
     // FP32 screen bound: rcut plus the fractional rounding margin in Angstrom
     const float rs = (float)rcut + 2.5e-4f * lsum + 1e-3f;
     const float r2max = rs * rs;
+    const float rc2f = (float)(rcut * rcut);
     const float ext[3] = {(float)si.ext[0], (float)si.ext[1], (float)si.ext[2]};
     double4 *oxyz = xyzr + (size_t)i * cap;
     int *oj = nj + (size_t)i * cap;
@@ -326,6 +343,7 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
         bool hit = false;
         double xyz[3] = {0, 0, 0};
         double dis = 0;
+        float4 fr = make_float4(0.f, 0.f, 0.f, 0.f);
         int jj = 0, sh = 0;
         if (t < qt) {
           const int e = t & (kQueue - 1);
@@ -333,21 +351,31 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
           sh = qs[e];
           const int n1 = ((sh >> 16) & 255) - 128, n2 = ((sh >> 8) & 255) - 128,
                     n3 = (sh & 255) - 128;
-          dis = ref_image(pi, apos[jj], si.lat, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
-                          s_dn[n3 + kMaxImage], xyz);
-          hit = !(dis > rcut);
+          if (EXACT) {
+            dis = ref_image(pi, apos[jj], si.lat, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
+                            s_dn[n3 + kMaxImage], xyz);
+            hit = !(dis > rcut);
+          } else {
+            fr = fast_rel(pi, apos[jj], si.lat, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
+                          s_dn[n3 + kMaxImage]);
+            hit = fr.w <= rc2f;
+          }
         }
         __syncwarp();
         const unsigned m = __ballot_sync(0xffffffffu, hit);
         const int q = total + __popc(m & lt_mask);
         if (hit && q < cap) {
-          oxyz[q] = make_double4(xyz[0], xyz[1], xyz[2], dis);
           oj[q] = jj;
           os[q] = sh;
-          // FP32 record for the FP32 kernels: deltaxj = xyz - pos(i)
-          // (wacsf.f90:90) in FP64, rounded once to FP32
-          od[q] = make_float4(d2f_rn(xyz[0] - pi.x), d2f_rn(xyz[1] - pi.y),
-                              d2f_rn(xyz[2] - pi.z), d2f_rn(dis));
+          if (EXACT) {
+            oxyz[q] = make_double4(xyz[0], xyz[1], xyz[2], dis);
+            // FP32 record for the FP32 kernels: deltaxj = xyz - pos(i)
+            // (wacsf.f90:90) in FP64, rounded once to FP32
+            od[q] = make_float4(d2f_rn(xyz[0] - pi.x), d2f_rn(xyz[1] - pi.y),
+                                d2f_rn(xyz[2] - pi.z), d2f_rn(dis));
+          } else {
+            od[q] = make_float4(fr.x, fr.y, fr.z, sqrtf(fr.w));
+          }
           ow[q] = frac32[jj].w;
         }
         total += __popc(m);
@@ -424,6 +452,7 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
 // reference's order - before they are written, so the list is identical to
 // the O(na) scan's.  The image of candidate j is n = s - m_j + m_i, with s the
 // bin-wrap shift and m the atoms' own wrap shifts.
+template <bool EXACT>
 __global__ void __launch_bounds__(128) k_nbr_build_binned(
     int N, int cap, int hit_cap, double rcut, const double4 *__restrict__ apos,
     const float4 *__restrict__ frac32, const int *__restrict__ atom_struct,
@@ -461,6 +490,7 @@ __global__ void __launch_bounds__(128) k_nbr_build_binned(
     }
     const float rs = (float)rcut + 2.5e-4f * lsum + 1e-3f;
     const float r2max = rs * rs;
+    const float rc2f = (float)(rcut * rcut);
     const int mi = atom_m[i];
     const int mi3[3] = {((mi >> 16) & 255) - 128, ((mi >> 8) & 255) - 128, (mi & 255) - 128};
     const int local = atom_bin[i] - si.bin0;
@@ -496,11 +526,18 @@ __global__ void __launch_bounds__(128) k_nbr_build_binned(
             const float4 fj = frac32[j];
             const float fd[3] = {fj.x - fi.x, fj.y - fi.y, fj.z - fi.z};
             if (screen_r2(L32, fd, n1, n2, n3) <= r2max) {
-              double xyz[3];
-              const double dis = ref_image(pi, apos[j], si.lat, s_dn[n1 + kMaxImage],
-                                           s_dn[n2 + kMaxImage], s_dn[n3 + kMaxImage], xyz);
-              hit = !(dis > rcut);
-              rec = make_double4(xyz[0], xyz[1], xyz[2], dis);
+              if (EXACT) {
+                double xyz[3];
+                const double dis = ref_image(pi, apos[j], si.lat, s_dn[n1 + kMaxImage],
+                                             s_dn[n2 + kMaxImage], s_dn[n3 + kMaxImage], xyz);
+                hit = !(dis > rcut);
+                rec = make_double4(xyz[0], xyz[1], xyz[2], dis);
+              } else {
+                const float4 fr = fast_rel(pi, apos[j], si.lat, s_dn[n1 + kMaxImage],
+                                           s_dn[n2 + kMaxImage], s_dn[n3 + kMaxImage]);
+                hit = fr.w <= rc2f;
+                *reinterpret_cast<float4 *>(&rec) = fr;  // FP32 record in the slot's bytes
+              }
               key = ((unsigned long long)j << 24) |
                     (unsigned long long)(((n1 + 128) << 16) | ((n2 + 128) << 8) | (n3 + 128));
             }
@@ -549,11 +586,16 @@ __global__ void __launch_bounds__(128) k_nbr_build_binned(
       const unsigned long long key = keys[q];
       const double4 rec = recs[order[q]];
       const int j = (int)(key >> 24);
-      oxyz[q] = rec;
       nj[(size_t)i * cap + q] = j;
       ns[(size_t)i * cap + q] = (int)(key & 0xFFFFFFull);
-      d32[(size_t)i * cap + q] = make_float4(d2f_rn(rec.x - pi.x), d2f_rn(rec.y - pi.y),
-                                             d2f_rn(rec.z - pi.z), d2f_rn(rec.w));
+      if (EXACT) {
+        oxyz[q] = rec;
+        d32[(size_t)i * cap + q] = make_float4(d2f_rn(rec.x - pi.x), d2f_rn(rec.y - pi.y),
+                                               d2f_rn(rec.z - pi.z), d2f_rn(rec.w));
+      } else {
+        const float4 fr = *reinterpret_cast<const float4 *>(&rec);
+        d32[(size_t)i * cap + q] = make_float4(fr.x, fr.y, fr.z, sqrtf(fr.w));
+      }
       w32[(size_t)i * cap + q] = frac32[j].w;
     }
     if (lane == 0) {
@@ -609,6 +651,7 @@ __global__ void k_nbr_reverse(int N, int cap, const int *__restrict__ cnt,
 // formula.  Slots now beyond an SF cutoff contribute exactly zero in every
 // descriptor kernel, so the result equals a fresh build's up to summation
 // order.  One thread per slot.
+template <bool EXACT>
 __global__ void k_nbr_refresh(int N, int cap, const int *__restrict__ cnt,
                               const int *__restrict__ nj, const int *__restrict__ ns,
                               const double4 *__restrict__ apos,
@@ -627,12 +670,18 @@ __global__ void k_nbr_refresh(int N, int cap, const int *__restrict__ cnt,
     const int n1 = ((sh >> 16) & 255) - 128, n2 = ((sh >> 8) & 255) - 128, n3 = (sh & 255) - 128;
     const double4 pi = apos[i];
     const double *L = sinfo[atom_struct[i]].lat;
-    double xyz[3];
-    const double dis = ref_image(pi, apos[j], L, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
-                                 s_dn[n3 + kMaxImage], xyz);
-    xyzr[idx] = make_double4(xyz[0], xyz[1], xyz[2], dis);
-    d32[idx] = make_float4(d2f_rn(xyz[0] - pi.x), d2f_rn(xyz[1] - pi.y), d2f_rn(xyz[2] - pi.z),
-                           d2f_rn(dis));
+    if (EXACT) {
+      double xyz[3];
+      const double dis = ref_image(pi, apos[j], L, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
+                                   s_dn[n3 + kMaxImage], xyz);
+      xyzr[idx] = make_double4(xyz[0], xyz[1], xyz[2], dis);
+      d32[idx] = make_float4(d2f_rn(xyz[0] - pi.x), d2f_rn(xyz[1] - pi.y),
+                             d2f_rn(xyz[2] - pi.z), d2f_rn(dis));
+    } else {
+      const float4 fr = fast_rel(pi, apos[j], L, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
+                                 s_dn[n3 + kMaxImage]);
+      d32[idx] = make_float4(fr.x, fr.y, fr.z, sqrtf(fr.w));
+    }
   }
 }
 
@@ -696,8 +745,10 @@ void launch_prep(const gapgb_model *m, Workspace &ws, int S, int N, const int *d
 }
 
 void launch_neighbors(Workspace &ws, int S, int N, int max_atoms, int cap, double rcut,
-                      cudaStream_t st) {
-  k_nbr_build<<<grid_for_warps(N), 32 * kWarpsPerBlock, 0, st>>>(
+                      cudaStream_t st, bool exact) {
+  auto build = exact ? k_nbr_build<true> : k_nbr_build<false>;
+  auto build_binned = exact ? k_nbr_build_binned<true> : k_nbr_build_binned<false>;
+  build<<<grid_for_warps(N), 32 * kWarpsPerBlock, 0, st>>>(
       N, cap, rcut, ws.apos, ws.frac32, ws.atom_struct, ws.sinfo, ws.nbr_cnt, ws.nbr_xyz,
       ws.nbr_j, ws.nbr_s, ws.nbr_d32, ws.nbr_w32, ws.d_flags);
   if (max_atoms < kBinMinAtoms) return;  // no structure was binned (launch_prep)
@@ -715,22 +766,23 @@ void launch_neighbors(Workspace &ws, int S, int N, int max_atoms, int cap, doubl
   int hit_cap = 32;
   while (hit_cap < cap && hit_cap < 1024) hit_cap <<= 1;
   const size_t smem = (size_t)kWarpsPerBlock * hit_cap * (8 + 32 + 4);
-  cudaFuncSetAttribute(k_nbr_build_binned, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_nbr_build_binned<<<grid_for_warps(N), 32 * kWarpsPerBlock, smem, st>>>(
+  cudaFuncSetAttribute(build_binned, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  build_binned<<<grid_for_warps(N), 32 * kWarpsPerBlock, smem, st>>>(
       N, cap, hit_cap, rcut, ws.apos, ws.frac32, ws.atom_struct, ws.sinfo, ws.bin_start,
       ws.bin_atoms, ws.atom_bin, ws.atom_m, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j, ws.nbr_s,
       ws.nbr_d32, ws.nbr_w32, ws.d_flags);
 }
 
-void launch_refresh(Workspace &ws, int N, int cap, cudaStream_t st) {
+void launch_refresh(Workspace &ws, int N, int cap, cudaStream_t st, bool exact) {
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const size_t total = (size_t)N * cap;
   const size_t want = (total + 255) / 256;
   const int grid = (int)std::min<size_t>(want > 0 ? want : 1, (size_t)sms * 8);
-  k_nbr_refresh<<<grid, 256, 0, st>>>(N, cap, ws.nbr_cnt, ws.nbr_j, ws.nbr_s, ws.apos,
-                                      ws.atom_struct, ws.sinfo, ws.nbr_xyz, ws.nbr_d32);
+  auto fn = exact ? k_nbr_refresh<true> : k_nbr_refresh<false>;
+  fn<<<grid, 256, 0, st>>>(N, cap, ws.nbr_cnt, ws.nbr_j, ws.nbr_s, ws.apos, ws.atom_struct,
+                           ws.sinfo, ws.nbr_xyz, ws.nbr_d32);
 }
 
 void launch_reverse(Workspace &ws, int N, int cap, cudaStream_t st) {

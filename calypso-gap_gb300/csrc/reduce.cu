@@ -27,21 +27,25 @@ __global__ void __launch_bounds__(128)
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
+  // accumulation type: FP64 for the FP64 path, FP32 for the FP32 forms
+  // (FP64 adds and conversions run on the narrow FP64 pipe; a per-atom force
+  // is a sum of ~2P slot terms, far inside FP32's precision needs here)
+  using A = T;
   for (int j = gw; j < N; j += nw) {
     const int P = cnt[j];
-    double fx = 0, fy = 0, fz = 0;
+    A fx = 0, fy = 0, fz = 0;
     for (int q = lane; q < P; q += 32) {
       const size_t idx = (size_t)j * cap + q;
       const auto g = gslot[idx];
-      fx += (double)g.x;
-      fy += (double)g.y;
-      fz += (double)g.z;
+      fx += (A)g.x;
+      fy += (A)g.y;
+      fz += (A)g.z;
       const int r = rev[idx];
       if (r >= 0) {
         const auto h = gslot[(size_t)nj[idx] * cap + r];
-        fx -= (double)h.x;
-        fy -= (double)h.y;
-        fz -= (double)h.z;
+        fx -= (A)h.x;
+        fy -= (A)h.y;
+        fz -= (A)h.z;
       }
     }
 #pragma unroll
@@ -51,9 +55,9 @@ __global__ void __launch_bounds__(128)
       fz += __shfl_xor_sync(0xffffffffu, fz, off);
     }
     if (lane == 0) {
-      force[(size_t)j * 3 + 0] = fx;
-      force[(size_t)j * 3 + 1] = fy;
-      force[(size_t)j * 3 + 2] = fz;
+      force[(size_t)j * 3 + 0] = (double)fx;
+      force[(size_t)j * 3 + 1] = (double)fy;
+      force[(size_t)j * 3 + 2] = (double)fz;
     }
   }
 }
