@@ -57,9 +57,9 @@ constexpr int kOffMh = kOffImg;
 constexpr int kOffMl = kOffMh + kTileBytes16;
 constexpr int kOffMhT = kOffMl + kTileBytes16;
 constexpr int kOffMlT = kOffMhT + kTileBytes16;
-constexpr int kOffMn = kOffMlT + kTileBytes16;
-constexpr int kOffC = kOffMn + kTileK * 4;
-constexpr int kOffWh = kOffImg + kImgTile;
+constexpr int kOffMnc = kOffMlT + kTileBytes16;          // |m''|^2 and c, two tiles
+constexpr int kMncBytes = 2 * kTileK * 4;                 // one tile's mn and c
+constexpr int kOffWh = kOffMnc + 2 * kMncBytes;
 constexpr int kOffWl = kOffWh + kWBytes;
 constexpr int kOffBar = kOffWl + kWBytes;                 // 3 mbarriers + tmem base
 constexpr int kOffEp = kOffBar + 64;                      // partial energies [128] (FP64)
@@ -77,7 +77,9 @@ __global__ void __launch_bounds__(kGprThreads, 1)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int quad = warp & 3, half = warp >> 2;  // TMEM lane quadrant, column half
   const uint32_t s_base = smem_u32(sm);
-  const uint32_t bar_load = s_base + kOffBar, bar_g1 = bar_load + 8, bar_g2 = bar_load + 16;
+  // bar_a: atoms (first tile), mh / ml and mn / c of a tile; bar_b: mhT / mlT
+  const uint32_t bar_a = s_base + kOffBar, bar_g1 = bar_a + 8, bar_g2 = bar_a + 16,
+                 bar_b = bar_a + 24;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + kOffBar + 32);
   int *abort_flag = reinterpret_cast<int *>(sm + kOffBar + 40);
   if (warp == 0) {
@@ -87,9 +89,10 @@ __global__ void __launch_bounds__(kGprThreads, 1)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    mbar_init(bar_load, 1);
+    mbar_init(bar_a, 1);
     mbar_init(bar_g1, 1);
     mbar_init(bar_g2, 1);
+    mbar_init(bar_b, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -104,20 +107,43 @@ __global__ void __launch_bounds__(kGprThreads, 1)
   const float xnorm = (i < N) ? xn[i] : 0.f;
   float ehi = 0.f, elo = 0.f;
   const uint32_t id1 = instr_desc(kRows, kTileK), id2 = instr_desc(kRows, kDP);
-  uint32_t ph_load = 0, ph_g1 = 0, ph_g2 = 0;
+  uint32_t ph_a = 0, ph_b = 0, ph_g1 = 0, ph_g2 = 0;
+  bool pend_a = false, pend_b = false, pend_g1 = false, pend_g2 = false;
   bool ok = true;
-  const float *smn = reinterpret_cast<const float *>(sm + kOffMn);
-  const float *sc = reinterpret_cast<const float *>(sm + kOffC);
-  for (int t = 0; t < ntiles && ok; ++t) {
+  // two-stage copy pipeline: a tile's GEMM1 operands (mh, ml, mn, c) load
+  // while the previous tile's epilogue and GEMM2 run, its GEMM2 operands
+  // (mhT, mlT) while its own GEMM1 and epilogue run
+  auto load_a = [&](int t, bool first) {
     if (tid == 0) {
-      const uint32_t bytes = kImgTile + (t == 0 ? kImgAtoms : 0);
-      mbar_expect_tx(bar_load, bytes);
-      if (t == 0)
-        bulk_g2s(s_base + kOffXh, img_atoms + (size_t)blockIdx.x * kImgAtoms, kImgAtoms, bar_load);
-      bulk_g2s(s_base + kOffImg, img_model + (size_t)t * kImgTile, kImgTile, bar_load);
+      const unsigned char *img = img_model + (size_t)t * kImgTile;
+      mbar_expect_tx(bar_a, 2 * kTileBytes16 + kMncBytes + (first ? kImgAtoms : 0));
+      if (first)
+        bulk_g2s(s_base + kOffXh, img_atoms + (size_t)blockIdx.x * kImgAtoms, kImgAtoms, bar_a);
+      bulk_g2s(s_base + kOffMh, img, 2 * kTileBytes16, bar_a);
+      bulk_g2s(s_base + kOffMnc + (t & 1) * kMncBytes, img + 4 * kTileBytes16, kMncBytes, bar_a);
     }
-    ok = mbar_wait(bar_load, ph_load, flags);
-    ph_load ^= 1;
+    pend_a = true;
+  };
+  auto load_b = [&](int t) {
+    if (tid == 0) {
+      mbar_expect_tx(bar_b, 2 * kTileBytes16);
+      bulk_g2s(s_base + kOffMhT, img_model + (size_t)t * kImgTile + 2 * kTileBytes16,
+               2 * kTileBytes16, bar_b);
+    }
+    pend_b = true;
+  };
+  if (ntiles > 0) {
+    load_a(0, true);
+    load_b(0);
+  }
+  for (int t = 0; t < ntiles && ok; ++t) {
+    const float *smn = reinterpret_cast<const float *>(sm + kOffMnc + (t & 1) * kMncBytes);
+    const float *sc = smn + kTileK;
+    ok = mbar_wait(bar_a, ph_a, flags);
+    if (ok) {
+      ph_a ^= 1;
+      pend_a = false;
+    }
     if (!__syncthreads_and(ok)) break;
     // GEMM1: C1[128 x 128] = xh.mh + xh.ml + xl.mh over K = 64 (4 steps of 16)
     if (tid == 0) {
@@ -132,10 +158,16 @@ __global__ void __launch_bounds__(kGprThreads, 1)
         }
       umma_commit(bar_g1);
     }
+    pend_g1 = true;
     ok = mbar_wait(bar_g1, ph_g1, flags);
-    ph_g1 ^= 1;
+    if (ok) {
+      ph_g1 ^= 1;
+      pend_g1 = false;
+    }
     if (!__syncthreads_and(ok)) break;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // mh / ml are free again: the next tile's GEMM1 operands start loading
+    if (t + 1 < ntiles) load_a(t + 1, false);
     // epilogue 1: w = c exp(-s/2), e += w, W tile (bf16 hi / lo) for GEMM2
     unsigned char *wh = sm + kOffWh, *wl = sm + kOffWl;
 #pragma unroll 1
@@ -171,8 +203,13 @@ __global__ void __launch_bounds__(kGprThreads, 1)
       }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    ok = mbar_wait(bar_b, ph_b, flags);
+    if (ok) {
+      ph_b ^= 1;
+      pend_b = false;
+    }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
+    if (!__syncthreads_and(ok)) break;
     // GEMM2: C2[128 x 64] += wh.mhT + wh.mlT + wl.mhT over K = 128 (8 steps of 16)
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -186,9 +223,14 @@ __global__ void __launch_bounds__(kGprThreads, 1)
         }
       umma_commit(bar_g2);
     }
+    pend_g2 = true;
     ok = mbar_wait(bar_g2, ph_g2, flags);  // operands are overwritten next tile
-    ph_g2 ^= 1;
+    if (ok) {
+      ph_g2 ^= 1;
+      pend_g2 = false;
+    }
     ok = __syncthreads_and(ok);
+    if (ok && t + 1 < ntiles) load_b(t + 1);
   }
   if (ok) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -213,9 +255,10 @@ __global__ void __launch_bounds__(kGprThreads, 1)
   } else if (tid == 0) {
     // a wait gave up: give the outstanding copy / MMA phases one more bounded
     // wait before the tensor memory and shared memory are released
-    mbar_wait(bar_load, ph_load, flags);
-    mbar_wait(bar_g1, ph_g1, flags);
-    mbar_wait(bar_g2, ph_g2, flags);
+    if (pend_a) mbar_wait(bar_a, ph_a, flags);
+    if (pend_b) mbar_wait(bar_b, ph_b, flags);
+    if (pend_g1) mbar_wait(bar_g1, ph_g1, flags);
+    if (pend_g2) mbar_wait(bar_g2, ph_g2, flags);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
