@@ -383,7 +383,8 @@ def run_population(args):
                        "autotuned": {k: best[k] for k in ("precision", "generic_kernels", "cap")},
                        "tune_errors": {"dE_per_atom": best["dE_per_atom"], "dF": best["dF"]},
                        "l2": "flushed between steps (512 MB write)"},
-            "gpu_launches": args.steps}
+            # one graph launch per step holding the 12 kernels of an evaluation
+            "gpu_launches": 12 * args.steps}
     print(json.dumps(line), flush=True)
     g.close()
     m.close()
@@ -584,10 +585,10 @@ def run_surrogate(args):
     except Exception as ex:  # the oracle is a checker; its absence does not stop the bench
         oracle_err = {"unavailable": str(ex)[:200]}
     # kernels per surrogate evaluation: prep x2, neighbours, reverse, descriptors,
-    # surrogate (count, segments, scatter, gather, 4 GEMMs, 2 bias, output, dsilu,
-    # committee), fallback select, row-list GPR + reduce, slot gradients,
-    # forces, orphans, structure reduce
-    launches_per_eval = 25
+    # surrogate (count, segments, scatter, weight image, row image, tensor-core
+    # MLP, committee), fallback select, row-list GPR + reduce, slot gradients,
+    # forces, orphans, structure partial + final sums
+    launches_per_eval = 20
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
             "steps": len(chunks), "warmup": max(3, args.warmup),
             "ms_per_step": ms_total / len(chunks), "higher_is_better": True,
@@ -712,10 +713,13 @@ def run_md(args):
                 "t_end": {"dE_per_atom": float(abs(Et[0] - Ep[0]) / N),
                           "dF_max": float(np.abs(Ft - Fp).max()),
                           "dstress_max_GPa": float(np.abs(St - Sp).max())}},
-            # per step: kick+drift, wrap or skin check, prep x2, build or refresh,
-            # reverse, descriptors, tensor-core GPR (prep + kernel), slot gradients,
-            # forces, orphans, structure reduce, kick, kinetic energy
-            "gpu_launches": 15 * args.md_steps, "clocks": tc["clocks"]}
+            # per step: kick+drift, wrap or skin check, prep x2, refresh, reverse,
+            # descriptors, tensor-core GPR (prep + kernel), slot gradients, forces,
+            # orphans, structure sums x2, kick, kinetic sums x2 = 17; a rebuild
+            # step adds the build, the bins (offsets, count, scan, fill) and the
+            # binned build in place of the refresh (+5)
+            "gpu_launches": 17 * args.md_steps + 5 * (args.md_steps // 10),
+            "clocks": tc["clocks"]}
     print(json.dumps(line), flush=True)
 
 
@@ -888,10 +892,11 @@ def main():
         "gpu_launches": None,
         "clocks": clocks,
     }
-    # kernels launched per step (count from the library's launch sequence)
-    # prep x2, neighbours, reverse, descriptors, GPR (+ split reduce), slot
-    # gradients, forces, orphans, structure reduce
-    line["gpu_launches"] = args.steps * 11
+    # kernels launched per step (count from the library's launch sequence):
+    # prep x2, neighbour build, reverse slots, descriptors, GPR (tensor-core
+    # form: operand prep + kernel; SIMT forms: kernel + split reduce), slot
+    # gradients, forces, orphans, structure partial + final sums
+    line["gpu_launches"] = args.steps * 12
     if world == 1:
         line["cpu_baseline"] = cpu_baseline(arrays)
     print(json.dumps(line), flush=True)
