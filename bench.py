@@ -61,6 +61,8 @@ def parse():
                    help="surrogate workload: training structures (512 atoms each)")
     p.add_argument("--epochs", type=int, default=4, help="surrogate workload: training epochs")
     p.add_argument("--md-steps", type=int, default=100, help="md workload: velocity-Verlet steps")
+    p.add_argument("--md-reps", type=int, default=16,
+                   help="md workload: diamond cells per axis (16: 32768 atoms; smaller for profiling)")
     p.add_argument("--threshold", type=float, default=0.005,
                    help="surrogate workload: committee std (eV) above which an atom takes the GPR")
     return p.parse_args()
@@ -639,9 +641,9 @@ def run_md(args):
     from gapgb.md import MD, masses_of, maxwell_boltzmann
     L = gapgb.load()
     dev = torch.device("cuda", 0)
-    lat, pos, z = S.sige(seed=0)
-    arrays = S.model_from_cells([S.sige(seed=1)], [14, 32], 8000, theta_scale=1.0,
-                                coeff_std=1e-3, seed=0)
+    lat, pos, z = S.sige(seed=0, reps=args.md_reps)
+    arrays = S.model_from_cells([S.sige(seed=1, reps=args.md_reps)], [14, 32], 8000,
+                                theta_scale=1.0, coeff_std=1e-3, seed=0)
     zt, wt, ty, al, rc, ze, theta, mm, coeff = arrays
     N = len(z)
     masses = masses_of(z)
@@ -696,7 +698,8 @@ def run_md(args):
             "steps": args.md_steps, "warmup": 0, "ms_per_step": tc["ms"] / args.md_steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16x3/f32 (tensor-core form)", "data": "synthetic",
-            "config": {"workload": "md: Si/Ge 50/50 diamond 16^3 (32768 atoms), a=5.54, jitter 0.1",
+            "config": {"workload": "md: Si/Ge 50/50 diamond %d^3 (%d atoms), a=5.54, jitter 0.1"
+                                   % (args.md_reps, N),
                        "model": "M=8000, D=64, theta=1 std", "integrator":
                        "NVE velocity Verlet dt=1 fs, 600 K MB start, rebuild every 10 (skin 0.5 A)",
                        "step": "one CUDA graph launch"},
