@@ -73,10 +73,27 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
+def shard_seeds(rank, batch):
+    """Seeds of rank `rank`'s structures: disjoint blocks of `batch` seeds, so
+    N ranks evaluate N x batch different cells (weak scaling, no data-path
+    collective)."""
+    return [100000 + rank * batch + s for s in range(batch)]
+
+
 def workload(rank, batch):
     import gapgb.synth as S
-    structs = [S.alloy512(seed=100000 + rank * batch + s) for s in range(batch)]
+    structs = [S.alloy512(seed=sd) for sd in shard_seeds(rank, batch)]
     return structs, S.pack(structs)
+
+
+def max_over_ranks(x, world, device):
+    """The largest value of x over all ranks (the job's time is its slowest
+    rank's); the only collective of the benchmark."""
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
 
 
 def make_model():
@@ -806,10 +823,7 @@ def main():
         barrier()
         m.check_device_status()
         ms = sum(a.elapsed_time(b) for a, b in evs)
-        t = torch.tensor([ms], dtype=torch.float64, device=dev)
-        if world > 1:
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item()) / steps, summarize_clocks(lines)
+        return max_over_ranks(ms, world, dev) / steps, summarize_clocks(lines)
 
     chosen = new_model(args.precision)
     ms_step, clocks = time_device(chosen, args.steps, args.warmup, sampler=(rank == 0))
@@ -853,10 +867,7 @@ def main():
         t0 = time.perf_counter()
         host_step(chosen)
         t_host += time.perf_counter() - t0
-    t = torch.tensor([t_host / args.steps], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    e2e_s = float(t.item())
+    e2e_s = max_over_ranks(t_host / args.steps, world, dev)
     h2d = off.nbytes + sp.nbytes + lat.nbytes + pos.nbytes
     d2h = S * 8 + N * 3 * 8 + S * 6 * 8
 
