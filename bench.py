@@ -49,12 +49,14 @@ def parse():
     p.add_argument("--batch", type=int, default=64, help="structures per step per GPU")
     p.add_argument("--precision", default="tc", choices=["fp32", "tc", "fp64", "mixed"])
     p.add_argument("--no-oracle", action="store_true", help="skip the oracle error check")
-    p.add_argument("--workload", default="alloy", choices=["alloy", "population", "surrogate", "md"],
+    p.add_argument("--workload", default="alloy", choices=["alloy", "population", "surrogate", "md", "precision"],
                    help="alloy: 512-atom ternary fcc cells (the headline metric); population: "
                         "a ragged structure-search population evaluated by one CUDA graph; "
                         "surrogate: the learned surrogate with GPR fallback on held-out alloy "
                         "cells, after training on GAP labels; md: 32768-atom Si/Ge NVE "
-                        "velocity Verlet, tensor-core form against the plain FP64 path")
+                        "velocity Verlet, tensor-core form against the plain FP64 path; "
+                        "precision: the alloy step in every arithmetic form (FP64, FP32, "
+                        "mixed, TF32, split-BF16x3) with each form's error")
     p.add_argument("--count", type=int, default=8192,
                    help="population size / held-out structures of the surrogate workload")
     p.add_argument("--train-structs", type=int, default=20000,
@@ -743,8 +745,83 @@ def run_md(args):
     print(json.dumps(line), flush=True)
 
 
+def run_precision(args):
+    """Config 2's comparison: the alloy step (64 cells x 512 atoms, M = 4000,
+    D = 64) in every arithmetic form of the contraction - FP64 (plain), FP32
+    SIMT, mixed (FP32 descriptors, FP64 GPR), TF32 tensor cores, split-BF16x3
+    tensor cores - each timed on device-resident inputs (CUDA events, L2
+    flushed) with its error against the FP64 path on every atom and against
+    the CPU oracle on one cell."""
+    import torch
+    import gapgb
+    dev = torch.device("cuda", 0)
+    arrays = make_model()
+    zt, wt, ty, al, rc, ze, theta, mm, coeff = arrays
+    structs, (off, sp, lat, pos) = workload(0, args.batch)
+    S, N = len(structs), int(off[-1])
+    t = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+         for k, v in (("off", off), ("sp", sp), ("lat", lat), ("pos", pos))}
+    E = torch.zeros(S, dtype=torch.float64, device=dev)
+    F = torch.zeros(N, 3, dtype=torch.float64, device=dev)
+    St = torch.zeros(S, 6, dtype=torch.float64, device=dev)
+    AE = torch.zeros(N, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    res, outs = {}, {}
+    for prec in ("fp64", "fp32", "mixed", "tf32", "tc"):
+        m = gapgb.GapModel.create(zt, wt, ty, al, rc, theta, mm, coeff, sf_zeta=ze)
+        m.set_precision(prec)
+        m.set_neighbour_cap(96)
+
+        def step():
+            m.eval_batch_ptrs(S, N, ATOMS, t["off"].data_ptr(), t["sp"].data_ptr(),
+                              t["lat"].data_ptr(), t["pos"].data_ptr(), 1, E.data_ptr(),
+                              F.data_ptr(), St.data_ptr(), AE.data_ptr(), stream.cuda_stream)
+        steps = 2 if prec in ("fp64", "mixed") else args.steps
+        for _ in range(max(3, args.warmup) if steps > 2 else 1):
+            step()
+        torch.cuda.synchronize()
+        m.check_device_status()
+        evs = []
+        for _ in range(steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step()
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        m.check_device_status()
+        ms = sum(a.elapsed_time(b) for a, b in evs) / steps
+        outs[prec] = (AE.cpu().numpy().copy(), F.cpu().numpy().copy(), St.cpu().numpy().copy(),
+                      E.cpu().numpy().copy())
+        res[prec] = {"atoms_per_s": N / (ms * 1e-3), "ms_per_step": ms}
+        m.close()
+    ae0, f0, s0, e0 = outs["fp64"]
+    for prec in res:
+        ae, f, st, e = outs[prec]
+        res[prec]["vs_fp64_path"] = {"dE_per_atom_max": float(np.abs(e - e0).max() / ATOMS),
+                                     "de_atom_max": float(np.abs(ae - ae0).max()),
+                                     "dF_max": float(np.abs(f - f0).max()),
+                                     "dstress_max_GPa": float(np.abs(st - s0).max())}
+    orc = None if args.no_oracle else oracle_errors(
+        arrays, structs, {k: (v[3], v[1], v[2]) for k, v in outs.items()})
+    line = {"metric": METRIC, "value": res["tc"]["atoms_per_s"], "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["tc"]["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16x3/f32", "data": "synthetic",
+            "config": {"workload": "precision forms on alloy512 x %d (D=64, M=4000)" % S,
+                       "atoms": N, "l2": "flushed between steps (512 MB write)"},
+            "forms": res, "errors_vs_oracle": orc,
+            "gpu_launches": 12 * args.steps}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "precision" and args.impl != "reference":
+        run_precision(args)
+        return
     if args.workload == "md" and args.impl != "reference":
         run_md(args)
         return

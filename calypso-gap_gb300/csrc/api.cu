@@ -143,7 +143,7 @@ gapgb_status ensure_ws(gapgb_model *m, int N, int S, int cap) {
     }
   }
   ws.gpr_scratch_size = sc;
-  ws.tc_scratch_size = tc_atom_scratch_bytes(nN);
+  ws.tc_scratch_size = std::max(tc_atom_scratch_bytes(nN), tf32_atom_scratch_bytes(nN));
   if (cudaMalloc(&ws.tc_scratch, ws.tc_scratch_size) != cudaSuccess) {
     free_ws(ws);
     return fail(GAPGB_ERR_ALLOC, "cudaMalloc failed for tensor-core scratch");
@@ -302,6 +302,11 @@ gapgb_status enqueue_tail(gapgb_model *m, int S, int N, int cap, int capS, int l
     gapgb_status s = build_tc_image(m);  // first call only (allocates)
     if (s) return s;
     launch_gpr_tc(m, ws, N, st);
+  }
+  else if (m->precision == GAPGB_PREC_TF32) {
+    gapgb_status s = build_tf32_image(m);  // first call only (allocates)
+    if (s) return s;
+    launch_gpr_tf32(m, ws, N, st);
   }
   else if (fp64) launch_gpr<double, double>(m, ws, N, st);
   else if (m->precision == GAPGB_PREC_MIXED) launch_gpr<double, float>(m, ws, N, st);
@@ -564,6 +569,7 @@ void gapgb_model_free(gapgb_model *m) {
   free_dev(m->fb_count);
   free_dev(m->fb_scratch);
   if (m->d_tc) cudaFree(m->d_tc);
+  if (m->d_tf32) cudaFree(m->d_tf32);
   for (auto &e : m->ev)
     if (e) cudaEventDestroy(e);
   if (m->stream) cudaStreamDestroy(m->stream);
@@ -608,8 +614,10 @@ gapgb_status gapgb_set_option(gapgb_model *m, gapgb_option opt, int64_t value) {
   switch (opt) {
     case GAPGB_OPT_PRECISION:
       if (value != GAPGB_PREC_FP64 && value != GAPGB_PREC_FP32 && value != GAPGB_PREC_MIXED &&
-          value != GAPGB_PREC_TC && value != GAPGB_PREC_SURROGATE)
+          value != GAPGB_PREC_TC && value != GAPGB_PREC_SURROGATE && value != GAPGB_PREC_TF32)
         return fail(GAPGB_ERR_ARG, "unknown precision");
+      if (value == GAPGB_PREC_TF32 && m->host.D > 64)
+        return fail(GAPGB_ERR_CAP_EXCEEDED, "tensor-core GPR supports D <= 64");
       if (value == GAPGB_PREC_SURROGATE && !m->surrogate)
         return fail(GAPGB_ERR_ARG, "attach a surrogate (gapgb_model_set_surrogate) first");
       if (value == GAPGB_PREC_TC && m->host.D > 64)

@@ -293,6 +293,9 @@ struct gapgb_model {
   void *d_tc = nullptr;                // tensor-core operand images (gpr_tc.cu)
   size_t tc_bytes = 0;
   int tc_tiles = 0;
+  void *d_tf32 = nullptr;              // TF32 operand images (gpr_tf32.cu)
+  size_t tf32_bytes = 0;
+  int tf32_tiles = 0;
   int device = 0;
   int precision = GAPGB_PREC_FP64;
   int cap = 256;
@@ -351,6 +354,9 @@ int gpr_nsplit(int N, int M);
 size_t gpr_scratch_bytes(int N, int M, int D, size_t elem);
 gapgb_status build_tc_image(gapgb_model *m);
 size_t tc_atom_scratch_bytes(int N);
+gapgb_status build_tf32_image(gapgb_model *m);
+size_t tf32_atom_scratch_bytes(int N);
+void launch_gpr_tf32(gapgb_model *m, Workspace &ws, int N, cudaStream_t st);
 void launch_gpr_rows(const gapgb_model *m, Workspace &ws, int cap, const int *d_rows,
                      const int *d_count, void *scratch, cudaStream_t st);
 size_t gpr_rows_scratch_bytes(int cap, int D);

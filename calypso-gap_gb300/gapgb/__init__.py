@@ -11,10 +11,10 @@ import numpy as np
 
 from . import build as _build
 
-PREC_FP64, PREC_FP32, PREC_TC, PREC_MIXED, PREC_SURROGATE = 0, 1, 2, 3, 4
+PREC_FP64, PREC_FP32, PREC_TC, PREC_MIXED, PREC_SURROGATE, PREC_TF32 = 0, 1, 2, 3, 4, 5
 OPT_PRECISION, OPT_NEIGHBOUR_CAP, OPT_DEVICE = 0, 1, 2
 PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "tc": PREC_TC, "mixed": PREC_MIXED,
-              "surrogate": PREC_SURROGATE}
+              "surrogate": PREC_SURROGATE, "tf32": PREC_TF32}
 
 STATUS = {
     0: "OK", 1: "ERR_FILE", 2: "ERR_PARSE", 3: "ERR_CAP_EXCEEDED", 4: "ERR_UNKNOWN_SPECIES",

@@ -1,7 +1,8 @@
 """Autotuner for the evaluation configuration of a model on a workload.
 
 For a calibration batch it evaluates every candidate configuration:
-  - precision form: "tc" (tensor-core GPR, D <= 64), "fp32", "mixed";
+  - precision form: "tc" (split-BF16x3 tensor-core GPR, D <= 64), "tf32"
+    (TF32 tensor-core GPR, D <= 64), "fp32", "mixed";
   - descriptor kernel family: grouped register-grid kernels or the generic
     ones (GAPGB_OPT_GENERIC_KERNELS);
   - neighbour capacity: the tight bound (the largest count rounded up to 8)
@@ -67,7 +68,7 @@ def autotune(model, off, species, lat, pos, tol_e=1e-3, tol_f=20e-3, reps=5, cac
     natoms = np.diff(off)
     mx = _max_count(model, off, species, lat, pos)
     caps = sorted({((mx + 7) // 8) * 8, ((int(mx * 1.25) + 7) // 8) * 8})
-    forms = (["tc"] if model.des_len <= 64 else []) + ["fp32", "mixed"]
+    forms = (["tc", "tf32"] if model.des_len <= 64 else []) + ["fp32", "mixed"]
     t_off = torch.from_numpy(off).to(dev)
     t_sp = torch.from_numpy(np.ascontiguousarray(species, np.int32)).to(dev)
     t_lat = torch.from_numpy(np.ascontiguousarray(lat, np.float64)).to(dev)

@@ -49,10 +49,12 @@ typedef enum {
                           accumulate), FP64 energy/virial sums */
   GAPGB_PREC_MIXED = 3, /* FP32 descriptors and gradients, FP64 GPR (for models
                           whose coefficients cancel strongly) */
-  GAPGB_PREC_SURROGATE = 4 /* FP32 descriptors, the attached learned surrogate
+  GAPGB_PREC_SURROGATE = 4, /* FP32 descriptors, the attached learned surrogate
                               for e and dE/dG, FP64 GPR (the mixed form) for
                               the atoms whose committee disagrees; needs
                               gapgb_model_set_surrogate first */
+  GAPGB_PREC_TF32 = 5      /* FP32 descriptors, tensor-core GPR with single
+                              TF32 products and FP32 accumulation; D <= 64 */
 } gapgb_precision;
 
 typedef enum {

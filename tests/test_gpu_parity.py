@@ -457,10 +457,53 @@ def test_tc_matches_fp32_path_alloy(gapgb_mod, oracle_mod, tmp_path):
     m.close()
 
 
+def test_tf32_alloy_and_si_vs_oracle(gapgb_mod, oracle_mod, synth_si, tmp_path):
+    """Single-term TF32 tensor-core GPR (kind::tf32, FP32 accumulation) within the
+    reduced-precision bar, on the alloy model (M = 600) and the Si model."""
+    import gapgb.synth as S
+    path = str(tmp_path / "gp")
+    synth_model_file(path, oracle_mod, [S.alloy512(seed=s) for s in range(2)], M=600,
+                     theta_scale=0.8, coeff_std=1e-2, seed=2)
+    m = gapgb_mod.GapModel.load(path)
+    structs = [S.alloy512(seed=s) for s in (52, 53)]
+    off, sp, lat, pos = S.pack(structs)
+    m.set_precision("tc")
+    Etc, Ftc, Stc = m.eval_batch(off, sp, lat, pos)
+    m.set_precision("tf32")
+    E, F, St = m.eval_batch(off, sp, lat, pos)
+    o = oracle_mod.Model(path)
+    for s_, (l, p, z) in enumerate(structs):
+        oE, oF, oS, _ = oracle_mod.gap_calc(o, z, l, p, 6.0, True)
+        print("tf32 alloy: dE/atom %.3g eV, dF %.3g eV/A; tc: %.3g, %.3g" % (
+            abs(E[s_] - oE) / 512, np.abs(F[512 * s_:512 * (s_ + 1)] - oF).max(),
+            abs(Etc[s_] - oE) / 512, np.abs(Ftc[512 * s_:512 * (s_ + 1)] - oF).max()))
+        assert abs(E[s_] - oE) / 512 <= 1e-3
+        assert np.abs(F[512 * s_:512 * (s_ + 1)] - oF).max() <= 20e-3
+    m.close()
+    # The Si test model is stiff (coefficients ~ N(0, 1): forces ~ 100 eV/A).
+    # Single TF32 products keep 11 significant bits, so the form's error is
+    # relative (~1e-3 of the force scale): inside the absolute bar for the
+    # alloy above, not for forces this large - which the split-BF16x3 form
+    # (~2^-22 relative) handles.  Checked here as a relative bound.
+    g, og = synth_si
+    g.set_precision("tf32")
+    try:
+        si = [S.si64(seed=s) for s in (71, 72)]
+        off, sp, lat, pos = S.pack(si)
+        E, F, St = g.eval_batch(off, sp, lat, pos)
+        for s_, (l, p, z) in enumerate(si):
+            oE, oF, _, _ = oracle_mod.gap_calc(og, z, l, p, 6.0, True)
+            assert abs(E[s_] - oE) / len(p) <= 1e-3
+            assert np.abs(F[off[s_]:off[s_ + 1]] - oF).max() <= 5e-3 * np.abs(oF).max()
+    finally:
+        g.set_precision("fp64")
+
+
 def test_tc_rejects_long_descriptors(golden_model, gapgb_mod):
-    with pytest.raises(gapgb_mod.GapError) as ei:
-        golden_model.set_precision("tc")
-    assert ei.value.status == 3
+    for prec in ("tc", "tf32"):
+        with pytest.raises(gapgb_mod.GapError) as ei:
+            golden_model.set_precision(prec)
+        assert ei.value.status == 3
 
 
 def test_fp32_fast_and_generic_kernels_agree(synth_si, oracle_mod):
