@@ -514,6 +514,13 @@ gapgb_status gapgb_model_load(const char *path, double rcut, gapgb_model **out) 
   return GAPGB_OK;
 }
 
+gapgb_status gapgb_model_write(const gapgb_model *model, const char *path) {
+  if (!model || !path) return fail(GAPGB_ERR_ARG, "null argument");
+  std::string err;
+  const gapgb_status st = write_model_file(model->host, path, &err);
+  return st ? fail(st, err) : GAPGB_OK;
+}
+
 gapgb_status gapgb_model_create(int nspecies, const int *species_z, const double *species_w,
                                 int nsf, const int *sf_type, const double *sf_alpha,
                                 const double *sf_cutoff, const double *sf_zeta, int nsparse,

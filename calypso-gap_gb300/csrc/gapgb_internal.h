@@ -319,6 +319,7 @@ namespace gapgb {
 
 // model.cpp
 gapgb_status parse_model_file(const char *path, HostModel *m, std::string *err);
+gapgb_status write_model_file(const HostModel &m, const char *path, std::string *err);
 gapgb_status build_sf_table(const HostModel &m, SFDev *t, std::string *err);
 
 // api.cu

@@ -149,6 +149,43 @@ gapgb_status parse_model_file(const char *path, HostModel *m, std::string *err) 
   return GAPGB_OK;
 }
 
+// Writes a model in the grammar above, every value as %.17g so that a read
+// gives back the same doubles.  The zeta column appears only on SF records
+// whose zeta differs from 1, so a file of the reference's own SF types is
+// one FGAP_READ / CAR2ACSF can read unchanged; the three records after
+// "M D" are left blank (FGAP_READ skips them, gap_calc.f90:352-354).
+gapgb_status write_model_file(const HostModel &m, const char *path, std::string *err) {
+  std::FILE *f = std::fopen(path, "w");
+  if (!f) {
+    *err = std::string("cannot create model file '") + path + "'";
+    return GAPGB_ERR_FILE;
+  }
+  std::fprintf(f, "%d\n", m.nspecies);
+  for (int i = 0; i < m.nspecies; ++i) std::fprintf(f, "%6d %.17g\n", m.species_z[i], m.species_w[i]);
+  std::fprintf(f, "%d\n", m.nsf);
+  for (int i = 0; i < m.nsf; ++i) {
+    if (m.sf_zeta[i] != 1.0)
+      std::fprintf(f, "%d %.17g %.17g %.17g\n", m.sf_type[i], m.sf_alpha[i], m.sf_cutoff[i],
+                   m.sf_zeta[i]);
+    else
+      std::fprintf(f, "%d %.17g %.17g\n", m.sf_type[i], m.sf_alpha[i], m.sf_cutoff[i]);
+  }
+  std::fprintf(f, "%d %d\n\n\n\n", m.M, m.D);
+  auto row = [&](const double *v, int n) {
+    for (int q = 0; q < n; ++q) std::fprintf(f, q ? " %.17g" : "%.17g", v[q]);
+    std::fputc('\n', f);
+  };
+  row(m.theta.data(), m.D);
+  for (int k = 0; k < m.M; ++k) row(m.mm.data() + (size_t)k * m.D, m.D);
+  row(m.coeff.data(), m.M);
+  const bool bad = std::ferror(f) != 0;
+  if (std::fclose(f) != 0 || bad) {
+    *err = std::string("write error on model file '") + path + "'";
+    return GAPGB_ERR_FILE;
+  }
+  return GAPGB_OK;
+}
+
 gapgb_status build_sf_table(const HostModel &m, SFDev *t, std::string *err) {
   std::memset(t, 0, sizeof(*t));
   t->nsf = m.nsf;

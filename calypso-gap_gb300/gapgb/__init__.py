@@ -32,6 +32,7 @@ SYMBOLS = [
     ("gapgb_version", C.c_char_p, []),
     ("gapgb_model_load", _I, [C.c_char_p, _D, C.POINTER(_P)]),
     ("gapgb_model_create", _I, [_I, _P, _P, _I, _P, _P, _P, _P, _I, _I, _P, _P, _P, _D, C.POINTER(_P)]),
+    ("gapgb_model_write", _I, [_P, C.c_char_p]),
     ("gapgb_model_free", None, [_P]),
     ("gapgb_model_info", _I, [_P, _P, _P, _P, _P, _P]),
     ("gapgb_model_arrays", _I, [_P, _P, _P, _P]),
@@ -162,6 +163,11 @@ class GapModel:
                                          _ptr(mm), _ptr(co), float(rcut), C.byref(h)),
                "gapgb_model_create")
         return cls(h)
+
+    def save(self, path):
+        """Write the model as a gap_parameters file (gapgb_model_write)."""
+        _check(load().gapgb_model_write(self._h, os.fsencode(path)), "gapgb_model_write")
+        return path
 
     def close(self):
         if getattr(self, "_h", None):
@@ -334,3 +340,17 @@ def min_bond(lat, pos, rcut=6.0):
     _check(load().gapgb_min_bond(pos.shape[0], _ptr(_f64(lat, (3, 3))), _ptr(pos), float(rcut),
                                  C.byref(out)), "gapgb_min_bond")
     return out.value
+
+
+def write_parameters(path, species_z, species_w, sf_type, sf_alpha, sf_cutoff, theta, mm, coeff,
+                     sf_zeta=None):
+    """Write a gap_parameters file from arrays: the species table (Z, weight),
+    the SF table (type, alpha, cutoff[, zeta]), theta[D], mm[M, D] and
+    coeff[M] - the file FGAP_READ / CAR2ACSF read (gap_calc.f90:303-364,
+    wacsf.f90:45-56).  Returns path."""
+    m = GapModel.create(species_z, species_w, sf_type, sf_alpha, sf_cutoff, theta, mm, coeff,
+                        sf_zeta=sf_zeta)
+    try:
+        return m.save(path)
+    finally:
+        m.close()

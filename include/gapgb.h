@@ -95,6 +95,15 @@ gapgb_status gapgb_model_create(int nspecies, const int *species_z,
                                 const double *mm, const double *coeff,
                                 double rcut, gapgb_model **out);
 
+/* Write the model as a gap_parameters file (the grammar FGAP_READ and
+ * CAR2ACSF read, gap_calc.f90:303-364 and wacsf.f90:45-56): the species
+ * and SF tables, "M D", three blank records, theta, one record per sparse
+ * point, coeff.  Values are written with 17 significant digits, so
+ * gapgb_model_load gives back the same arrays; the zeta column appears only
+ * where zeta != 1.  With gapgb_model_create this is the writer a fitting
+ * code uses to hand a new model to the reference's readers. */
+gapgb_status gapgb_model_write(const gapgb_model *model, const char *path);
+
 void gapgb_model_free(gapgb_model *model);
 
 gapgb_status gapgb_model_info(const gapgb_model *model, int *nsparse,

@@ -114,3 +114,50 @@ def test_libgap_fgap_read_shapes(gapgb_mod, tmp_path, monkeypatch):
     c = Calculator(rcut=6.0)
     assert c.nsparseX == 129 and c.des_len == 66
     assert c.get_elenum(["B", "C"]) == [5, 6]
+
+
+def _same_model(a, b):
+    for x, y in zip(a.arrays(), b.arrays()):
+        assert np.array_equal(x, y)
+    for x, y in zip(a.tables(), b.tables()):
+        assert np.array_equal(x, y)
+    assert (a.nsparse, a.des_len, a.nsf, a.nspecies) == (b.nsparse, b.des_len, b.nsf, b.nspecies)
+
+
+def test_model_writer_round_trip(gapgb_mod, oracle_mod, tmp_path):
+    """gapgb_model_write: the written file reads back (library and oracle) to
+    the same doubles, and the reference's example model round-trips."""
+    m = gapgb_mod.GapModel.load(GOLDEN_MODEL)
+    p = m.save(str(tmp_path / "gp"))
+    m2 = gapgb_mod.GapModel.load(p)
+    _same_model(m, m2)
+    o = oracle_mod.Model(p)
+    th, mm, co = m.arrays()
+    assert np.array_equal(o.theta, th) and np.array_equal(o.mm, mm)
+    assert np.array_equal(o.coeff, co)
+    # the reference's own SF types have zeta 1: no fourth column is written
+    lines = open(p).read().split("\n")
+    assert all(len(ln.split()) == 3 for ln in lines[4:4 + m.nsf])
+    m.close()
+    m2.close()
+
+
+def test_write_parameters_matches_test_writer(gapgb_mod, tmp_path):
+    """The package's writer and the test suite's independent writer give the
+    same bytes, zeta column included."""
+    from helpers import write_model_file
+    rng = np.random.default_rng(4)
+    ty = np.array([1, 1, 3, 2, 4, 2], np.int32)
+    al = rng.uniform(0.01, 2.0, 6)
+    cu = np.full(6, 6.0)
+    ze = np.array([1, 1, 1, 2, 4, 1.0])
+    th = rng.uniform(0.5, 3.0, 12)
+    mm = rng.normal(size=(7, 12)) * 1e3
+    co = rng.normal(size=7) * 1e-3
+    a = gapgb_mod.write_parameters(str(tmp_path / "a"), [14, 32], [1.0, -2.5], ty, al, cu, th, mm,
+                                   co, sf_zeta=ze)
+    b = write_model_file(str(tmp_path / "b"), [14, 32], [1.0, -2.5], ty, al, cu, th, mm, co, ze)
+    assert open(a).read() == open(b).read()
+    m = gapgb_mod.GapModel.load(a)
+    assert np.array_equal(m.arrays()[1], mm) and np.array_equal(m.tables()[5], ze)
+    m.close()
