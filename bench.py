@@ -49,14 +49,16 @@ def parse():
     p.add_argument("--batch", type=int, default=64, help="structures per step per GPU")
     p.add_argument("--precision", default="tc", choices=["fp32", "tc", "fp64", "mixed"])
     p.add_argument("--no-oracle", action="store_true", help="skip the oracle error check")
-    p.add_argument("--workload", default="alloy", choices=["alloy", "population", "surrogate", "md", "precision"],
+    p.add_argument("--workload", default="alloy", choices=["alloy", "population", "surrogate", "md", "precision",
+                                             "variance"],
                    help="alloy: 512-atom ternary fcc cells (the headline metric); population: "
                         "a ragged structure-search population evaluated by one CUDA graph; "
                         "surrogate: the learned surrogate with GPR fallback on held-out alloy "
                         "cells, after training on GAP labels; md: 32768-atom Si/Ge NVE "
                         "velocity Verlet, tensor-core form against the plain FP64 path; "
                         "precision: the alloy step in every arithmetic form (FP64, FP32, "
-                        "mixed, TF32, split-BF16x3) with each form's error")
+                        "mixed, TF32, split-BF16x3) with each form's error; variance: the "
+                        "GPR variance block (qmm attached) on the alloy workload")
     p.add_argument("--count", type=int, default=8192,
                    help="population size / held-out structures of the surrogate workload")
     p.add_argument("--train-structs", type=int, default=20000,
@@ -274,13 +276,17 @@ def stage_bytes_per_atom(D):
             "chain_rule": P * 36.0 + D * 4.0 + 72.0 + P * 36.0 + 24.0}
 
 
-def roofline(stages, N, D, precision):
-    """Roofline entries from the per-stage device times (ms per step)."""
+def load_peaks():
+    """The measured denominators (MEASURED_PEAKS.json) or the fallback."""
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(peaks_path):
-        peaks, src = json.load(open(peaks_path)), "measured"
-    else:
-        peaks, src = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+        return json.load(open(peaks_path)), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def roofline(stages, N, D, precision):
+    """Roofline entries from the per-stage device times (ms per step)."""
+    peaks, src = load_peaks()
     dom = int(np.argmax(stages))
     name = STAGES[dom]
     bpa = stage_bytes_per_atom(D)
@@ -817,8 +823,115 @@ def run_precision(args):
     print(json.dumps(line), flush=True)
 
 
+def qmm_of(mm, theta, lam=1e-2):
+    """(K_MM + lam I)^-1 of a model's sparse points (the inverse covariance a
+    fitting code would hand over as qmm)."""
+    X = mm / theta
+    n2 = (X * X).sum(1)
+    d2 = np.maximum(n2[:, None] + n2[None, :] - 2.0 * (X @ X.T), 0.0)
+    return np.linalg.inv(np.exp(-0.5 * d2) + lam * np.eye(len(mm)))
+
+
+def run_variance(args):
+    """The GPR variance block (gap_calc.f90:206-210, commented out in the
+    reference) on the alloy workload: 64 alloy512 cells (32768 atoms),
+    M = 4000, D = 64, qmm = (K_MM + 0.01 I)^-1 of the model's sparse points.
+    The tensor-core form (FP32 K, split-BF16x3 products, FP32 accumulation)
+    is timed through gapgb_variance with host buffers (e2e) and its kernels
+    alone with device events; the FP64 form runs once for the comparison on
+    every atom, and the CPU oracle on one cell."""
+    os.environ["GAPGB_PROFILE_STAGES"] = "1"  # read at the model's device upload
+    import gapgb
+    arrays = make_model()
+    zt, wt, ty, al, rc, ze, theta, mm, coeff = arrays
+    Q = qmm_of(mm, theta)
+    structs, (off, sp, lat, pos) = workload(0, args.batch)
+    S, N, M = len(structs), int(off[-1]), len(mm)
+    m = gapgb.GapModel.create(zt, wt, ty, al, rc, theta, mm, coeff, sf_zeta=ze)
+    m.set_qmm(Q)
+    m.set_precision("tc")
+    m.set_neighbour_cap(96)
+    for _ in range(max(3, args.warmup)):
+        m.variance(off, sp, lat, pos)
+    stop, lines = threading.Event(), []
+    th = threading.Thread(target=clocks_sampler, args=(stop, lines), daemon=True)
+    th.start()
+    time.sleep(0.3)
+    wall, kern = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        covf, var = m.variance(off, sp, lat, pos)
+        wall.append(time.perf_counter() - t0)
+        kern.append(m.variance_time())
+    stop.set()
+    th.join()
+    m.set_precision("fp64")
+    t0 = time.perf_counter()
+    c64, v64 = m.variance(off, sp, lat, pos)
+    t64 = time.perf_counter() - t0
+    k64 = m.variance_time()
+    m.close()
+    kms = sum(kern) / len(kern)
+    wms = 1e3 * sum(wall) / len(wall)
+    peaks, src = load_peaks()
+    peak = peaks["bf16_tflops"]
+    Mp = (M + 255) // 256 * 256
+    flops = 2.0 * N * M * M  # the contraction K qmm^T, once
+    mma = 3 * 2.0 * ((N + 127) // 128 * 128) * Mp * Mp  # three split products, padded
+    achieved = flops / (kms * 1e-3) / 1e12
+    orc = None
+    if not args.no_oracle:
+        from oracle import oracle
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import tempfile
+        from helpers import write_model_file
+        with tempfile.TemporaryDirectory() as d:
+            om = oracle.Model(write_model_file(os.path.join(d, "gp"), zt, wt, ty, al, rc, theta,
+                                               mm, coeff, ze))
+            l0, p0, z0 = structs[0]
+            *_, ex = oracle.gap_calc(om, z0, l0, p0, 6.0, False, extras=True)
+            oc, ov = oracle.variance(om, ex["xx"], Q)
+        n0 = len(p0)
+        orc = {"tc_dcovf_max": float(np.abs(covf[:n0] - oc).max()),
+               "fp64_dcovf_max": float(np.abs(c64[:n0] - oc).max()),
+               "tc_dvariance": float(abs(var[0] - ov)), "atoms": n0}
+    line = {"metric": "atom variance evals/s", "value": N / (kms * 1e-3), "unit": "atoms/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": kms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16x3/f32 (tensor-core form)", "data": "synthetic",
+            "config": {"workload": "variance: alloy512 x %d (%d atoms), M=%d, D=64, "
+                                   "qmm=(K_MM+0.01 I)^-1" % (S, N, M),
+                       "l2": "inputs larger than L2 (K tiles %d MB)" % (N * Mp * 4 >> 20)},
+            "e2e": {"value": N / (wms * 1e-3), "unit": "atoms/s", "ms_per_call": wms,
+                    "h2d_bytes_per_step": int(off.nbytes + sp.nbytes + lat.nbytes + pos.nbytes),
+                    "d2h_bytes_per_step": int(covf.nbytes + var.nbytes),
+                    "note": "gapgb_variance: neighbour list, descriptors and the variance"},
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak,
+                         "peak_source": src + " bf16_tflops",
+                         "traffic": None, "mma_tflops": mma / (kms * 1e-3) / 1e12,
+                         "note": "achieved counts 2*N*M^2 (the contraction once); mma_tflops the "
+                                 "three split-BF16 products issued on padded tiles"},
+            "fp64_form": {"value": N / (k64 * 1e-3), "unit": "atoms/s", "kernel_ms": k64,
+                          "call_ms": 1e3 * t64},
+            "speedup_vs_fp64_form": k64 / kms,
+            "tc_vs_fp64_form": {"dcovf_max": float(np.abs(covf - c64).max()),
+                                "dcovf_mean": float(np.abs(covf - c64).mean()),
+                                "dvariance_max": float(np.abs(var - v64).max()),
+                                "covf_range": [float(c64.min()), float(c64.max())]},
+            "errors_vs_oracle": orc,
+            # per call: prep x2, neighbour build, reverse, descriptors, centring,
+            # K tiles, contraction, row sums, structure means
+            "gpu_launches": 10 * args.steps,
+            "clocks": summarize_clocks(lines)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "variance" and args.impl != "reference":
+        run_variance(args)
+        return
     if args.workload == "precision" and args.impl != "reference":
         run_precision(args)
         return

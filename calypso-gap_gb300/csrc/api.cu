@@ -577,6 +577,7 @@ void gapgb_model_free(gapgb_model *m) {
   free_dev(m->fb_scratch);
   if (m->d_tc) cudaFree(m->d_tc);
   if (m->d_tf32) cudaFree(m->d_tf32);
+  variance_free(m->var);
   for (auto &e : m->ev)
     if (e) cudaEventDestroy(e);
   if (m->stream) cudaStreamDestroy(m->stream);
@@ -666,7 +667,61 @@ gapgb_status gapgb_eval(gapgb_model *m, int natoms, const int *species, const do
   gapgb_status st = eval_host(m, 1, off, species, lat, pos, lgrad, energy, force,
                               stress ? stress : stress_local, nullptr, nullptr);
   if (variance) *variance = 0.0;  // gap_calc.f90:206
-  return st;
+  if (st || !variance || m->var.qmm.empty()) return st;
+  // a qmm is attached: the variance block of gap_calc.f90:207-210 on this
+  // evaluation's descriptors
+  cudaStream_t s = m->stream;
+  st = variance_enqueue(m, 1, natoms, m->ws.d_atom_off, m->ws.G,
+                        m->precision == GAPGB_PREC_FP64, s);
+  if (st) return st;
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(variance, m->var.var, sizeof(double), cudaMemcpyDeviceToHost, s));
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(m->ws.h_flags, m->ws.d_flags, 8 * sizeof(int),
+                                 cudaMemcpyDeviceToHost, s));
+  GAPGB_CUDA_TRY(cudaStreamSynchronize(s));
+  return flags_to_status(m->ws.h_flags);
+}
+
+gapgb_status gapgb_model_set_qmm(gapgb_model *m, const double *qmm, int nsparse) {
+  if (!m) return fail(GAPGB_ERR_ARG, "null argument");
+  if (qmm && nsparse != m->host.M)
+    return fail(GAPGB_ERR_ARG, "qmm must be nsparse x nsparse of the model (M = " +
+                                   std::to_string(m->host.M) + ")");
+  if (m->d_sf) cudaSetDevice(m->device);
+  return variance_set_qmm(m, qmm);
+}
+
+gapgb_status gapgb_variance(gapgb_model *m, int nstruct, const int *atom_off, const int *species,
+                            const double *lat, const double *pos, double *covf, double *variance) {
+  if (!m || !atom_off || !species || !lat || !pos || !variance)
+    return fail(GAPGB_ERR_ARG, "null argument");
+  if (m->var.qmm.empty()) return fail(GAPGB_ERR_ARG, "no qmm attached (gapgb_model_set_qmm)");
+  gapgb_status st = check_batch_host(nstruct, atom_off, lat, pos);
+  if (st) return st;
+  double *dG = nullptr;
+  st = eval_host(m, nstruct, atom_off, species, lat, pos, 0, nullptr, nullptr, nullptr, nullptr,
+                 &dG);  // neighbour list and descriptors in the model's precision
+  if (st) return st;
+  const int N = atom_off[nstruct];
+  cudaStream_t s = m->stream;
+  if (m->profile_stages) cudaEventRecord(m->ev[0], s);
+  st = variance_enqueue(m, nstruct, N, m->ws.d_atom_off, dG, m->precision == GAPGB_PREC_FP64, s);
+  if (st) return st;
+  if (m->profile_stages) cudaEventRecord(m->ev[1], s);
+  if (covf)
+    GAPGB_CUDA_TRY(cudaMemcpyAsync(covf, m->var.covf, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(variance, m->var.var, sizeof(double) * nstruct,
+                                 cudaMemcpyDeviceToHost, s));
+  GAPGB_CUDA_TRY(cudaMemcpyAsync(m->ws.h_flags, m->ws.d_flags, 8 * sizeof(int),
+                                 cudaMemcpyDeviceToHost, s));
+  GAPGB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (m->profile_stages) cudaEventElapsedTime(&m->var_ms, m->ev[0], m->ev[1]);
+  return flags_to_status(m->ws.h_flags);
+}
+
+gapgb_status gapgb_variance_time(gapgb_model *m, float *ms) {
+  if (!m || !ms) return fail(GAPGB_ERR_ARG, "null argument");
+  *ms = m->var_ms;
+  return GAPGB_OK;
 }
 
 gapgb_status gapgb_eval_batch(gapgb_model *m, int nstruct, const int *atom_off, const int *species,

@@ -275,6 +275,21 @@ struct Workspace {
   size_t tc_scratch_size = 0;
 };
 
+// GPR predictive variance (variance.cu): the caller's qmm and its device forms
+struct VarState {
+  std::vector<double> qmm;            // [M][M] row-major; empty = none attached
+  double *d_q64 = nullptr;            // [Mp][Mp] FP64, zero-padded (FP64 form)
+  unsigned char *d_qimg = nullptr;    // split-BF16 operand tiles (tensor-core form)
+  double *d_mu64 = nullptr;           // [D] mean of mm / theta (tensor-core form)
+  float *d_mc32 = nullptr;            // [M][D] mm / theta - mu (tensor-core form)
+  void *kbuf = nullptr;               // K of one chunk of atoms (FP64 rows or tiles)
+  void *part = nullptr;               // per-row partial dots [rows][column tiles]
+  void *covf = nullptr;               // [N] covf of the last call (FP64)
+  void *var = nullptr;                // [S] VARIANCE of the last call (FP64)
+  void *xc = nullptr;                 // centred FP32 descriptors of one chunk
+  size_t kbuf_bytes = 0, part_bytes = 0, covf_bytes = 0, var_bytes = 0, xc_bytes = 0;
+};
+
 }  // namespace gapgb
 
 struct gapgb_model {
@@ -313,9 +328,21 @@ struct gapgb_model {
   int *fb_rows = nullptr;      // atoms that take the GPR
   int *fb_count = nullptr;
   void *fb_scratch = nullptr;  // partial sums of the fallback GPR
+  gapgb::VarState var;         // predictive variance (gapgb_model_set_qmm)
+  float var_ms = 0.f;          // device time of the last variance kernels (profiling)
 };
 
 namespace gapgb {
+
+// variance.cu
+gapgb_status variance_set_qmm(gapgb_model *m, const double *qmm);
+bool variance_fp64_form(const gapgb_model *m);
+size_t variance_tc_smem_bytes();
+// covf of the N atoms (G: the descriptors of the last evaluation, FP64 when
+// g64) and the per-structure VARIANCE into m->var.covf / m->var.var
+gapgb_status variance_enqueue(gapgb_model *m, int S, int N, const int *d_atom_off, const void *G,
+                              bool g64, cudaStream_t st);
+void variance_free(VarState &v);
 
 // model.cpp
 gapgb_status parse_model_file(const char *path, HostModel *m, std::string *err);

@@ -33,6 +33,9 @@ SYMBOLS = [
     ("gapgb_model_load", _I, [C.c_char_p, _D, C.POINTER(_P)]),
     ("gapgb_model_create", _I, [_I, _P, _P, _I, _P, _P, _P, _P, _I, _I, _P, _P, _P, _D, C.POINTER(_P)]),
     ("gapgb_model_write", _I, [_P, C.c_char_p]),
+    ("gapgb_model_set_qmm", _I, [_P, _P, _I]),
+    ("gapgb_variance", _I, [_P, _I, _P, _P, _P, _P, _P, _P]),
+    ("gapgb_variance_time", _I, [_P, C.POINTER(C.c_float)]),
     ("gapgb_model_free", None, [_P]),
     ("gapgb_model_info", _I, [_P, _P, _P, _P, _P, _P]),
     ("gapgb_model_arrays", _I, [_P, _P, _P, _P]),
@@ -203,6 +206,27 @@ class GapModel:
                                          _ptr(ze)), "gapgb_model_tables")
         return z, w, ty, al, cu, ze
 
+    def set_qmm(self, qmm):
+        """Attach qmm [M, M] for the predictive variance (None detaches)."""
+        if qmm is None:
+            _check(load().gapgb_model_set_qmm(self._h, None, 0), "gapgb_model_set_qmm")
+            return
+        q = _f64(qmm, (self.nsparse, self.nsparse))
+        _check(load().gapgb_model_set_qmm(self._h, _ptr(q), self.nsparse), "gapgb_model_set_qmm")
+
+    def variance(self, atom_off, species, lat, pos):
+        """Packed batch: (covf[N], variance[S]) of the GPR variance block."""
+        off = _i32(atom_off)
+        S = off.shape[0] - 1
+        N = int(off[-1])
+        sp = _i32(species)
+        covf = np.zeros(N)
+        var = np.zeros(S)
+        _check(load().gapgb_variance(self._h, S, _ptr(off), _ptr(sp), _ptr(_f64(lat, (S, 3, 3))),
+                                     _ptr(_f64(pos, (N, 3))), _ptr(covf), _ptr(var)),
+               "gapgb_variance")
+        return covf, var
+
     def set_precision(self, prec):
         prec = PRECISIONS.get(prec, prec)
         _check(load().gapgb_set_option(self._h, OPT_PRECISION, int(prec)), "gapgb_set_option")
@@ -286,6 +310,13 @@ class GapModel:
 
     def check_device_status(self):
         _check(load().gapgb_check_device_status(self._h), "gapgb_check_device_status")
+
+    def variance_time(self):
+        """Device ms of the last gapgb_variance call's variance kernels
+        (GAPGB_PROFILE_STAGES set before the model's first GPU call)."""
+        t = C.c_float()
+        _check(load().gapgb_variance_time(self._h, C.byref(t)), "gapgb_variance_time")
+        return t.value
 
     def stage_times(self):
         t = (C.c_float * 4)()

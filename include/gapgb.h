@@ -129,13 +129,42 @@ gapgb_status gapgb_set_option(gapgb_model *model, gapgb_option opt,
 gapgb_status gapgb_get_option(const gapgb_model *model, gapgb_option opt,
                               int64_t *value);
 
+/* ---- predictive variance ------------------------------------------------ */
+
+/* Attach qmm, the nsparse x nsparse matrix of the reference's variance block
+ * (FGAP_CALC's qmm argument, gap_calc.f90:40; the block itself,
+ * gap_calc.f90:206-210, is commented out there and FGAP_READ zero-fills
+ * qmm, so the reference always reports 0).  qmm is row-major,
+ * qmm[m * nsparse + n] = qmm(m, n), copied; NULL detaches it.  nsparse must
+ * equal the model's M. */
+gapgb_status gapgb_model_set_qmm(gapgb_model *model, const double *qmm,
+                                 int nsparse);
+
+/* The variance block for a packed batch (host buffers):
+ *   covf_i = delta - k_i^T qmm k_i,  k_i = GET_COV row of atom i, delta = 1
+ *   variance[s] = mean of covf over structure s's atoms
+ * covf [natoms] may be NULL.  FP64 and MIXED models compute K and the
+ * N x M x M contraction in FP64; the other forms use FP32 K and tcgen05
+ * split-BF16 products with FP32 accumulation.  Needs an attached qmm. */
+gapgb_status gapgb_variance(gapgb_model *model, int nstruct,
+                            const int *atom_off, const int *species,
+                            const double *lat, const double *pos,
+                            double *covf, double *variance);
+
+/* Device time (ms) of the variance kernels of the last gapgb_variance call
+ * (K, contraction, sums; not the neighbour list and descriptors).  Only
+ * filled when GAPGB_PROFILE_STAGES is set in the environment. */
+gapgb_status gapgb_variance_time(gapgb_model *model, float *ms);
+
 /* ---- evaluation, host buffers ------------------------------------------- */
 
 /* One structure.  Replaces FGAP_CALC (gappy/libgap/gap_calc.f90:1-301):
  * same inputs (species as atomic numbers, lattice rows, Cartesian
  * positions), same outputs (energy eV, forces eV/A, stress GPa in the order
  * XX YY ZZ XY YZ ZX, variance = 0 as in gap_calc.f90:206).  With lgrad == 0
- * force and stress are set to zero, as the reference leaves them. */
+ * force and stress are set to zero, as the reference leaves them.  When a
+ * qmm is attached (gapgb_model_set_qmm) and variance is not NULL, variance
+ * is the mean covf of gapgb_variance instead. */
 gapgb_status gapgb_eval(gapgb_model *model, int natoms, const int *species,
                         const double *lat, const double *pos, int lgrad,
                         double *energy, double *force, double *stress,

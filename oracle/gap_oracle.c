@@ -665,6 +665,48 @@ int orc_gap_calc_batch(const orc_model *m, int nstruct, const int *atom_off,
 }
 
 /* FGET_BOND, get_bond.f90:4-116 */
+/* ------------------------------------------------------------------------ */
+/* The predictive variance of the commented-out block of FGAP_CALC,
+ * gap_calc.f90:206-210:
+ *   covf(i)  = delta - dot_product(ckm(i,:), matmul(qmm, ckm(i,:)))
+ *   VARIANCE = VARIANCE + covf(i)/na          (atom order)
+ * with ckm from GET_COV (gap_calc.f90:268-288) on the descriptors xx[na][D].
+ * qmm is [M][M] row-major, qmm[m*M+n] = qmm(m,n).  The reference zero-fills
+ * qmm in FGAP_READ (gap_calc.f90:361) and returns VARIANCE = 0; this is the
+ * formula it would evaluate for a caller-supplied qmm. */
+int orc_variance(const orc_model *m, int na, const double *xx, const double *qmm,
+                 double *covf, double *variance) {
+  const int D = m->des_len, M = m->nsparse;
+  if (na <= 0) return ORC_ERR_ARG;
+  double *ck = (double *)malloc(sizeof(double) * M);
+  double *tmp = (double *)malloc(sizeof(double) * M);
+  if (!ck || !tmp) { free(ck); free(tmp); return ORC_ERR_ALLOC; }
+  double var = 0.0;
+  for (int i = 0; i < na; i++) {
+    for (int k = 0; k < M; k++) {
+      double temp = 0.0;
+      for (int d = 0; d < D; d++) {
+        double q = (xx[(size_t)i * D + d] - m->mm[(size_t)k * D + d]) / m->theta[d];
+        temp = temp + q * q;
+      }
+      ck[k] = ORC_DELTA * exp(-0.5 * temp);
+    }
+    for (int a = 0; a < M; a++) {
+      double s = 0.0;
+      for (int b = 0; b < M; b++) s = s + qmm[(size_t)a * M + b] * ck[b];
+      tmp[a] = s;
+    }
+    double dot = 0.0;
+    for (int a = 0; a < M; a++) dot = dot + ck[a] * tmp[a];
+    covf[i] = ORC_DELTA - dot;
+    var = var + covf[i] / na;
+  }
+  *variance = var;
+  free(ck);
+  free(tmp);
+  return ORC_OK;
+}
+
 double orc_min_bond(int na, const double *lat, const double *pos, double rcut) {
   int nabc[3];
   orc_nabc(lat, rcut, nabc);

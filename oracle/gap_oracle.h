@@ -84,6 +84,10 @@ int orc_gap_calc_batch(const orc_model *m, int nstruct, const int *atom_off,
                        double *ene, double *force, double *stress);
 
 /* get_bond.f90:4-116: minimum image distance within rcut (10.0 if none). */
+/* gap_calc.f90:206-210 (commented out in the reference): per-atom
+ * covf = delta - k^T qmm k and their mean, from descriptors xx[na][D]. */
+int orc_variance(const orc_model *m, int na, const double *xx, const double *qmm,
+                 double *covf, double *variance);
 double orc_min_bond(int na, const double *lat, const double *pos, double rcut);
 
 #ifdef __cplusplus

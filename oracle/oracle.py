@@ -9,6 +9,7 @@ Each function names the reference routine it restates:
   car2acsf          CAR2ACSF        gappy/libgap/wacsf.f90:2-796
   gap_calc          FGAP_CALC       gappy/libgap/gap_calc.f90:1-301
   min_bond          FGET_BOND       gappy/libgap/get_bond.f90:4-116
+  variance          FGAP_CALC       gappy/libgap/gap_calc.f90:206-210 (commented out there)
 """
 import ctypes as C
 import os
@@ -68,6 +69,8 @@ def lib():
                                    C.POINTER(C.c_double), C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_gap_calc_batch.argtypes = [C.POINTER(OrcModel), C.c_int, _ip, _ip, _dp, _dp,
                                          C.c_double, C.c_int, _dp, _dp, _dp]
+        L.orc_variance.argtypes = [C.POINTER(OrcModel), C.c_int, _dp, _dp, _dp,
+                                   C.POINTER(C.c_double)]
         L.orc_min_bond.argtypes = [C.c_int, _dp, _dp, C.c_double]
         L.orc_min_bond.restype = C.c_double
         _lib = L
@@ -188,6 +191,20 @@ def gap_calc_batch(model, atom_off, species, lat, pos, rcut=6.0, nthreads=0):
     if st:
         raise OracleError(f"orc_gap_calc_batch status {st}")
     return ene, force, stress
+
+
+def variance(model, xx, qmm):
+    """FGAP_CALC's commented-out variance block (gap_calc.f90:206-210) for
+    descriptors xx[na, D] and qmm[M, M]: (covf[na], VARIANCE = mean)."""
+    xx = _f64(xx)
+    qmm = _f64(qmm)
+    na = xx.shape[0]
+    covf = np.zeros(na)
+    var = C.c_double()
+    st = lib().orc_variance(C.byref(model._m), na, xx, qmm, covf, C.byref(var))
+    if st:
+        raise OracleError(f"orc_variance status {st}")
+    return covf, var.value
 
 
 def min_bond(lat, pos, rcut=6.0):
