@@ -50,7 +50,7 @@ def parse():
     p.add_argument("--precision", default="tc", choices=["fp32", "tc", "fp64", "mixed"])
     p.add_argument("--no-oracle", action="store_true", help="skip the oracle error check")
     p.add_argument("--workload", default="alloy", choices=["alloy", "population", "surrogate", "md", "precision",
-                                             "variance"],
+                                             "variance", "fit"],
                    help="alloy: 512-atom ternary fcc cells (the headline metric); population: "
                         "a ragged structure-search population evaluated by one CUDA graph; "
                         "surrogate: the learned surrogate with GPR fallback on held-out alloy "
@@ -58,12 +58,15 @@ def parse():
                         "velocity Verlet, tensor-core form against the plain FP64 path; "
                         "precision: the alloy step in every arithmetic form (FP64, FP32, "
                         "mixed, TF32, split-BF16x3) with each form's error; variance: the "
-                        "GPR variance block (qmm attached) on the alloy workload")
+                        "GPR variance block (qmm attached) on the alloy workload; fit: the "
+                        "coefficients refitted from teacher energies of --fit-structs cells")
     p.add_argument("--count", type=int, default=8192,
                    help="population size / held-out structures of the surrogate workload")
     p.add_argument("--train-structs", type=int, default=20000,
                    help="surrogate workload: training structures (512 atoms each)")
     p.add_argument("--epochs", type=int, default=4, help="surrogate workload: training epochs")
+    p.add_argument("--fit-structs", type=int, default=512,
+                   help="fit workload: training cells (512 atoms each)")
     p.add_argument("--md-steps", type=int, default=100, help="md workload: velocity-Verlet steps")
     p.add_argument("--md-reps", type=int, default=16,
                    help="md workload: diamond cells per axis (16: 32768 atoms; smaller for profiling)")
@@ -927,8 +930,63 @@ def run_variance(args):
     print(json.dumps(line), flush=True)
 
 
+def run_fit(args):
+    """Sparse-GPR fitting on the device (gapgb_fit_energies): the alloy
+    model's M = 4000 sparse points, teacher energies from the model itself
+    (FP64 path) on --fit-structs alloy512 cells, refitted from those energies
+    (sigma_e = 1 meV/atom, jitter 1e-6); reported: the fit's wall time per
+    call, training atoms per second, the refit's training RMSE and its
+    held-out RMSE against the teacher on 16 further cells."""
+    import gapgb
+    import gapgb.synth as S
+    arrays = make_model()
+    zt, wt, ty, al, rc, ze, theta, mm, coeff = arrays
+    ns = args.fit_structs
+    off, sp, lat, pos = S.pack([S.alloy512(seed=2000 + s) for s in range(ns)])
+    N = int(off[-1])
+    n = np.diff(off)
+    teacher = gapgb.GapModel.create(zt, wt, ty, al, rc, theta, mm, coeff, sf_zeta=ze)
+    teacher.set_precision("fp64")
+    E, _, _ = teacher.eval_batch(off, sp, lat, pos, lgrad=False)
+    offh, sph, lath, posh = S.pack([S.alloy512(seed=9000 + s) for s in range(16)])
+    Eh_t, _, _ = teacher.eval_batch(offh, sph, lath, posh, lgrad=False)
+    teacher.close()
+    m = gapgb.GapModel.create(zt, wt, ty, al, rc, theta, mm, np.zeros_like(coeff), sf_zeta=ze)
+    m.set_precision("fp64")
+    m.fit_energies(off, sp, lat, pos, E, sigma_e=1e-3, jitter=1e-6)  # warm-up
+    times = []
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        c = m.fit_energies(off, sp, lat, pos, E, sigma_e=1e-3, jitter=1e-6)
+        times.append(time.perf_counter() - t0)
+    E2, _, _ = m.eval_batch(off, sp, lat, pos, lgrad=False)
+    Eh, _, _ = m.eval_batch(offh, sph, lath, posh, lgrad=False)
+    m.close()
+    ms = 1e3 * sum(times) / len(times)
+    line = {"metric": "training atoms fitted per second", "value": N / (ms * 1e-3),
+            "unit": "atoms/s", "n_gpus": 1, "steps": len(times), "warmup": 1, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "fit: %d alloy512 cells (%d atoms), M=%d, D=64, sigma_e=1 meV/atom, "
+                                   "jitter 1e-6" % (ns, N, len(mm)),
+                       "step": "gapgb_fit_energies: FP64 descriptors, design rows, Gram, "
+                               "Cholesky, solves"},
+            "train_rmse_eV_per_atom": float(np.sqrt(np.mean(((E2 - E) / n) ** 2))),
+            "heldout_rmse_eV_per_atom": float(np.sqrt(np.mean(((Eh - Eh_t) / 512) ** 2))),
+            "teacher_energy_scale_eV_per_atom": float(np.abs(Eh_t / 512).max()),
+            "coeff_max": float(np.abs(c).max()),
+            # per call: prep x2, neighbour build, reverse, FP64 descriptors, K_MM, jitter,
+            # weights, design rows, Gram, right-hand side, 3 per Cholesky panel (2 for the
+            # last), solves
+            "gpu_launches": (5 + 6 + 3 * ((len(mm) + 63) // 64) - 2 + 1) * len(times)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "fit" and args.impl != "reference":
+        run_fit(args)
+        return
     if args.workload == "variance" and args.impl != "reference":
         run_variance(args)
         return

@@ -341,6 +341,8 @@ gapgb_status flags_to_status(const int *f) {
   if (f[0] & kFlagNeighbourOverflow) return fail(GAPGB_ERR_NEIGHBOUR_OVERFLOW, "neighbour capacity exceeded (max count " + std::to_string(f[1]) + ")");
   if (f[0] & kFlagOrphanOverflow) return fail(GAPGB_ERR_CAP_EXCEEDED, "too many unpaired neighbour slots");
   if (f[0] & kFlagTimeout) return fail(GAPGB_ERR_TIMEOUT, "a bounded device wait gave up");
+  if (f[0] & kFlagNotPositiveDefinite)
+    return fail(GAPGB_ERR_ARG, "the fit's normal matrix is not positive definite (raise the jitter)");
   if (f[0] & kFlagSkinExceeded)
     return fail(GAPGB_ERR_CAP_EXCEEDED, "an atom moved more than half the Verlet skin between rebuilds");
   return GAPGB_OK;
@@ -679,6 +681,57 @@ gapgb_status gapgb_eval(gapgb_model *m, int natoms, const int *species, const do
                                  cudaMemcpyDeviceToHost, s));
   GAPGB_CUDA_TRY(cudaStreamSynchronize(s));
   return flags_to_status(m->ws.h_flags);
+}
+
+gapgb_status gapgb_model_set_coeff(gapgb_model *m, const double *coeff) {
+  if (!m || !coeff) return fail(GAPGB_ERR_ARG, "null argument");
+  const int M = m->host.M;
+  for (int k = 0; k < M; ++k)
+    if (!std::isfinite(coeff[k])) return fail(GAPGB_ERR_ARG, "coefficients must be finite");
+  m->host.coeff.assign(coeff, coeff + M);
+  if (!m->d_sf) return GAPGB_OK;  // not on the device yet: the upload takes the new values
+  GAPGB_CUDA_TRY(cudaSetDevice(m->device));
+  GAPGB_CUDA_TRY(cudaStreamSynchronize(m->stream));
+  std::vector<float> c32(M);
+  for (int k = 0; k < M; ++k) c32[k] = (float)coeff[k];
+  GAPGB_CUDA_TRY(cudaMemcpy(m->d_coeff, coeff, sizeof(double) * M, cudaMemcpyHostToDevice));
+  GAPGB_CUDA_TRY(cudaMemcpy(m->d_coeff32, c32.data(), sizeof(float) * M, cudaMemcpyHostToDevice));
+  // the tensor-core operand images carry c: rebuilt by the next call that needs them
+  if (m->d_tc) cudaFree(m->d_tc);
+  if (m->d_tf32) cudaFree(m->d_tf32);
+  m->d_tc = nullptr;
+  m->d_tf32 = nullptr;
+  return GAPGB_OK;
+}
+
+gapgb_status gapgb_fit_energies(gapgb_model *m, int nstruct, const int *atom_off,
+                                const int *species, const double *lat, const double *pos,
+                                const double *energy, double sigma_e, double jitter,
+                                double *coeff) {
+  if (!m || !atom_off || !species || !lat || !pos || !energy)
+    return fail(GAPGB_ERR_ARG, "null argument");
+  if (!(sigma_e > 0.0) || !(jitter >= 0.0))
+    return fail(GAPGB_ERR_ARG, "sigma_e must be positive and jitter non-negative");
+  gapgb_status st = check_batch_host(nstruct, atom_off, lat, pos);
+  if (st) return st;
+  // FP64 descriptors of the training structures (the exact neighbour list)
+  const int saved = m->precision;
+  m->precision = GAPGB_PREC_FP64;
+  double *dG = nullptr;
+  st = eval_host(m, nstruct, atom_off, species, lat, pos, 0, nullptr, nullptr, nullptr, nullptr,
+                 &dG);
+  m->precision = saved;
+  if (st) return st;
+  std::vector<double> c(m->host.M);
+  GAPGB_CUDA_TRY(cudaMemsetAsync(m->ws.d_flags, 0, 8 * sizeof(int), m->stream));
+  st = fit_energies_enqueue(m, nstruct, atom_off[nstruct], m->ws.d_atom_off, dG, energy, sigma_e,
+                            jitter, c.data(), m->stream);
+  if (st) return st;
+  GAPGB_CUDA_TRY(cudaMemcpy(m->ws.h_flags, m->ws.d_flags, 8 * sizeof(int), cudaMemcpyDeviceToHost));
+  st = flags_to_status(m->ws.h_flags);
+  if (st) return st;
+  if (coeff) std::copy(c.begin(), c.end(), coeff);
+  return gapgb_model_set_coeff(m, c.data());
 }
 
 gapgb_status gapgb_model_set_qmm(gapgb_model *m, const double *qmm, int nsparse) {

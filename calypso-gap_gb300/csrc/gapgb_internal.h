@@ -46,6 +46,7 @@ enum : int {
   kFlagOrphanOverflow = 8,
   kFlagTimeout = 16,
   kFlagSkinExceeded = 32,  // MD: an atom moved more than half the skin since the last rebuild
+  kFlagNotPositiveDefinite = 64,  // fit: a Cholesky pivot was not positive
 };
 
 // Symmetry-function table as the kernels read it.  Angular SFs are grouped by
@@ -333,6 +334,11 @@ struct gapgb_model {
 };
 
 namespace gapgb {
+
+// fit.cu
+gapgb_status fit_energies_enqueue(gapgb_model *m, int S, int N, const int *d_off, const double *d_G,
+                                  const double *energy, double sigma_e, double jitter,
+                                  double *coeff, cudaStream_t st);
 
 // variance.cu
 gapgb_status variance_set_qmm(gapgb_model *m, const double *qmm);

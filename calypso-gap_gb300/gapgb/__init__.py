@@ -34,6 +34,8 @@ SYMBOLS = [
     ("gapgb_model_create", _I, [_I, _P, _P, _I, _P, _P, _P, _P, _I, _I, _P, _P, _P, _D, C.POINTER(_P)]),
     ("gapgb_model_write", _I, [_P, C.c_char_p]),
     ("gapgb_model_set_qmm", _I, [_P, _P, _I]),
+    ("gapgb_model_set_coeff", _I, [_P, _P]),
+    ("gapgb_fit_energies", _I, [_P, _I, _P, _P, _P, _P, _P, _D, _D, _P]),
     ("gapgb_variance", _I, [_P, _I, _P, _P, _P, _P, _P, _P]),
     ("gapgb_variance_time", _I, [_P, C.POINTER(C.c_float)]),
     ("gapgb_model_free", None, [_P]),
@@ -205,6 +207,23 @@ class GapModel:
         _check(load().gapgb_model_tables(self._h, _ptr(z), _ptr(w), _ptr(ty), _ptr(al), _ptr(cu),
                                          _ptr(ze)), "gapgb_model_tables")
         return z, w, ty, al, cu, ze
+
+    def set_coeff(self, coeff):
+        c = _f64(coeff, (self.nsparse,))
+        _check(load().gapgb_model_set_coeff(self._h, _ptr(c)), "gapgb_model_set_coeff")
+
+    def fit_energies(self, atom_off, species, lat, pos, energy, sigma_e=1e-3, jitter=1e-8):
+        """Fit the coefficients to structure energies (eV) on the device and
+        set them on the model; returns them."""
+        off = _i32(atom_off)
+        S = off.shape[0] - 1
+        N = int(off[-1])
+        c = np.zeros(self.nsparse)
+        _check(load().gapgb_fit_energies(self._h, S, _ptr(off), _ptr(_i32(species)),
+                                         _ptr(_f64(lat, (S, 3, 3))), _ptr(_f64(pos, (N, 3))),
+                                         _ptr(_f64(energy, (S,))), float(sigma_e), float(jitter),
+                                         _ptr(c)), "gapgb_fit_energies")
+        return c
 
     def set_qmm(self, qmm):
         """Attach qmm [M, M] for the predictive variance (None detaches)."""

@@ -129,6 +129,28 @@ gapgb_status gapgb_set_option(gapgb_model *model, gapgb_option opt,
 gapgb_status gapgb_get_option(const gapgb_model *model, gapgb_option opt,
                               int64_t *value);
 
+/* ---- fitting ------------------------------------------------------------ */
+
+/* Replace the model's coefficients c[M] (host and device copies). */
+gapgb_status gapgb_model_set_coeff(gapgb_model *model, const double *coeff);
+
+/* Fit c from training energies, on the device, and set it on the model.
+ * The reference only evaluates E = sum_i sum_k c_k K(x_i, m_k)
+ * (gap_calc.f90:143-154); its fitting codes are not part of the repository.
+ * Sparse (subset-of-regressors) normal equations in FP64:
+ *   Phi_sk = sum_{i in s} K(x_i, m_k)
+ *   (K_MM + jitter I + sum_s w_s Phi_s^T Phi_s) c = sum_s w_s Phi_s^T E_s
+ *   w_s = 1 / (sigma_e^2 n_s)   (sigma_e: energy noise per atom, eV)
+ * solved by a blocked Cholesky factorisation.  Descriptors are the FP64
+ * path's; the sparse points and theta are the model's.  energy[nstruct]
+ * in eV; coeff[M] (may be NULL) receives c.  A matrix that is not positive
+ * definite gives GAPGB_ERR_ARG (raise jitter). */
+gapgb_status gapgb_fit_energies(gapgb_model *model, int nstruct,
+                                const int *atom_off, const int *species,
+                                const double *lat, const double *pos,
+                                const double *energy, double sigma_e,
+                                double jitter, double *coeff);
+
 /* ---- predictive variance ------------------------------------------------ */
 
 /* Attach qmm, the nsparse x nsparse matrix of the reference's variance block

@@ -1,0 +1,99 @@
+"""Sparse-GPR fitting from structure energies (gapgb_fit_energies).
+
+The reference only evaluates fitted models (its fitting codes, calypso.x and
+ngap.x, are not in the repository), so the oracle here is the same normal
+equations written out in numpy on the CPU oracle's FP64 descriptors:
+  Phi_sk = sum_{i in s} K(x_i, m_k),  A = K_MM + jitter I + Phi^T W Phi,
+  b = Phi^T W E,  W = diag(1 / (sigma_e^2 n_s)),  c = A^-1 b.
+"""
+import numpy as np
+import pytest
+
+from helpers import synth_model_file
+
+pytestmark = pytest.mark.gpu
+
+
+def _kmat(xx, mm, theta):
+    return np.exp(-0.5 * (((xx[:, None, :] - mm[None, :, :]) / theta) ** 2).sum(-1))
+
+
+def _phi(oracle_mod, o, structs):
+    rows = []
+    for lat, pos, z in structs:
+        *_, ex = oracle_mod.gap_calc(o, z, lat, pos, 6.0, False, extras=True)
+        rows.append(_kmat(ex["xx"], o.mm, o.theta).sum(0))
+    return np.array(rows)
+
+
+def _normal(o, phi, E, n, sigma_e, jitter):
+    w = 1.0 / (sigma_e ** 2 * n)
+    A = _kmat(o.mm, o.mm, o.theta) + jitter * np.eye(len(o.mm)) + (phi * w[:, None]).T @ phi
+    b = phi.T @ (w * E)
+    return A, b
+
+
+@pytest.mark.parametrize("kind", ["si", "alloy"])
+def test_fit_energies_matches_normal_equations(gapgb_mod, oracle_mod, tmp_path, kind):
+    import gapgb.synth as S
+    path = str(tmp_path / "gp")
+    if kind == "si":
+        # M = 300: five 64-wide Cholesky panels, the last one padded
+        synth_model_file(path, oracle_mod, [S.si64(seed=s) for s in range(3)], M=300,
+                         theta_scale=1.0, coeff_std=0.05, seed=1)
+        train = [S.si64(seed=100 + s, jitter=0.1) for s in range(48)]
+        test = [S.si64(seed=500 + s, jitter=0.1) for s in range(6)]
+    else:
+        # M = 600: ten panels; 512-atom structures span many passes of the design-row kernel
+        synth_model_file(path, oracle_mod, [S.alloy512(seed=s) for s in range(2)], M=600,
+                         theta_scale=0.8, coeff_std=1e-3, seed=2)
+        train = [S.alloy512(seed=100 + s) for s in range(12)]
+        test = [S.alloy512(seed=500 + s) for s in range(2)]
+    o = oracle_mod.Model(path)
+    m = gapgb_mod.GapModel.load(path)
+    m.set_precision("fp64")
+    off, sp, lat, pos = S.pack(train)
+    E_teacher, _, _ = m.eval_batch(off, sp, lat, pos, lgrad=False)
+    n = np.diff(off).astype(float)
+    rng = np.random.default_rng(3)
+    E = E_teacher + rng.normal(0, 1e-3, len(n)) * np.sqrt(n)
+    sigma_e, jitter = 1e-3, 1e-6
+    c = m.fit_energies(off, sp, lat, pos, E, sigma_e=sigma_e, jitter=jitter)
+    phi = _phi(oracle_mod, o, train)
+    A, b = _normal(o, phi, E, n, sigma_e, jitter)
+    c_ref = np.linalg.solve(A, b)
+    res = np.linalg.norm(A @ c - b) / (np.linalg.norm(A, 2) * np.linalg.norm(c))
+    pred, pred_ref = phi @ c, phi @ c_ref
+    phi_t = _phi(oracle_mod, o, test)
+    dt = np.abs(phi_t @ c - phi_t @ c_ref).max()
+    print("%s fit: backward error %.3g, |c| %.3g, train dE %.3g eV, held-out dE %.3g eV, "
+          "train rmse vs labels %.3g eV/atom" % (kind, res, np.abs(c).max(),
+                                                np.abs(pred - pred_ref).max(), dt,
+                                                np.sqrt(np.mean(((pred - E) / n) ** 2))))
+    # Cholesky is backward stable: the device solution solves A to rounding
+    assert res <= 1e-12
+    # and predicts what the numpy solution predicts (energies of 1e2-1e4 eV)
+    assert np.abs(pred - pred_ref).max() <= 1e-6 * np.abs(pred_ref).max()
+    assert dt <= 1e-6 * np.abs(phi_t @ c_ref).max()
+    # the model now carries the fitted coefficients in every form
+    assert np.array_equal(m.arrays()[2], c)
+    E_fit, _, _ = m.eval_batch(off, sp, lat, pos, lgrad=False)
+    assert np.abs(E_fit - pred_ref).max() <= 1e-6 * np.abs(pred_ref).max()
+    m.set_precision("tc")
+    E_tc, _, _ = m.eval_batch(off, sp, lat, pos, lgrad=False)
+    assert np.abs(E_tc - E_fit).max() / n.min() <= 1e-3
+    m.close()
+
+
+def test_fit_rejects_bad_arguments(gapgb_mod, tmp_path, oracle_mod):
+    import gapgb.synth as S
+    path = str(tmp_path / "gp")
+    synth_model_file(path, oracle_mod, [S.si64(seed=0)], M=50, seed=1)
+    m = gapgb_mod.GapModel.load(path)
+    off, sp, lat, pos = S.pack([S.si64(seed=1)])
+    with pytest.raises(gapgb_mod.GapError) as ei:
+        m.fit_energies(off, sp, lat, pos, [0.0], sigma_e=0.0)
+    assert ei.value.status == 8
+    with pytest.raises(gapgb_mod.GapError):
+        m.set_coeff(np.full(m.nsparse, np.nan))
+    m.close()
