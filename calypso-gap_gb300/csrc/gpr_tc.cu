@@ -9,16 +9,16 @@
 //   s_ik  = |x''_i|^2 + |m''_k|^2 - 2 x''_i . m''_k
 //   GEMM1 (N x M, K = D):  x''.m'' ~ xh.mh + xh.ml + xl.mh  (3-term BF16 split,
 //                          x'' = xh + xl, m'' = mh + ml, every product exact in FP32)
-//   w_ik  = c_k exp(-s_ik / 2),  e_i = sum_k w_ik  (compensated FP32)
+//   w_ik  = c_k exp(-s_ik / 2),  e_i = sum_k w_ik  (compensated FP32, Kahan)
 //   GEMM2 (N x D, K = M):  (W M'')_id ~ wh.mh + wh.ml + wl.mh
 //   dE/dG_id = -(1/theta_d) (x''_id e_i - (W M'')_id)
 //
-// One CTA (4 warps) owns 128 atoms.  For each tile of 128 sparse points: one
+// One CTA (8 warps) owns 128 atoms.  For each tile of 64 sparse points: one
 // 1-D bulk copy brings the pre-arranged operand tiles into shared memory,
-// one thread issues GEMM1 (12 tcgen05.mma, M=128 N=128 K=16) into a TMEM
-// accumulator, the four warps read it back with tcgen05.ld (thread = atom
+// one thread issues GEMM1 (12 tcgen05.mma, M=128 N=64 K=16) into a TMEM
+// accumulator, the eight warps read it back with tcgen05.ld (thread = atom
 // row), form w, accumulate e and write wh/wl into shared memory as GEMM2's A
-// operand, and one thread issues GEMM2 (24 tcgen05.mma, M=128 N=64 K=16)
+// operand, and one thread issues GEMM2 (12 tcgen05.mma, M=128 N=64 K=16)
 // accumulating over all sparse tiles in a second TMEM region.
 //
 // Operand tiles use the no-swizzle K-major canonical layout: 8-row x 16-byte
@@ -41,23 +41,25 @@ namespace {
 using namespace tc;
 
 constexpr int kRows = 128;   // atoms per CTA (UMMA M)
-constexpr int kTileK = 128;  // sparse points per tile (GEMM1 N, GEMM2 K)
+constexpr int kTileK = 64;   // sparse points per tile (GEMM1 N, GEMM2 K)
 constexpr int kDP = 64;      // padded descriptor length (GEMM1 K, GEMM2 N)
-constexpr int kTileBytes16 = kRows * kDP * 2;        // 128 x 64 bf16: 16 KB
-constexpr int kWBytes = kRows * kTileK * 2;          // 128 x 128 bf16: 32 KB
-// per sparse tile image: mh, ml (128 x 64), mhT, mlT (64 x 128), mn[128], c[128]
-constexpr int kImgTile = 4 * kTileBytes16 + 2 * kTileK * 4;  // 66 KB
-constexpr int kImgAtoms = 2 * kTileBytes16;                   // xh, xl per 128 atoms
+constexpr int kXBytes16 = kRows * kDP * 2;           // 128 x 64 bf16: 16 KB
+constexpr int kMBytes16 = kTileK * kDP * 2;          // 64 x 64 bf16: 8 KB
+constexpr int kWBytes = kRows * kTileK * 2;          // 128 x 64 bf16: 16 KB
+// per sparse tile image: mh, ml (64 x 64), mhT, mlT (64 x 64), b2[64], c[64]
+constexpr int kImgTile = 4 * kMBytes16 + 2 * kTileK * 4;     // 32.5 KB
+constexpr int kImgAtoms = 2 * kXBytes16;                      // xh, xl per 128 atoms
 
-// shared memory map (bytes from the 1024-aligned base)
+// shared memory map (bytes from the 1024-aligned base); about 99 KB, so two
+// CTAs share an SM and one's GEMMs run under the other's epilogue
 constexpr int kOffXh = 0;
-constexpr int kOffXl = kOffXh + kTileBytes16;
-constexpr int kOffImg = kOffXl + kTileBytes16;           // one sparse tile image
+constexpr int kOffXl = kOffXh + kXBytes16;
+constexpr int kOffImg = kOffXl + kXBytes16;              // one sparse tile image
 constexpr int kOffMh = kOffImg;
-constexpr int kOffMl = kOffMh + kTileBytes16;
-constexpr int kOffMhT = kOffMl + kTileBytes16;
-constexpr int kOffMlT = kOffMhT + kTileBytes16;
-constexpr int kOffMnc = kOffMlT + kTileBytes16;          // |m''|^2 and c, two tiles
+constexpr int kOffMl = kOffMh + kMBytes16;
+constexpr int kOffMhT = kOffMl + kMBytes16;
+constexpr int kOffMlT = kOffMhT + kMBytes16;
+constexpr int kOffMnc = kOffMlT + kMBytes16;             // b2 and c, two tiles
 constexpr int kMncBytes = 2 * kTileK * 4;                 // one tile's mn and c
 constexpr int kOffWh = kOffMnc + 2 * kMncBytes;
 constexpr int kOffWl = kOffWh + kWBytes;
@@ -65,8 +67,17 @@ constexpr int kOffBar = kOffWl + kWBytes;                 // 3 mbarriers + tmem 
 constexpr int kOffEp = kOffBar + 64;                      // partial energies [128] (FP64)
 constexpr int kSmemBytes = kOffEp + kRows * 8 + 1024;     // + alignment slack
 constexpr int kGprThreads = 256;  // warps w and w + 4 share TMEM lanes and split the columns
+constexpr int kTmemCols = 128;    // C1 (kTileK columns) and C2 (kDP columns)
+constexpr float kLog2e = 1.4426950408889634f;
 
-__global__ void __launch_bounds__(kGprThreads, 1)
+// 2^x (PTX ex2.approx.ftz: relative error ~2^-22, flushes subnormal results)
+__device__ __forceinline__ float ex2_approx(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+__global__ void __launch_bounds__(kGprThreads, 2)
     k_gpr_tc(int N, int ntiles, const unsigned char *__restrict__ img_model,
              const unsigned char *__restrict__ img_atoms, const float *__restrict__ xs,
              const float *__restrict__ xn, const float *__restrict__ invth, int D,
@@ -83,8 +94,9 @@ __global__ void __launch_bounds__(kGprThreads, 1)
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + kOffBar + 32);
   int *abort_flag = reinterpret_cast<int *>(sm + kOffBar + 40);
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
-                     smem_u32(tmem_slot))
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "n"(kTmemCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -100,12 +112,18 @@ __global__ void __launch_bounds__(kGprThreads, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const uint32_t tC1 = tmem, tC2 = tmem + 128;
+  const uint32_t tC1 = tmem, tC2 = tmem + kTileK;
   const uint32_t lane_base = (uint32_t)(quad * 32) << 16;  // this warp's TMEM lanes
   const int row = quad * 32 + lane;                         // atom row of this thread
   const int i = blockIdx.x * kRows + row;
   const float xnorm = (i < N) ? xn[i] : 0.f;
-  float ehi = 0.f, elo = 0.f;
+  // w = c exp(-s/2) = c 2^(log2e v + a2_i + b2_k) with a2_i = -log2e |x''_i|^2 / 2
+  // and b2_k = -log2e |m''_k|^2 / 2 (the image stores b2): one add, one FMA
+  // and ex2 per element.  e = sum w in four independent Kahan chains, one per
+  // element pair of a core-matrix row, so consecutive elements do not wait
+  // on each other.
+  const float a2 = -0.5f * kLog2e * xnorm;
+  float esum[4] = {0.f, 0.f, 0.f, 0.f}, ecmp[4] = {0.f, 0.f, 0.f, 0.f};
   const uint32_t id1 = instr_desc(kRows, kTileK), id2 = instr_desc(kRows, kDP);
   uint32_t ph_a = 0, ph_b = 0, ph_g1 = 0, ph_g2 = 0;
   bool pend_a = false, pend_b = false, pend_g1 = false, pend_g2 = false;
@@ -116,19 +134,19 @@ __global__ void __launch_bounds__(kGprThreads, 1)
   auto load_a = [&](int t, bool first) {
     if (tid == 0) {
       const unsigned char *img = img_model + (size_t)t * kImgTile;
-      mbar_expect_tx(bar_a, 2 * kTileBytes16 + kMncBytes + (first ? kImgAtoms : 0));
+      mbar_expect_tx(bar_a, 2 * kMBytes16 + kMncBytes + (first ? kImgAtoms : 0));
       if (first)
         bulk_g2s(s_base + kOffXh, img_atoms + (size_t)blockIdx.x * kImgAtoms, kImgAtoms, bar_a);
-      bulk_g2s(s_base + kOffMh, img, 2 * kTileBytes16, bar_a);
-      bulk_g2s(s_base + kOffMnc + (t & 1) * kMncBytes, img + 4 * kTileBytes16, kMncBytes, bar_a);
+      bulk_g2s(s_base + kOffMh, img, 2 * kMBytes16, bar_a);
+      bulk_g2s(s_base + kOffMnc + (t & 1) * kMncBytes, img + 4 * kMBytes16, kMncBytes, bar_a);
     }
     pend_a = true;
   };
   auto load_b = [&](int t) {
     if (tid == 0) {
-      mbar_expect_tx(bar_b, 2 * kTileBytes16);
-      bulk_g2s(s_base + kOffMhT, img_model + (size_t)t * kImgTile + 2 * kTileBytes16,
-               2 * kTileBytes16, bar_b);
+      mbar_expect_tx(bar_b, 2 * kMBytes16);
+      bulk_g2s(s_base + kOffMhT, img_model + (size_t)t * kImgTile + 2 * kMBytes16,
+               2 * kMBytes16, bar_b);
     }
     pend_b = true;
   };
@@ -145,7 +163,7 @@ __global__ void __launch_bounds__(kGprThreads, 1)
       pend_a = false;
     }
     if (!__syncthreads_and(ok)) break;
-    // GEMM1: C1[128 x 128] = xh.mh + xh.ml + xl.mh over K = 64 (4 steps of 16)
+    // GEMM1: C1[128 x 64] = xh.mh + xh.ml + xl.mh over K = 64 (4 steps of 16)
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t a_off[3] = {kOffXh, kOffXh, kOffXl};
@@ -170,25 +188,32 @@ __global__ void __launch_bounds__(kGprThreads, 1)
     if (t + 1 < ntiles) load_a(t + 1, false);
     // epilogue 1: w = c exp(-s/2), e += w, W tile (bf16 hi / lo) for GEMM2
     unsigned char *wh = sm + kOffWh, *wl = sm + kOffWl;
+    constexpr int kHalfBlocks = kTileK / 64;  // 32-column blocks per column half
 #pragma unroll 1
-    for (int cc = 2 * half; cc < 2 * half + 2; ++cc) {
+    for (int cc = kHalfBlocks * half; cc < kHalfBlocks * (half + 1); ++cc) {
       float v[32];
       tmem_ld32(tC1 + lane_base + cc * 32, v);
 #pragma unroll
       for (int g = 0; g < 4; ++g) {
         uint32_t hpk[4], lpk[4];
+        const int kg = cc * 32 + g * 8;
+        const float4 b0 = *reinterpret_cast<const float4 *>(smn + kg);
+        const float4 b1 = *reinterpret_cast<const float4 *>(smn + kg + 4);
+        const float4 c0 = *reinterpret_cast<const float4 *>(sc + kg);
+        const float4 c1 = *reinterpret_cast<const float4 *>(sc + kg + 4);
+        const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+        const float cv[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
 #pragma unroll
         for (int h = 0; h < 4; ++h) {
           float w2[2];
 #pragma unroll
           for (int u = 0; u < 2; ++u) {
-            const int k = cc * 32 + g * 8 + h * 2 + u;
-            const float s = xnorm + smn[k] - 2.f * v[g * 8 + h * 2 + u];
-            const float w = sc[k] * __expf(-0.5f * s);
-            const float tt = ehi + w;  // two-sum
-            const float bb = tt - ehi;
-            elo += (ehi - (tt - bb)) + (w - bb);
-            ehi = tt;
+            const int q = h * 2 + u;
+            const float w = cv[q] * ex2_approx(fmaf(v[g * 8 + q], kLog2e, a2 + bv[q]));
+            const float y = w - ecmp[h];  // Kahan
+            const float tt = esum[h] + y;
+            ecmp[h] = (tt - esum[h]) - y;
+            esum[h] = tt;
             w2[u] = w;
           }
           const __nv_bfloat162 hi = __floats2bfloat162_rn(w2[0], w2[1]);
@@ -210,7 +235,7 @@ __global__ void __launch_bounds__(kGprThreads, 1)
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     if (!__syncthreads_and(ok)) break;
-    // GEMM2: C2[128 x 64] += wh.mhT + wh.mlT + wl.mhT over K = 128 (8 steps of 16)
+    // GEMM2: C2[128 x 64] += wh.mhT + wh.mlT + wl.mhT over K = 64 (4 steps of 16)
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t a_off[3] = {kOffWh, kOffWh, kOffWl};
@@ -236,9 +261,12 @@ __global__ void __launch_bounds__(kGprThreads, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     // the two column halves' partial energies, summed in a fixed order
     double *ep = reinterpret_cast<double *>(sm + kOffEp);
-    if (half == 1) ep[row] = (double)ehi + (double)elo;
+    double emine = 0.0;
+#pragma unroll
+    for (int h = 0; h < 4; ++h) emine += (double)esum[h] - (double)ecmp[h];
+    if (half == 1) ep[row] = emine;
     __syncthreads();
-    if (half == 0) ep[row] = ((double)ehi + (double)elo) + ep[row];
+    if (half == 0) ep[row] = emine + ep[row];
     __syncthreads();
     const double etot = ep[row];
     float c2[32];
@@ -263,7 +291,9 @@ __global__ void __launch_bounds__(kGprThreads, 1)
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "n"(kTmemCols)
+                 : "memory");
 }
 
 // x'' = G / theta - mu (FP32, row-padded to 64), |x''|^2, and the xh/xl tiles
@@ -296,7 +326,7 @@ __global__ void k_tc_prep_atoms(int N, int D, const float *__restrict__ G,
     }
     const int off = kmajor_off(r, k0, kDP / 8);
     *reinterpret_cast<uint4 *>(tile + off) = make_uint4(hp[0], hp[1], hp[2], hp[3]);
-    *reinterpret_cast<uint4 *>(tile + kTileBytes16 + off) = make_uint4(lp[0], lp[1], lp[2], lp[3]);
+    *reinterpret_cast<uint4 *>(tile + kXBytes16 + off) = make_uint4(lp[0], lp[1], lp[2], lp[3]);
   }
   if (i < N) xn[i] = nrm;
 }
@@ -322,7 +352,8 @@ float bf16_val(uint16_t b) {
 size_t tc_smem_bytes() { return kSmemBytes; }
 
 // Builds the model's tensor-core image: per sparse tile mh, ml (K-major over
-// D), mhT, mlT (K-major over the tile's points), |m''|^2 and c (FP32), plus mu.
+// D), mhT, mlT (K-major over the tile's points), b2 = -log2e |m''|^2 / 2 and c
+// (FP32), plus mu.
 gapgb_status build_tc_image(gapgb_model *m) {
   if (m->d_tc) return GAPGB_OK;
   const HostModel &h = m->host;
@@ -342,7 +373,7 @@ gapgb_status build_tc_image(gapgb_model *m) {
   std::vector<unsigned char> img((size_t)nt * kImgTile, 0);
   for (int t = 0; t < nt; ++t) {
     unsigned char *T = img.data() + (size_t)t * kImgTile;
-    float *mn = reinterpret_cast<float *>(T + 4 * kTileBytes16);
+    float *mn = reinterpret_cast<float *>(T + 4 * kMBytes16);
     float *cf = mn + kTileK;
     for (int kk = 0; kk < kTileK; ++kk) {
       const int k = t * kTileK + kk;
@@ -355,12 +386,12 @@ gapgb_status build_tc_image(gapgb_model *m) {
         const uint16_t lb = bf16_bits((float)(v - (double)bf16_val(hb)));
         // GEMM1 B operand: rows = sparse points, K = descriptor components
         std::memcpy(T + kmajor_off(kk, d, kDP / 8), &hb, 2);
-        std::memcpy(T + kTileBytes16 + kmajor_off(kk, d, kDP / 8), &lb, 2);
+        std::memcpy(T + kMBytes16 + kmajor_off(kk, d, kDP / 8), &lb, 2);
         // GEMM2 B operand: rows = descriptor components, K = sparse points
-        std::memcpy(T + 2 * kTileBytes16 + kmajor_off(d, kk, kTileK / 8), &hb, 2);
-        std::memcpy(T + 3 * kTileBytes16 + kmajor_off(d, kk, kTileK / 8), &lb, 2);
+        std::memcpy(T + 2 * kMBytes16 + kmajor_off(d, kk, kTileK / 8), &hb, 2);
+        std::memcpy(T + 3 * kMBytes16 + kmajor_off(d, kk, kTileK / 8), &lb, 2);
       }
-      mn[kk] = (float)nrm;
+      mn[kk] = (float)(-0.5 * 1.4426950408889634 * nrm);  // b2_k = -log2e |m''_k|^2 / 2
       cf[kk] = (float)h.coeff[k];
     }
   }
@@ -391,6 +422,8 @@ void launch_gpr_tc(gapgb_model *m, Workspace &ws, int N, cudaStream_t st) {
   k_tc_prep_atoms<<<(tiles * kRows + 127) / 128, 128, 0, st>>>(N, D, (const float *)ws.G,
                                                                 m->d_invth32, mu, xs, xn, img_atoms);
   cudaFuncSetAttribute(k_gpr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+  cudaFuncSetAttribute(k_gpr_tc, cudaFuncAttributePreferredSharedMemoryCarveout,
+                       cudaSharedmemCarveoutMaxShared);
   k_gpr_tc<<<tiles, kGprThreads, kSmemBytes, st>>>(N, m->tc_tiles, (const unsigned char *)m->d_tc,
                                           img_atoms, xs, xn, m->d_invth32, D, ws.e,
                                           (float *)ws.dedg, ws.d_flags);
