@@ -413,8 +413,10 @@ def run_population(args):
                        "autotuned": {k: best[k] for k in ("precision", "generic_kernels", "cap")},
                        "tune_errors": {"dE_per_atom": best["dE_per_atom"], "dF": best["dF"]},
                        "l2": "flushed between steps (512 MB write)"},
-            # one graph launch per step holding the 12 kernels of an evaluation
-            "gpu_launches": 12 * args.steps}
+            # one graph launch per step holding the 9 kernels of a grouped-kernel
+            # evaluation (see the headline workload's count); the generic
+            # kernels add the reverse slots, the force gather and the orphans
+            "gpu_launches": (12 if best["generic_kernels"] else 9) * args.steps}
     print(json.dumps(line), flush=True)
     g.close()
     m.close()
@@ -614,11 +616,11 @@ def run_surrogate(args):
                           "dF_max": max(x[1] for x in errs), "structures": 2}
     except Exception as ex:  # the oracle is a checker; its absence does not stop the bench
         oracle_err = {"unavailable": str(ex)[:200]}
-    # kernels per surrogate evaluation: prep x2, neighbours, reverse, descriptors,
+    # kernels per surrogate evaluation: prep x2, neighbours, descriptors,
     # surrogate (count, segments, scatter, weight image, row image, tensor-core
-    # MLP, committee), fallback select, row-list GPR + reduce, slot gradients,
-    # forces, orphans, structure partial + final sums
-    launches_per_eval = 20
+    # MLP, committee), fallback select, row-list GPR + reduce, slot gradients
+    # (forces scattered in the same kernel), structure partial + final sums
+    launches_per_eval = 17
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
             "steps": len(chunks), "warmup": max(3, args.warmup),
             "ms_per_step": ms_total / len(chunks), "higher_is_better": True,
@@ -744,12 +746,12 @@ def run_md(args):
                 "t_end": {"dE_per_atom": float(abs(Et[0] - Ep[0]) / N),
                           "dF_max": float(np.abs(Ft - Fp).max()),
                           "dstress_max_GPa": float(np.abs(St - Sp).max())}},
-            # per step: kick+drift, wrap or skin check, prep x2, refresh, reverse,
-            # descriptors, tensor-core GPR (prep + kernel), slot gradients, forces,
-            # orphans, structure sums x2, kick, kinetic sums x2 = 17; a rebuild
-            # step adds the build, the bins (offsets, count, scan, fill) and the
-            # binned build in place of the refresh (+5)
-            "gpu_launches": 17 * args.md_steps + 5 * (args.md_steps // 10),
+            # per step: kick+drift, wrap or skin check, prep x2, refresh,
+            # descriptors, tensor-core GPR (prep + kernel), slot gradients with
+            # the force scatter, structure sums x2, kick, kinetic sums x2 = 14; a
+            # rebuild step adds the build, the bins (offsets, count, scan, fill)
+            # and the binned build in place of the refresh (+5)
+            "gpu_launches": 14 * args.md_steps + 5 * (args.md_steps // 10),
             "clocks": tc["clocks"]}
     print(json.dumps(line), flush=True)
 
@@ -822,7 +824,7 @@ def run_precision(args):
             "config": {"workload": "precision forms on alloy512 x %d (D=64, M=4000)" % S,
                        "atoms": N, "l2": "flushed between steps (512 MB write)"},
             "forms": res, "errors_vs_oracle": orc,
-            "gpu_launches": 12 * args.steps}
+            "gpu_launches": 9 * args.steps}
     print(json.dumps(line), flush=True)
 
 
@@ -1155,10 +1157,10 @@ def main():
         "clocks": clocks,
     }
     # kernels launched per step (count from the library's launch sequence):
-    # prep x2, neighbour build, reverse slots, descriptors, GPR (tensor-core
-    # form: operand prep + kernel; SIMT forms: kernel + split reduce), slot
-    # gradients, forces, orphans, structure partial + final sums
-    line["gpu_launches"] = args.steps * 12
+    # prep x2, neighbour build, descriptors, GPR (tensor-core form: operand
+    # prep + kernel; SIMT forms: kernel + split reduce), slot gradients (the
+    # grouped kernel scatters the forces itself), structure partial + final sums
+    line["gpu_launches"] = args.steps * 9
     if world == 1:
         line["cpu_baseline"] = cpu_baseline(arrays)
     print(json.dumps(line), flush=True)

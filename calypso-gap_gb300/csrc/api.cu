@@ -284,7 +284,8 @@ gapgb_status enqueue_tail(gapgb_model *m, int S, int N, int cap, int capS, int l
                           double *d_stress, double *d_atom_e, cudaStream_t st) {
   Workspace &ws = m->ws;
   const bool prof = m->profile_stages;
-  launch_reverse(ws, N, cap, st);
+  // reverse slots serve the force gather only
+  if (lgrad && !bwd_scatters_forces(m)) launch_reverse(ws, N, cap, st);
   if (prof) cudaEventRecord(m->ev[1], st);
   const bool fp64 = m->precision == GAPGB_PREC_FP64;
   if (fp64) launch_wacsf_fwd<double>(m, ws, N, cap, capS, st);
@@ -314,11 +315,11 @@ gapgb_status enqueue_tail(gapgb_model *m, int S, int N, int cap, int capS, int l
   if (prof) cudaEventRecord(m->ev[3], st);
   if (lgrad) {
     if (fp64) {
-      launch_wacsf_bwd<double>(m, ws, N, cap, capS, st);
+      launch_wacsf_bwd<double>(m, ws, N, cap, capS, d_force, st);
       launch_forces<double>(ws, N, cap, d_force, st);
     } else {
-      launch_wacsf_bwd<float>(m, ws, N, cap, capS, st);
-      launch_forces<float>(ws, N, cap, d_force, st);
+      if (!launch_wacsf_bwd<float>(m, ws, N, cap, capS, d_force, st))
+        launch_forces<float>(ws, N, cap, d_force, st);
     }
   } else {
     cudaMemsetAsync(d_force, 0, sizeof(double) * 3 * (size_t)N, st);
@@ -396,8 +397,7 @@ gapgb_status eval_host(gapgb_model *m, int S, const int *atom_off, const int *sp
     if (st) return st;
     const int capS = maxcnt > 0 ? maxcnt : 1;
     if (d_G_out) {
-      // descriptors only (gapgb_descriptors)
-      launch_reverse(ws, N, cap, s);
+      // descriptors only (gapgb_descriptors, gapgb_variance, gapgb_fit_energies)
       if (m->precision == GAPGB_PREC_FP64) launch_wacsf_fwd<double>(m, ws, N, cap, capS, s);
       else launch_wacsf_fwd<float>(m, ws, N, cap, capS, s);
       GAPGB_CUDA_TRY(cudaGetLastError());

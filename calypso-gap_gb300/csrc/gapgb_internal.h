@@ -372,9 +372,14 @@ void launch_refresh(Workspace &ws, int N, int cap, cudaStream_t st, bool exact =
 template <typename T>
 void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int cap_smem,
                       cudaStream_t st);
+// whether the FP32 gradient kernel of this model scatters the forces itself
+// (the reverse slots are then not needed)
+bool bwd_scatters_forces(const gapgb_model *m);
+// returns true when the kernel scattered the forces into d_force itself
+// (grouped FP32 kernels); otherwise launch_forces gathers the slot gradients
 template <typename T>
-void launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int cap_smem,
-                      cudaStream_t st);
+bool launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int cap_smem,
+                      double *d_force, cudaStream_t st);
 template <typename T, typename TG>
 void launch_gpr(const gapgb_model *m, Workspace &ws, int N, cudaStream_t st);
 void launch_gpr_tc(gapgb_model *m, Workspace &ws, int N, cudaStream_t st);

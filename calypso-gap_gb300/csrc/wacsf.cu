@@ -539,9 +539,16 @@ void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
                                                (T *)ws.G);
 }
 
+bool bwd_scatters_forces(const gapgb_model *m) {
+  GrpFwd gf;
+  GrpBwd gb;
+  return m->precision != GAPGB_PREC_FP64 && !m->generic_kernels &&
+         grouped_kernels(m->sft32h, &gf, &gb);
+}
+
 template <typename T>
-void launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int capS,
-                      cudaStream_t st) {
+bool launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int capS,
+                      double *d_force, cudaStream_t st) {
   const size_t smem = wacsf_smem_bytes(m->sfh, capS, false, sizeof(T));
   if constexpr (std::is_same<T, float>::value) {
     GrpFwd gf;
@@ -554,11 +561,11 @@ void launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
       cudaFuncSetAttribute(gb, cudaFuncAttributePreferredSharedMemoryCarveout,
                            cudaSharedmemCarveoutMaxShared);
       const int grid = warp_grid(N, smg, (const void *)gb);
+      cudaMemsetAsync(d_force, 0, sizeof(double) * 3 * (size_t)N, st);
       gb<<<grid, 32 * kWarpsPerBlock, smg, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
                                                    ws.apos, ws.nbr_d32, ws.nbr_w32, m->d_sft32,
-                                                   (const float *)ws.dedg, (float4 *)ws.gslot,
-                                                   ws.wvir);
-      return;
+                                                   (const float *)ws.dedg, d_force, ws.wvir);
+      return true;  // forces scattered by the kernel
     }
   }
   auto fn = k_wacsf_bwd<T>;
@@ -568,11 +575,15 @@ void launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
                                                ws.apos, ws.nbr_d32, ws.nbr_w32, sft_of<T>(m),
                                                (const T *)ws.dedg,
                                                (typename Vec4<T>::type *)ws.gslot, ws.wvir);
+  (void)d_force;
+  return false;  // slot gradients in ws.gslot: launch_forces gathers them
 }
 
 template void launch_wacsf_fwd<double>(const gapgb_model *, Workspace &, int, int, int, cudaStream_t);
 template void launch_wacsf_fwd<float>(const gapgb_model *, Workspace &, int, int, int, cudaStream_t);
-template void launch_wacsf_bwd<double>(const gapgb_model *, Workspace &, int, int, int, cudaStream_t);
-template void launch_wacsf_bwd<float>(const gapgb_model *, Workspace &, int, int, int, cudaStream_t);
+template bool launch_wacsf_bwd<double>(const gapgb_model *, Workspace &, int, int, int, double *,
+                                       cudaStream_t);
+template bool launch_wacsf_bwd<float>(const gapgb_model *, Workspace &, int, int, int, double *,
+                                      cudaStream_t);
 
 }  // namespace gapgb

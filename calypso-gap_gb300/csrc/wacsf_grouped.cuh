@@ -17,7 +17,8 @@
 // arithmetic, so all lanes work on contributing pairs.  The gradient kernel
 // accumulates slot gradients with shared-memory FP32 atomics (summation
 // order, hence the last bits, may vary between runs; the FP64 path keeps the
-// deterministic round-robin schedule).
+// deterministic round-robin schedule) and scatters the forces with FP64
+// atomics in place of the reverse-slot gather.
 
 constexpr int kPairQ = 64;
 // resident blocks per SM the grouped kernels are compiled for (80 registers
@@ -323,10 +324,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
                     const double4 *__restrict__ xyzr, const int *__restrict__ nj,
                     const double4 *__restrict__ apos, const float4 *__restrict__ d32,
                     const float *__restrict__ w32, const SFT<float> *__restrict__ sfg,
-                    const float *__restrict__ dedg, float4 *__restrict__ gslot,
+                    const float *__restrict__ dedg, double *__restrict__ force,
                     double *__restrict__ wvir) {
   (void)xyzr;
-  (void)nj;
   (void)apos;
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ int s_qjk[kWarpsPerBlock][kPairQ];
@@ -462,10 +462,20 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
         });
     }
     __syncwarp();
+    // forces by scatter: with g_q = sum_d dE/dG_id dG_id/dp_q and the
+    // translation invariance of G_i, atom i receives +sum_q g_q and slot q's
+    // atom -g_q (FP64 atomics; F is zeroed before the launch)
     float W[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    float fx = 0.f, fy = 0.f, fz = 0.f;
     for (int q = lane; q < P; q += 32) {
       const float gx = L.gx[q], gy = L.gy[q], gz = L.gz[q];
-      gslot[(size_t)i * cap + q] = make_float4(gx, gy, gz, 0.f);
+      const int j = nj[(size_t)i * cap + q];
+      atomicAdd(force + (size_t)j * 3 + 0, -(double)gx);
+      atomicAdd(force + (size_t)j * 3 + 1, -(double)gy);
+      atomicAdd(force + (size_t)j * 3 + 2, -(double)gz);
+      fx += gx;
+      fy += gy;
+      fz += gz;
       const float4 aq = L.a[q];
       const float d3[3] = {aq.x, aq.y, aq.z};
       const float g3[3] = {gx, gy, gz};
@@ -473,6 +483,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
       for (int aa = 0; aa < 3; ++aa)
 #pragma unroll
         for (int bb = 0; bb < 3; ++bb) W[aa * 3 + bb] += d3[aa] * g3[bb];
+    }
+    fx = warp_sum<float>(fx);
+    fy = warp_sum<float>(fy);
+    fz = warp_sum<float>(fz);
+    if (lane == 0) {
+      atomicAdd(force + (size_t)i * 3 + 0, (double)fx);
+      atomicAdd(force + (size_t)i * 3 + 1, (double)fy);
+      atomicAdd(force + (size_t)i * 3 + 2, (double)fz);
     }
     // per-atom virial in FP32 (a sum over its own slots); the sums over
     // atoms are FP64 (k_struct_reduce)
