@@ -120,6 +120,13 @@ __device__ __forceinline__ float pow_iz(float b, int iz, float *pm1) {
   return p * b;
 }
 
+// (1 + cos), (1 - cos), (1 + cos)^2, (1 - cos)^2, (1 + cos)^4, (1 - cos)^4 in the
+// degree-4 Bernstein basis u^n w^(4-n), u = (1 + cos)/2, w = 1 - u:
+// 2u = 2u(u+w)^3, 2w = 2w(u+w)^3, 4u^2 = 4u^2(u+w)^2, ..., 16u^4, 16w^4
+__constant__ float kBern[6][5] = {{0.f, 2.f, 6.f, 6.f, 2.f},  {2.f, 6.f, 6.f, 2.f, 0.f},
+                                  {0.f, 0.f, 4.f, 8.f, 4.f},  {4.f, 8.f, 4.f, 0.f, 0.f},
+                                  {0.f, 0.f, 0.f, 0.f, 16.f}, {16.f, 0.f, 0.f, 0.f, 0.f}};
+
 // A_c = (1 + lambda_c cos)^zeta_c and dA_c/dcos for the combinations of a
 // pair: closed form for the standard set (STD: c = 2 log2(zeta) + (lambda < 0)),
 // integer powers otherwise
@@ -244,6 +251,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
   __shared__ int s_qjk[kWarpsPerBlock][kPairQ];
   __shared__ float s_qc2[kWarpsPerBlock][kPairQ];
   __shared__ float s_acc[kWarpsPerBlock][2 * NAL * NC];
+  __shared__ float s_out[kWarpsPerBlock][(STD && NC == 6) ? 2 * NAL * NC : 1];
   load_table<float>(smraw, sfg);
   const SFT<float> &sf = *reinterpret_cast<const SFT<float> *>(smraw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -266,11 +274,17 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
     float *Gi = G + (size_t)i * D;
     radial_fwd(L, sf, P, capS, lane, Gi);
     if (nang == 0) continue;
-    float acc[NAL][NC], accw[NAL][NC];
+    // the standard set accumulates the degree-4 Bernstein moments
+    // sum EF u^n w^(4-n) (u = (1 + cos)/2, w = 1 - u), from which every
+    // (1 +- cos)^zeta follows with non-negative weights (kBern); other sets
+    // accumulate their NC powers directly
+    constexpr bool kB = STD && NC == 6;
+    constexpr int NB = kB ? 5 : NC;
+    float acc[NAL][NB], accw[NAL][NB];
 #pragma unroll
     for (int q = 0; q < NAL; ++q)
 #pragma unroll
-      for (int c = 0; c < NC; ++c) acc[q][c] = accw[q][c] = 0.f;
+      for (int c = 0; c < NB; ++c) acc[q][c] = accw[q][c] = 0.f;
     if (P > 1)
       pair_stream(L.a, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
         if (!ok) return;
@@ -285,34 +299,57 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
 #pragma unroll
         for (int q = 0; q < NAL; ++q)
           EF[q] = q < nal ? f4get(Ej, q) * f4get(Ek, q) * __expf(-alv[q] * c2) * F : 0.f;
-        float Ac[NC];
-        ang_powers<NC, STD>(cosv, clam, ciz, Ac, nullptr);
+        float basis[NB];
+        if constexpr (kB) {
+          const float u = fmaf(0.5f, cosv, 0.5f), w = fmaf(-0.5f, cosv, 0.5f);
+          const float u2 = u * u, w2 = w * w, uw = u * w;
+          basis[0] = w2 * w2;
+          basis[1] = uw * w2;
+          basis[2] = u2 * w2;
+          basis[3] = uw * u2;
+          basis[4] = u2 * u2;
+        } else {
+          ang_powers<NC, STD>(cosv, clam, ciz, basis, nullptr);
+        }
 #pragma unroll
-        for (int cc = 0; cc < NC; ++cc) {
+        for (int q = 0; q < NAL; ++q) {
+          const float efw = EF[q] * wjk;
 #pragma unroll
-          for (int q = 0; q < NAL; ++q) {
-            const float v = Ac[cc] * EF[q];
-            acc[q][cc] += v;
-            accw[q][cc] += v * wjk;
+          for (int n = 0; n < NB; ++n) {
+            acc[q][n] = fmaf(basis[n], EF[q], acc[q][n]);
+            accw[q][n] = fmaf(basis[n], efw, accw[q][n]);
           }
         }
       });
 #pragma unroll
     for (int q = 0; q < NAL; ++q)
 #pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        const float x = warp_sum(acc[q][c]), y = warp_sum(accw[q][c]);
+      for (int n = 0; n < NB; ++n) {
+        const float x = warp_sum(acc[q][n]), y = warp_sum(accw[q][n]);
         if (lane == 0) {
-          s_acc[warp][q * NC + c] = x;
-          s_acc[warp][NAL * NC + q * NC + c] = y;
+          s_acc[warp][q * NB + n] = x;
+          s_acc[warp][NAL * NB + q * NB + n] = y;
         }
       }
     __syncwarp();
+    if constexpr (kB) {
+      // moments -> the six (1 +- cos)^zeta grids, combination order of ang_powers
+      for (int e = lane; e < 2 * NAL * NC; e += 32) {
+        const int part = e / (NAL * NC), q = (e / NC) % NAL, cc = e % NC;
+        const float *mo = &s_acc[warp][part * NAL * NB + q * NB];
+        float v = 0.f;
+#pragma unroll
+        for (int n = 0; n < 5; ++n) v = fmaf(kBern[cc][n], mo[n], v);
+        s_out[warp][part * NAL * NC + q * NC + cc] = v;
+      }
+      __syncwarp();
+    }
+    const float *grid = kB ? s_out[warp] : s_acc[warp];
     for (int s = lane; s < nang; s += 32) {
       const int cell = ((sf.ang_code[s] >> 8) & 255) * NC + sf.ang_comb[s];
       const int d = sf.ang_d[s];
-      Gi[d] = sf.ang_pref[s] * s_acc[warp][cell];
-      Gi[d + nsf] = sf.ang_pref[s] * s_acc[warp][NAL * NC + cell];
+      Gi[d] = sf.ang_pref[s] * grid[cell];
+      Gi[d + nsf] = sf.ang_pref[s] * grid[NAL * NC + cell];
     }
     __syncwarp();
   }
