@@ -373,11 +373,41 @@ gapgb_status eval_host(gapgb_model *m, int S, const int *atom_off, const int *sp
   GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_species, species, sizeof(int) * N, cudaMemcpyHostToDevice, s));
   GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_lat, lat, sizeof(double) * 9 * S, cudaMemcpyHostToDevice, s));
   GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_pos, pos, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s));
+  const int maxa = max_struct_atoms(S, atom_off);
+  if (!d_G_out && m->caps_hint > 0 && m->caps_hint <= m->cap) {
+    // one synchronisation: the descriptor kernels take the slot count of the
+    // previous call; the neighbour kernel reports the true maximum, and a
+    // batch that needs more slots (or overflows the capacity) is recomputed
+    // by the general path below
+    const int cap = m->cap, capS = m->caps_hint;
+    if (m->precision == GAPGB_PREC_SURROGATE) {
+      st = ensure_surrogate(m, N);
+      if (st) return st;
+    }
+    GAPGB_CUDA_TRY(cudaMemsetAsync(ws.d_flags, 0, 8 * sizeof(int), s));
+    if (m->profile_stages) cudaEventRecord(m->ev[0], s);
+    launch_prep(m, ws, S, N, ws.d_atom_off, ws.d_species, ws.d_lat, ws.d_pos, m->host.rcut, s,
+                maxa >= kBinMinAtoms);
+    launch_neighbors(ws, S, N, maxa, cap, m->host.rcut, s, m->precision == GAPGB_PREC_FP64);
+    st = enqueue_tail(m, S, N, cap, capS, lgrad, ws.d_species, ws.d_energy, ws.d_force,
+                      ws.d_stress, ws.d_atom_e, s);
+    if (st) return st;
+    GAPGB_CUDA_TRY(cudaMemcpyAsync(energy, ws.d_energy, sizeof(double) * S, cudaMemcpyDeviceToHost, s));
+    if (force) GAPGB_CUDA_TRY(cudaMemcpyAsync(force, ws.d_force, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, s));
+    if (stress) GAPGB_CUDA_TRY(cudaMemcpyAsync(stress, ws.d_stress, sizeof(double) * 6 * S, cudaMemcpyDeviceToHost, s));
+    if (atom_e) GAPGB_CUDA_TRY(cudaMemcpyAsync(atom_e, ws.d_atom_e, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+    GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.h_flags, ws.d_flags, 8 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    GAPGB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (!(ws.h_flags[0] & kFlagNeighbourOverflow) && ws.h_flags[1] <= capS) {
+      read_stage_times(m);
+      m->caps_hint = std::min(cap, std::max(8, (ws.h_flags[1] + 7) / 8 * 8));
+      return flags_to_status(ws.h_flags);
+    }
+  }
   for (int attempt = 0; attempt < 3; ++attempt) {
     const int cap = m->cap;
     GAPGB_CUDA_TRY(cudaMemsetAsync(ws.d_flags, 0, 8 * sizeof(int), s));
     if (m->profile_stages) cudaEventRecord(m->ev[0], s);
-    const int maxa = max_struct_atoms(S, atom_off);
     launch_prep(m, ws, S, N, ws.d_atom_off, ws.d_species, ws.d_lat, ws.d_pos, m->host.rcut, s,
                 maxa >= kBinMinAtoms);
     launch_neighbors(ws, S, N, maxa, cap, m->host.rcut, s,
@@ -419,6 +449,7 @@ gapgb_status eval_host(gapgb_model *m, int S, const int *atom_off, const int *sp
     GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.h_flags, ws.d_flags, 8 * sizeof(int), cudaMemcpyDeviceToHost, s));
     GAPGB_CUDA_TRY(cudaStreamSynchronize(s));
     read_stage_times(m);
+    m->caps_hint = std::min(cap, std::max(8, (maxcnt + 7) / 8 * 8));
     return flags_to_status(ws.h_flags);
   }
   return fail(GAPGB_ERR_NEIGHBOUR_OVERFLOW, "neighbour capacity could not be grown");

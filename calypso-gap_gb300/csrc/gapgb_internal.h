@@ -315,6 +315,7 @@ struct gapgb_model {
   int device = 0;
   int precision = GAPGB_PREC_FP64;
   int cap = 256;
+  int caps_hint = 0;                   // slot count the host-buffer calls size the descriptor kernels for
   bool generic_kernels = false;        // force the generic FP32 descriptor kernels
   cudaStream_t stream = nullptr;       // internal stream of the host-buffer calls
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
