@@ -262,21 +262,21 @@ def cpu_baseline(arrays):
 STAGES = ["neighbours", "descriptors", "gpr", "chain_rule"]
 # algorithmic HBM bytes per atom of each stage's kernels (P = 56 neighbour
 # slots per atom on this workload, D = 64, FP32 slot records):
-#   neighbours : positions in, slot records out (xyz+r 32 B, j 4, shift 4,
-#                FP32 record 16, weight 4, reverse index 4) per slot
+#   neighbours : positions in, slot records out per slot (j 4, shift 4,
+#                FP32 record 16, weight 4)
 #   descriptors: FP32 slot record + weight in per slot, D FP32 descriptors out
-#   chain_rule : slot record + weight in, slot gradient (16 B) out per slot,
-#                dE/dG row in, per-atom virial (72 B) out, force gather
-#                (2 slot gradients + index per slot) and 24 B of force out
+#   chain_rule : slot record + weight + partner index in per slot, dE/dG row
+#                in, per-atom virial (72 B) out, and the force scatter: 24 B
+#                (an FP64 atomic add per component) per slot and per atom
 P_SLOTS = 56.0
 
 
 def stage_bytes_per_atom(D):
     P = P_SLOTS
-    return {"neighbours": 32.0 + P * 64.0,
+    return {"neighbours": 32.0 + P * 28.0,
             "descriptors": P * 20.0 + D * 4.0,
             "gpr": D * 4.0 * 2 + 8.0,
-            "chain_rule": P * 36.0 + D * 4.0 + 72.0 + P * 36.0 + 24.0}
+            "chain_rule": P * 24.0 + D * 4.0 + 72.0 + P * 24.0 + 24.0}
 
 
 def load_peaks():
