@@ -68,14 +68,6 @@ constexpr int kOffEp = kOffBar + 64;                      // partial energies [1
 constexpr int kSmemBytes = kOffEp + kRows * 8 + 1024;     // + alignment slack
 constexpr int kGprThreads = 256;  // warps w and w + 4 share TMEM lanes and split the columns
 constexpr int kTmemCols = 128;    // C1 (kTileK columns) and C2 (kDP columns)
-constexpr float kLog2e = 1.4426950408889634f;
-
-// 2^x (PTX ex2.approx.ftz: relative error ~2^-22, flushes subnormal results)
-__device__ __forceinline__ float ex2_approx(float x) {
-  float r;
-  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-  return r;
-}
 
 __global__ void __launch_bounds__(kGprThreads, 2)
     k_gpr_tc(int N, int ntiles, const unsigned char *__restrict__ img_model,

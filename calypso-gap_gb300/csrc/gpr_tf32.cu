@@ -8,12 +8,12 @@
 //           = |x~_i - m~_k|^2 up to FP32 rounding, so a close pair keeps a
 //             small distance error (the rounding of x and m enters as
 //             (x - m).(dx - dm), not as |x| |m| 2^-11)
-//   w_ik    = c_k exp(-s_ik / 2),  e_i = sum_k w_ik (compensated FP32)
+//   w_ik    = c_k exp(-s_ik / 2),  e_i = sum_k w_ik (compensated FP32, Kahan)
 //   (W M~)  GEMM2 with W rounded to TF32, K = M
 //   dE/dG_id = -(1/theta_d) (x''_id e_i - (W M~)_id)
 // The same CTA structure as the split-BF16 kernel: 128 atoms per CTA, tiles of
-// 128 sparse points whose GEMM1 half (m~, |m~|^2, c) and GEMM2 half (m~^T)
-// load under the other half's compute; 8 warps share the epilogue.  Operands
+// 64 sparse points whose GEMM1 half (m~, b2, c) and GEMM2 half (m~^T) load
+// under the other half's compute; 8 warps share the epilogue; two CTAs per SM.  Operands
 // are K-major, no swizzle, 32-bit elements: core matrices of 8 rows x 4
 // elements (16 B), K-adjacent cores 128 B apart, 8-row groups (K/4) * 128 B
 // apart; one MMA consumes K = 8.  Every mbarrier wait is bounded.
@@ -29,12 +29,12 @@ namespace {
 using namespace tc;
 
 constexpr int kRows = 128;  // atoms per CTA (UMMA M)
-constexpr int kTK = 128;    // sparse points per tile
+constexpr int kTK = 64;     // sparse points per tile
 constexpr int kDP = 64;     // padded descriptor length
 constexpr int kXBytes = kRows * kDP * 4;   // 32 KB
-constexpr int kMBytes = kTK * kDP * 4;     // 32 KB (m~ and m~^T each)
-constexpr int kWBytes = kRows * kTK * 4;   // 64 KB
-constexpr int kMncBytes = 2 * kTK * 4;     // |m~|^2 and c of one tile
+constexpr int kMBytes = kTK * kDP * 4;     // 16 KB (m~ and m~^T each)
+constexpr int kWBytes = kRows * kTK * 4;   // 32 KB
+constexpr int kMncBytes = 2 * kTK * 4;     // b2 and c of one tile
 constexpr int kImgTile = 2 * kMBytes + kMncBytes;
 // shared memory map (from the 1024-aligned base)
 constexpr int kOffX = 0;
@@ -44,8 +44,9 @@ constexpr int kOffMnc = kOffMT + kMBytes;   // two tiles' vectors
 constexpr int kOffW = kOffMnc + 2 * kMncBytes;
 constexpr int kOffBar = kOffW + kWBytes;
 constexpr int kOffEp = kOffBar + 64;
-constexpr int kSmem = kOffEp + kRows * 8 + 1024;
+constexpr int kSmem = kOffEp + kRows * 8 + 1024;  // about 99 KB: two CTAs per SM
 constexpr int kThreads = 256;
+constexpr int kTmemCols = 128;  // C1 (kTK columns) and C2 (kDP columns)
 
 __host__ __device__ __forceinline__ int kmajor32(int r, int k, int kcores) {
   return (r & 7) * 16 + (r >> 3) * (kcores * 128) + (k & 3) * 4 + (k >> 2) * 128;
@@ -72,7 +73,7 @@ __device__ __forceinline__ uint32_t to_tf32(float x) {
   return r;
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads, 2)
     k_gpr_tf32(int N, int ntiles, const unsigned char *__restrict__ img_model,
                const unsigned char *__restrict__ img_atoms, const float *__restrict__ xs,
                const float *__restrict__ xn, const float *__restrict__ invth, int D,
@@ -87,8 +88,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                  bar_b = bar_a + 24;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + kOffBar + 32);
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
-                     smem_u32(tmem_slot))
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "n"(kTmemCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -103,12 +105,15 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const uint32_t tC1 = tmem, tC2 = tmem + 128;
+  const uint32_t tC1 = tmem, tC2 = tmem + kTK;
   const uint32_t lane_base = (uint32_t)(quad * 32) << 16;
   const int row = quad * 32 + lane;
   const int i = blockIdx.x * kRows + row;
   const float xnorm = (i < N) ? xn[i] : 0.f;
-  float ehi = 0.f, elo = 0.f;
+  // w = c 2^(log2e v + a2_i + b2_k) (the image stores b2_k = -log2e |m~_k|^2 / 2);
+  // e in four Kahan chains
+  const float a2 = -0.5f * kLog2e * xnorm;
+  float esum[4] = {0.f, 0.f, 0.f, 0.f}, ecmp[4] = {0.f, 0.f, 0.f, 0.f};
   const uint32_t id1 = idesc_tf32(kRows, kTK), id2 = idesc_tf32(kRows, kDP);
   uint32_t ph_a = 0, ph_b = 0, ph_g1 = 0, ph_g2 = 0;
   bool pend_a = false, pend_b = false, pend_g1 = false, pend_g2 = false;
@@ -143,7 +148,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       pend_a = false;
     }
     if (!__syncthreads_and(ok)) break;
-    // GEMM1: C1[128 x 128] = x~ . m~ over K = 64 (8 steps of 8)
+    // GEMM1: C1[128 x 64] = x~ . m~ over K = 64 (8 steps of 8)
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       for (int kk = 0; kk < kDP / 8; ++kk) {
@@ -164,22 +169,24 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (t + 1 < ntiles) load_a(t + 1, false);
     // epilogue: w = c exp(-s/2), e += w, W tile (TF32) for GEMM2
     unsigned char *wt = sm + kOffW;
+    constexpr int kHalfBlocks = kTK / 64;  // 32-column blocks per column half
 #pragma unroll 1
-    for (int cc = 2 * half; cc < 2 * half + 2; ++cc) {
+    for (int cc = kHalfBlocks * half; cc < kHalfBlocks * (half + 1); ++cc) {
       float v[32];
       tmem_ld32(tC1 + lane_base + cc * 32, v);
 #pragma unroll
       for (int g = 0; g < 8; ++g) {
         uint32_t pk[4];
+        const float4 b4 = *reinterpret_cast<const float4 *>(smn + cc * 32 + g * 4);
+        const float4 c4 = *reinterpret_cast<const float4 *>(sc + cc * 32 + g * 4);
+        const float bv[4] = {b4.x, b4.y, b4.z, b4.w}, cv[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          const int k = cc * 32 + g * 4 + u;
-          const float s = xnorm + smn[k] - 2.f * v[g * 4 + u];
-          const float w = sc[k] * __expf(-0.5f * s);
-          const float tt = ehi + w;  // two-sum
-          const float bb = tt - ehi;
-          elo += (ehi - (tt - bb)) + (w - bb);
-          ehi = tt;
+          const float w = cv[u] * ex2_approx(fmaf(v[g * 4 + u], kLog2e, a2 + bv[u]));
+          const float y = w - ecmp[u];  // Kahan
+          const float tt = esum[u] + y;
+          ecmp[u] = (tt - esum[u]) - y;
+          esum[u] = tt;
           pk[u] = to_tf32(w);
         }
         *reinterpret_cast<uint4 *>(wt + kmajor32(row, cc * 32 + g * 4, kTK / 4)) =
@@ -194,7 +201,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     if (!__syncthreads_and(ok)) break;
-    // GEMM2: C2[128 x 64] += W . m~^T over K = 128 (16 steps of 8)
+    // GEMM2: C2[128 x 64] += W . m~^T over K = 64 (8 steps of 8)
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       for (int kk = 0; kk < kTK / 8; ++kk) {
@@ -216,9 +223,12 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (ok) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     double *ep = reinterpret_cast<double *>(sm + kOffEp);
-    if (half == 1) ep[row] = (double)ehi + (double)elo;
+    double emine = 0.0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) emine += (double)esum[u] - (double)ecmp[u];
+    if (half == 1) ep[row] = emine;
     __syncthreads();
-    if (half == 0) ep[row] = ((double)ehi + (double)elo) + ep[row];
+    if (half == 0) ep[row] = emine + ep[row];
     __syncthreads();
     const double etot = ep[row];
     float c2[32];
@@ -241,7 +251,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "n"(kTmemCols)
+                 : "memory");
 }
 
 // x'' = G / theta - mu (FP32, row-padded to 64), the TF32 tiles of x~ and
@@ -288,7 +300,7 @@ float tf32_round(float f) {
 }  // namespace
 
 // The model's TF32 image: per sparse tile m~ (K-major over D), m~^T (K-major
-// over the tile's points), |m~|^2 and c, plus mu.
+// over the tile's points), b2 = -log2e |m~|^2 / 2 and c, plus mu.
 gapgb_status build_tf32_image(gapgb_model *m) {
   if (m->d_tf32) return GAPGB_OK;
   const HostModel &h = m->host;
@@ -317,7 +329,7 @@ gapgb_status build_tf32_image(gapgb_model *m) {
         std::memcpy(T + kmajor32(kk, d, kDP / 4), &vr, 4);            // GEMM1 B: rows = points
         std::memcpy(T + kMBytes + kmajor32(d, kk, kTK / 4), &vr, 4);  // GEMM2 B: rows = d
       }
-      mn[kk] = (float)nrm;
+      mn[kk] = (float)(-0.5 * 1.4426950408889634 * nrm);  // b2_k = -log2e |m~_k|^2 / 2
       cf[kk] = (float)h.coeff[k];
     }
   }
@@ -349,6 +361,8 @@ void launch_gpr_tf32(gapgb_model *m, Workspace &ws, int N, cudaStream_t st) {
                                                                   m->d_invth32, mu, xs, xn,
                                                                   img_atoms);
   cudaFuncSetAttribute(k_gpr_tf32, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
+  cudaFuncSetAttribute(k_gpr_tf32, cudaFuncAttributePreferredSharedMemoryCarveout,
+                       cudaSharedmemCarveoutMaxShared);
   k_gpr_tf32<<<tiles, kThreads, kSmem, st>>>(N, m->tf32_tiles, (const unsigned char *)m->d_tf32,
                                              img_atoms, xs, xn, m->d_invth32, D, ws.e,
                                              (float *)ws.dedg, ws.d_flags);

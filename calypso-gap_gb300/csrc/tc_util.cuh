@@ -103,6 +103,15 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
 }
 
+constexpr float kLog2e = 1.4426950408889634f;
+
+// 2^x (PTX ex2.approx.ftz: relative error ~2^-22, flushes subnormal results)
+__device__ __forceinline__ float ex2_approx(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<const uint32_t *>(&h);
