@@ -179,3 +179,29 @@ def test_variance_tc_alloy_many_tiles(gapgb_mod, oracle_mod, tmp_path):
     assert np.abs(ctc[512:] - rc).max() <= 2e-3
     assert np.abs(vtc - v64).max() <= 1e-3
     m.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec,ncells", [("fp64", 136), ("tc", 1026)])
+def test_variance_chunks_are_row_independent(gapgb_mod, si_var, prec, ncells):
+    """Batches longer than one chunk of atoms (FP64 form: 8192, tensor-core
+    form: 65536): a cell after the chunk boundary gets bit for bit the covf
+    it gets alone, since every row of K qmm^T is its own."""
+    import gapgb.synth as S
+    path, Q, *_ = si_var
+    m = gapgb_mod.GapModel.load(path)
+    m.set_precision(prec)
+    m.set_qmm(Q)
+    cells = [S.si64(seed=700 + s % 7, jitter=0.08) for s in range(ncells - 1)]
+    cells.append(S.si64(seed=999, jitter=0.08))
+    off, sp, lat, pos = S.pack(cells)
+    covf, var = m.variance(off, sp, lat, pos)
+    last = S.pack(cells[-1:])
+    c1, v1 = m.variance(*last)
+    assert off[-1] > (8192 if prec == "fp64" else 65536)
+    assert np.array_equal(covf[int(off[-2]):], c1)
+    assert var[-1] == v1[0]
+    # the first cells repeat with period 7: their rows agree across the batch
+    n7 = int(off[7])
+    assert np.array_equal(covf[:n7], covf[n7:2 * n7])
+    m.close()
