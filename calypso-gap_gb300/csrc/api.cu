@@ -67,6 +67,8 @@ void free_ws(Workspace &ws) {
   free_dev(ws.atom_bin);
   free_dev(ws.atom_slot);
   free_dev(ws.atom_m);
+  free_dev(ws.pairs);
+  free_dev(ws.pair_cnt);
   free_dev(ws.d_flags);
   free_dev(ws.orphans);
   free_dev(ws.gpr_scratch);
@@ -131,6 +133,8 @@ gapgb_status ensure_ws(gapgb_model *m, int N, int S, int cap) {
   WS_ALLOC(ws.atom_bin, nN);
   WS_ALLOC(ws.atom_slot, nN);
   WS_ALLOC(ws.atom_m, nN);
+  WS_ALLOC(ws.pairs, (size_t)nN * kPairCap);
+  WS_ALLOC(ws.pair_cnt, nN);
   WS_ALLOC(ws.d_flags, 8);
   ws.orphan_cap = 1 << 16;
   WS_ALLOC(ws.orphans, ws.orphan_cap);

@@ -225,6 +225,7 @@ struct StructInfo {
   int bin0;
 };
 
+constexpr int kPairCap = 1024;  // recorded angular pairs per atom
 constexpr int kBinMinAtoms = 2048;  // cells smaller than this use the O(na) scan
 
 template <typename T> struct Vec4;
@@ -274,6 +275,10 @@ struct Workspace {
   size_t gpr_scratch_size = 0;
   void *tc_scratch = nullptr;   // atom operand tiles of the tensor-core GPR
   size_t tc_scratch_size = 0;
+  // contributing angular pairs (j | k << 8) of every atom, recorded by the
+  // grouped FP32 descriptor kernel and streamed by its gradient kernel
+  unsigned short *pairs = nullptr;  // [N][kPairCap]
+  int *pair_cnt = nullptr;      // [N] pairs found (may exceed kPairCap: then re-enumerated)
 };
 
 // GPR predictive variance (variance.cu): the caller's qmm and its device forms

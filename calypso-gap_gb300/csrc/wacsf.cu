@@ -527,7 +527,8 @@ void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
       const int grid = warp_grid(N, smg, (const void *)gf);
       gf<<<grid, 32 * kWarpsPerBlock, smg, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
                                                    ws.apos, ws.nbr_d32, ws.nbr_w32, m->d_sft32,
-                                                   (float *)ws.G);
+                                                   (float *)ws.G, ws.pairs, ws.pair_cnt,
+                                                   capS <= 256 ? kPairCap : 0);
       return;
     }
   }
@@ -564,7 +565,9 @@ bool launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
       cudaMemsetAsync(d_force, 0, sizeof(double) * 3 * (size_t)N, st);
       gb<<<grid, 32 * kWarpsPerBlock, smg, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
                                                    ws.apos, ws.nbr_d32, ws.nbr_w32, m->d_sft32,
-                                                   (const float *)ws.dedg, d_force, ws.wvir);
+                                                   (const float *)ws.dedg, d_force, ws.wvir,
+                                                   ws.pairs, ws.pair_cnt,
+                                                   capS <= 256 ? kPairCap : 0);
       return true;  // forces scattered by the kernel
     }
   }

@@ -243,7 +243,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
                     const double4 *__restrict__ xyzr, const int *__restrict__ nj,
                     const double4 *__restrict__ apos, const float4 *__restrict__ d32,
                     const float *__restrict__ w32, const SFT<float> *__restrict__ sfg,
-                    float *__restrict__ G) {
+                    float *__restrict__ G, unsigned short *__restrict__ pairs,
+                    int *__restrict__ pcount, int pcap) {
   (void)xyzr;
   (void)nj;
   (void)apos;
@@ -285,8 +286,16 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
     for (int q = 0; q < NAL; ++q)
 #pragma unroll
       for (int c = 0; c < NB; ++c) acc[q][c] = accw[q][c] = 0.f;
+    // the contributing pairs are recorded for the gradient kernel as
+    // j | k << 8 (pcap > 0 only when every slot index fits 8 bits; valid
+    // lanes are the low ones of each batch); the count may exceed pcap
+    int np = 0;
+    unsigned short *prow = pairs + (size_t)i * pcap;
     if (P > 1)
       pair_stream(L.a, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
+        const unsigned vm = __ballot_sync(0xffffffffu, ok);
+        if (ok && np + lane < pcap) prow[np + lane] = (unsigned short)(j | (k << 8));
+        np += __popc(vm);
         if (!ok) return;
         const float a = L.a[j].w, b = L.a[k].w;
         const float4 Bj = L.b[j], Bk = L.b[k], Ej = L.e[j], Ek = L.e[k];
@@ -321,6 +330,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
           }
         }
       });
+    if (lane == 0 && pcap > 0) pcount[i] = np;
 #pragma unroll
     for (int q = 0; q < NAL; ++q)
 #pragma unroll
@@ -362,7 +372,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
                     const double4 *__restrict__ apos, const float4 *__restrict__ d32,
                     const float *__restrict__ w32, const SFT<float> *__restrict__ sfg,
                     const float *__restrict__ dedg, double *__restrict__ force,
-                    double *__restrict__ wvir) {
+                    double *__restrict__ wvir, const unsigned short *__restrict__ pairs,
+                    const int *__restrict__ pcount, int pcap) {
   (void)xyzr;
   (void)apos;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -429,74 +440,89 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
           UA[q][c] = s_u[warp][q * NC + c];
           UB[q][c] = s_u[warp][NAL * NC + q * NC + c];
         }
-      if (P > 1)
-        pair_stream(L.a, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
-          const float4 Aj = L.a[j], Ak = L.a[k], Bj = L.b[j], Bk = L.b[k];
-          const float4 Ej = L.e[j], Ek = L.e[k];
-          const float a = Aj.w, b = Ak.w;
-          const float ic = c2 > 0.f ? rsqrtf(c2) : 0.f, c = c2 * ic;
-          const float ia = Bj.x, ib = Bk.x;
-          const float cosv = (a * a + b * b - c2) * 0.5f * ia * ib;
-          const float dcda = ib - cosv * ia, dcdb = ia - cosv * ib, dcdc = -c * ia * ib;
-          float sn, cs;
-          __sincosf(pirc * c, &sn, &cs);
-          const float fcc = 0.5f * (cs + 1.f), dfcc = -0.5f * sn * pirc;
-          const float fa = Bj.z, fb = Bk.z, dfa = Bj.w, dfb = Bk.w;
-          const float F = fa * fb * fcc;
-          const float wjk = Bj.y * Bk.y;
-          float A[NC], dAl[NC];
-          ang_powers<NC, STD>(cosv, clam, ciz, A, dAl);
-          float SP = 0.f, SQ = 0.f, SU = 0.f;
+      auto work = [&](int j, int k, float c2, bool ok) {
+        const float4 Aj = L.a[j], Ak = L.a[k], Bj = L.b[j], Bk = L.b[k];
+        const float4 Ej = L.e[j], Ek = L.e[k];
+        const float a = Aj.w, b = Ak.w;
+        const float ic = c2 > 0.f ? rsqrtf(c2) : 0.f, c = c2 * ic;
+        const float ia = Bj.x, ib = Bk.x;
+        const float cosv = (a * a + b * b - c2) * 0.5f * ia * ib;
+        const float dcda = ib - cosv * ia, dcdb = ia - cosv * ib, dcdc = -c * ia * ib;
+        float sn, cs;
+        __sincosf(pirc * c, &sn, &cs);
+        const float fcc = 0.5f * (cs + 1.f), dfcc = -0.5f * sn * pirc;
+        const float fa = Bj.z, fb = Bk.z, dfa = Bj.w, dfb = Bk.w;
+        const float F = fa * fb * fcc;
+        const float wjk = Bj.y * Bk.y;
+        float A[NC], dAl[NC];
+        ang_powers<NC, STD>(cosv, clam, ciz, A, dAl);
+        float SP = 0.f, SQ = 0.f, SU = 0.f;
 #pragma unroll
-          for (int q = 0; q < NAL; ++q) {
-            const float E = q < nal ? f4get(Ej, q) * f4get(Ek, q) * __expf(-alv[q] * c2) : 0.f;
-            float sp = 0.f, sq = 0.f;
+        for (int q = 0; q < NAL; ++q) {
+          const float E = q < nal ? f4get(Ej, q) * f4get(Ek, q) * __expf(-alv[q] * c2) : 0.f;
+          float sp = 0.f, sq = 0.f;
 #pragma unroll
-            for (int cc = 0; cc < NC; ++cc) {
-              const float V = UA[q][cc] + wjk * UB[q][cc];
-              sp += dAl[cc] * V;
-              sq += A[cc] * V;
-            }
-            SP += E * sp;
-            SQ += E * sq;
-            SU += alv[q] * E * sq;
+          for (int cc = 0; cc < NC; ++cc) {
+            const float V = UA[q][cc] + wjk * UB[q][cc];
+            sp += dAl[cc] * V;
+            sq += A[cc] * V;
           }
-          // dG/da = E [A' dcos/da F + A (-2 alpha a F + fc'(a) fc(b) fc(c))], etc.
-          const float S1 = F * (SP * dcda - 2.f * SU * a) + SQ * (dfa * fb * fcc);
-          const float S2 = F * (SP * dcdb - 2.f * SU * b) + SQ * (fa * dfb * fcc);
-          const float S3 = F * (SP * dcdc - 2.f * SU * c) + SQ * (fa * fb * dfcc);
-          const float s1 = S1 * ia, s2 = S2 * ib, s3 = S3 * ic;
-          const float cx = Aj.x - Ak.x, cy = Aj.y - Ak.y, cz = Aj.z - Ak.z;
-          float vx = ok ? s1 * Aj.x + s3 * cx : 0.f;
-          float vy = ok ? s1 * Aj.y + s3 * cy : 0.f;
-          float vz = ok ? s1 * Aj.z + s3 * cz : 0.f;
-          // slot j: the batch's pairs share few j values (enumeration order),
-          // so each run of equal j (contiguous lanes) is summed by a
-          // segmented scan and its last lane adds it: one atomic per run
-          const unsigned run = __match_any_sync(0xffffffffu, ok ? j : 0x10000 + lane);
-          const int first = __ffs(run) - 1, last = 31 - __clz(run);
+          SP += E * sp;
+          SQ += E * sq;
+          SU += alv[q] * E * sq;
+        }
+        // dG/da = E [A' dcos/da F + A (-2 alpha a F + fc'(a) fc(b) fc(c))], etc.
+        const float S1 = F * (SP * dcda - 2.f * SU * a) + SQ * (dfa * fb * fcc);
+        const float S2 = F * (SP * dcdb - 2.f * SU * b) + SQ * (fa * dfb * fcc);
+        const float S3 = F * (SP * dcdc - 2.f * SU * c) + SQ * (fa * fb * dfcc);
+        const float s1 = S1 * ia, s2 = S2 * ib, s3 = S3 * ic;
+        const float cx = Aj.x - Ak.x, cy = Aj.y - Ak.y, cz = Aj.z - Ak.z;
+        float vx = ok ? s1 * Aj.x + s3 * cx : 0.f;
+        float vy = ok ? s1 * Aj.y + s3 * cy : 0.f;
+        float vz = ok ? s1 * Aj.z + s3 * cz : 0.f;
+        // slot j: the batch's pairs share few j values (enumeration order),
+        // so each run of equal j (contiguous lanes) is summed by a
+        // segmented scan and its last lane adds it: one atomic per run
+        const unsigned run = __match_any_sync(0xffffffffu, ok ? j : 0x10000 + lane);
+        const int first = __ffs(run) - 1, last = 31 - __clz(run);
 #pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const float tx = __shfl_up_sync(0xffffffffu, vx, o);
-            const float ty = __shfl_up_sync(0xffffffffu, vy, o);
-            const float tz = __shfl_up_sync(0xffffffffu, vz, o);
-            if (lane - o >= first) {
-              vx += tx;
-              vy += ty;
-              vz += tz;
-            }
+        for (int o = 1; o < 32; o <<= 1) {
+          const float tx = __shfl_up_sync(0xffffffffu, vx, o);
+          const float ty = __shfl_up_sync(0xffffffffu, vy, o);
+          const float tz = __shfl_up_sync(0xffffffffu, vz, o);
+          if (lane - o >= first) {
+            vx += tx;
+            vy += ty;
+            vz += tz;
           }
-          if (ok && lane == last) {
-            atomicAdd(&L.gx[j], vx);
-            atomicAdd(&L.gy[j], vy);
-            atomicAdd(&L.gz[j], vz);
-          }
-          if (ok) {
-            atomicAdd(&L.gx[k], s2 * Ak.x - s3 * cx);
-            atomicAdd(&L.gy[k], s2 * Ak.y - s3 * cy);
-            atomicAdd(&L.gz[k], s2 * Ak.z - s3 * cz);
-          }
-        });
+        }
+        if (ok && lane == last) {
+          atomicAdd(&L.gx[j], vx);
+          atomicAdd(&L.gy[j], vy);
+          atomicAdd(&L.gz[j], vz);
+        }
+        if (ok) {
+          atomicAdd(&L.gx[k], s2 * Ak.x - s3 * cx);
+          atomicAdd(&L.gy[k], s2 * Ak.y - s3 * cy);
+          atomicAdd(&L.gz[k], s2 * Ak.z - s3 * cz);
+        }
+      };
+      const int np = pcap > 0 ? pcount[i] : -1;
+      if (np >= 0 && np <= pcap) {
+        // the pairs the descriptor kernel found, in its order
+        const unsigned short *prow = pairs + (size_t)i * pcap;
+        for (int base = 0; base < np; base += 32) {
+          const int t = base + lane;
+          const bool ok = t < np;
+          const int jk = ok ? (int)prow[t] : (1 << 8);
+          const int j = jk & 0xff, k = jk >> 8;
+          const float4 aj = L.a[j], ak = L.a[k];
+          const float cx = aj.x - ak.x, cy = aj.y - ak.y, cz = aj.z - ak.z;
+          work(j, k, ok ? cx * cx + cy * cy + cz * cz : 1.f, ok);
+        }
+      } else if (P > 1) {
+        pair_stream(L.a, P, rc, lane, s_qjk[warp], s_qc2[warp], work);
+      }
     }
     __syncwarp();
     // forces by scatter: with g_q = sum_d dE/dG_id dG_id/dp_q and the
