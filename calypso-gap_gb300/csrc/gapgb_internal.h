@@ -346,6 +346,12 @@ gapgb_status fit_energies_enqueue(gapgb_model *m, int S, int N, const int *d_off
                                   const double *energy, double sigma_e, double jitter,
                                   double *coeff, cudaStream_t st);
 
+// launch_cache.cpp: launch attributes set / queried once per device
+// (a larger shared-memory size raises the limit; the limit never shrinks)
+void kernel_smem(const void *fn, int bytes, bool max_carveout = false);
+int kernel_occupancy(const void *fn, int threads, size_t smem);
+int device_sms();
+
 // variance.cu
 gapgb_status variance_set_qmm(gapgb_model *m, const double *qmm);
 bool variance_fp64_form(const gapgb_model *m);

@@ -258,9 +258,7 @@ __global__ void k_gpr_reduce(int N, int D, int nsplit, const double *__restrict_
 }  // namespace
 
 int gpr_nsplit(int N, int M) {
-  int dev = 0, sms = 148;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = device_sms();
   const int bx = (N + kBM - 1) / kBM;
   const int kt = (M + kBK - 1) / kBK;
   int ns = (2 * sms + bx - 1) / bx;
@@ -292,7 +290,7 @@ void launch_gpr(const gapgb_model *m, Workspace &ws, int N, cudaStream_t st) {
   T *d_part = reinterpret_cast<T *>(e_part + (size_t)nsp * N);
   const TG *G = (const TG *)ws.G;
   auto run = [&](auto fn) {
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kernel_smem((const void *)fn, (int)smem);
     fn<<<grid, 256, smem, st>>>(N, M, D, klen, G, mmt, invth, m->d_coeff, m->d_coeff32, e_part,
                                 d_part);
   };
@@ -306,9 +304,7 @@ void launch_gpr(const gapgb_model *m, Workspace &ws, int N, cudaStream_t st) {
 constexpr int kRowBlocksPerSm = 2;
 
 int gpr_rows_blocks() {
-  int dev = 0, sms = 148;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = device_sms();
   return kRowBlocksPerSm * sms;
 }
 
@@ -331,7 +327,7 @@ void launch_gpr_rows(const gapgb_model *m, Workspace &ws, int cap, const int *d_
   double *d_part = e_part + prow;
   const float *G = (const float *)ws.G;
   auto run = [&](auto fn) {
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kernel_smem((const void *)fn, (int)smem);
     fn<<<nb, 256, smem, st>>>(d_count, d_rows, M, D, G, m->d_mmt, m->d_invth, m->d_coeff,
                               m->d_coeff32, e_part, d_part);
   };

@@ -413,9 +413,7 @@ void launch_gpr_tc(gapgb_model *m, Workspace &ws, int N, cudaStream_t st) {
   const float *mu = reinterpret_cast<const float *>((const unsigned char *)m->d_tc + m->tc_bytes);
   k_tc_prep_atoms<<<(tiles * kRows + 127) / 128, 128, 0, st>>>(N, D, (const float *)ws.G,
                                                                 m->d_invth32, mu, xs, xn, img_atoms);
-  cudaFuncSetAttribute(k_gpr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-  cudaFuncSetAttribute(k_gpr_tc, cudaFuncAttributePreferredSharedMemoryCarveout,
-                       cudaSharedmemCarveoutMaxShared);
+  kernel_smem((const void *)k_gpr_tc, kSmemBytes, true);
   k_gpr_tc<<<tiles, kGprThreads, kSmemBytes, st>>>(N, m->tc_tiles, (const unsigned char *)m->d_tc,
                                           img_atoms, xs, xn, m->d_invth32, D, ws.e,
                                           (float *)ws.dedg, ws.d_flags);

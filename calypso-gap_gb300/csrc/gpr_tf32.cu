@@ -360,9 +360,7 @@ void launch_gpr_tf32(gapgb_model *m, Workspace &ws, int N, cudaStream_t st) {
   k_tf32_prep_atoms<<<(tiles * kRows + 127) / 128, 128, 0, st>>>(N, D, (const float *)ws.G,
                                                                   m->d_invth32, mu, xs, xn,
                                                                   img_atoms);
-  cudaFuncSetAttribute(k_gpr_tf32, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
-  cudaFuncSetAttribute(k_gpr_tf32, cudaFuncAttributePreferredSharedMemoryCarveout,
-                       cudaSharedmemCarveoutMaxShared);
+  kernel_smem((const void *)k_gpr_tf32, kSmem, true);
   k_gpr_tf32<<<tiles, kThreads, kSmem, st>>>(N, m->tf32_tiles, (const unsigned char *)m->d_tf32,
                                              img_atoms, xs, xn, m->d_invth32, D, ws.e,
                                              (float *)ws.dedg, ws.d_flags);

@@ -373,13 +373,11 @@ void launch_mlp_tc(int members, int nsp, int D, int Mpad, const unsigned char *w
                    cudaStream_t st) {
   const int nx = Mpad * (kDp / 8);
   k_mlp_x_image<<<(nx + 255) / 256, 256, 0, st>>>(Mpad, D, idx, G, mu, isig, ximg);
-  int dev = 0, sms = 148;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = device_sms();
   const int ntiles = Mpad / kR;
   const int per_member = std::max(1, std::min(ntiles, (sms + members - 1) / members));
   MlpTcArgs a{ntiles, Mpad, D, nsp, wimg, ximg, tile_sp64, y, gx, flags};
-  cudaFuncSetAttribute(k_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kMlpSmem);
+  kernel_smem((const void *)k_mlp_tc, kMlpSmem);
   k_mlp_tc<<<dim3(per_member, members), kThreads, kMlpSmem, st>>>(a);
 }
 

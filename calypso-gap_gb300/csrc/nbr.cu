@@ -766,7 +766,7 @@ void launch_neighbors(Workspace &ws, int S, int N, int max_atoms, int cap, doubl
   int hit_cap = 32;
   while (hit_cap < cap && hit_cap < 1024) hit_cap <<= 1;
   const size_t smem = (size_t)kWarpsPerBlock * hit_cap * (8 + 32 + 4);
-  cudaFuncSetAttribute(build_binned, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  kernel_smem((const void *)build_binned, (int)smem);
   build_binned<<<grid_for_warps(N), 32 * kWarpsPerBlock, smem, st>>>(
       N, cap, hit_cap, rcut, ws.apos, ws.frac32, ws.atom_struct, ws.sinfo, ws.bin_start,
       ws.bin_atoms, ws.atom_bin, ws.atom_m, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j, ws.nbr_s,

@@ -139,9 +139,7 @@ __global__ void k_struct_final(int S, int parts, int lgrad, const StructInfo *__
 template <typename T>
 void launch_forces(Workspace &ws, int N, int cap, double *d_force, cudaStream_t st) {
   using V4 = typename Vec4<T>::type;
-  int dev = 0, sms = 148;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = device_sms();
   int blocks = (N + 3) / 4;
   if (blocks > sms * 16) blocks = sms * 16;
   if (blocks < 1) blocks = 1;

@@ -17,7 +17,9 @@
 // neighbour slot q (an image position p_q) it writes
 //     gslot[i][q] = sum_d dE/dG_id * dG_id/dp_q
 // and the per-atom virial sum_q (p_q - r_i) (x) gslot[i][q]; forces follow by
-// a gather over reverse slots (reduce.cu).  No N x N array exists.
+// a gather over reverse slots (reduce.cu), or, in the grouped FP32 kernels
+// (wacsf_grouped.cuh), by a scatter in the gradient kernel itself.  No N x N
+// array exists.
 //
 // Work layout: one warp per centre atom.  The warp stages its neighbour
 // slots (relative vectors, distances, weights) and per-slot tables
@@ -482,11 +484,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 #include "wacsf_grouped.cuh"
 
 int warp_grid(int N, size_t smem_per_block, const void *fn) {
-  int dev = 0, sms = 148, per_sm = 1;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * kWarpsPerBlock, smem_per_block);
-  if (per_sm < 1) per_sm = 1;
+  const int sms = device_sms();
+  const int per_sm = kernel_occupancy(fn, 32 * kWarpsPerBlock, smem_per_block);
   int need = (N + kWarpsPerBlock - 1) / kWarpsPerBlock;
   int maxb = sms * per_sm;
   return need < maxb ? (need > 0 ? need : 1) : maxb;
@@ -521,9 +520,7 @@ void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
       const size_t smg = kTableBytes(sizeof(SFT<float>)) +
                          (size_t)kWarpsPerBlock * 4 *
                              grp_warp_floats(capS, m->sfh.nrc, m->sfh.D, true);
-      cudaFuncSetAttribute(gf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smg);
-      cudaFuncSetAttribute(gf, cudaFuncAttributePreferredSharedMemoryCarveout,
-                           cudaSharedmemCarveoutMaxShared);
+      kernel_smem((const void *)gf, (int)smg, true);
       const int grid = warp_grid(N, smg, (const void *)gf);
       gf<<<grid, 32 * kWarpsPerBlock, smg, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
                                                    ws.apos, ws.nbr_d32, ws.nbr_w32, m->d_sft32,
@@ -533,7 +530,7 @@ void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
     }
   }
   auto fn = k_wacsf_fwd<T>;
-  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  kernel_smem((const void *)fn, (int)smem);
   const int grid = warp_grid(N, smem, (const void *)fn);
   fn<<<grid, 32 * kWarpsPerBlock, smem, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
                                                ws.apos, ws.nbr_d32, ws.nbr_w32, sft_of<T>(m),
@@ -558,9 +555,7 @@ bool launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
       const size_t smg = kTableBytes(sizeof(SFT<float>)) +
                          (size_t)kWarpsPerBlock * 4 *
                              grp_warp_floats(capS, m->sfh.nrc, m->sfh.D, false);
-      cudaFuncSetAttribute(gb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smg);
-      cudaFuncSetAttribute(gb, cudaFuncAttributePreferredSharedMemoryCarveout,
-                           cudaSharedmemCarveoutMaxShared);
+      kernel_smem((const void *)gb, (int)smg, true);
       const int grid = warp_grid(N, smg, (const void *)gb);
       cudaMemsetAsync(d_force, 0, sizeof(double) * 3 * (size_t)N, st);
       gb<<<grid, 32 * kWarpsPerBlock, smg, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
@@ -572,7 +567,7 @@ bool launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
     }
   }
   auto fn = k_wacsf_bwd<T>;
-  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  kernel_smem((const void *)fn, (int)smem);
   const int grid = warp_grid(N, smem, (const void *)fn);
   fn<<<grid, 32 * kWarpsPerBlock, smem, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
                                                ws.apos, ws.nbr_d32, ws.nbr_w32, sft_of<T>(m),
