@@ -264,19 +264,22 @@ STAGES = ["neighbours", "descriptors", "gpr", "chain_rule"]
 # slots per atom on this workload, D = 64, FP32 slot records):
 #   neighbours : positions in, slot records out per slot (j 4, shift 4,
 #                FP32 record 16, weight 4)
-#   descriptors: FP32 slot record + weight in per slot, D FP32 descriptors out
-#   chain_rule : slot record + weight + partner index in per slot, dE/dG row
-#                in, per-atom virial (72 B) out, and the force scatter: 24 B
-#                (an FP64 atomic add per component) per slot and per atom
+#   descriptors: FP32 slot record + weight in per slot, D FP32 descriptors
+#                out, and the contributing angular pairs out (2 B each)
+#   chain_rule : slot record + weight + partner index in per slot, the pair
+#                list in, dE/dG row in, per-atom virial (72 B) out, and the
+#                force scatter: 24 B (an FP64 atomic add per component) per
+#                slot and per atom
 P_SLOTS = 56.0
+T_PAIRS = 690.0  # contributing angular pairs per atom on this workload
 
 
 def stage_bytes_per_atom(D):
-    P = P_SLOTS
+    P, T = P_SLOTS, T_PAIRS
     return {"neighbours": 32.0 + P * 28.0,
-            "descriptors": P * 20.0 + D * 4.0,
+            "descriptors": P * 20.0 + D * 4.0 + T * 2.0,
             "gpr": D * 4.0 * 2 + 8.0,
-            "chain_rule": P * 24.0 + D * 4.0 + 72.0 + P * 24.0 + 24.0}
+            "chain_rule": P * 24.0 + T * 2.0 + D * 4.0 + 72.0 + P * 24.0 + 24.0}
 
 
 def load_peaks():
