@@ -739,14 +739,14 @@ gapgb_status gapgb_model_set_coeff(gapgb_model *m, const double *coeff) {
   return GAPGB_OK;
 }
 
-gapgb_status gapgb_fit_energies(gapgb_model *m, int nstruct, const int *atom_off,
-                                const int *species, const double *lat, const double *pos,
-                                const double *energy, double sigma_e, double jitter,
-                                double *coeff) {
+gapgb_status gapgb_fit(gapgb_model *m, int nstruct, const int *atom_off, const int *species,
+                       const double *lat, const double *pos, const double *energy,
+                       const double *forces, double sigma_e, double sigma_f, double jitter,
+                       double *coeff) {
   if (!m || !atom_off || !species || !lat || !pos || !energy)
     return fail(GAPGB_ERR_ARG, "null argument");
-  if (!(sigma_e > 0.0) || !(jitter >= 0.0))
-    return fail(GAPGB_ERR_ARG, "sigma_e must be positive and jitter non-negative");
+  if (!(sigma_e > 0.0) || !(jitter >= 0.0) || (forces && !(sigma_f > 0.0)))
+    return fail(GAPGB_ERR_ARG, "sigma_e (and sigma_f with forces) positive, jitter non-negative");
   gapgb_status st = check_batch_host(nstruct, atom_off, lat, pos);
   if (st) return st;
   // FP64 descriptors of the training structures (the exact neighbour list)
@@ -755,18 +755,30 @@ gapgb_status gapgb_fit_energies(gapgb_model *m, int nstruct, const int *atom_off
   double *dG = nullptr;
   st = eval_host(m, nstruct, atom_off, species, lat, pos, 0, nullptr, nullptr, nullptr, nullptr,
                  &dG);
-  m->precision = saved;
-  if (st) return st;
+  if (st) {
+    m->precision = saved;
+    return st;
+  }
+  const int capS = std::max(1, m->ws.h_flags[1]);  // slot count of that list
   std::vector<double> c(m->host.M);
   GAPGB_CUDA_TRY(cudaMemsetAsync(m->ws.d_flags, 0, 8 * sizeof(int), m->stream));
-  st = fit_energies_enqueue(m, nstruct, atom_off[nstruct], m->ws.d_atom_off, dG, energy, sigma_e,
-                            jitter, c.data(), m->stream);
+  st = fit_enqueue(m, nstruct, atom_off[nstruct], m->cap, capS, m->ws.d_atom_off, dG, energy,
+                   forces, sigma_e, sigma_f, jitter, c.data(), m->stream);
+  m->precision = saved;
   if (st) return st;
   GAPGB_CUDA_TRY(cudaMemcpy(m->ws.h_flags, m->ws.d_flags, 8 * sizeof(int), cudaMemcpyDeviceToHost));
   st = flags_to_status(m->ws.h_flags);
   if (st) return st;
   if (coeff) std::copy(c.begin(), c.end(), coeff);
   return gapgb_model_set_coeff(m, c.data());
+}
+
+gapgb_status gapgb_fit_energies(gapgb_model *m, int nstruct, const int *atom_off,
+                                const int *species, const double *lat, const double *pos,
+                                const double *energy, double sigma_e, double jitter,
+                                double *coeff) {
+  return gapgb_fit(m, nstruct, atom_off, species, lat, pos, energy, nullptr, sigma_e, 1.0,
+                   jitter, coeff);
 }
 
 gapgb_status gapgb_model_set_qmm(gapgb_model *m, const double *qmm, int nsparse) {

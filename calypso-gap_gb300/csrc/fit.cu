@@ -3,16 +3,19 @@
 // The reference evaluates E = sum_i sum_k c_k K(x_i, m_k) (GET_COV and the
 // energy sum of FGAP_CALC, gappy/libgap/gap_calc.f90:143-154, 268-288) with
 // coefficients fitted elsewhere (calypso.x / ngap.x, not part of the
-// repository).  This file fits them from structure energies with the
-// sparse (subset-of-regressors) normal equations:
+// repository).  This file fits them from structure energies, and optionally
+// forces, with the sparse (subset-of-regressors) normal equations:
 //   Phi_sk = sum_{i in s} K(x_i, m_k)                  (structure design rows)
-//   A      = K_MM + jitter I + sum_s w_s Phi_s^T Phi_s,  w_s = 1 / (sigma_e^2 n_s)
-//   b      = sum_s w_s Phi_s^T E_s
+//   PhiF_rk = force component r of the model with c = e_k  (force design rows)
+//   A      = K_MM + jitter I + sum_s w_s Phi_s^T Phi_s + PhiF^T PhiF / sigma_f^2
+//   b      = sum_s w_s Phi_s^T E_s + PhiF^T F / sigma_f^2,  w_s = 1 / (sigma_e^2 n_s)
 //   A c = b                                           (Cholesky, FP64)
 // sigma_e is a per-atom energy noise (independent per atom, so a structure of
 // n_s atoms has variance n_s sigma_e^2).  Everything is FP64: A inherits
 // K_MM's conditioning.
 //
+// Force column k runs the FP64 gradient kernel and the force gather on the
+// dE/dG of the unit coefficient e_k (M passes over the training atoms).
 // Kernels: the design rows with the structure sum fused in (no N x M
 // buffer), a tiled FP64 Gram product, a blocked right-looking Cholesky
 // (64-wide diagonal factor in shared memory, row-parallel triangular solve
@@ -176,7 +179,7 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// b[k] = sum_s w_s Phi_sk E_s (fixed order over s)
+// b[k] += sum_s w_s Phi_sk E_s (fixed order over s)
 __global__ void k_fit_rhs(int S, int Mp, const double *__restrict__ phi,
                           const double *__restrict__ w, const double *__restrict__ E,
                           double *__restrict__ b) {
@@ -184,7 +187,48 @@ __global__ void k_fit_rhs(int S, int Mp, const double *__restrict__ phi,
   if (k >= Mp) return;
   double acc = 0.0;
   for (int s = 0; s < S; ++s) acc = fma(w[s] * E[s], phi[(size_t)s * Mp + k], acc);
-  b[k] = acc;
+  b[k] += acc;
+}
+
+// dE/dG of the model with c = e_k (one sparse point, unit coefficient), the
+// loop of gap_calc.f90:157-166 for one k:
+//   dedg_id = -K_ik (x_id - m_kd) / theta_d^2,  K_ik = exp(-1/2 sum_d ((x_id - m_kd)/theta_d)^2)
+// one warp per atom
+__global__ void __launch_bounds__(128)
+    k_fit_dedg_unit(int N, int D, int k, const double *__restrict__ G,
+                    const double *__restrict__ invth, const double *__restrict__ mmt,
+                    double *__restrict__ dedg) {
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= N) return;
+  double q[4];
+  double s = 0.0;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int d = lane + 32 * t;
+    q[t] = d < D ? G[(size_t)i * D + d] * invth[d] - mmt[(size_t)k * D + d] : 0.0;
+    s += q[t] * q[t];
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  const double K = exp(-0.5 * s);
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int d = lane + 32 * t;
+    if (d < D) dedg[(size_t)i * D + d] = -K * q[t] * invth[d];
+  }
+}
+
+// column k of the force design matrix: PhiF[r][k] = F_r for the unit coefficient
+__global__ void k_fit_col(int R, int k, int Mp, const double *__restrict__ F,
+                          double *__restrict__ PhiF) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < R) PhiF[(size_t)r * Mp + k] = F[r];
+}
+
+__global__ void k_fit_fill(int n, double v, double *__restrict__ x) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) x[r] = v;
 }
 
 __global__ void k_fit_weights(int S, const int *__restrict__ off, double inv_var,
@@ -381,24 +425,29 @@ gapgb_status dev_alloc(T **p, size_t n) {
 }  // namespace
 
 // Fits the coefficients from FP64 descriptors d_G[N][D] (structures by
-// d_off, S + 1 offsets on the device) and host energies[S]; writes the M
-// coefficients to host coeff.  Synchronises the stream.
-gapgb_status fit_energies_enqueue(gapgb_model *m, int S, int N, const int *d_off, const double *d_G,
-                                  const double *energy, double sigma_e, double jitter,
-                                  double *coeff, cudaStream_t st) {
+// d_off, S + 1 offsets on the device), host energies[S] and, when forces is
+// not null, host forces[N][3] (the neighbour list of the descriptors, built
+// with capacity cap and slot count capS, must still be in the workspace);
+// writes the M coefficients to host coeff.  Synchronises the stream.
+gapgb_status fit_enqueue(gapgb_model *m, int S, int N, int cap, int capS, const int *d_off,
+                         const double *d_G, const double *energy, const double *forces,
+                         double sigma_e, double sigma_f, double jitter, double *coeff,
+                         cudaStream_t st) {
   const int M = m->host.M, D = m->host.D, Mp = (M + kT - 1) / kT * kT;
-  (void)N;
+  const int R = forces ? 3 * N : 0;  // force rows
   double *phi = nullptr, *A = nullptr, *b = nullptr, *y = nullptr, *c = nullptr, *w = nullptr,
-         *E = nullptr;
+         *E = nullptr, *phif = nullptr, *wf = nullptr, *Fv = nullptr, *Fk = nullptr;
   gapgb_status s = GAPGB_OK;
   auto cleanup = [&]() {
-    for (double *p : {phi, A, b, y, c, w, E})
+    for (double *p : {phi, A, b, y, c, w, E, phif, wf, Fv, Fk})
       if (p) cudaFree(p);
   };
   if ((s = dev_alloc(&phi, (size_t)S * Mp)) || (s = dev_alloc(&A, (size_t)Mp * Mp)) ||
       (s = dev_alloc(&b, (size_t)Mp)) || (s = dev_alloc(&y, (size_t)Mp)) ||
       (s = dev_alloc(&c, (size_t)Mp)) || (s = dev_alloc(&w, (size_t)S)) ||
-      (s = dev_alloc(&E, (size_t)S))) {
+      (s = dev_alloc(&E, (size_t)S)) ||
+      (R > 0 && ((s = dev_alloc(&phif, (size_t)R * Mp)) || (s = dev_alloc(&wf, (size_t)R)) ||
+                 (s = dev_alloc(&Fv, (size_t)R)) || (s = dev_alloc(&Fk, (size_t)R))))) {
     cleanup();
     return s;
   }
@@ -410,6 +459,7 @@ gapgb_status fit_energies_enqueue(gapgb_model *m, int S, int N, const int *d_off
   };
   tryc(cudaMemcpyAsync(E, energy, sizeof(double) * S, cudaMemcpyHostToDevice, st));
   tryc(cudaMemsetAsync(A, 0, sizeof(double) * (size_t)Mp * Mp, st));
+  tryc(cudaMemsetAsync(b, 0, sizeof(double) * (size_t)Mp, st));
   const int nt = Mp / kT;
   k_fit_kmm<<<dim3(nt, (M + kRowsPerPass - 1) / kRowsPerPass), 256, 0, st>>>(M, Mp, D, m->d_mmt, A);
   k_fit_jitter<<<(M + 255) / 256, 256, 0, st>>>(M, Mp, jitter, A);
@@ -417,6 +467,24 @@ gapgb_status fit_energies_enqueue(gapgb_model *m, int S, int N, const int *d_off
   k_fit_phi<<<dim3(nt, S), 256, 0, st>>>(M, Mp, D, d_off, d_G, m->d_invth, m->d_mmt, phi);
   k_fit_gram<<<dim3(nt, nt), 256, 0, st>>>(S, M, Mp, phi, w, A);
   k_fit_rhs<<<(Mp + 255) / 256, 256, 0, st>>>(S, Mp, phi, w, E, b);
+  if (R > 0) {
+    // force rows: column k is the force field of the unit coefficient e_k,
+    // through the FP64 gradient kernel and the reverse-slot gather
+    Workspace &ws = m->ws;
+    tryc(cudaMemcpyAsync(Fv, forces, sizeof(double) * R, cudaMemcpyHostToDevice, st));
+    tryc(cudaMemsetAsync(phif, 0, sizeof(double) * (size_t)R * Mp, st));
+    k_fit_fill<<<(R + 255) / 256, 256, 0, st>>>(R, 1.0 / (sigma_f * sigma_f), wf);
+    launch_reverse(ws, N, cap, st);
+    for (int k = 0; k < M; ++k) {
+      k_fit_dedg_unit<<<(N + 3) / 4, 128, 0, st>>>(N, D, k, d_G, m->d_invth, m->d_mmt,
+                                                   (double *)ws.dedg);
+      launch_wacsf_bwd<double>(m, ws, N, cap, capS, Fk, st);
+      launch_forces<double>(ws, N, cap, Fk, st);
+      k_fit_col<<<(R + 255) / 256, 256, 0, st>>>(R, k, Mp, Fk, phif);
+    }
+    k_fit_gram<<<dim3(nt, nt), 256, 0, st>>>(R, M, Mp, phif, wf, A);
+    k_fit_rhs<<<(Mp + 255) / 256, 256, 0, st>>>(R, Mp, phif, wf, Fv, b);
+  }
   for (int j0 = 0; j0 < Mp; j0 += kT) {
     k_chol_diag<<<1, 256, 0, st>>>(Mp, j0, A, m->ws.d_flags);
     const int rest = Mp - j0 - kT;

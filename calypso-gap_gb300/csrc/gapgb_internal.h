@@ -342,9 +342,10 @@ struct gapgb_model {
 namespace gapgb {
 
 // fit.cu
-gapgb_status fit_energies_enqueue(gapgb_model *m, int S, int N, const int *d_off, const double *d_G,
-                                  const double *energy, double sigma_e, double jitter,
-                                  double *coeff, cudaStream_t st);
+gapgb_status fit_enqueue(gapgb_model *m, int S, int N, int cap, int capS, const int *d_off,
+                         const double *d_G, const double *energy, const double *forces,
+                         double sigma_e, double sigma_f, double jitter, double *coeff,
+                         cudaStream_t st);
 
 // launch_cache.cpp: launch attributes set / queried once per device
 // (a larger shared-memory size raises the limit; the limit never shrinks)

@@ -1,10 +1,13 @@
-"""Sparse-GPR fitting from structure energies (gapgb_fit_energies).
+"""Sparse-GPR fitting from structure energies and forces (gapgb_fit,
+gapgb_fit_energies).
 
 The reference only evaluates fitted models (its fitting codes, calypso.x and
 ngap.x, are not in the repository), so the oracle here is the same normal
 equations written out in numpy on the CPU oracle's FP64 descriptors:
   Phi_sk = sum_{i in s} K(x_i, m_k),  A = K_MM + jitter I + Phi^T W Phi,
-  b = Phi^T W E,  W = diag(1 / (sigma_e^2 n_s)),  c = A^-1 b.
+  b = Phi^T W E,  W = diag(1 / (sigma_e^2 n_s)),  c = A^-1 b,
+plus, with forces, PhiF^T PhiF / sigma_f^2 and PhiF^T F / sigma_f^2, where
+column k of PhiF is the oracle's force field with coefficients e_k.
 """
 import numpy as np
 import pytest
@@ -96,4 +99,47 @@ def test_fit_rejects_bad_arguments(gapgb_mod, tmp_path, oracle_mod):
     assert ei.value.status == 8
     with pytest.raises(gapgb_mod.GapError):
         m.set_coeff(np.full(m.nsparse, np.nan))
+    m.close()
+
+
+def test_fit_with_forces_matches_normal_equations(gapgb_mod, oracle_mod, tmp_path):
+    """Energy and force rows.  The oracle's force design column k is the
+    oracle's force field with the coefficients set to the unit vector e_k."""
+    import gapgb.synth as S
+    path = str(tmp_path / "gp")
+    synth_model_file(path, oracle_mod, [S.si64(seed=s) for s in range(3)], M=60,
+                     theta_scale=1.0, coeff_std=0.05, seed=5)
+    o = oracle_mod.Model(path)
+    m = gapgb_mod.GapModel.load(path)
+    m.set_precision("fp64")
+    train = [S.si64(seed=300 + s, jitter=0.1) for s in range(4)]
+    off, sp, lat, pos = S.pack(train)
+    E, F, _ = m.eval_batch(off, sp, lat, pos)  # teacher: the model itself
+    n = np.diff(off).astype(float)
+    sigma_e, sigma_f, jitter = 1e-3, 1e-2, 1e-8
+    c = m.fit(off, sp, lat, pos, E, forces=F, sigma_e=sigma_e, sigma_f=sigma_f, jitter=jitter)
+    # oracle design matrices
+    phi = _phi(oracle_mod, o, train)
+    cview = np.ctypeslib.as_array(o._m.coeff, (o.M,))
+    saved = cview.copy()
+    phif = np.zeros((3 * len(sp), o.M))
+    for k in range(o.M):
+        cview[:] = 0.0
+        cview[k] = 1.0
+        cols = [oracle_mod.gap_calc(o, z, l, p, 6.0, True)[1].ravel() for l, p, z in train]
+        phif[:, k] = np.concatenate(cols)
+    cview[:] = saved
+    A, b = _normal(o, phi, E, n, sigma_e, jitter)
+    A = A + phif.T @ phif / sigma_f ** 2
+    b = b + phif.T @ F.ravel() / sigma_f ** 2
+    c_ref = np.linalg.solve(A, b)
+    res = np.linalg.norm(A @ c - b) / (np.linalg.norm(A, 2) * np.linalg.norm(c))
+    df = np.abs(phif @ c - phif @ c_ref).max()
+    print("fit with forces: backward error %.3g, dF (device vs numpy solution) %.3g eV/A, "
+          "|F - F_teacher| max %.3g eV/A" % (res, df, np.abs(phif @ c - F.ravel()).max()))
+    assert res <= 1e-12
+    assert df <= 1e-6 * np.abs(F).max()
+    # the fitted model evaluates to the solution's forces
+    _, F2, _ = m.eval_batch(off, sp, lat, pos)
+    assert np.abs(F2.ravel() - phif @ c).max() <= 1e-9 * np.abs(F).max()
     m.close()
