@@ -741,12 +741,13 @@ gapgb_status gapgb_model_set_coeff(gapgb_model *m, const double *coeff) {
 
 gapgb_status gapgb_fit(gapgb_model *m, int nstruct, const int *atom_off, const int *species,
                        const double *lat, const double *pos, const double *energy,
-                       const double *forces, double sigma_e, double sigma_f, double jitter,
-                       double *coeff) {
+                       const double *forces, const double *stress, double sigma_e,
+                       double sigma_f, double sigma_s, double jitter, double *coeff) {
   if (!m || !atom_off || !species || !lat || !pos || !energy)
     return fail(GAPGB_ERR_ARG, "null argument");
-  if (!(sigma_e > 0.0) || !(jitter >= 0.0) || (forces && !(sigma_f > 0.0)))
-    return fail(GAPGB_ERR_ARG, "sigma_e (and sigma_f with forces) positive, jitter non-negative");
+  if (!(sigma_e > 0.0) || !(jitter >= 0.0) || (forces && !(sigma_f > 0.0)) ||
+      (stress && !(sigma_s > 0.0)))
+    return fail(GAPGB_ERR_ARG, "the sigma of every fitted quantity positive, jitter non-negative");
   gapgb_status st = check_batch_host(nstruct, atom_off, lat, pos);
   if (st) return st;
   // FP64 descriptors of the training structures (the exact neighbour list)
@@ -763,7 +764,7 @@ gapgb_status gapgb_fit(gapgb_model *m, int nstruct, const int *atom_off, const i
   std::vector<double> c(m->host.M);
   GAPGB_CUDA_TRY(cudaMemsetAsync(m->ws.d_flags, 0, 8 * sizeof(int), m->stream));
   st = fit_enqueue(m, nstruct, atom_off[nstruct], m->cap, capS, m->ws.d_atom_off, dG, energy,
-                   forces, sigma_e, sigma_f, jitter, c.data(), m->stream);
+                   forces, stress, sigma_e, sigma_f, sigma_s, jitter, c.data(), m->stream);
   m->precision = saved;
   if (st) return st;
   GAPGB_CUDA_TRY(cudaMemcpy(m->ws.h_flags, m->ws.d_flags, 8 * sizeof(int), cudaMemcpyDeviceToHost));
@@ -777,8 +778,8 @@ gapgb_status gapgb_fit_energies(gapgb_model *m, int nstruct, const int *atom_off
                                 const int *species, const double *lat, const double *pos,
                                 const double *energy, double sigma_e, double jitter,
                                 double *coeff) {
-  return gapgb_fit(m, nstruct, atom_off, species, lat, pos, energy, nullptr, sigma_e, 1.0,
-                   jitter, coeff);
+  return gapgb_fit(m, nstruct, atom_off, species, lat, pos, energy, nullptr, nullptr, sigma_e,
+                   1.0, 1.0, jitter, coeff);
 }
 
 gapgb_status gapgb_model_set_qmm(gapgb_model *m, const double *qmm, int nsparse) {

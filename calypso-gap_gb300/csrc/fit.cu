@@ -7,8 +7,11 @@
 // forces, with the sparse (subset-of-regressors) normal equations:
 //   Phi_sk = sum_{i in s} K(x_i, m_k)                  (structure design rows)
 //   PhiF_rk = force component r of the model with c = e_k  (force design rows)
+//   PhiS_rk = stress component r (GPa) of the model with c = e_k  (stress rows)
 //   A      = K_MM + jitter I + sum_s w_s Phi_s^T Phi_s + PhiF^T PhiF / sigma_f^2
-//   b      = sum_s w_s Phi_s^T E_s + PhiF^T F / sigma_f^2,  w_s = 1 / (sigma_e^2 n_s)
+//            + PhiS^T PhiS / sigma_s^2
+//   b      = sum_s w_s Phi_s^T E_s + PhiF^T F / sigma_f^2 + PhiS^T sigma / sigma_s^2,
+//   w_s = 1 / (sigma_e^2 n_s)
 //   A c = b                                           (Cholesky, FP64)
 // sigma_e is a per-atom energy noise (independent per atom, so a structure of
 // n_s atoms has variance n_s sigma_e^2).  Everything is FP64: A inherits
@@ -431,23 +434,30 @@ gapgb_status dev_alloc(T **p, size_t n) {
 // writes the M coefficients to host coeff.  Synchronises the stream.
 gapgb_status fit_enqueue(gapgb_model *m, int S, int N, int cap, int capS, const int *d_off,
                          const double *d_G, const double *energy, const double *forces,
-                         double sigma_e, double sigma_f, double jitter, double *coeff,
-                         cudaStream_t st) {
+                         const double *stress, double sigma_e, double sigma_f, double sigma_s,
+                         double jitter, double *coeff, cudaStream_t st) {
   const int M = m->host.M, D = m->host.D, Mp = (M + kT - 1) / kT * kT;
-  const int R = forces ? 3 * N : 0;  // force rows
+  const int R = forces ? 3 * N : 0;   // force rows
+  const int RS = stress ? 6 * S : 0;  // stress rows
   double *phi = nullptr, *A = nullptr, *b = nullptr, *y = nullptr, *c = nullptr, *w = nullptr,
-         *E = nullptr, *phif = nullptr, *wf = nullptr, *Fv = nullptr, *Fk = nullptr;
+         *E = nullptr, *phif = nullptr, *wf = nullptr, *Fv = nullptr, *Fk = nullptr,
+         *phis = nullptr, *ws6 = nullptr, *Sv = nullptr, *Sk = nullptr, *Ek = nullptr;
   gapgb_status s = GAPGB_OK;
   auto cleanup = [&]() {
-    for (double *p : {phi, A, b, y, c, w, E, phif, wf, Fv, Fk})
+    for (double *p : {phi, A, b, y, c, w, E, phif, wf, Fv, Fk, phis, ws6, Sv, Sk, Ek})
       if (p) cudaFree(p);
   };
   if ((s = dev_alloc(&phi, (size_t)S * Mp)) || (s = dev_alloc(&A, (size_t)Mp * Mp)) ||
       (s = dev_alloc(&b, (size_t)Mp)) || (s = dev_alloc(&y, (size_t)Mp)) ||
       (s = dev_alloc(&c, (size_t)Mp)) || (s = dev_alloc(&w, (size_t)S)) ||
       (s = dev_alloc(&E, (size_t)S)) ||
+      ((R > 0 || RS > 0) && ((s = dev_alloc(&Fk, (size_t)3 * N)) ||
+                             (s = dev_alloc(&Sk, (size_t)6 * S)) ||
+                             (s = dev_alloc(&Ek, (size_t)S)))) ||
       (R > 0 && ((s = dev_alloc(&phif, (size_t)R * Mp)) || (s = dev_alloc(&wf, (size_t)R)) ||
-                 (s = dev_alloc(&Fv, (size_t)R)) || (s = dev_alloc(&Fk, (size_t)R))))) {
+                 (s = dev_alloc(&Fv, (size_t)R)))) ||
+      (RS > 0 && ((s = dev_alloc(&phis, (size_t)RS * Mp)) || (s = dev_alloc(&ws6, (size_t)RS)) ||
+                  (s = dev_alloc(&Sv, (size_t)RS))))) {
     cleanup();
     return s;
   }
@@ -467,23 +477,43 @@ gapgb_status fit_enqueue(gapgb_model *m, int S, int N, int cap, int capS, const 
   k_fit_phi<<<dim3(nt, S), 256, 0, st>>>(M, Mp, D, d_off, d_G, m->d_invth, m->d_mmt, phi);
   k_fit_gram<<<dim3(nt, nt), 256, 0, st>>>(S, M, Mp, phi, w, A);
   k_fit_rhs<<<(Mp + 255) / 256, 256, 0, st>>>(S, Mp, phi, w, E, b);
-  if (R > 0) {
-    // force rows: column k is the force field of the unit coefficient e_k,
-    // through the FP64 gradient kernel and the reverse-slot gather
+  if (R > 0 || RS > 0) {
+    // force / stress rows: column k is the force field / stress of the unit
+    // coefficient e_k, through the FP64 gradient kernel, the reverse-slot
+    // gather and the structure sums
     Workspace &ws = m->ws;
-    tryc(cudaMemcpyAsync(Fv, forces, sizeof(double) * R, cudaMemcpyHostToDevice, st));
-    tryc(cudaMemsetAsync(phif, 0, sizeof(double) * (size_t)R * Mp, st));
-    k_fit_fill<<<(R + 255) / 256, 256, 0, st>>>(R, 1.0 / (sigma_f * sigma_f), wf);
+    if (R > 0) {
+      tryc(cudaMemcpyAsync(Fv, forces, sizeof(double) * R, cudaMemcpyHostToDevice, st));
+      tryc(cudaMemsetAsync(phif, 0, sizeof(double) * (size_t)R * Mp, st));
+      k_fit_fill<<<(R + 255) / 256, 256, 0, st>>>(R, 1.0 / (sigma_f * sigma_f), wf);
+    }
+    if (RS > 0) {
+      tryc(cudaMemcpyAsync(Sv, stress, sizeof(double) * RS, cudaMemcpyHostToDevice, st));
+      tryc(cudaMemsetAsync(phis, 0, sizeof(double) * (size_t)RS * Mp, st));
+      k_fit_fill<<<(RS + 255) / 256, 256, 0, st>>>(RS, 1.0 / (sigma_s * sigma_s), ws6);
+    }
     launch_reverse(ws, N, cap, st);
     for (int k = 0; k < M; ++k) {
       k_fit_dedg_unit<<<(N + 3) / 4, 128, 0, st>>>(N, D, k, d_G, m->d_invth, m->d_mmt,
                                                    (double *)ws.dedg);
       launch_wacsf_bwd<double>(m, ws, N, cap, capS, Fk, st);
-      launch_forces<double>(ws, N, cap, Fk, st);
-      k_fit_col<<<(R + 255) / 256, 256, 0, st>>>(R, k, Mp, Fk, phif);
+      if (R > 0) {
+        launch_forces<double>(ws, N, cap, Fk, st);
+        k_fit_col<<<(R + 255) / 256, 256, 0, st>>>(R, k, Mp, Fk, phif);
+      }
+      if (RS > 0) {
+        launch_struct_reduce(ws, S, 1, Ek, Sk, nullptr, N, st);
+        k_fit_col<<<(RS + 255) / 256, 256, 0, st>>>(RS, k, Mp, Sk, phis);
+      }
     }
-    k_fit_gram<<<dim3(nt, nt), 256, 0, st>>>(R, M, Mp, phif, wf, A);
-    k_fit_rhs<<<(Mp + 255) / 256, 256, 0, st>>>(R, Mp, phif, wf, Fv, b);
+    if (R > 0) {
+      k_fit_gram<<<dim3(nt, nt), 256, 0, st>>>(R, M, Mp, phif, wf, A);
+      k_fit_rhs<<<(Mp + 255) / 256, 256, 0, st>>>(R, Mp, phif, wf, Fv, b);
+    }
+    if (RS > 0) {
+      k_fit_gram<<<dim3(nt, nt), 256, 0, st>>>(RS, M, Mp, phis, ws6, A);
+      k_fit_rhs<<<(Mp + 255) / 256, 256, 0, st>>>(RS, Mp, phis, ws6, Sv, b);
+    }
   }
   for (int j0 = 0; j0 < Mp; j0 += kT) {
     k_chol_diag<<<1, 256, 0, st>>>(Mp, j0, A, m->ws.d_flags);

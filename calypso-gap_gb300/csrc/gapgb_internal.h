@@ -344,8 +344,8 @@ namespace gapgb {
 // fit.cu
 gapgb_status fit_enqueue(gapgb_model *m, int S, int N, int cap, int capS, const int *d_off,
                          const double *d_G, const double *energy, const double *forces,
-                         double sigma_e, double sigma_f, double jitter, double *coeff,
-                         cudaStream_t st);
+                         const double *stress, double sigma_e, double sigma_f, double sigma_s,
+                         double jitter, double *coeff, cudaStream_t st);
 
 // launch_cache.cpp: launch attributes set / queried once per device
 // (a larger shared-memory size raises the limit; the limit never shrinks)

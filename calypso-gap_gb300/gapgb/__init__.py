@@ -36,7 +36,7 @@ SYMBOLS = [
     ("gapgb_model_set_qmm", _I, [_P, _P, _I]),
     ("gapgb_model_set_coeff", _I, [_P, _P]),
     ("gapgb_fit_energies", _I, [_P, _I, _P, _P, _P, _P, _P, _D, _D, _P]),
-    ("gapgb_fit", _I, [_P, _I, _P, _P, _P, _P, _P, _P, _D, _D, _D, _P]),
+    ("gapgb_fit", _I, [_P, _I, _P, _P, _P, _P, _P, _P, _P, _D, _D, _D, _D, _P]),
     ("gapgb_variance", _I, [_P, _I, _P, _P, _P, _P, _P, _P]),
     ("gapgb_variance_time", _I, [_P, C.POINTER(C.c_float)]),
     ("gapgb_model_free", None, [_P]),
@@ -226,19 +226,22 @@ class GapModel:
                                          _ptr(c)), "gapgb_fit_energies")
         return c
 
-    def fit(self, atom_off, species, lat, pos, energy, forces=None, sigma_e=1e-3, sigma_f=0.1,
-            jitter=1e-8):
+    def fit(self, atom_off, species, lat, pos, energy, forces=None, stress=None, sigma_e=1e-3,
+            sigma_f=0.1, sigma_s=0.1, jitter=1e-8):
         """Fit the coefficients to structure energies (eV) and, when given,
-        forces [N, 3] (eV/A) on the device; sets and returns them."""
+        forces [N, 3] (eV/A) and stresses [S, 6] (GPa, XX YY ZZ XY YZ ZX) on
+        the device; sets and returns them."""
         off = _i32(atom_off)
         S = off.shape[0] - 1
         N = int(off[-1])
         c = np.zeros(self.nsparse)
         fv = _f64(forces, (N, 3)) if forces is not None else None
+        sv = _f64(stress, (S, 6)) if stress is not None else None
         _check(load().gapgb_fit(self._h, S, _ptr(off), _ptr(_i32(species)),
                                 _ptr(_f64(lat, (S, 3, 3))), _ptr(_f64(pos, (N, 3))),
-                                _ptr(_f64(energy, (S,))), _ptr(fv), float(sigma_e),
-                                float(sigma_f), float(jitter), _ptr(c)), "gapgb_fit")
+                                _ptr(_f64(energy, (S,))), _ptr(fv), _ptr(sv), float(sigma_e),
+                                float(sigma_f), float(sigma_s), float(jitter), _ptr(c)),
+               "gapgb_fit")
         return c
 
     def set_qmm(self, qmm):

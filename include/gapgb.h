@@ -151,17 +151,21 @@ gapgb_status gapgb_fit_energies(gapgb_model *model, int nstruct,
                                 const double *energy, double sigma_e,
                                 double jitter, double *coeff);
 
-/* gapgb_fit_energies with force rows as well: forces[natoms*3] (eV/A, may
- * be NULL) are fitted with noise sigma_f (eV/A) per component,
- *   (K_MM + jitter I + sum_s w_s Phi_s^T Phi_s + PhiF^T PhiF / sigma_f^2) c
- *       = sum_s w_s Phi_s^T E_s + PhiF^T F / sigma_f^2,
- * where column k of PhiF is the force field of the model with c = e_k (the
- * FP64 chain rule run once per sparse point: meant for training sets of
- * the usual GAP size, hundreds of cells). */
+/* gapgb_fit_energies with force and stress rows as well: forces[natoms*3]
+ * (eV/A) and stress[nstruct*6] (GPa, XX YY ZZ XY YZ ZX as gapgb_eval
+ * reports it), either may be NULL, fitted with noise sigma_f (eV/A) and
+ * sigma_s (GPa) per component,
+ *   (K_MM + jitter I + sum_s w_s Phi_s^T Phi_s + PhiF^T PhiF / sigma_f^2
+ *      + PhiS^T PhiS / sigma_s^2) c
+ *       = sum_s w_s Phi_s^T E_s + PhiF^T F / sigma_f^2 + PhiS^T sigma / sigma_s^2,
+ * where column k of PhiF / PhiS is the force field / stress of the model
+ * with c = e_k (the FP64 chain rule run once per sparse point: meant for
+ * training sets of the usual GAP size, hundreds of cells). */
 gapgb_status gapgb_fit(gapgb_model *model, int nstruct, const int *atom_off,
                        const int *species, const double *lat,
                        const double *pos, const double *energy,
-                       const double *forces, double sigma_e, double sigma_f,
+                       const double *forces, const double *stress,
+                       double sigma_e, double sigma_f, double sigma_s,
                        double jitter, double *coeff);
 
 /* ---- predictive variance ------------------------------------------------ */

@@ -6,8 +6,9 @@ ngap.x, are not in the repository), so the oracle here is the same normal
 equations written out in numpy on the CPU oracle's FP64 descriptors:
   Phi_sk = sum_{i in s} K(x_i, m_k),  A = K_MM + jitter I + Phi^T W Phi,
   b = Phi^T W E,  W = diag(1 / (sigma_e^2 n_s)),  c = A^-1 b,
-plus, with forces, PhiF^T PhiF / sigma_f^2 and PhiF^T F / sigma_f^2, where
-column k of PhiF is the oracle's force field with coefficients e_k.
+plus, with forces and stresses, PhiF^T PhiF / sigma_f^2, PhiF^T F / sigma_f^2
+and the same for stress, where column k of PhiF (PhiS) is the oracle's force
+field (stress) with coefficients e_k.
 """
 import numpy as np
 import pytest
@@ -102,9 +103,10 @@ def test_fit_rejects_bad_arguments(gapgb_mod, tmp_path, oracle_mod):
     m.close()
 
 
-def test_fit_with_forces_matches_normal_equations(gapgb_mod, oracle_mod, tmp_path):
-    """Energy and force rows.  The oracle's force design column k is the
-    oracle's force field with the coefficients set to the unit vector e_k."""
+def test_fit_with_forces_and_stress_matches_normal_equations(gapgb_mod, oracle_mod, tmp_path):
+    """Energy, force and stress rows.  The oracle's force and stress design
+    columns k are the oracle's forces and stress with the coefficients set
+    to the unit vector e_k."""
     import gapgb.synth as S
     path = str(tmp_path / "gp")
     synth_model_file(path, oracle_mod, [S.si64(seed=s) for s in range(3)], M=60,
@@ -114,32 +116,39 @@ def test_fit_with_forces_matches_normal_equations(gapgb_mod, oracle_mod, tmp_pat
     m.set_precision("fp64")
     train = [S.si64(seed=300 + s, jitter=0.1) for s in range(4)]
     off, sp, lat, pos = S.pack(train)
-    E, F, _ = m.eval_batch(off, sp, lat, pos)  # teacher: the model itself
+    E, F, St = m.eval_batch(off, sp, lat, pos)  # teacher: the model itself
     n = np.diff(off).astype(float)
-    sigma_e, sigma_f, jitter = 1e-3, 1e-2, 1e-8
-    c = m.fit(off, sp, lat, pos, E, forces=F, sigma_e=sigma_e, sigma_f=sigma_f, jitter=jitter)
+    sigma_e, sigma_f, sigma_s, jitter = 1e-3, 1e-2, 1e-2, 1e-8
+    c = m.fit(off, sp, lat, pos, E, forces=F, stress=St, sigma_e=sigma_e, sigma_f=sigma_f,
+              sigma_s=sigma_s, jitter=jitter)
     # oracle design matrices
     phi = _phi(oracle_mod, o, train)
     cview = np.ctypeslib.as_array(o._m.coeff, (o.M,))
     saved = cview.copy()
     phif = np.zeros((3 * len(sp), o.M))
+    phis = np.zeros((6 * len(train), o.M))
     for k in range(o.M):
         cview[:] = 0.0
         cview[k] = 1.0
-        cols = [oracle_mod.gap_calc(o, z, l, p, 6.0, True)[1].ravel() for l, p, z in train]
-        phif[:, k] = np.concatenate(cols)
+        outs = [oracle_mod.gap_calc(o, z, l, p, 6.0, True) for l, p, z in train]
+        phif[:, k] = np.concatenate([x[1].ravel() for x in outs])
+        phis[:, k] = np.concatenate([x[2] for x in outs])
     cview[:] = saved
     A, b = _normal(o, phi, E, n, sigma_e, jitter)
-    A = A + phif.T @ phif / sigma_f ** 2
-    b = b + phif.T @ F.ravel() / sigma_f ** 2
+    A = A + phif.T @ phif / sigma_f ** 2 + phis.T @ phis / sigma_s ** 2
+    b = b + phif.T @ F.ravel() / sigma_f ** 2 + phis.T @ St.ravel() / sigma_s ** 2
     c_ref = np.linalg.solve(A, b)
     res = np.linalg.norm(A @ c - b) / (np.linalg.norm(A, 2) * np.linalg.norm(c))
     df = np.abs(phif @ c - phif @ c_ref).max()
-    print("fit with forces: backward error %.3g, dF (device vs numpy solution) %.3g eV/A, "
-          "|F - F_teacher| max %.3g eV/A" % (res, df, np.abs(phif @ c - F.ravel()).max()))
+    ds = np.abs(phis @ c - phis @ c_ref).max()
+    print("fit with forces and stress: backward error %.3g, dF %.3g eV/A, dS %.3g GPa "
+          "(device vs numpy solution); |F - F_teacher| max %.3g eV/A"
+          % (res, df, ds, np.abs(phif @ c - F.ravel()).max()))
     assert res <= 1e-12
     assert df <= 1e-6 * np.abs(F).max()
-    # the fitted model evaluates to the solution's forces
-    _, F2, _ = m.eval_batch(off, sp, lat, pos)
+    assert ds <= 1e-6 * np.abs(St).max()
+    # the fitted model evaluates to the solution's forces and stress
+    _, F2, S2 = m.eval_batch(off, sp, lat, pos)
     assert np.abs(F2.ravel() - phif @ c).max() <= 1e-9 * np.abs(F).max()
+    assert np.abs(S2.ravel() - phis @ c).max() <= 1e-9 * np.abs(St).max()
     m.close()
