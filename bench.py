@@ -325,6 +325,24 @@ def roofline(stages, N, D, precision):
                               "flops": "12 N M 64 (bf16 MMA, padded to 128)"}
     roof["gpr_algorithmic_tflops"] = 4.0 * m * D * N / (stages[2] * 1e-3) / 1e12
     roof["fp32_nominal_tflops"] = nominal_fp32
+    # the GPR's exp rate (one per atom and sparse point) against the nominal
+    # MUFU rate (16 per SM per clock)
+    exps = N * m / (stages[2] * 1e-3)
+    mufu = 152 * 16 * 2.07e9
+    roof["gpr_exp"] = {"per_s": exps, "nominal_per_s": mufu, "frac": exps / mufu}
+    # FP32 arithmetic of the descriptor-side stages, counted per contributing
+    # angular pair and per (slot, radial SF) with the grouped formulation's
+    # flops (an FMA = 2): forward 70 per pair (geometry 10, the NAL exponential
+    # factors 6, fc(r_jk) 4, Bernstein basis 10, 2 x NAL x 5 moment FMAs 40)
+    # and 8 per radial term; gradient 150 per pair and 15 per radial term
+    P, T, R = P_SLOTS, T_PAIRS, 20
+    fl_fwd = N * (70.0 * T + 8.0 * P * R)
+    fl_bwd = N * (150.0 * T + 15.0 * P * R)
+    for name, fl, st in (("descriptors_fp32", fl_fwd, stages[1]), ("chain_rule_fp32", fl_bwd, stages[3])):
+        ach = fl / (st * 1e-3) / 1e12
+        roof[name] = {"achieved_tflops": ach, "nominal_tflops": nominal_fp32,
+                      "frac": ach / nominal_fp32,
+                      "flops_per_atom": fl / N}
     return roof
 
 
