@@ -161,3 +161,26 @@ def test_write_parameters_matches_test_writer(gapgb_mod, tmp_path):
     m = gapgb_mod.GapModel.load(a)
     assert np.array_equal(m.arrays()[1], mm) and np.array_equal(m.tables()[5], ze)
     m.close()
+
+
+def test_fit_and_variance_argument_checks(gapgb_mod):
+    """Argument errors come back as statuses before any device work."""
+    import gapgb.synth as S
+    m = gapgb_mod.GapModel.load(GOLDEN_MODEL)
+    L = gapgb_mod.load()
+    off, sp, lat, pos = S.pack([S.si64(seed=1)])
+    off, sp = np.ascontiguousarray(off, np.int32), np.ascontiguousarray(sp, np.int32)
+    lat, pos = np.ascontiguousarray(lat), np.ascontiguousarray(pos)
+    e = np.zeros(1)
+    args = (m.handle, 1, off.ctypes.data, sp.ctypes.data, lat.ctypes.data, pos.ctypes.data,
+            e.ctypes.data)
+    # sigma_e must be positive; a force fit needs a positive sigma_f
+    assert L.gapgb_fit(*args, None, None, 0.0, 1.0, 1.0, 1e-8, None) == 8
+    f = np.zeros((64, 3))
+    assert L.gapgb_fit(*args, f.ctypes.data, None, 1e-3, 0.0, 1.0, 1e-8, None) == 8
+    assert L.gapgb_fit(*args, None, None, 1e-3, 1.0, 1.0, -1.0, None) == 8
+    # the variance needs an attached qmm
+    covf, var = np.zeros(64), np.zeros(1)
+    assert L.gapgb_variance(m.handle, 1, off.ctypes.data, sp.ctypes.data, lat.ctypes.data,
+                            pos.ctypes.data, covf.ctypes.data, var.ctypes.data) == 8
+    m.close()
