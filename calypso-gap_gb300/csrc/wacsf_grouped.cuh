@@ -162,47 +162,56 @@ __device__ __forceinline__ void ang_powers(float cosv, const float *clam, const 
 
 // Walks the upper triangle of P slots, screens pairs (r_jk <= rc) and calls
 // `work(j, k, rjk^2, valid)` on all 32 lanes for every batch of up to 32
-// contributing pairs (valid is false on the idle lanes of the last batch).
-// Within a batch the pairs are in enumeration order: j is non-decreasing
-// across the valid lanes, which sit below the invalid ones.
+// contributing pairs (valid is false on the idle lanes of the last batch;
+// the valid lanes sit below the invalid ones).  Rows r and P - 2 - r are
+// walked together (they hold P candidates between them, so a lane finds its
+// (j, k) with two comparisons and no loop); the pairs of one row j are
+// contiguous in the stream, so equal j values are contiguous in a batch.
 template <typename Work>
 __device__ __forceinline__ void pair_stream(const float4 *__restrict__ A, int P, float rc, int lane,
                                             int *qjk, float *qc2, Work work) {
-  const int npair = P * (P - 1) / 2;
   const float rc2 = rc * rc;
   const unsigned lt = (1u << lane) - 1u;
-  int j = 0, k = 1 + lane;
-  while (j < P - 1 && k >= P) { const int o = k - P; ++j; k = j + 1 + o; }
   int qh = 0, qn = 0;  // ring queue: entries [qh, qn) are pending
-  for (int base = 0; base < npair; base += 32) {
-    bool valid = false;
-    float c2 = 0.f;
-    if (base + lane < npair) {
-      const float4 aj = A[j], ak = A[k];
-      if (aj.w <= rc && ak.w <= rc) {
-        const float cx = aj.x - ak.x, cy = aj.y - ak.y, cz = aj.z - ak.z;
-        c2 = cx * cx + cy * cy + cz * cz;
-        valid = c2 <= rc2;
+  const int nfold = P / 2;  // row pairs (r, P - 2 - r); the middle row of an even P is alone
+  for (int r = 0; r < nfold; ++r) {
+    const int r2 = P - 2 - r;
+    const int n1 = P - 1 - r;                // candidates of row r
+    const int tot = r2 > r ? P : n1;         // with row r2's r + 1
+    for (int base = 0; base < tot; base += 32) {
+      const int t = base + lane;
+      bool valid = false;
+      float c2 = 0.f;
+      int j = r, k = r + 1 + t;
+      if (t >= n1) {
+        j = r2;
+        k = r2 + 1 + (t - n1);
+      }
+      if (t < tot) {
+        const float4 aj = A[j], ak = A[k];
+        if (aj.w <= rc && ak.w <= rc) {
+          const float cx = aj.x - ak.x, cy = aj.y - ak.y, cz = aj.z - ak.z;
+          c2 = cx * cx + cy * cy + cz * cz;
+          valid = c2 <= rc2;
+        }
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, valid);
+      if (valid) {
+        const int e = (qn + __popc(m & lt)) & (kPairQ - 1);
+        qjk[e] = j | (k << 16);
+        qc2[e] = c2;
+      }
+      qn += __popc(m);
+      __syncwarp();
+      if (qn - qh >= 32) {
+        const int e = (qh + lane) & (kPairQ - 1);
+        const int jk = qjk[e];
+        const float cc = qc2[e];
+        __syncwarp();
+        work(jk & 0xffff, jk >> 16, cc, true);
+        qh += 32;
       }
     }
-    const unsigned m = __ballot_sync(0xffffffffu, valid);
-    if (valid) {
-      const int e = (qn + __popc(m & lt)) & (kPairQ - 1);
-      qjk[e] = j | (k << 16);
-      qc2[e] = c2;
-    }
-    qn += __popc(m);
-    __syncwarp();
-    if (qn - qh >= 32) {
-      const int e = (qh + lane) & (kPairQ - 1);
-      const int jk = qjk[e];
-      const float cc = qc2[e];
-      __syncwarp();
-      work(jk & 0xffff, jk >> 16, cc, true);
-      qh += 32;
-    }
-    k += 32;
-    while (j < P - 1 && k >= P) { const int o = k - P; ++j; k = j + 1 + o; }
   }
   if (qn > qh) {
     const int e = (qh + lane) & (kPairQ - 1);
