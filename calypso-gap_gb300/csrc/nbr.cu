@@ -395,6 +395,25 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
         fd[2] = fj.z - fi.z;
         image_box(ext, si.nabc, fi, fj, lo, hi);
       }
+      // Every lane's box holds at most one image (cells wider than twice the
+      // cutoff): one screen per lane, survivors queued in lane order - the
+      // candidates and the order of the general loops below, without them
+      const bool none = hi[0] < lo[0] || hi[1] < lo[1] || hi[2] < lo[2];
+      const bool one = hi[0] == lo[0] && hi[1] == lo[1] && hi[2] == lo[2];
+      if (__all_sync(0xffffffffu, none || one)) {
+        const bool keep = one && !(j == i && lo[0] == 0 && lo[1] == 0 && lo[2] == 0) &&
+                          screen_r2(L32, fd, lo[0], lo[1], lo[2]) <= r2max;
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+          const int e = (qt + __popc(m & lt_mask)) & (kQueue - 1);
+          qj[e] = j;
+          qs[e] = ((lo[0] + 128) << 16) | ((lo[1] + 128) << 8) | (lo[2] + 128);
+        }
+        qt += __popc(m);
+        __syncwarp();
+        drain(false);
+        continue;
+      }
       // FP32 screen: survivors of this lane's image box, in (n1, n2, n3) order
       int c = 0;
       if (valid)
