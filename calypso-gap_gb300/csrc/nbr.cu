@@ -382,14 +382,17 @@ __global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
         qh += min(32, qt - qh);
       }
     };
+    // the next chunk's fractional coordinates are loaded one chunk ahead
+    float4 fj_next = lane < si.na ? frac32[si.a0 + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
     for (int base = 0; base < si.na; base += 32) {
       const int jl = base + lane;
       const bool valid = jl < si.na;
       const int j = si.a0 + jl;
+      const float4 fj = fj_next;
+      if (jl + 32 < si.na) fj_next = frac32[j + 32];
       int lo[3] = {0, 0, 0}, hi[3] = {-1, -1, -1};
       float fd[3] = {0.f, 0.f, 0.f};
       if (valid) {
-        const float4 fj = frac32[j];
         fd[0] = fj.x - fi.x;
         fd[1] = fj.y - fi.y;
         fd[2] = fj.z - fi.z;
@@ -742,10 +745,7 @@ __global__ void __launch_bounds__(128) k_min_bond(int N, double rcut,
 }
 
 int grid_for_warps(int nwarps_needed) {
-  int dev = 0;
-  cudaGetDevice(&dev);
-  int sms = 148;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = device_sms();
   int blocks = (nwarps_needed + kWarpsPerBlock - 1) / kWarpsPerBlock;
   int maxb = sms * 16;
   return blocks < maxb ? (blocks > 0 ? blocks : 1) : maxb;
@@ -793,9 +793,7 @@ void launch_neighbors(Workspace &ws, int S, int N, int max_atoms, int cap, doubl
 }
 
 void launch_refresh(Workspace &ws, int N, int cap, cudaStream_t st, bool exact) {
-  int dev = 0, sms = 148;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = device_sms();
   const size_t total = (size_t)N * cap;
   const size_t want = (total + 255) / 256;
   const int grid = (int)std::min<size_t>(want > 0 ? want : 1, (size_t)sms * 8);
