@@ -1,13 +1,18 @@
 // api.cu - the C ABI (include/gapgb.h): models, workspace, evaluation.
 //
 // One evaluation of a packed batch is, in stream order:
-//   prep (lattice images, weights)  -> neighbour list -> reverse slots
+//   prep (lattice images, weights)  -> neighbour list
 //   -> descriptors G -> GPR (e, dE/dG) -> slot gradients + per-atom virial
-//   -> forces (gather) -> per-structure energy and stress.
-// This is FGAP_CALC (gappy/libgap/gap_calc.f90:1-301) for many structures at
-// once, without the dense Jacobian.  The host-buffer calls synchronise once
-// after the neighbour list to size shared memory and grow the neighbour
-// capacity on overflow; the device-buffer call never synchronises.
+//   -> forces -> per-structure energy and stress.
+// The grouped FP32 gradient kernel scatters the forces itself; the FP64 path
+// and the generic FP32 kernels add reverse slots after the neighbour list and
+// gather the forces (deterministic).  This is FGAP_CALC
+// (gappy/libgap/gap_calc.f90:1-301) for many structures at once, without the
+// dense Jacobian.  The host-buffer calls synchronise once: the descriptor
+// kernels take the previous call's slot count, and a batch that needs more
+// slots or overflows the neighbour capacity is recomputed after a sync that
+// sizes shared memory and grows the capacity.  The device-buffer call never
+// synchronises.
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
