@@ -239,7 +239,8 @@ def run_reference(args):
 
 def cpu_baseline(arrays):
     """The oracle on the host cores on a bounded sample (one alloy512
-    structure per core)."""
+    structure per core), plus the latency of one structure on one core (the
+    reference is single-threaded and farmed one structure per process)."""
     import tempfile
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from helpers import write_model_file
@@ -255,8 +256,14 @@ def cpu_baseline(arrays):
         t0 = time.perf_counter()
         oracle.gap_calc_batch(om, off, sp, lat, pos, 6.0, cores)
         dt = time.perf_counter() - t0
+        off1, sp1, lat1, pos1 = S.pack(structs[:1])
+        t0 = time.perf_counter()
+        oracle.gap_calc_batch(om, off1, sp1, lat1, pos1, 6.0, 1)
+        lat_s = time.perf_counter() - t0
     return {"value": cores * ATOMS / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d alloy512 structures (one per host thread), %.1f s" % (cores, dt)}
+            "sample": "%d alloy512 structures (one per host thread), %.1f s" % (cores, dt),
+            "latency_1core_s": lat_s,
+            "latency_sample": "one alloy512 structure (E, F, stress) on one host thread"}
 
 
 STAGES = ["neighbours", "descriptors", "gpr", "chain_rule"]
