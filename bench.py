@@ -46,7 +46,9 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gapgb", choices=["gapgb", "reference"])
-    p.add_argument("--batch", type=int, default=64, help="structures per step per GPU")
+    p.add_argument("--batch", type=int, default=None,
+                   help="structures per step per GPU (default: one full wave of the tensor-core "
+                        "GPR, two 128-atom CTAs per SM: 76 alloy512 cells on 152 SMs)")
     p.add_argument("--precision", default="tc", choices=["fp32", "tc", "fp64", "mixed"])
     p.add_argument("--no-oracle", action="store_true", help="skip the oracle error check")
     p.add_argument("--workload", default="alloy", choices=["alloy", "population", "surrogate", "md", "precision",
@@ -85,6 +87,17 @@ def shard_seeds(rank, batch):
     N ranks evaluate N x batch different cells (weak scaling, no data-path
     collective)."""
     return [100000 + rank * batch + s for s in range(batch)]
+
+
+def default_batch(args, device):
+    """Structures per step: by default one full wave of the tensor-core GPR
+    kernel, which holds 128 atoms per CTA and two CTAs per SM (76 alloy512
+    cells = 38912 atoms on 152 SMs)."""
+    if args.batch is None:
+        import torch
+        sms = torch.cuda.get_device_properties(device).multi_processor_count
+        args.batch = max(1, sms * 2 * 128 // ATOMS)
+    return args.batch
 
 
 def workload(rank, batch):
@@ -796,7 +809,7 @@ def run_precision(args):
     dev = torch.device("cuda", 0)
     arrays = make_model()
     zt, wt, ty, al, rc, ze, theta, mm, coeff = arrays
-    structs, (off, sp, lat, pos) = workload(0, args.batch)
+    structs, (off, sp, lat, pos) = workload(0, default_batch(args, dev))
     S, N = len(structs), int(off[-1])
     t = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
          for k, v in (("off", off), ("sp", sp), ("lat", lat), ("pos", pos))}
@@ -878,7 +891,7 @@ def run_variance(args):
     arrays = make_model()
     zt, wt, ty, al, rc, ze, theta, mm, coeff = arrays
     Q = qmm_of(mm, theta)
-    structs, (off, sp, lat, pos) = workload(0, args.batch)
+    structs, (off, sp, lat, pos) = workload(0, args.batch or 64)
     S, N, M = len(structs), int(off[-1]), len(mm)
     m = gapgb.GapModel.create(zt, wt, ty, al, rc, theta, mm, coeff, sf_zeta=ze)
     m.set_qmm(Q)
@@ -1054,7 +1067,7 @@ def main():
         m.set_neighbour_cap(96)
         return m
 
-    structs, (off, sp, lat, pos) = workload(rank, args.batch)
+    structs, (off, sp, lat, pos) = workload(rank, default_batch(args, dev))
     S, N = len(structs), int(off[-1])
     d_off = torch.from_numpy(off).to(dev)
     d_sp = torch.from_numpy(sp).to(dev)
@@ -1174,6 +1187,7 @@ def main():
         "data": "synthetic",
         "config": {"workload": "alloy512 ternary fcc (Z 13/28/40), D=64, M=4000",
                    "structures_per_step": S, "atoms_per_step_per_gpu": N,
+                   "batch_rule": "one wave of the tensor-core GPR: 2 CTAs x 128 atoms per SM",
                    "precision": args.precision, "l2": "flushed between steps (512 MB write)"},
         "e2e": {"value": world * N / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
