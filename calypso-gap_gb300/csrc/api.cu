@@ -101,6 +101,10 @@ gapgb_status ensure_ws(gapgb_model *m, int N, int S, int cap) {
   if (ws.d_flags && N <= ws.N && S <= ws.S && cap <= ws.cap && D == ws.D &&
       scratch <= ws.gpr_scratch_size)
     return GAPGB_OK;
+  if (m->live_graphs->load() > 0)
+    return fail(GAPGB_ERR_ARG,
+                "the workspace would move while a CUDA graph built from this model is alive "
+                "(free the graph first, or create it for the largest batch)");
   // grow with headroom so that slightly larger batches do not reallocate
   int nN = N > ws.N ? N + N / 8 : ws.N;
   int nS = S > ws.S ? S + S / 8 : ws.S;
@@ -271,6 +275,8 @@ gapgb_status ensure_surrogate(gapgb_model *m, int N) {
   gapgb_status st = surrogate_prepare(m->surrogate, N);
   if (st) return st;
   if (N <= m->surr_cap) return GAPGB_OK;
+  if (m->live_graphs->load() > 0)
+    return fail(GAPGB_ERR_ARG, "surrogate buffers would move while a CUDA graph is alive");
   free_dev(m->surr_std);
   free_dev(m->fb_rows);
   free_dev(m->fb_count);
@@ -661,6 +667,8 @@ gapgb_status gapgb_model_tables(const gapgb_model *m, int *species_z, double *sp
 
 gapgb_status gapgb_set_option(gapgb_model *m, gapgb_option opt, int64_t value) {
   if (!m) return fail(GAPGB_ERR_ARG, "null model");
+  if (m->live_graphs->load() > 0 && opt != GAPGB_OPT_DEVICE)
+    return fail(GAPGB_ERR_ARG, "the model is bound to a live CUDA graph (free it first)");
   switch (opt) {
     case GAPGB_OPT_PRECISION:
       if (value != GAPGB_PREC_FP64 && value != GAPGB_PREC_FP32 && value != GAPGB_PREC_MIXED &&
@@ -736,11 +744,16 @@ gapgb_status gapgb_model_set_coeff(gapgb_model *m, const double *coeff) {
   for (int k = 0; k < M; ++k) c32[k] = (float)coeff[k];
   GAPGB_CUDA_TRY(cudaMemcpy(m->d_coeff, coeff, sizeof(double) * M, cudaMemcpyHostToDevice));
   GAPGB_CUDA_TRY(cudaMemcpy(m->d_coeff32, c32.data(), sizeof(float) * M, cudaMemcpyHostToDevice));
-  // the tensor-core operand images carry c: rebuilt by the next call that needs them
-  if (m->d_tc) cudaFree(m->d_tc);
-  if (m->d_tf32) cudaFree(m->d_tf32);
-  m->d_tc = nullptr;
-  m->d_tf32 = nullptr;
+  // the tensor-core operand images carry c: rewritten in place, so graphs
+  // that captured them replay with the new coefficients
+  if (m->d_tc) {
+    const gapgb_status st = build_tc_image(m, true);
+    if (st) return st;
+  }
+  if (m->d_tf32) {
+    const gapgb_status st = build_tf32_image(m, true);
+    if (st) return st;
+  }
   return GAPGB_OK;
 }
 
@@ -878,6 +891,7 @@ struct gapgb_graph {
   gapgb_model *model = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  std::shared_ptr<std::atomic<int>> live;  // the model's live-graph count
 };
 
 gapgb_status gapgb_graph_create(gapgb_model *m, int nstruct, int natoms, int max_atoms,
@@ -916,6 +930,8 @@ gapgb_status gapgb_graph_create(gapgb_model *m, int nstruct, int natoms, int max
     delete g;
     return fail(GAPGB_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
   }
+  g->live = m->live_graphs;
+  g->live->fetch_add(1);
   *out = g;
   return GAPGB_OK;
 }
@@ -930,6 +946,7 @@ void gapgb_graph_free(gapgb_graph *g) {
   if (!g) return;
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);
+  if (g->live) g->live->fetch_sub(1);
   delete g;
 }
 
@@ -953,6 +970,8 @@ gapgb_status gapgb_stage_times(gapgb_model *m, float t[4]) {
 
 gapgb_status gapgb_model_set_surrogate(gapgb_model *m, gapgb_surrogate *s, double threshold_ev) {
   if (!m) return fail(GAPGB_ERR_ARG, "null model");
+  if (m->live_graphs->load() > 0)
+    return fail(GAPGB_ERR_ARG, "the model is bound to a live CUDA graph (free it first)");
   if (!s) {
     m->surrogate = nullptr;
     if (m->precision == GAPGB_PREC_SURROGATE) m->precision = GAPGB_PREC_MIXED;

@@ -21,7 +21,9 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -337,6 +339,10 @@ struct gapgb_model {
   void *fb_scratch = nullptr;  // partial sums of the fallback GPR
   gapgb::VarState var;         // predictive variance (gapgb_model_set_qmm)
   float var_ms = 0.f;          // device time of the last variance kernels (profiling)
+  // CUDA graphs (gapgb_graph, gapgb_md) that captured this model's buffers:
+  // while any is alive, nothing they captured may move.  Shared, so a graph
+  // freed after its model still decrements valid memory.
+  std::shared_ptr<std::atomic<int>> live_graphs = std::make_shared<std::atomic<int>>(0);
 };
 
 namespace gapgb {
@@ -404,9 +410,12 @@ void launch_min_bond(Workspace &ws, int N, double rcut, double *d_out, cudaStrea
 size_t wacsf_smem_bytes(const SFDev &t, int cap_smem, bool fwd, size_t elem);
 int gpr_nsplit(int N, int M);
 size_t gpr_scratch_bytes(int N, int M, int D, size_t elem);
-gapgb_status build_tc_image(gapgb_model *m);
+// The tensor-core operand images: built by the first call that needs them;
+// `refresh` rewrites an existing image in place (new coefficients) so that
+// captured graphs keep valid addresses.
+gapgb_status build_tc_image(gapgb_model *m, bool refresh = false);
 size_t tc_atom_scratch_bytes(int N);
-gapgb_status build_tf32_image(gapgb_model *m);
+gapgb_status build_tf32_image(gapgb_model *m, bool refresh = false);
 size_t tf32_atom_scratch_bytes(int N);
 void launch_gpr_tf32(gapgb_model *m, Workspace &ws, int N, cudaStream_t st);
 void launch_gpr_rows(const gapgb_model *m, Workspace &ws, int cap, const int *d_rows,

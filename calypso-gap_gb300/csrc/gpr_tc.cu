@@ -346,8 +346,8 @@ size_t tc_smem_bytes() { return kSmemBytes; }
 // Builds the model's tensor-core image: per sparse tile mh, ml (K-major over
 // D), mhT, mlT (K-major over the tile's points), b2 = -log2e |m''|^2 / 2 and c
 // (FP32), plus mu.
-gapgb_status build_tc_image(gapgb_model *m) {
-  if (m->d_tc) return GAPGB_OK;
+gapgb_status build_tc_image(gapgb_model *m, bool refresh) {
+  if (m->d_tc && !refresh) return GAPGB_OK;
   const HostModel &h = m->host;
   const int M = h.M, D = h.D;
   if (D > kDP) {
@@ -390,7 +390,7 @@ gapgb_status build_tc_image(gapgb_model *m) {
   std::vector<float> muf(kDP);
   for (int d = 0; d < kDP; ++d) muf[d] = (float)mu[d];
   const size_t bytes = img.size() + kDP * sizeof(float);
-  GAPGB_CUDA_TRY(cudaMalloc(&m->d_tc, bytes));
+  if (!m->d_tc) GAPGB_CUDA_TRY(cudaMalloc(&m->d_tc, bytes));  // same size on a refresh
   GAPGB_CUDA_TRY(cudaMemcpy(m->d_tc, img.data(), img.size(), cudaMemcpyHostToDevice));
   GAPGB_CUDA_TRY(cudaMemcpy((unsigned char *)m->d_tc + img.size(), muf.data(), kDP * sizeof(float),
                             cudaMemcpyHostToDevice));

@@ -301,8 +301,8 @@ float tf32_round(float f) {
 
 // The model's TF32 image: per sparse tile m~ (K-major over D), m~^T (K-major
 // over the tile's points), b2 = -log2e |m~|^2 / 2 and c, plus mu.
-gapgb_status build_tf32_image(gapgb_model *m) {
-  if (m->d_tf32) return GAPGB_OK;
+gapgb_status build_tf32_image(gapgb_model *m, bool refresh) {
+  if (m->d_tf32 && !refresh) return GAPGB_OK;
   const HostModel &h = m->host;
   const int M = h.M, D = h.D;
   if (D > kDP) {
@@ -336,7 +336,7 @@ gapgb_status build_tf32_image(gapgb_model *m) {
   std::vector<float> muf(kDP);
   for (int d = 0; d < kDP; ++d) muf[d] = (float)mu[d];
   const size_t bytes = img.size() + kDP * sizeof(float);
-  GAPGB_CUDA_TRY(cudaMalloc(&m->d_tf32, bytes));
+  if (!m->d_tf32) GAPGB_CUDA_TRY(cudaMalloc(&m->d_tf32, bytes));  // same size on a refresh
   GAPGB_CUDA_TRY(cudaMemcpy(m->d_tf32, img.data(), img.size(), cudaMemcpyHostToDevice));
   GAPGB_CUDA_TRY(cudaMemcpy((unsigned char *)m->d_tf32 + img.size(), muf.data(),
                             kDP * sizeof(float), cudaMemcpyHostToDevice));

@@ -155,6 +155,7 @@ struct gapgb_md {
   int kin_parts = 1;
   cudaStream_t stream = nullptr;
   cudaGraphExec_t g_rebuild = nullptr, g_refresh = nullptr;
+  std::shared_ptr<std::atomic<int>> live;  // the model's live-graph count, once captured
   long step = 0;
 };
 
@@ -212,6 +213,7 @@ void gapgb_md_free(gapgb_md *md) {
   if (!md) return;
   if (md->g_rebuild) cudaGraphExecDestroy(md->g_rebuild);
   if (md->g_refresh) cudaGraphExecDestroy(md->g_refresh);
+  if (md->live) md->live->fetch_sub(1);
   void *ps[] = {md->accf, md->energy, md->force, md->stress, md->ekin, md->pos_ref, md->kin_part};
   for (void *p : ps)
     if (p) cudaFree(p);
@@ -298,6 +300,8 @@ gapgb_status gapgb_md_create(gapgb_model *m, int nstruct, int natoms, const int 
     gapgb_md_free(md);
     return st;
   }
+  md->live = m->live_graphs;
+  md->live->fetch_add(1);
   *out = md;
   return GAPGB_OK;
 }

@@ -245,8 +245,12 @@ gapgb_status gapgb_check_device_status(gapgb_model *model);
  * the same launch sequence; the graph stays bound to these buffers, so the
  * caller refills d_pos / d_lat (same sizes) between launches.  Structure
  * search evaluates a whole ragged population with one graph launch; MD
- * replays it every step.  The model must not be reconfigured (precision,
- * capacity) while a graph built from it is alive. */
+ * replays it every step.  While a graph (or an MD object) built from a model
+ * is alive, the model refuses with GAPGB_ERR_ARG what would move the buffers
+ * the graph captured: gapgb_set_option, gapgb_model_set_surrogate, and any
+ * host-buffer call larger than the workspace the graph was built with.
+ * gapgb_model_set_coeff is allowed: the tensor-core operand images are
+ * rewritten in place and the graph replays with the new coefficients. */
 typedef struct gapgb_graph gapgb_graph;
 gapgb_status gapgb_graph_create(gapgb_model *model, int nstruct, int natoms,
                                 int max_atoms, const int *d_atom_off,

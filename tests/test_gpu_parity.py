@@ -577,6 +577,52 @@ def test_graph_replay_matches_direct(synth_pop):
     gr.close()
 
 
+def test_graph_follows_new_coefficients_and_pins_its_buffers(gapgb_mod, oracle_mod, tmp_path):
+    """A graph captured on the tensor-core form replays with coefficients set
+    after the capture (the operand image is rewritten in place), and while it
+    is alive the model refuses what would move the buffers it captured: a
+    precision change, or a batch larger than the workspace."""
+    import torch
+    import gapgb.synth as S
+    path = str(tmp_path / "gp")
+    synth_model_file(path, oracle_mod, [S.si64(seed=s) for s in range(2)], M=200, seed=3)
+    m = gapgb_mod.GapModel.load(path)
+    m.set_precision("tc")
+    batch = [S.si64(seed=40 + s, jitter=0.1) for s in range(3)]
+    (off, sp, lat, pos), t = _dev_batch(batch)
+    gr = m.graph(len(batch), int(off[-1]), int(np.diff(off).max()), t["off"].data_ptr(),
+                 t["sp"].data_ptr(), t["lat"].data_ptr(), t["pos"].data_ptr(), 1,
+                 t["E"].data_ptr(), t["F"].data_ptr(), t["S"].data_ptr())
+    stream = torch.cuda.current_stream().cuda_stream
+    gr.launch(stream)
+    torch.cuda.synchronize()
+    m.check_device_status()
+    E1, F1 = t["E"].cpu().numpy().copy(), t["F"].cpu().numpy().copy()
+    m.set_coeff(2.0 * m.arrays()[2])
+    gr.launch(stream)
+    torch.cuda.synchronize()
+    m.check_device_status()
+    E2, F2 = t["E"].cpu().numpy(), t["F"].cpu().numpy()
+    # the energy is linear in c; forces too (their FP64 atomic sums reorder)
+    assert np.allclose(E2, 2.0 * E1, rtol=1e-12, atol=0.0)
+    assert np.abs(F2 - 2.0 * F1).max() <= 1e-9 * np.abs(F2).max()
+    # the host-buffer path (same sizes: the workspace stays) agrees; a stale
+    # image would be off by a factor of two
+    Eh, Fh, _ = m.eval_batch(off, sp, lat, pos)
+    assert np.allclose(E2, Eh, rtol=1e-6, atol=0.0)
+    assert np.abs(F2 - Fh).max() <= 1e-5 * np.abs(F2).max()
+    with pytest.raises(gapgb_mod.GapError):
+        m.set_precision("fp64")
+    o2, s2, l2, p2 = S.pack(batch * 4)
+    with pytest.raises(gapgb_mod.GapError):
+        m.eval_batch(o2, s2, l2, p2)
+    gr.close()
+    m.set_precision("fp64")
+    E3, _, _ = m.eval_batch(o2, s2, l2, p2)
+    assert np.allclose(E3[:3], E3[3:6], rtol=0.0, atol=1e-9 * np.abs(E3).max())
+    m.close()
+
+
 def test_autotune_choice_within_tolerance(synth_si):
     import gapgb.synth as S
     from gapgb import tune
