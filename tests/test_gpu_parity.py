@@ -178,6 +178,50 @@ def test_fp64_vs_oracle_population_batch(synth_pop, oracle_mod):
         assert np.abs(ae[off[s]:off[s + 1]] - ex["e"]).max() <= 1e-9 * max(1.0, np.abs(ex["e"]).max())
 
 
+def _edge_structures():
+    """Atoms with no neighbour at all (15 A apart in a 30 A cell), one atom
+    whose only neighbours are its own images (2.7 A cubic cell), and a dimer
+    whose atoms have exactly one neighbour each (no angular pair)."""
+    iso = (np.eye(3) * 30.0, np.array([[1.0, 1.0, 1.0], [16.0, 16.0, 16.0]]),
+           np.array([14, 8], np.int32))
+    lone = (np.eye(3) * 2.7 + np.array([[0.0, 0.0, 0.0], [0.3, 0.0, 0.0], [0.0, 0.2, 0.0]]),
+            np.array([[0.4, 0.5, 0.6]]), np.array([14], np.int32))
+    dimer = (np.eye(3) * 25.0, np.array([[5.0, 5.0, 5.0], [6.2, 5.9, 5.8]]),
+             np.array([8, 14], np.int32))
+    return [iso, lone, dimer]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "tc"])
+def test_edge_structures_match_oracle(synth_pop, oracle_mod, prec):
+    """No neighbours, only self-images, one neighbour: alone and as one
+    ragged batch, against the oracle (FP64 bar for fp64, the
+    reduced-precision bar otherwise)."""
+    import gapgb.synth as S
+    g, o, _ = synth_pop
+    g.set_precision(prec)
+    e_tol, f_tol, s_tol = (E_REL, F_ABS, S_ABS) if prec == "fp64" else (1e-3, 20e-3, 1e-2)
+    edge = _edge_structures()
+    ref = [oracle_mod.gap_calc(o, z, l, p, 6.0, True) for l, p, z in edge]
+    for k, (l, p, z) in enumerate(edge):
+        E, F, St, _ = g.eval(z, l, p)
+        oE, oF, oS, _ = ref[k]
+        assert abs(E - oE) <= (e_tol * max(1.0, abs(oE)) if prec == "fp64" else e_tol * len(z)), k
+        assert np.abs(F - oF).max() <= f_tol, k
+        assert np.abs(St - oS).max() <= s_tol, k
+    # the isolated atoms feel nothing
+    E0, F0, S0, _ = g.eval(edge[0][2], edge[0][0], edge[0][1])
+    assert np.abs(F0).max() == 0.0 and np.abs(S0).max() == 0.0
+    off, sp, lat, pos = S.pack(edge)
+    E, F, St = g.eval_batch(off, sp, lat, pos)
+    for k in range(len(edge)):
+        oE, oF, oS, _ = ref[k]
+        n = off[k + 1] - off[k]
+        assert abs(E[k] - oE) <= (e_tol * max(1.0, abs(oE)) if prec == "fp64" else e_tol * n), k
+        assert np.abs(F[off[k]:off[k + 1]] - oF).max() <= f_tol, k
+        assert np.abs(St[k] - oS).max() <= s_tol, k
+    g.set_precision("fp64")
+
+
 def test_batch_equals_single(synth_si):
     import gapgb.synth as S
     g, _ = synth_si
