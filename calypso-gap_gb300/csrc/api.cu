@@ -431,6 +431,9 @@ gapgb_status eval_host(gapgb_model *m, int S, const int *atom_off, const int *sp
     GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.h_flags, ws.d_flags, 8 * sizeof(int), cudaMemcpyDeviceToHost, s));
     GAPGB_CUDA_TRY(cudaStreamSynchronize(s));
     const int maxcnt = ws.h_flags[1];
+    // unknown species and the image limit end the call before any growth (a
+    // clamped image range can overflow every capacity)
+    if (ws.h_flags[0] & (kFlagUnknownSpecies | kFlagImageLimit)) return flags_to_status(ws.h_flags);
     if (ws.h_flags[0] & kFlagNeighbourOverflow) {
       const int newcap = ((maxcnt + 31) / 32) * 32;
       m->cap = newcap;

@@ -417,6 +417,23 @@ def test_unknown_species_is_an_error(golden_model, frames, gapgb_mod):
     assert ei.value.status == 4
 
 
+def test_image_limit_is_an_error(golden_model, gapgb_mod):
+    """A 0.02 A lattice vector needs ~300 images along it, beyond the 127 the
+    shift encoding holds: CAP_EXCEEDED, reported before any capacity growth
+    (the clamped range overflows every capacity)."""
+    lat = np.diag([10.0, 10.0, 0.02])
+    pos = np.array([[1.0, 2.0, 0.01]])
+    with pytest.raises(gapgb_mod.GapError) as ei:
+        golden_model.eval(np.array([6], np.int32), lat, pos)
+    assert ei.value.status == 3
+    # the model stays usable
+    golden_model.set_precision("fp64")
+    lat2 = np.eye(3) * 8.0
+    E, F, S, _ = golden_model.eval(np.array([6, 6], np.int32), lat2,
+                                   np.array([[0.0, 0.0, 0.0], [1.5, 0.2, 0.1]]))
+    assert np.isfinite(E)
+
+
 def test_neighbour_capacity_grows(gapgb_mod, frames):
     m = gapgb_mod.GapModel.load(GOLDEN_MODEL)
     m.set_neighbour_cap(16)
