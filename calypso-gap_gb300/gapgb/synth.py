@@ -14,7 +14,7 @@ workloads the evaluator is measured on:
   surrogate the alloy512 generator with a smooth alloy GAP (theta = 4 std):
             the narrow theta = 0.8 std GAP is a sum of 4000 sharp bumps that a
             64-128-128-1 network cannot represent, so the learned surrogate is
-            trained and judged on the smooth one
+            trained and evaluated on the smooth one
 
 SF set (used by all synthetic models): 20 type-1 radial functions with alpha
 log-spaced 0.003..2.0 A^-2, cutoff 6 A; 12 angular functions = zeta {1,2,4}
