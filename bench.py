@@ -655,7 +655,7 @@ def run_surrogate(args):
                 errs.append((abs(E_s[s] - eo) / (a1 - a0), float(np.abs(F_s[a0:a1] - fo).max())))
             oracle_err = {"dE_per_atom_max": max(x[0] for x in errs),
                           "dF_max": max(x[1] for x in errs), "structures": 2}
-    except Exception as ex:  # the oracle is a checker; its absence does not stop the bench
+    except Exception as ex:  # the oracle is test infrastructure; its absence does not stop the bench
         oracle_err = {"unavailable": str(ex)[:200]}
     # kernels per surrogate evaluation: prep x2, neighbours, descriptors,
     # surrogate (count, segments, scatter, weight image, row image, tensor-core
@@ -698,7 +698,7 @@ def run_surrogate(args):
 
 
 def run_md(args):
-    """Config 5: 32768-atom Si/Ge (50/50) diamond cell, a = 5.54 A, jitter
+    """MD workload: 32768-atom Si/Ge (50/50) diamond cell, a = 5.54 A, jitter
     0.1 A; GAP with M = 8000 sparse points (library descriptors of a second
     seeded cell, theta = 1 std, coeff ~ N(0, 1e-3)); Maxwell-Boltzmann
     velocities at 600 K; NVE velocity Verlet, dt = 1 fs, neighbour rebuild
@@ -798,7 +798,8 @@ def run_md(args):
 
 
 def run_precision(args):
-    """Config 2's comparison: the alloy step (64 cells x 512 atoms, M = 4000,
+    """Precision-form comparison: the alloy step (512-atom cells, the default
+    batch as in the headline workload, M = 4000,
     D = 64) in every arithmetic form of the contraction - FP64 (plain), FP32
     SIMT, mixed (FP32 descriptors, FP64 GPR), TF32 tensor cores, split-BF16x3
     tensor cores - each timed on device-resident inputs (CUDA events, L2

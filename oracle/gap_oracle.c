@@ -2,7 +2,7 @@
  * gap_oracle.c - CPU FP64 restatement of CALYPSO-GAP's FGAP_CALC / CAR2ACSF /
  * FGAP_READ / FGET_BOND.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA product path and the
+ * TEST INFRASTRUCTURE ONLY: the oracle for the CUDA product path and the
  * CPU baseline timed by bench.py.  Nothing in the product links or calls it.
  *
  * Pinned against the reference's own outputs: the 11 frames of

@@ -3,7 +3,7 @@
  * evaluation (gappy/libgap/gap_calc.f90, gappy/libgap/wacsf.f90,
  * gappy/libgap/get_bond.f90).
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker that the CUDA
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle that the CUDA
  * product path is compared against, and the CPU baseline that bench.py times.
  * The product library never links, loads or calls it.
  *

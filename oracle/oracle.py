@@ -1,6 +1,6 @@
 """ctypes wrapper around liboracle.so (gap_oracle.c).
 
-TEST INFRASTRUCTURE ONLY - the checker and the CPU baseline.  The product
+TEST INFRASTRUCTURE ONLY - the oracle and the CPU baseline.  The product
 path never imports this module.
 
 Each function names the reference routine it restates:
