@@ -1,0 +1,43 @@
+"""The benchmark line's derived fields, on the CPU: the roofline entry's keys
+and arithmetic, and the default batch (one wave of the tensor-core GPR)."""
+import json
+import os
+import sys
+import types
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+
+
+def test_roofline_entry_keys_and_arithmetic():
+    stages = [0.22, 0.35, 0.24, 0.52]  # ms: neighbours, descriptors, gpr, chain rule
+    N, D = 38912, 64
+    roof = bench.roofline(stages, N, D, "tc")
+    peaks, _ = bench.load_peaks()
+    assert roof["kernel"] == "chain_rule" and roof["bound"] == "hbm" and roof["unit"] == "GB/s"
+    bpa = bench.stage_bytes_per_atom(D)["chain_rule"]
+    assert np.isclose(roof["achieved"], bpa * N / (0.52e-3) / 1e9)
+    assert roof["peak"] == peaks["hbm_gbs"]
+    assert np.isclose(roof["frac"], roof["achieved"] / roof["peak"])
+    inputs = json.load(open(os.path.join(ROOT, "profiles", "roofline_inputs.txt")))
+    assert np.isclose(roof["traffic"], inputs["dram_bytes_per_atom"]["chain_rule"] * N)
+    t = roof["gpr_tensor"]
+    assert t["bound"] == "tensor" and t["unit"] == "TFLOP/s"
+    assert np.isclose(t["frac"], t["achieved"] / t["peak"])
+    assert set(roof["stage_ms"]) == set(bench.STAGES)
+    # forms without the tensor-core GPR report no tensor entry
+    assert "gpr_tensor" not in bench.roofline(stages, N, D, "fp32")
+
+
+def test_default_batch_is_one_gpr_wave(monkeypatch):
+    import torch
+    monkeypatch.setattr(torch.cuda, "get_device_properties",
+                        lambda dev: types.SimpleNamespace(multi_processor_count=152))
+    args = types.SimpleNamespace(batch=None)
+    assert bench.default_batch(args, 0) == 76  # 152 SMs x 2 CTAs x 128 atoms / 512
+    args = types.SimpleNamespace(batch=64)
+    assert bench.default_batch(args, 0) == 64  # an explicit --batch wins
