@@ -310,8 +310,12 @@ def load_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def roofline(stages, N, D, precision):
-    """Roofline entries from the per-stage device times (ms per step)."""
+def roofline(stages, N, D, precision, simt=None, plain_stages=None):
+    """Roofline entries from the per-stage device times (ms per step).
+
+    `simt` holds the measured FP32 / FP64 FMA and MUFU ex2 rates of the device
+    (gapgb.measure_peaks); `plain_stages` the stage times of the plain FP64
+    path on the same workload."""
     peaks, src = load_peaks()
     dom = int(np.argmax(stages))
     name = STAGES[dom]
@@ -331,8 +335,13 @@ def roofline(stages, N, D, precision):
             "stage_ms": {n: float(s) for n, s in zip(STAGES, stages)},
             "algorithmic_bytes_per_atom": bpa[name]}
     # FP32 arithmetic of the chain-rule / descriptor kernels (counted FLOPs per
-    # angular pair and radial term, 32 SFs) against 152 SMs x 128 lanes x 2 x clock
+    # angular pair and radial term, 32 SFs) against the measured FP32 FMA rate
+    # (fallback: 152 SMs x 128 lanes x 2 x 2.07 GHz)
     nominal_fp32 = 152 * 128 * 2 * 2.07e9 / 1e12
+    fp32_peak = simt["fp32_tflops"] if simt else nominal_fp32
+    fp32_src = "measured fp32 FMA (gapgb_measure_peaks)" if simt else "nominal"
+    if simt:
+        roof["simt_peaks"] = simt
     m = M_SPARSE
     if precision == "tc":
         mp = ((m + 127) // 128) * 128
@@ -348,8 +357,9 @@ def roofline(stages, N, D, precision):
     # the GPR's exp rate (one per atom and sparse point) against the nominal
     # MUFU rate (16 per SM per clock)
     exps = N * m / (stages[2] * 1e-3)
-    mufu = 152 * 16 * 2.07e9
-    roof["gpr_exp"] = {"per_s": exps, "nominal_per_s": mufu, "frac": exps / mufu}
+    mufu = simt["ex2_per_s_1e12"] * 1e12 if simt else 152 * 16 * 2.07e9
+    roof["gpr_exp"] = {"per_s": exps, "peak_per_s": mufu, "frac": exps / mufu,
+                       "peak_source": "measured ex2.approx" if simt else "nominal"}
     # FP32 arithmetic of the descriptor-side stages, counted per contributing
     # angular pair and per (slot, radial SF) with the grouped formulation's
     # flops (an FMA = 2): forward 70 per pair (geometry 10, the NAL exponential
@@ -360,9 +370,24 @@ def roofline(stages, N, D, precision):
     fl_bwd = N * (150.0 * T + 15.0 * P * R)
     for name, fl, st in (("descriptors_fp32", fl_fwd, stages[1]), ("chain_rule_fp32", fl_bwd, stages[3])):
         ach = fl / (st * 1e-3) / 1e12
-        roof[name] = {"achieved_tflops": ach, "nominal_tflops": nominal_fp32,
-                      "frac": ach / nominal_fp32,
+        roof[name] = {"achieved_tflops": ach, "peak_tflops": fp32_peak,
+                      "peak_source": fp32_src, "frac": ach / fp32_peak,
                       "flops_per_atom": fl / N}
+    if plain_stages is not None:
+        # the plain FP64 path: GPR 4 M D flops per atom (two N x M x D
+        # contractions) and the descriptor / chain-rule stages with the same
+        # counted flops as above, all against the measured FP64 FMA rate
+        fp64_peak = simt["fp64_tflops"] if simt else None
+        pl = {"stage_ms": {n: float(x) for n, x in zip(STAGES, plain_stages)},
+              "peak_tflops": fp64_peak,
+              "peak_source": "measured fp64 FMA (gapgb_measure_peaks)" if simt else None}
+        for name, fl, st in (("gpr", 4.0 * m * D * N, plain_stages[2]),
+                             ("descriptors", fl_fwd, plain_stages[1]),
+                             ("chain_rule", fl_bwd, plain_stages[3])):
+            ach = fl / (st * 1e-3) / 1e12
+            pl[name] = {"achieved_tflops": ach,
+                        "frac": ach / fp64_peak if fp64_peak else None}
+        roof["plain_fp64"] = pl
     return roof
 
 
@@ -1117,6 +1142,7 @@ def main():
         ms = sum(a.elapsed_time(b) for a, b in evs)
         return max_over_ranks(ms, world, dev) / steps, summarize_clocks(lines)
 
+    simt = gapgb.measure_peaks()  # the SIMT roofline denominators of this device
     chosen = new_model(args.precision)
     ms_step, clocks = time_device(chosen, args.steps, args.warmup, sampler=(rank == 0))
     value = world * N / (ms_step * 1e-3)
@@ -1169,6 +1195,20 @@ def main():
     ms_plain, _ = time_device(plain, psteps, max(1, args.warmup // 2))
     res_plain = (d_E.cpu().numpy().copy(), d_F.cpu().numpy().copy(), d_S.cpu().numpy().copy())
     plain_value = world * N / (ms_plain * 1e-3)
+    plain.close()
+    # stage times of the plain FP64 path (two steps after one warm-up)
+    os.environ["GAPGB_PROFILE_STAGES"] = "1"
+    pprof = new_model("fp64")
+    plain_stages = np.zeros(4)
+    for it in range(3):
+        flush.zero_()
+        device_step(pprof)
+        pprof.check_device_status()
+        if it >= 1:
+            plain_stages += np.array(pprof.stage_times())
+    plain_stages /= 2
+    pprof.close()
+    os.environ["GAPGB_PROFILE_STAGES"] = "0"
 
     if rank != 0:
         if world > 1:
@@ -1178,7 +1218,7 @@ def main():
     errors = None if args.no_oracle else oracle_errors(
         arrays, structs, {"chosen": res_chosen, "plain": res_plain})
 
-    roof = roofline(stages, N, 2 * len(ty), args.precision)
+    roof = roofline(stages, N, 2 * len(ty), args.precision, simt=simt, plain_stages=plain_stages)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -5,10 +5,11 @@
 // the call: the model's resident arrays, the caller's input and output
 // buffers, and one file-scope scratch array in device memory.  It is meant
 // for callers that cannot call cudaMalloc at the point where they need the
-// energies: code running inside a CUDA stream capture (an allocation there
-// invalidates the capture), host programs that reserve all device memory up
-// front in their own pool, and latency-critical loops that cannot afford the
-// device-wide synchronisation an allocation may cause.
+// energies: host programs (simulation engines, serving processes) that
+// reserve all device memory up front in their own pool, so a cudaMalloc
+// behind their back fails or eats into that pool, and latency-critical loops
+// that cannot afford the device-wide synchronisation cudaMalloc / cudaFree
+// may cause.
 //
 // The scratch array holds the partial sums of the split over sparse points
 // (the same split as the regular GPR kernel) and is a fixed 8 MiB
@@ -21,10 +22,13 @@
 // that overlap on the GPU (other streams or host threads) race on it and must
 // be serialised by the caller.
 //
-// The device address of the array is looked up once per device with
-// cudaGetSymbolAddress, by the first call on that device with that device
-// current; a caller that captures graphs should make one call before its
-// first capture.
+// Set-up, once per device, is done by the first call on that device with
+// that device current: the device address of the array (cudaGetSymbolAddress;
+// in host code the array's name is only a host-side stand-in) and the
+// kernel's shared-memory limit for the largest descriptor length.  That
+// first call should come before any stream capture.  The coefficients are
+// read from the model's device copy: finish (synchronise) every call of this
+// entry point before gapgb_model_set_coeff rewrites them.
 #include <mutex>
 
 #include "gapgb_internal.h"
@@ -40,8 +44,14 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratch];
 
+// shared memory of k_gpr_noalloc for descriptor length D
+constexpr size_t noalloc_smem(int D) {
+  return ((size_t)(kNBM + kNBK) * (D + 1) + (size_t)kNBM * (kNBK + 1)) * sizeof(double);
+}
+
 std::mutex g_ptr_mu;
 double *g_ptr[kMaxDevices] = {nullptr};
+int g_sms[kMaxDevices] = {0};
 
 // FP64 GPR over a range of sparse points per blockIdx.y; partial e and
 // dE/dG of split y go to part_e[y*N + i] and part_d[(y*N + i)*D + d].
@@ -166,7 +176,10 @@ extern "C" gapgb_status gapgb_gpr_noalloc(gapgb_model *m, int natoms, const doub
     return fail_na(GAPGB_ERR_ARG, "device ordinal out of range");
   GAPGB_CUDA_TRY(cudaSetDevice(m->device));
   double *scratch = nullptr;
+  int sms = 0;
   {
+    // once per device: the array's device address, the kernel's shared-memory
+    // limit (for the largest D it accepts) and the SM count
     std::lock_guard<std::mutex> lock(g_ptr_mu);
     if (!g_ptr[m->device]) {
       void *p = nullptr;
@@ -174,13 +187,23 @@ extern "C" gapgb_status gapgb_gpr_noalloc(gapgb_model *m, int natoms, const doub
       if (e != cudaSuccess)
         return fail_na(GAPGB_ERR_CUDA,
                        std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      e = cudaFuncSetAttribute(k_gpr_noalloc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)noalloc_smem(8 * kNMaxV));
+      if (e != cudaSuccess)
+        return fail_na(GAPGB_ERR_CUDA,
+                       std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+      int n = 0;
+      e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, m->device);
+      if (e != cudaSuccess || n < 1)
+        return fail_na(GAPGB_ERR_CUDA,
+                       std::string("cudaDeviceGetAttribute: ") + cudaGetErrorString(e));
+      g_sms[m->device] = n;
       g_ptr[m->device] = static_cast<double *>(p);
     }
     scratch = g_ptr[m->device];
+    sms = g_sms[m->device];
   }
   // split over sparse points: enough blocks for the GPU, bounded by the scratch
-  int dev = m->device, sms = 148;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int bx = (natoms + kNBM - 1) / kNBM;
   const int kt = (M + kNBK - 1) / kNBK;
   int ns = (2 * sms + bx - 1) / bx;
@@ -192,10 +215,8 @@ extern "C" gapgb_status gapgb_gpr_noalloc(gapgb_model *m, int natoms, const doub
   const int nsp = (M + klen - 1) / klen;
   double *part_e = scratch;
   double *part_d = scratch + (size_t)nsp * natoms;
-  const size_t smem = ((size_t)(kNBM + kNBK) * (D + 1) + (size_t)kNBM * (kNBK + 1)) * sizeof(double);
+  const size_t smem = noalloc_smem(D);
   cudaStream_t st = (cudaStream_t)stream;
-  GAPGB_CUDA_TRY(cudaFuncSetAttribute(k_gpr_noalloc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
   k_gpr_noalloc<<<dim3(bx, nsp), 256, smem, st>>>(natoms, M, D, klen, d_G, m->d_mmt, m->d_invth,
                                                    m->d_coeff, part_e, part_d);
   const size_t nd = (size_t)natoms * D;

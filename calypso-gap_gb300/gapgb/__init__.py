@@ -54,6 +54,7 @@ SYMBOLS = [
     ("gapgb_graph_free", None, [_P]),
     ("gapgb_gpr_noalloc", _I, [_P, _I, _P, _P, _P, _P]),
     ("gapgb_stage_times", _I, [_P, _P]),
+    ("gapgb_measure_peaks", _I, [_P]),
     ("gapgb_surrogate_create", _I, [_I, _P, _I, _I, _I, C.c_ulonglong, C.POINTER(_P)]),
     ("gapgb_surrogate_free", None, [_P]),
     ("gapgb_surrogate_info", _I, [_P, _P, _P, _P, _P, _P]),
@@ -130,6 +131,15 @@ def _f64(a, shape=None):
 
 def _i32(a):
     return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def measure_peaks():
+    """Measured FP32 / FP64 FMA rates (TFLOP/s) and MUFU ex2 rate (1e12/s)
+    of the current device, with the SM clock (MHz) each kernel ran at."""
+    out = (C.c_double * 6)()
+    _check(load().gapgb_measure_peaks(out), "gapgb_measure_peaks")
+    return {"fp32_tflops": out[0], "fp64_tflops": out[1], "ex2_per_s_1e12": out[2],
+            "fp32_mhz": out[3], "fp64_mhz": out[4], "ex2_mhz": out[5]}
 
 
 class GapModel:

@@ -24,6 +24,9 @@ import numpy as np
 from . import GapModel, OPT_NEIGHBOUR_CAP, load
 
 OPT_GENERIC_KERNELS = 3
+# every precision form the tuner can return: the timed candidates, and the
+# plain FP64 path when no candidate passes the error gates
+FORMS = ("tc", "tf32", "fp32", "mixed", "fp64")
 
 
 def _signature(model, off, device_name):

@@ -267,23 +267,35 @@ void gapgb_graph_free(gapgb_graph *graph);
  * Only filled when GAPGB_PROFILE_STAGES is set in the environment. */
 gapgb_status gapgb_stage_times(gapgb_model *model, float t[4]);
 
+/* Measured arithmetic peaks of the current device, the roofline denominators
+ * of the SIMT kernels (no counterpart in the reference, which has no device
+ * code): out[0] FP32 FMA TFLOP/s, out[1] FP64 FMA TFLOP/s (an FMA = 2 flops),
+ * out[2] MUFU ex2 rate in 1e12 per second; out[3..5] the SM clock (MHz) each
+ * of the three kernels ran at.  Each is one kernel of independent FMA / ex2
+ * chains on every SM, timed by CUDA events after a warm-up launch (about
+ * 0.1 s in all). */
+gapgb_status gapgb_measure_peaks(double out[6]);
+
 /* ---- GPR step without device allocation ---------------------------------- */
 
 /* Atomic energies e[natoms] and dE/dG[natoms*D] (FP64, row-major) from FP64
  * descriptors d_G[natoms*D] already in device memory, enqueued on `stream`
  * with no device allocation of any kind.  No counterpart in the reference:
- * it serves callers that cannot allocate when they need the GPR - code inside
- * a CUDA stream capture (an allocation would invalidate the capture), hosts
- * that reserve all device memory up front in their own pool, and loops that
- * cannot take the device-wide synchronisation an allocation may cause.
+ * it serves callers that cannot allocate when they need the GPR - hosts
+ * (simulation engines, serving processes) that reserve all device memory up
+ * front in their own pool, where a cudaMalloc behind their back fails or
+ * eats into the pool, and loops that cannot take the device-wide
+ * synchronisation cudaMalloc / cudaFree may cause.
  * Working memory is one fixed 8 MiB array in device memory per GPU, held
  * until the process exits; calls with natoms * (D + 1) > 1048576 (16131 atoms
  * at D = 64) return GAPGB_ERR_CAP_EXCEEDED.  The model must already be
  * resident on the device (any evaluation uploads it; this call never does).
- * The first call on a device looks up the array's device address, so make
- * one call before capturing it in a graph.  All calls share the array: calls
- * that overlap on the GPU (other streams, other host threads) race and must
- * be serialised by the caller. */
+ * The first call on a device does a one-time set-up (the array's device
+ * address, the kernel's shared-memory limit), so make that first call before
+ * any stream capture.  All calls share the array: calls that overlap on the
+ * GPU (other streams, other host threads) race and must be serialised by the
+ * caller, and every call must have finished before gapgb_model_set_coeff
+ * rewrites the coefficients it reads. */
 gapgb_status gapgb_gpr_noalloc(gapgb_model *model, int natoms,
                                const double *d_G, double *d_e, double *d_dedg,
                                void *stream);

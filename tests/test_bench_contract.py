@@ -33,6 +33,23 @@ def test_roofline_entry_keys_and_arithmetic():
     assert "gpr_tensor" not in bench.roofline(stages, N, D, "fp32")
 
 
+def test_roofline_uses_measured_simt_peaks_and_plain_stages():
+    stages = [0.22, 0.35, 0.24, 0.52]
+    plain = [0.9, 60.0, 75.0, 35.0]
+    N, D = 38912, 64
+    simt = {"fp32_tflops": 70.0, "fp64_tflops": 1.2, "ex2_per_s_1e12": 4.5,
+            "fp32_mhz": 2000.0, "fp64_mhz": 2000.0, "ex2_mhz": 2000.0}
+    roof = bench.roofline(stages, N, D, "tc", simt=simt, plain_stages=plain)
+    c = roof["chain_rule_fp32"]
+    assert c["peak_tflops"] == 70.0 and np.isclose(c["frac"], c["achieved_tflops"] / 70.0)
+    assert np.isclose(roof["gpr_exp"]["peak_per_s"], 4.5e12)
+    pl = roof["plain_fp64"]
+    assert pl["peak_tflops"] == 1.2
+    # the plain GPR: 4 M D flops per atom over its stage time
+    assert np.isclose(pl["gpr"]["achieved_tflops"], 4.0 * bench.M_SPARSE * D * N / 75e-3 / 1e12)
+    assert np.isclose(pl["gpr"]["frac"], pl["gpr"]["achieved_tflops"] / 1.2)
+
+
 def test_default_batch_is_one_gpr_wave(monkeypatch):
     import torch
     monkeypatch.setattr(torch.cuda, "get_device_properties",

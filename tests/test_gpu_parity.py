@@ -691,7 +691,9 @@ def test_autotune_choice_within_tolerance(synth_si):
     batch = [S.si64(seed=s) for s in (71, 72, 73, 74)]
     off, sp, lat, pos = S.pack(batch)
     best = tune.autotune(g, off, sp, lat, pos, reps=2)
-    assert best["precision"] in ("tc", "fp32", "mixed")
+    # any form the tuner can return is acceptable, as long as its measured
+    # errors against the FP64 form pass the gates
+    assert best["precision"] in tune.FORMS
     assert best["dE_per_atom"] <= 1e-3 and best["dF"] <= 20e-3
     E, F, _ = g.eval_batch(off, sp, lat, pos)
     g.set_precision("fp64")
