@@ -519,7 +519,7 @@ void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
     if (!m->generic_kernels && grouped_kernels(m->sft32h, &gf, &gb)) {
       const size_t smg = kTableBytes(sizeof(SFT<float>)) +
                          (size_t)kWarpsPerBlock * 4 *
-                             grp_warp_floats(capS, m->sfh.nrc, m->sfh.D, true);
+                             grp_warp_floats(capS, m->sfh.nrc, m->sfh.D, m->sfh.nrad, true);
       kernel_smem((const void *)gf, (int)smg, true);
       const int grid = warp_grid(N, smg, (const void *)gf);
       gf<<<grid, 32 * kWarpsPerBlock, smg, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
@@ -554,7 +554,7 @@ bool launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
     if (!m->generic_kernels && grouped_kernels(m->sft32h, &gf, &gb)) {
       const size_t smg = kTableBytes(sizeof(SFT<float>)) +
                          (size_t)kWarpsPerBlock * 4 *
-                             grp_warp_floats(capS, m->sfh.nrc, m->sfh.D, false);
+                             grp_warp_floats(capS, m->sfh.nrc, m->sfh.D, m->sfh.nrad, false);
       kernel_smem((const void *)gb, (int)smg, true);
       const int grid = warp_grid(N, smg, (const void *)gb);
       cudaMemsetAsync(d_force, 0, sizeof(double) * 3 * (size_t)N, st);

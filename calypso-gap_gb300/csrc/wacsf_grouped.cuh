@@ -32,27 +32,30 @@ constexpr int kGrpMinBlocks = 6;
 //   a[q] = (dx, dy, dz, r)        b[q] = (1/r, w, fc, fc') at the angular cutoff
 //   e[q] = exp(-alpha_t r^2), t < 4
 //   fc[g][q], dfc[g][q]           cutoff function of every cutoff group g
+//   rco[s]                        (kx, rs, dE/dG_d, dE/dG_{d+nsf}) of radial SF s
+//                                 (gradient kernel)
 //   gx, gy, gz [q], dg[D]         slot gradients and dE/dG (gradient kernel)
 struct GLay {
-  float4 *a, *b, *e;
+  float4 *a, *b, *e, *rco;
   float *fc, *dfc, *gx, *gy, *gz, *dg;
 };
 
-__host__ __device__ inline size_t grp_warp_floats(int capS, int nrc, int D, bool fwd) {
+__host__ __device__ inline size_t grp_warp_floats(int capS, int nrc, int D, int nrad, bool fwd) {
   const size_t n = (size_t)12 * capS + (size_t)nrc * capS * (fwd ? 1 : 2) +
-                   (fwd ? 0 : (size_t)3 * capS + D);
+                   (fwd ? 0 : (size_t)4 * nrad + (size_t)3 * capS + D);
   return (n + 3) / 4 * 4;  // keeps every warp's records 16-byte aligned
 }
 
 __device__ __forceinline__ GLay grp_carve(unsigned char *raw, int warp, int capS, int nrc, int D,
-                                          bool fwd) {
+                                          int nrad, bool fwd) {
   float *base = reinterpret_cast<float *>(raw + kTableBytes(sizeof(SFT<float>))) +
-                grp_warp_floats(capS, nrc, D, fwd) * warp;
+                grp_warp_floats(capS, nrc, D, nrad, fwd) * warp;
   GLay L;
   L.a = reinterpret_cast<float4 *>(base);
   L.b = L.a + capS;
   L.e = L.b + capS;
-  L.fc = reinterpret_cast<float *>(L.e + capS);
+  L.rco = fwd ? nullptr : L.e + capS;  // gradient kernel: per-SF radial records
+  L.fc = reinterpret_cast<float *>(fwd ? L.e + capS : L.rco + nrad);
   L.dfc = fwd ? nullptr : L.fc + (size_t)nrc * capS;
   L.gx = fwd ? nullptr : L.dfc + (size_t)nrc * capS;
   L.gy = fwd ? nullptr : L.gx + capS;
@@ -224,21 +227,43 @@ __device__ __forceinline__ void pair_stream(const float4 *__restrict__ A, int P,
   __syncwarp();
 }
 
-// radial part shared by both grouped kernels (one SF per lane, slot order)
+constexpr float kLog2e = 1.4426950408889634f;
+constexpr float kTwoLn2 = 1.3862943611198906f;
+
+// 2^x on the MUFU pipe (the __expf form: exp(y) = ex2(y log2 e))
+__device__ __forceinline__ float ex2f(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// radial part of the forward kernel: one SF per lane over the slots in
+// order, exp(-alpha (r - rs)^2) = 2^(kx (r - rs)^2) with kx = -alpha log2 e.
+// A term beyond its cutoff has fc = 0 and adds exactly zero.  With a single
+// cutoff group the slot's fc and weight come from its packed record.
 __device__ __forceinline__ void radial_fwd(const GLay &L, const SFT<float> &sf, int P, int capS,
                                            int lane, float *Gi) {
   for (int s = lane; s < sf.nrad; s += 32) {
-    const int rr = sf.rad_rc[s];
-    const float alpha = sf.rad_alpha[s], rs = sf.rad_rs[s];
-    const float *f_ = L.fc + rr * capS;
+    const float kx = -sf.rad_alpha[s] * kLog2e, rs = sf.rad_rs[s];
     float acc = 0.f, accw = 0.f;
-    for (int q = 0; q < P; ++q) {
-      const float f = f_[q];
-      if (f == 0.f) continue;
-      const float u = L.a[q].w - rs;
-      const float v = __expf(-alpha * u * u) * f;
-      acc += v;
-      accw += v * L.b[q].y;
+    if (sf.nrc == 1) {
+#pragma unroll 4
+      for (int q = 0; q < P; ++q) {
+        const float4 bq = L.b[q];
+        const float u = L.a[q].w - rs;
+        const float v = ex2f(kx * (u * u)) * bq.z;
+        acc += v;
+        accw = fmaf(v, bq.y, accw);
+      }
+    } else {
+      const float *f_ = L.fc + sf.rad_rc[s] * capS;
+#pragma unroll 4
+      for (int q = 0; q < P; ++q) {
+        const float u = L.a[q].w - rs;
+        const float v = ex2f(kx * (u * u)) * f_[q];
+        acc += v;
+        accw = fmaf(v, L.b[q].y, accw);
+      }
     }
     const int d = sf.rad_d[s];
     Gi[d] = acc;
@@ -266,7 +291,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
   const SFT<float> &sf = *reinterpret_cast<const SFT<float> *>(smraw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nal = sf.nalpha, D = sf.D, nsf = sf.nsf, nang = sf.nang;
-  const GLay L = grp_carve(smraw, warp, capS, sf.nrc, D, true);
+  const GLay L = grp_carve(smraw, warp, capS, sf.nrc, D, sf.nrad, true);
   const int rci = nang > 0 ? sf.ang_grp_rc[0] : 0;
   const float rc = sf.rc_val[rci], pirc = sf.pi_over_rc[rci];
   float alv[NAL], clam[NC];
@@ -374,6 +399,129 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
   }
 }
 
+// dE/dG of one atom contracted onto the (alpha, combination) grid,
+//   P_q(cos) = sum_c (UA_qc + w_j w_k UB_qc) A_c(cos),
+// UA / UB the unweighted and weighted copies (2^(1-zeta) included).  For the
+// standard set (A_c = (1 +- cos)^{1,2,4}) P_q is a degree-4 polynomial in
+// cos: its coefficients are formed once per atom and a pair evaluates P_q
+// and P_q' by one Horner pass; other sets combine the powers A_c directly.
+template <int NAL, int NC, bool STD>
+struct AngCoef {
+  static constexpr bool kPoly = STD && NC == 6;
+  float U[2][NAL][kPoly ? 5 : NC];  // [weighting][alpha][coefficient or combination]
+
+  __device__ __forceinline__ void load(const float *su) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+      for (int q = 0; q < NAL; ++q) {
+        const float *u = su + h * NAL * NC + q * NC;
+        if constexpr (kPoly) {
+          // (1+x), (1-x), (1+x)^2, (1-x)^2, (1+x)^4, (1-x)^4 expanded in x
+          U[h][q][0] = u[0] + u[1] + u[2] + u[3] + u[4] + u[5];
+          U[h][q][1] = (u[0] - u[1]) + 2.f * (u[2] - u[3]) + 4.f * (u[4] - u[5]);
+          U[h][q][2] = (u[2] + u[3]) + 6.f * (u[4] + u[5]);
+          U[h][q][3] = 4.f * (u[4] - u[5]);
+          U[h][q][4] = u[4] + u[5];
+        } else {
+#pragma unroll
+          for (int c = 0; c < NC; ++c) U[h][q][c] = u[c];
+        }
+      }
+  }
+
+  // P_q(cos) and dP_q/dcos for every alpha q
+  __device__ __forceinline__ void eval(float x, float wjk, const float (&clam)[NC],
+                                       const int (&ciz)[NC], float (&Pv)[NAL],
+                                       float (&Pd)[NAL]) const {
+    if constexpr (kPoly) {
+      (void)clam;
+      (void)ciz;
+#pragma unroll
+      for (int q = 0; q < NAL; ++q) {
+        float c[5];
+#pragma unroll
+        for (int m = 0; m < 5; ++m) c[m] = fmaf(wjk, U[1][q][m], U[0][q][m]);
+        float p = fmaf(c[4], x, c[3]), d = c[4];
+        d = fmaf(d, x, p);
+        p = fmaf(p, x, c[2]);
+        d = fmaf(d, x, p);
+        p = fmaf(p, x, c[1]);
+        d = fmaf(d, x, p);
+        p = fmaf(p, x, c[0]);
+        Pv[q] = p;
+        Pd[q] = d;
+      }
+    } else {
+      float A[NC], dAl[NC];
+      ang_powers<NC, STD>(x, clam, ciz, A, dAl);
+#pragma unroll
+      for (int q = 0; q < NAL; ++q) {
+        float sp = 0.f, sq = 0.f;
+#pragma unroll
+        for (int cc = 0; cc < NC; ++cc) {
+          const float V = U[0][q][cc] + wjk * U[1][q][cc];
+          sp += dAl[cc] * V;
+          sq += A[cc] * V;
+        }
+        Pv[q] = sq;
+        Pd[q] = sp;
+      }
+    }
+  }
+};
+
+// Gradient of one angular pair's contribution sum_s dE/dG_s G_s(j, k) with
+// respect to the positions of slots j and k: vj and vk.
+template <int NAL, int NC, bool STD>
+__device__ __forceinline__ void pair_grad(const GLay &L, int j, int k, float pirc, int nal,
+                                          const float (&alv)[NAL], const float (&clam)[NC],
+                                          const int (&ciz)[NC], const AngCoef<NAL, NC, STD> &U,
+                                          float3 &vj, float3 &vk) {
+  const float4 Aj = L.a[j], Ak = L.a[k], Bj = L.b[j], Bk = L.b[k];
+  const float4 Ej = L.e[j], Ek = L.e[k];
+  const float cx = Aj.x - Ak.x, cy = Aj.y - Ak.y, cz = Aj.z - Ak.z;
+  const float c2 = cx * cx + cy * cy + cz * cz;
+  const float a = Aj.w, b = Ak.w;
+  const float ic = c2 > 0.f ? rsqrtf(c2) : 0.f, c = c2 * ic;
+  const float ia = Bj.x, ib = Bk.x;
+  const float cosv = (a * a + b * b - c2) * 0.5f * ia * ib;
+  const float dcda = ib - cosv * ia, dcdb = ia - cosv * ib, dcdc = -c * ia * ib;
+  float sn, cs;
+  __sincosf(pirc * c, &sn, &cs);
+  const float fcc = 0.5f * (cs + 1.f), dfcc = -0.5f * sn * pirc;
+  const float fa = Bj.z, fb = Bk.z, dfa = Bj.w, dfb = Bk.w;
+  const float F = fa * fb * fcc;
+  float Pv[NAL], Pd[NAL];
+  U.eval(cosv, Bj.y * Bk.y, clam, ciz, Pv, Pd);
+  float SP = 0.f, SQ = 0.f, SU = 0.f;
+#pragma unroll
+  for (int q = 0; q < NAL; ++q) {
+    const float E = q < nal ? f4get(Ej, q) * f4get(Ek, q) * __expf(-alv[q] * c2) : 0.f;
+    SP += E * Pd[q];
+    SQ += E * Pv[q];
+    SU += alv[q] * E * Pv[q];
+  }
+  // dG/da = E [A' dcos/da F + A (-2 alpha a F + fc'(a) fc(b) fc(c))], etc.
+  const float S1 = F * (SP * dcda - 2.f * SU * a) + SQ * (dfa * fb * fcc);
+  const float S2 = F * (SP * dcdb - 2.f * SU * b) + SQ * (fa * dfb * fcc);
+  const float S3 = F * (SP * dcdc - 2.f * SU * c) + SQ * (fa * fb * dfcc);
+  const float s1 = S1 * ia, s2 = S2 * ib, s3 = S3 * ic;
+  vj = make_float3(s1 * Aj.x + s3 * cx, s1 * Aj.y + s3 * cy, s1 * Aj.z + s3 * cz);
+  vk = make_float3(s2 * Ak.x - s3 * cx, s2 * Ak.y - s3 * cy, s2 * Ak.z - s3 * cz);
+}
+
+// Slot gradients g_q = sum_d dE/dG_id dG_id/dp_q of each atom, the force
+// scatter and the per-atom virial.
+//  - radial terms: lanes own slots; per SF one broadcast record
+//    (kx, rs, dE/dG_d, dE/dG_{d+nsf}) staged per atom;
+//  - angular pairs: the pair list the forward kernel recorded is split into
+//    32 contiguous chunks, one per lane.  The list is j-major, so a lane's
+//    consecutive pairs share slot j: its j-side gradient stays in registers
+//    and is added to shared memory only when j changes (a few times per
+//    atom); the k side is added per pair by shared-memory atomics.  Atoms
+//    whose list overflowed re-enumerate their pairs (pair_stream) and sum
+//    the j side by a segmented warp scan.
 template <int NAL, int NC, bool STD>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
     k_wacsf_bwd_grp(int N, int cap, int capS, const int *__restrict__ cnt,
@@ -393,7 +541,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
   const SFT<float> &sf = *reinterpret_cast<const SFT<float> *>(smraw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nal = sf.nalpha, D = sf.D, nsf = sf.nsf, nrad = sf.nrad, nang = sf.nang;
-  const GLay L = grp_carve(smraw, warp, capS, sf.nrc, D, false);
+  const GLay L = grp_carve(smraw, warp, capS, sf.nrc, D, nrad, false);
   const int rci = nang > 0 ? sf.ang_grp_rc[0] : 0;
   const float rc = sf.rc_val[rci], pirc = sf.pi_over_rc[rci];
   float alv[NAL], clam[NC];
@@ -409,22 +557,47 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
     const int P = grp_stage(L, sf, i, cap, capS, lane, rci, cnt, d32, w32, true);
     for (int d = lane; d < D; d += 32) L.dg[d] = dedg[(size_t)i * D + d];
     for (int q = lane; q < P; q += 32) L.gx[q] = L.gy[q] = L.gz[q] = 0.f;
-    if (lane < 2 * NAL * NC) s_u[warp][lane] = 0.f;
+    for (int e = lane; e < 2 * NAL * NC; e += 32) s_u[warp][e] = 0.f;
     __syncwarp();
-    // radial terms: lanes own slots
+    // per-atom radial records: (kx, rs, dE/dG_d, dE/dG_{d+nsf})
+    for (int s = lane; s < nrad; s += 32) {
+      const int d = sf.rad_d[s];
+      L.rco[s] = make_float4(-sf.rad_alpha[s] * kLog2e, sf.rad_rs[s], L.dg[d], L.dg[d + nsf]);
+    }
+    // dE/dG contracted onto the (alpha, combination) grid: one SF per lane
+    for (int s = lane; s < nang; s += 32) {
+      const int cell = ((sf.ang_code[s] >> 8) & 255) * NC + sf.ang_comb[s];
+      const int d = sf.ang_d[s];
+      atomicAdd(&s_u[warp][cell], sf.ang_pref[s] * L.dg[d]);
+      atomicAdd(&s_u[warp][NAL * NC + cell], sf.ang_pref[s] * L.dg[d + nsf]);
+    }
+    __syncwarp();
+    // radial terms: lanes own slots.  d/dr [ex fc] = ex (fc' - 2 alpha u fc),
+    // -2 alpha = 2 ln2 kx
     for (int q = lane; q < P; q += 32) {
-      const float4 aq = L.a[q];
-      const float r = aq.w, w = L.b[q].y;
+      const float4 aq = L.a[q], bq = L.b[q];
+      const float r = aq.w, w = bq.y;
       float S = 0.f;
-      for (int s = 0; s < nrad; ++s) {
-        const int rr = sf.rad_rc[s];
-        if (r > sf.rc_val[rr]) continue;
-        const float f = L.fc[rr * capS + q], df = L.dfc[rr * capS + q];
-        const float alpha = sf.rad_alpha[s];
-        const float u = r - sf.rad_rs[s];
-        const float ex = __expf(-alpha * u * u);
-        const int d = sf.rad_d[s];
-        S += (L.dg[d] + L.dg[d + nsf] * w) * (-2.f * alpha * u * ex * f + ex * df);
+      if (sf.nrc == 1) {
+        const float f = bq.z, df = bq.w;
+#pragma unroll 4
+        for (int s = 0; s < nrad; ++s) {
+          const float4 c = L.rco[s];
+          const float u = r - c.y;
+          const float ex = ex2f(c.x * (u * u));
+          const float t = fmaf(c.x * kTwoLn2 * u, f, df);
+          S = fmaf(fmaf(c.w, w, c.z) * ex, t, S);
+        }
+      } else {
+        for (int s = 0; s < nrad; ++s) {
+          const float4 c = L.rco[s];
+          const int rr = sf.rad_rc[s];
+          const float f = L.fc[rr * capS + q], df = L.dfc[rr * capS + q];
+          const float u = r - c.y;
+          const float ex = ex2f(c.x * (u * u));
+          const float t = fmaf(c.x * kTwoLn2 * u, f, df);
+          S = fmaf(fmaf(c.w, w, c.z) * ex, t, S);
+        }
       }
       const float ir = S / r;
       L.gx[q] += ir * aq.x;
@@ -432,105 +605,79 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
       L.gz[q] += ir * aq.z;
     }
     if (nang > 0) {
-      // dE/dG contracted onto the (alpha, combination) grid (one lane, fixed order)
-      if (lane == 0)
-        for (int s = 0; s < nang; ++s) {
-          const int cell = ((sf.ang_code[s] >> 8) & 255) * NC + sf.ang_comb[s];
-          const int d = sf.ang_d[s];
-          s_u[warp][cell] += sf.ang_pref[s] * L.dg[d];
-          s_u[warp][NAL * NC + cell] += sf.ang_pref[s] * L.dg[d + nsf];
-        }
-      __syncwarp();
-      float UA[NAL][NC], UB[NAL][NC];
-#pragma unroll
-      for (int q = 0; q < NAL; ++q)
-#pragma unroll
-        for (int c = 0; c < NC; ++c) {
-          UA[q][c] = s_u[warp][q * NC + c];
-          UB[q][c] = s_u[warp][NAL * NC + q * NC + c];
-        }
-      auto work = [&](int j, int k, float c2, bool ok) {
-        const float4 Aj = L.a[j], Ak = L.a[k], Bj = L.b[j], Bk = L.b[k];
-        const float4 Ej = L.e[j], Ek = L.e[k];
-        const float a = Aj.w, b = Ak.w;
-        const float ic = c2 > 0.f ? rsqrtf(c2) : 0.f, c = c2 * ic;
-        const float ia = Bj.x, ib = Bk.x;
-        const float cosv = (a * a + b * b - c2) * 0.5f * ia * ib;
-        const float dcda = ib - cosv * ia, dcdb = ia - cosv * ib, dcdc = -c * ia * ib;
-        float sn, cs;
-        __sincosf(pirc * c, &sn, &cs);
-        const float fcc = 0.5f * (cs + 1.f), dfcc = -0.5f * sn * pirc;
-        const float fa = Bj.z, fb = Bk.z, dfa = Bj.w, dfb = Bk.w;
-        const float F = fa * fb * fcc;
-        const float wjk = Bj.y * Bk.y;
-        float A[NC], dAl[NC];
-        ang_powers<NC, STD>(cosv, clam, ciz, A, dAl);
-        float SP = 0.f, SQ = 0.f, SU = 0.f;
-#pragma unroll
-        for (int q = 0; q < NAL; ++q) {
-          const float E = q < nal ? f4get(Ej, q) * f4get(Ek, q) * __expf(-alv[q] * c2) : 0.f;
-          float sp = 0.f, sq = 0.f;
-#pragma unroll
-          for (int cc = 0; cc < NC; ++cc) {
-            const float V = UA[q][cc] + wjk * UB[q][cc];
-            sp += dAl[cc] * V;
-            sq += A[cc] * V;
-          }
-          SP += E * sp;
-          SQ += E * sq;
-          SU += alv[q] * E * sq;
-        }
-        // dG/da = E [A' dcos/da F + A (-2 alpha a F + fc'(a) fc(b) fc(c))], etc.
-        const float S1 = F * (SP * dcda - 2.f * SU * a) + SQ * (dfa * fb * fcc);
-        const float S2 = F * (SP * dcdb - 2.f * SU * b) + SQ * (fa * dfb * fcc);
-        const float S3 = F * (SP * dcdc - 2.f * SU * c) + SQ * (fa * fb * dfcc);
-        const float s1 = S1 * ia, s2 = S2 * ib, s3 = S3 * ic;
-        const float cx = Aj.x - Ak.x, cy = Aj.y - Ak.y, cz = Aj.z - Ak.z;
-        float vx = ok ? s1 * Aj.x + s3 * cx : 0.f;
-        float vy = ok ? s1 * Aj.y + s3 * cy : 0.f;
-        float vz = ok ? s1 * Aj.z + s3 * cz : 0.f;
-        // slot j: the batch's pairs share few j values (enumeration order),
-        // so each run of equal j (contiguous lanes) is summed by a
-        // segmented scan and its last lane adds it: one atomic per run
-        const unsigned run = __match_any_sync(0xffffffffu, ok ? j : 0x10000 + lane);
-        const int first = __ffs(run) - 1, last = 31 - __clz(run);
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const float tx = __shfl_up_sync(0xffffffffu, vx, o);
-          const float ty = __shfl_up_sync(0xffffffffu, vy, o);
-          const float tz = __shfl_up_sync(0xffffffffu, vz, o);
-          if (lane - o >= first) {
-            vx += tx;
-            vy += ty;
-            vz += tz;
-          }
-        }
-        if (ok && lane == last) {
-          atomicAdd(&L.gx[j], vx);
-          atomicAdd(&L.gy[j], vy);
-          atomicAdd(&L.gz[j], vz);
-        }
-        if (ok) {
-          atomicAdd(&L.gx[k], s2 * Ak.x - s3 * cx);
-          atomicAdd(&L.gy[k], s2 * Ak.y - s3 * cy);
-          atomicAdd(&L.gz[k], s2 * Ak.z - s3 * cz);
-        }
-      };
+      AngCoef<NAL, NC, STD> U;
+      U.load(s_u[warp]);
       const int np = pcap > 0 ? pcount[i] : -1;
       if (np >= 0 && np <= pcap) {
-        // the pairs the descriptor kernel found, in its order
+        // the pairs the descriptor kernel found: lane-contiguous chunks
         const unsigned short *prow = pairs + (size_t)i * pcap;
-        for (int base = 0; base < np; base += 32) {
-          const int t = base + lane;
-          const bool ok = t < np;
-          const int jk = ok ? (int)prow[t] : (1 << 8);
-          const int j = jk & 0xff, k = jk >> 8;
-          const float4 aj = L.a[j], ak = L.a[k];
-          const float cx = aj.x - ak.x, cy = aj.y - ak.y, cz = aj.z - ak.z;
-          work(j, k, ok ? cx * cx + cy * cy + cz * cz : 1.f, ok);
+        const int C = (np + 31) >> 5;
+        const int p0 = lane * C, pe = min(np, p0 + C);
+        int nxt = p0 < pe ? (int)prow[p0] : 0;
+        int cur = -1;
+        float gjx = 0.f, gjy = 0.f, gjz = 0.f;
+        for (int t = 0; t < C; ++t) {
+          const int p = p0 + t;
+          const int jk = nxt;
+          if (p + 1 < pe) nxt = (int)prow[p + 1];  // next pair's entry, loaded ahead
+          if (p < pe) {
+            const int j = jk & 0xff, k = jk >> 8;
+            float3 vj, vk;
+            pair_grad<NAL, NC, STD>(L, j, k, pirc, nal, alv, clam, ciz, U, vj, vk);
+            if (j != cur) {
+              if (cur >= 0) {
+                atomicAdd(&L.gx[cur], gjx);
+                atomicAdd(&L.gy[cur], gjy);
+                atomicAdd(&L.gz[cur], gjz);
+              }
+              cur = j;
+              gjx = gjy = gjz = 0.f;
+            }
+            gjx += vj.x;
+            gjy += vj.y;
+            gjz += vj.z;
+            atomicAdd(&L.gx[k], vk.x);
+            atomicAdd(&L.gy[k], vk.y);
+            atomicAdd(&L.gz[k], vk.z);
+          }
+        }
+        if (cur >= 0) {
+          atomicAdd(&L.gx[cur], gjx);
+          atomicAdd(&L.gy[cur], gjy);
+          atomicAdd(&L.gz[cur], gjz);
         }
       } else if (P > 1) {
-        pair_stream(L.a, P, rc, lane, s_qjk[warp], s_qc2[warp], work);
+        pair_stream(L.a, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
+          (void)c2;
+          float3 vj, vk;
+          pair_grad<NAL, NC, STD>(L, j, k, pirc, nal, alv, clam, ciz, U, vj, vk);
+          float vx = ok ? vj.x : 0.f, vy = ok ? vj.y : 0.f, vz = ok ? vj.z : 0.f;
+          // slot j: equal j values are contiguous lanes of the batch, summed
+          // by a segmented scan whose last lane adds the run
+          const unsigned run = __match_any_sync(0xffffffffu, ok ? j : 0x10000 + lane);
+          const int first = __ffs(run) - 1, last = 31 - __clz(run);
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const float tx = __shfl_up_sync(0xffffffffu, vx, o);
+            const float ty = __shfl_up_sync(0xffffffffu, vy, o);
+            const float tz = __shfl_up_sync(0xffffffffu, vz, o);
+            if (lane - o >= first) {
+              vx += tx;
+              vy += ty;
+              vz += tz;
+            }
+          }
+          if (ok && lane == last) {
+            atomicAdd(&L.gx[j], vx);
+            atomicAdd(&L.gy[j], vy);
+            atomicAdd(&L.gz[j], vz);
+          }
+          if (ok) {
+            atomicAdd(&L.gx[k], vk.x);
+            atomicAdd(&L.gy[k], vk.y);
+            atomicAdd(&L.gz[k], vk.z);
+          }
+        });
       }
     }
     __syncwarp();

@@ -135,11 +135,10 @@ def _i32(a):
 
 def measure_peaks():
     """Measured FP32 / FP64 FMA rates (TFLOP/s) and MUFU ex2 rate (1e12/s)
-    of the current device, with the SM clock (MHz) each kernel ran at."""
-    out = (C.c_double * 6)()
+    of the current device."""
+    out = (C.c_double * 3)()
     _check(load().gapgb_measure_peaks(out), "gapgb_measure_peaks")
-    return {"fp32_tflops": out[0], "fp64_tflops": out[1], "ex2_per_s_1e12": out[2],
-            "fp32_mhz": out[3], "fp64_mhz": out[4], "ex2_mhz": out[5]}
+    return {"fp32_tflops": out[0], "fp64_tflops": out[1], "ex2_per_s_1e12": out[2]}
 
 
 class GapModel:

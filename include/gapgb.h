@@ -270,11 +270,10 @@ gapgb_status gapgb_stage_times(gapgb_model *model, float t[4]);
 /* Measured arithmetic peaks of the current device, the roofline denominators
  * of the SIMT kernels (no counterpart in the reference, which has no device
  * code): out[0] FP32 FMA TFLOP/s, out[1] FP64 FMA TFLOP/s (an FMA = 2 flops),
- * out[2] MUFU ex2 rate in 1e12 per second; out[3..5] the SM clock (MHz) each
- * of the three kernels ran at.  Each is one kernel of independent FMA / ex2
- * chains on every SM, timed by CUDA events after a warm-up launch (about
- * 0.1 s in all). */
-gapgb_status gapgb_measure_peaks(double out[6]);
+ * out[2] MUFU ex2 rate in 1e12 per second.  Each is one kernel of
+ * independent FMA / ex2 chains on every SM (one resident wave), timed by
+ * CUDA events after a warm-up launch (well under a second in all). */
+gapgb_status gapgb_measure_peaks(double out[3]);
 
 /* ---- GPR step without device allocation ---------------------------------- */
 

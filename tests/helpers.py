@@ -50,3 +50,15 @@ def synth_model_file(path, oracle, structs, M, theta_scale=1.0, coeff_std=1e-3, 
     os.remove(tmp)
     theta, mm, coeff = S.model_arrays(np.concatenate(X), M, theta_scale, coeff_std, seed)
     return write_model_file(path, sz, sw, ty, al, rc, theta, mm, coeff, ze)
+
+
+def three_species_cell(seed):
+    """2x2x2 fcc cell (a = 3.9 A) of Z 13/28/40, jittered."""
+    rng = np.random.default_rng(seed)
+    basis = np.array([[0, 0, 0], [0, .5, .5], [.5, 0, .5], [.5, .5, 0]])
+    g = np.stack(np.meshgrid(np.arange(2), np.arange(2), np.arange(2), indexing="ij"), -1)
+    frac = (g.reshape(-1, 1, 3) + basis[None]).reshape(-1, 3)
+    lat = np.diag([7.8, 7.8, 7.8]) + rng.normal(0.0, 0.05, (3, 3))
+    pos = (frac / 2.0) @ lat + rng.normal(0.0, 0.08, (len(frac), 3))
+    z = np.array([13, 28, 40], np.int32)[rng.permutation(np.arange(len(frac)) % 3)]
+    return lat, pos, z

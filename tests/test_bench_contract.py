@@ -37,8 +37,7 @@ def test_roofline_uses_measured_simt_peaks_and_plain_stages():
     stages = [0.22, 0.35, 0.24, 0.52]
     plain = [0.9, 60.0, 75.0, 35.0]
     N, D = 38912, 64
-    simt = {"fp32_tflops": 70.0, "fp64_tflops": 1.2, "ex2_per_s_1e12": 4.5,
-            "fp32_mhz": 2000.0, "fp64_mhz": 2000.0, "ex2_mhz": 2000.0}
+    simt = {"fp32_tflops": 70.0, "fp64_tflops": 1.2, "ex2_per_s_1e12": 4.5}
     roof = bench.roofline(stages, N, D, "tc", simt=simt, plain_stages=plain)
     c = roof["chain_rule_fp32"]
     assert c["peak_tflops"] == 70.0 and np.isclose(c["frac"], c["achieved_tflops"] / 70.0)

@@ -109,3 +109,36 @@ def test_zeta_extension_matches_finite_difference(oracle_mod, tmp_path):
         e1 = oracle_mod.gap_calc(m, z, lat, p1, 6.0, False)[0]
         e2 = oracle_mod.gap_calc(m, z, lat, p2, 6.0, False)[0]
         assert abs(-(e1 - e2) / (2 * h) - F[atom, c]) < 1e-5 * max(1.0, abs(F[atom, c]))
+
+
+def test_three_species_weighting_matches_finite_difference(oracle_mod, tmp_path):
+    """Species-weighted copies (wacsf.f90:86-87, 326-328) with three species:
+    the oracle's forces equal -dE/dr and its stress -(1/V) dE/d(strain), on a
+    jittered 3-species fcc cell (no reference fixture covers mixed weights)."""
+    from helpers import synth_model_file, three_species_cell as _three_species_cell
+    path = synth_model_file(str(tmp_path / "gp"), oracle_mod,
+                            [_three_species_cell(s) for s in range(4)], M=60, theta_scale=1.0,
+                            coeff_std=0.1, seed=9)
+    m = oracle_mod.Model(path)
+    assert sorted(m.species_z.tolist()) == [13, 28, 40]
+    lat, pos, z = _three_species_cell(11)
+    _, F, S, _ = oracle_mod.gap_calc(m, z, lat, pos, 6.0, True)
+    h = 1e-5
+    for atom, c in [(0, 0), (5, 1), (17, 2), (30, 0)]:
+        p1, p2 = pos.copy(), pos.copy()
+        p1[atom, c] += h
+        p2[atom, c] -= h
+        e1 = oracle_mod.gap_calc(m, z, lat, p1, 6.0, False)[0]
+        e2 = oracle_mod.gap_calc(m, z, lat, p2, 6.0, False)[0]
+        assert abs(-(e1 - e2) / (2 * h) - F[atom, c]) < 1e-5 * max(1.0, abs(F[atom, c]))
+    V = abs(np.linalg.det(lat))
+    hs = 1e-6
+    for q, (a, b) in enumerate([(0, 0), (1, 1), (2, 2), (0, 1), (1, 2), (0, 2)]):
+        es = []
+        for sgn in (1, -1):
+            eps = np.eye(3)
+            eps[a, b] += sgn * hs / (1 if a == b else 2)
+            eps[b, a] += 0 if a == b else sgn * hs / 2
+            es.append(oracle_mod.gap_calc(m, z, lat @ eps, pos @ eps, 6.0, False)[0])
+        dEde = (es[0] - es[1]) / (2 * hs)
+        assert abs(-dEde / V / 6.24219e-3 - S[q]) < 1e-4 * max(1.0, abs(S[q]))
