@@ -279,6 +279,83 @@ def cpu_baseline(arrays):
             "latency_sample": "one alloy512 structure (E, F, stress) on one host thread"}
 
 
+def dropin_latency(reps=30):
+    """Latency of one evaluation as the reference is used: one structure per
+    ASE call (gappy/ASE/gap_calc.py:29-52, gappy/example/ASE-GAPPY/run_md.py:
+    10-21).  The reference's own example model and the first frame of its MD
+    trajectory (64-atom C diamond, committed under tests/golden), plain FP64
+    path, median milliseconds per call after two warm-up calls:
+      ase_calculate    ase_gap.GAP.calculate (a new libgap Calculator per
+                       call, as the reference builds one; the file is read
+                       and the device model reused while it is unchanged)
+      libgap_gap_calc  libgap.GAP.Calculator.gap_calc
+      c_abi_eval       gapgb_eval with host buffers
+    and beside them the oracle (the CPU restatement of FGAP_CALC) on one host
+    core on the same frame.  first_call_ms is the first ASE call of the
+    process (model upload, workspace allocation)."""
+    import shutil
+    import tempfile
+    import gapgb
+    from oracle import oracle
+    golden = os.path.join(ROOT, "tests", "golden")
+    fr = np.load(os.path.join(golden, "ase_traj_frames.npz"))
+    z, lat, pos = fr["numbers"][0], fr["cell"][0], fr["positions"][0]
+
+    class Atoms:  # the part of ase.Atoms the calculator reads
+        def __init__(self, z, cell, pos):
+            self.numbers, self.cell, self.positions = z, cell, pos
+
+        def get_atomic_numbers(self):
+            return self.numbers
+
+        def copy(self):
+            return Atoms(self.numbers.copy(), self.cell.copy(), self.positions.copy())
+
+    def median_ms(fn, n):
+        ts = []
+        for _ in range(n):
+            t0 = time.perf_counter()
+            fn()
+            ts.append((time.perf_counter() - t0) * 1e3)
+        return float(np.median(ts))
+
+    cwd = os.getcwd()
+    d = tempfile.mkdtemp()
+    try:
+        shutil.copy(os.path.join(golden, "gap_parameters_c_diamond"),
+                    os.path.join(d, "gap_parameters"))
+        os.chdir(d)
+        from ase_gap.gap_calc import GAP
+        from libgap.GAP import Calculator
+        atoms = Atoms(z, lat, pos)
+        calc = GAP(rcut=6.0)
+        t0 = time.perf_counter()
+        calc.calculate(atoms, ["energy", "forces", "stress"])
+        first = (time.perf_counter() - t0) * 1e3
+        out = {"first_call_ms": first}
+        for _ in range(2):
+            calc.calculate(atoms, ["energy", "forces", "stress"])
+        out["ase_calculate"] = median_ms(
+            lambda: calc.calculate(atoms, ["energy", "forces", "stress"]), reps)
+        c = Calculator(rcut=6.0)
+        c.gap_calc(z, lat, pos, True)
+        out["libgap_gap_calc"] = median_ms(lambda: c.gap_calc(z, lat, pos, True), reps)
+        m = gapgb.GapModel.load("gap_parameters")
+        m.eval(z, lat, pos)
+        m.eval(z, lat, pos)
+        out["c_abi_eval"] = median_ms(lambda: m.eval(z, lat, pos), reps)
+        m.close()
+        oracle.build()
+        om = oracle.Model("gap_parameters")
+        out["oracle_1core"] = median_ms(lambda: oracle.gap_calc(om, z, lat, pos, 6.0, True), 3)
+    finally:
+        os.chdir(cwd)
+        shutil.rmtree(d, ignore_errors=True)
+    out["sample"] = ("reference example model (M = 129, D = 66), ase.traj frame 0: 64 C "
+                     "atoms, 158 neighbours per atom; E, F and stress per call")
+    return out
+
+
 STAGES = ["neighbours", "descriptors", "gpr", "chain_rule"]
 # algorithmic HBM bytes per atom of each stage's kernels (P = 56 neighbour
 # slots per atom on this workload, D = 64, FP32 slot records):
@@ -330,8 +407,9 @@ def roofline(stages, N, D, precision, simt=None, plain_stages=None):
     roof = {"kernel": name, "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"],
             "unit": "GB/s", "frac": ach / peaks["hbm_gbs"], "traffic": traffic,
             "peak_source": src + " hbm_gbs",
-            "note": "descriptor-side kernels are FP32-pipe bound; fp32 gives their "
-                    "arithmetic rate against the nominal FP32 peak",
+            "note": "descriptor-side kernels are FP32-pipe bound; descriptors_fp32 and "
+                    "chain_rule_fp32 give their arithmetic rate against the measured FP32 "
+                    "FMA rate",
             "stage_ms": {n: float(s) for n, s in zip(STAGES, stages)},
             "algorithmic_bytes_per_atom": bpa[name]}
     # FP32 arithmetic of the chain-rule / descriptor kernels (counted FLOPs per
@@ -354,8 +432,8 @@ def roofline(stages, N, D, precision, simt=None, plain_stages=None):
                               "flops": "12 N M 64 (bf16 MMA, padded to 128)"}
     roof["gpr_algorithmic_tflops"] = 4.0 * m * D * N / (stages[2] * 1e-3) / 1e12
     roof["fp32_nominal_tflops"] = nominal_fp32
-    # the GPR's exp rate (one per atom and sparse point) against the nominal
-    # MUFU rate (16 per SM per clock)
+    # the GPR's exp rate (one per atom and sparse point) against the measured
+    # MUFU ex2 rate (fallback: 16 per SM per clock)
     exps = N * m / (stages[2] * 1e-3)
     mufu = simt["ex2_per_s_1e12"] * 1e12 if simt else 152 * 16 * 2.07e9
     roof["gpr_exp"] = {"per_s": exps, "peak_per_s": mufu, "frac": exps / mufu,
@@ -1147,6 +1225,21 @@ def main():
     ms_step, clocks = time_device(chosen, args.steps, args.warmup, sampler=(rank == 0))
     value = world * N / (ms_step * 1e-3)
     res_chosen = (d_E.cpu().numpy().copy(), d_F.cpu().numpy().copy(), d_S.cpu().numpy().copy())
+    gather = None
+    if world > 1:
+        # every structure's (E, F, stress) to rank 0: the job's only data
+        # exchange, after the timed steps (the shards are the ranks' seed blocks)
+        from gapgb import shard
+        g_off = np.arange(world * S + 1, dtype=np.int64) * ATOMS
+        shards = [np.arange(r * S, (r + 1) * S) for r in range(world)]
+        barrier()
+        t0 = time.perf_counter()
+        got = shard.gather_results(d_E, d_F, d_S, g_off, shards, rank, device=dev)
+        gather = {"ms": (time.perf_counter() - t0) * 1e3,
+                  "bytes_per_rank": int(S * 7 * 8 + N * 3 * 8), "backend": "nccl all_gather"}
+        if rank == 0:
+            assert np.array_equal(got[0][:S], res_chosen[0])
+            assert np.array_equal(got[1][:N], res_chosen[1])
 
     # per-stage device times (library CUDA events on the launch stream)
     os.environ["GAPGB_PROFILE_STAGES"] = "1"
@@ -1239,6 +1332,8 @@ def main():
         "gpu_launches": None,
         "clocks": clocks,
     }
+    if gather is not None:
+        line["gather_to_rank0"] = gather
     # kernels launched per step (count from the library's launch sequence):
     # prep x2, neighbour build, descriptors, GPR (tensor-core form: operand
     # prep + kernel; SIMT forms: kernel + split reduce), slot gradients (the
@@ -1246,6 +1341,7 @@ def main():
     line["gpu_launches"] = args.steps * 9
     if world == 1:
         line["cpu_baseline"] = cpu_baseline(arrays)
+        line["dropin_latency_ms"] = dropin_latency()
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

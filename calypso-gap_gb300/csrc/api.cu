@@ -389,12 +389,15 @@ gapgb_status eval_host(gapgb_model *m, int S, const int *atom_off, const int *sp
   GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_lat, lat, sizeof(double) * 9 * S, cudaMemcpyHostToDevice, s));
   GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_pos, pos, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s));
   const int maxa = max_struct_atoms(S, atom_off);
-  if (!d_G_out && m->caps_hint > 0 && m->caps_hint <= m->cap) {
-    // one synchronisation: the descriptor kernels take the slot count of the
-    // previous call; the neighbour kernel reports the true maximum, and a
-    // batch that needs more slots (or overflows the capacity) is recomputed
-    // by the general path below
-    const int cap = m->cap, capS = m->caps_hint;
+  // the slot count the descriptor kernels are sized for: the previous call's
+  // maximum, or on a model's first call the whole capacity (a bound on any
+  // count that does not overflow it), so the first call also synchronises once
+  const int caps_guess = m->caps_hint > 0 ? m->caps_hint : (m->cap <= 256 ? m->cap : 0);
+  if (!d_G_out && caps_guess > 0 && caps_guess <= m->cap) {
+    // one synchronisation: the descriptor kernels take that slot count; the
+    // neighbour kernel reports the true maximum, and a batch that needs more
+    // slots (or overflows the capacity) is recomputed by the general path below
+    const int cap = m->cap, capS = caps_guess;
     if (m->precision == GAPGB_PREC_SURROGATE) {
       st = ensure_surrogate(m, N);
       if (st) return st;

@@ -31,6 +31,9 @@ _NSPARSE_MAX = 4000  # gap_calc.f90:307
 _MODEL_FILE = "gap_parameters"
 
 _cache = {"key": None, "model": None, "arrays": None}
+# fgap_read's parse of the file, reused while the file is unchanged (same
+# path, size and modification time); every call still returns fresh arrays
+_read_cache = {"key": None, "arrays": None}
 
 
 def _file_key():
@@ -44,11 +47,15 @@ def _file_key():
 
 def fgap_read():
     key = _file_key()
-    m = gapgb.GapModel.load(key[0])
-    try:
-        th, mm, co = m.arrays()
-    finally:
-        m.close()
+    if _read_cache["key"] == key:
+        th, mm, co = _read_cache["arrays"]
+    else:
+        m = gapgb.GapModel.load(key[0])
+        try:
+            th, mm, co = m.arrays()
+        finally:
+            m.close()
+        _read_cache.update(key=key, arrays=(th, mm, co))
     M, D = mm.shape
     nsf = max(_NSF_MAX, D)
     nsp = max(_NSPARSE_MAX, M)
