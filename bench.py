@@ -49,7 +49,7 @@ def parse():
     p.add_argument("--batch", type=int, default=None,
                    help="structures per step per GPU (default: one full wave of the tensor-core "
                         "GPR, two 128-atom CTAs per SM: 76 alloy512 cells on 152 SMs)")
-    p.add_argument("--precision", default="tc", choices=["fp32", "tc", "fp64", "mixed"])
+    p.add_argument("--precision", default="tc", choices=["fp32", "tc", "tf32", "fp64", "mixed"])
     p.add_argument("--no-oracle", action="store_true", help="skip the oracle error check")
     p.add_argument("--workload", default="alloy", choices=["alloy", "population", "surrogate", "md", "precision",
                                              "variance", "fit"],
@@ -74,6 +74,13 @@ def parse():
                    help="md workload: diamond cells per axis (16: 32768 atoms; smaller for profiling)")
     p.add_argument("--threshold", type=float, default=0.005,
                    help="surrogate workload: committee std (eV) above which an atom takes the GPR")
+    p.add_argument("--contact", type=float, default=None,
+                   help="surrogate workload: neighbour distance (A) below which an atom takes "
+                        "the GPR (default: the 0.2%% quantile of the training cells' nearest-"
+                        "neighbour distances; 0 = off)")
+    p.add_argument("--surrogate-theta", type=float, default=4.0,
+                   help="surrogate workload: theta of the GAP in units of std(MM) (4: the smooth "
+                        "alloy GAP; 0.8: the throughput workload's GAP)")
     return p.parse_args()
 
 
@@ -566,6 +573,18 @@ def run_population(args):
     m.close()
 
 
+def nn_distances(lat, pos):
+    """Nearest-neighbour distance of every atom of one cell (minimum image;
+    the cell is at least twice as wide as the distances of interest)."""
+    inv = np.linalg.inv(lat)
+    f = pos @ inv
+    d = f[:, None, :] - f[None, :, :]
+    d -= np.round(d)
+    r = np.sqrt(((d @ lat) ** 2).sum(-1))
+    np.fill_diagonal(r, np.inf)
+    return r.min(1)
+
+
 def _alloy_chunk(args):
     seed0, count = args
     import gapgb.synth as S
@@ -607,7 +626,8 @@ def run_surrogate(args):
     import gapgb.synth as S
     import gapgb.surrogate as SU
     dev = torch.device("cuda", 0)
-    arrays = S.alloy_model(M=M_SPARSE, theta_scale=4.0, coeff_std=1e-3, seed=0, ncells=8)
+    arrays = S.alloy_model(M=M_SPARSE, theta_scale=args.surrogate_theta, coeff_std=1e-3, seed=0,
+                           ncells=8)
     zt, wt, ty, al, rc, ze, theta, mm, coeff = arrays
 
     def new_model(prec):
@@ -633,6 +653,13 @@ def run_surrogate(args):
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     n_train = int(off[-1])
+    # the contact radius of the force-sensitive trigger, from the training
+    # cells alone: a low quantile of their atoms' nearest-neighbour distances
+    contact = args.contact
+    if contact is None:
+        nn = np.concatenate([nn_distances(lat[s_], pos[off[s_]:off[s_ + 1]])
+                             for s_ in range(min(400, len(off) - 1))])
+        contact = float(np.quantile(nn, 0.002))
     del G, e, t, Zd
     torch.cuda.empty_cache()
 
@@ -700,25 +727,42 @@ def run_surrogate(args):
             E.append(d_E[:c["S"]].cpu().numpy().copy())
         return np.concatenate(ae), np.concatenate(F), np.concatenate(E)
 
+    m_p = new_model("fp64")
+    ae_p, F_p, E_p = outputs(m_p, chunks)
+
+    def with_fallback(m, thr, con):
+        m.attach_surrogate(sur, threshold=thr, contact=con)
+        m.set_precision("surrogate")
+        ae, F, E = [], [], []
+        nfb = 0
+        for c in chunks:
+            step(m, c)
+            torch.cuda.synchronize()
+            m.check_device_status()
+            nfb += m.fallback_count()
+            ae.append(d_ae[:c["N"]].cpu().numpy().copy())
+            F.append(d_F[:c["N"]].cpu().numpy().copy())
+            E.append(d_E[:c["S"]].cpu().numpy().copy())
+        return np.concatenate(ae), np.concatenate(F), np.concatenate(E), nfb
+
+    # fallback fraction against the largest errors, over committee thresholds
+    # and contact radii (the chosen configuration is the last entry)
     m_s = new_model("mixed")
-    m_s.attach_surrogate(sur, threshold=args.threshold)
-    m_s.set_precision("surrogate")
+    sweep = []
+    for thr, con in ((args.threshold, 0.0), (0.002, 0.0), (0.001, 0.0), (0.0005, 0.0),
+                     (0.0002, 0.0), (args.threshold, contact), (args.threshold, contact + 0.1),
+                     (0.001, contact + 0.1)):
+        ae_x, F_x, _, nfb_x = with_fallback(m_s, thr, con)
+        sweep.append({"threshold_eV": thr, "contact_A": con, "fallback_fraction": nfb_x / Nh,
+                      "F_max": float(np.abs(F_x - F_p).max()),
+                      "F_p999": float(np.quantile(np.abs(F_x - F_p), 0.999)),
+                      "e_atom_max": float(np.abs(ae_x - ae_p).max())})
+    ae_s, F_s, E_s, nfb = with_fallback(m_s, args.threshold, contact)
     value, ms_total, clocks = timed(m_s, chunks, sampler=True)
-    ae_s, F_s, E_s = [], [], []
-    nfb = 0
-    for c in chunks:
-        step(m_s, c)
-        torch.cuda.synchronize()
-        m_s.check_device_status()
-        nfb += m_s.fallback_count()
-        ae_s.append(d_ae[:c["N"]].cpu().numpy().copy())
-        F_s.append(d_F[:c["N"]].cpu().numpy().copy())
-        E_s.append(d_E[:c["S"]].cpu().numpy().copy())
-    ae_s, F_s, E_s = np.concatenate(ae_s), np.concatenate(F_s), np.concatenate(E_s)
     # stage times of the surrogate form on one chunk
     os.environ["GAPGB_PROFILE_STAGES"] = "1"
     prof = new_model("mixed")
-    prof.attach_surrogate(sur, threshold=args.threshold)
+    prof.attach_surrogate(sur, threshold=args.threshold, contact=contact)
     prof.set_precision("surrogate")
     stages = np.zeros(4)
     for it in range(6):
@@ -733,9 +777,7 @@ def run_surrogate(args):
     m_tc = new_model("tc")
     tc_value, _, _ = timed(m_tc, chunks)
     m_tc.close()
-    m_p = new_model("fp64")
     plain_value, _, _ = timed(m_p, chunks[:2])
-    ae_p, F_p, E_p = outputs(m_p, chunks)
     m_p.close()
     de = ae_s - ae_p
     dF = F_s - F_p
@@ -772,14 +814,18 @@ def run_surrogate(args):
             "data": "synthetic",
             "config": {"workload": "surrogate: %d held-out alloy512 cells" % Sh,
                        "atoms": Nh, "step": "one chunk of %d cells" % CH,
-                       "model": "alloy GAP M=4000 theta=4 std, D=64",
+                       "model": "alloy GAP M=4000 theta=%g std, D=64" % args.surrogate_theta,
                        "network": "per-species 64-128-128-1 SiLU, 4-member committee",
-                       "threshold_eV": args.threshold,
+                       "threshold_eV": args.threshold, "contact_A": contact,
                        "l2": "flushed between steps (512 MB write)"},
             "train": {"structures": args.train_structs, "atoms": n_train, "epochs": args.epochs,
                       "rows_per_species": 1024, "label_s": t_label, "train_s": t_train,
                       "loss_first_last": [hist[0], hist[-1]]},
-            "fallback": {"atoms": int(nfb), "fraction": nfb / Nh},
+            "fallback": {"atoms": int(nfb), "fraction": nfb / Nh,
+                         "trigger": "committee std > threshold, or a neighbour closer than "
+                                    "contact_A (0.2% quantile of the training cells' "
+                                    "nearest-neighbour distances)"},
+            "fallback_sweep": sweep,
             "errors_vs_fp64": {"e_atom_rms": float(np.sqrt(np.mean(de ** 2))),
                                "e_atom_p999": float(np.quantile(np.abs(de), 0.999)),
                                "e_atom_max": float(np.abs(de).max()),
@@ -1317,7 +1363,8 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": {"fp32": "f32", "tc": "bf16x3/f32", "fp64": "f64", "mixed": "f32/f64"}[args.precision],
+        "dtype": {"fp32": "f32", "tc": "bf16x3/f32", "tf32": "tf32/f32", "fp64": "f64",
+                  "mixed": "f32/f64"}[args.precision],
         "data": "synthetic",
         "config": {"workload": "alloy512 ternary fcc (Z 13/28/40), D=64, M=4000",
                    "structures_per_step": S, "atoms_per_step_per_gpu": N,

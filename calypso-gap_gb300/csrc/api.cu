@@ -310,8 +310,8 @@ gapgb_status enqueue_tail(gapgb_model *m, int S, int N, int cap, int capS, int l
     // committee for every atom, then the exact GPR for the atoms it flags
     surrogate_enqueue(m->surrogate, N, d_species, (const float *)ws.G, ws.e, m->surr_std,
                       (float *)ws.dedg, ws.d_flags, st);
-    surrogate_select_fallback(N, m->surr_std, (float)m->surr_threshold, m->fb_rows, m->fb_count,
-                              st);
+    surrogate_select_fallback(N, m->surr_std, (float)m->surr_threshold, ws.nbr_cnt, ws.nbr_d32,
+                              cap, (float)m->surr_contact, m->fb_rows, m->fb_count, st);
     launch_gpr_rows(m, ws, m->surr_cap, m->fb_rows, m->fb_count, m->fb_scratch, st);
   }
   else if (m->precision == GAPGB_PREC_TC) {
@@ -993,6 +993,15 @@ gapgb_status gapgb_model_set_surrogate(gapgb_model *m, gapgb_surrogate *s, doubl
       return fail(GAPGB_ERR_UNKNOWN_SPECIES, "surrogate lacks species Z=" + std::to_string(z));
   m->surrogate = s;
   m->surr_threshold = threshold_ev;
+  return GAPGB_OK;
+}
+
+gapgb_status gapgb_model_set_fallback_contact(gapgb_model *m, double r_contact) {
+  if (!m) return fail(GAPGB_ERR_ARG, "null model");
+  if (!(r_contact >= 0.0)) return fail(GAPGB_ERR_ARG, "r_contact must be >= 0");
+  if (m->live_graphs->load() > 0)
+    return fail(GAPGB_ERR_ARG, "the model is bound to a live CUDA graph (free it first)");
+  m->surr_contact = r_contact;
   return GAPGB_OK;
 }
 

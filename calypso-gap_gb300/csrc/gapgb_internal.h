@@ -332,6 +332,7 @@ struct gapgb_model {
   // learned surrogate (not owned) and its fallback buffers
   gapgb_surrogate *surrogate = nullptr;
   double surr_threshold = 0.005;
+  double surr_contact = 0.0;   // Angstrom: a neighbour closer than this forces the GPR
   int surr_cap = 0;
   float *surr_std = nullptr;   // committee std per atom (eV)
   int *fb_rows = nullptr;      // atoms that take the GPR
@@ -435,7 +436,8 @@ gapgb_status md_clear_flags(gapgb_model *m);
 gapgb_status surrogate_prepare(gapgb_surrogate *s, int N);
 void surrogate_enqueue(gapgb_surrogate *s, int N, const int *d_Z, const float *d_G, double *d_e,
                        float *d_std, float *d_dedg, int *d_err, cudaStream_t st);
-void surrogate_select_fallback(int N, const float *d_std, float threshold, int *d_rows,
+void surrogate_select_fallback(int N, const float *d_std, float threshold, const int *d_cnt,
+                               const float4 *d_d32, int cap, float r_contact, int *d_rows,
                                int *d_count, cudaStream_t st);
 int surrogate_device(const gapgb_surrogate *s);
 // mlp_tc.cu (surrogate inference on the tensor cores)

@@ -401,10 +401,20 @@ __global__ void k_mlp_committee(int Mpad, int D, int members, const int *__restr
   }
 }
 
-__global__ void k_mlp_fallback(int N, const float *__restrict__ sd, float thr, int *__restrict__ rows,
+// atom i takes the GPR when its committee std is above thr (or NaN), or when
+// a neighbour slot lies closer than r_contact (FP32 records, .w = distance)
+__global__ void k_mlp_fallback(int N, const float *__restrict__ sd, float thr,
+                               const int *__restrict__ cnt, const float4 *__restrict__ d32,
+                               int cap, float rcon, int *__restrict__ rows,
                                int *__restrict__ count) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < N && !(sd[i] <= thr)) rows[atomicAdd(count, 1)] = i;
+  if (i >= N) return;
+  bool fb = !(sd[i] <= thr);
+  if (!fb && rcon > 0.f) {
+    const int P = min(cnt[i], cap);
+    for (int q = 0; q < P && !fb; ++q) fb = d32[(size_t)i * cap + q].w < rcon;
+  }
+  if (fb) rows[atomicAdd(count, 1)] = i;
 }
 
 unsigned nblk(size_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
@@ -601,11 +611,14 @@ bool surrogate_has_species(const gapgb_surrogate *s, int z) {
   return std::find(s->species_z.begin(), s->species_z.end(), z) != s->species_z.end();
 }
 
-// rows[0 .. *count) = atoms whose committee std is above the threshold (or NaN)
-void surrogate_select_fallback(int N, const float *d_std, float threshold, int *d_rows,
+// rows[0 .. *count) = atoms whose committee std is above the threshold (or
+// NaN), or that have a neighbour closer than r_contact (0: no contact test)
+void surrogate_select_fallback(int N, const float *d_std, float threshold, const int *d_cnt,
+                               const float4 *d_d32, int cap, float r_contact, int *d_rows,
                                int *d_count, cudaStream_t st) {
   cudaMemsetAsync(d_count, 0, sizeof(int), st);
-  k_mlp_fallback<<<nblk(N), 256, 0, st>>>(N, d_std, threshold, d_rows, d_count);
+  k_mlp_fallback<<<nblk(N), 256, 0, st>>>(N, d_std, threshold, d_cnt, d_d32, cap, r_contact,
+                                          d_rows, d_count);
 }
 
 }  // namespace gapgb

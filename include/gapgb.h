@@ -370,6 +370,15 @@ gapgb_status gapgb_surrogate_predict(gapgb_surrogate *s, int natoms,
 gapgb_status gapgb_model_set_surrogate(gapgb_model *model, gapgb_surrogate *s,
                                        double threshold_ev);
 
+/* Force-sensitive fallback of the surrogate form (no counterpart in the
+ * reference): at GAPGB_PREC_SURROGATE an atom also takes the exact GPR when
+ * any of its neighbours is closer than r_contact (Angstrom), whatever its
+ * committee spread.  Short contacts are where the descriptor Jacobian
+ * amplifies a small dE/dG error into a large force error while the energy
+ * committee stays quiet; both atoms of such a contact see it.  0 (the
+ * default) turns the trigger off.  Refused while a graph of the model lives. */
+gapgb_status gapgb_model_set_fallback_contact(gapgb_model *model, double r_contact);
+
 /* Number of atoms that took the GPR fallback in the model's last
  * GAPGB_PREC_SURROGATE evaluation (synchronises the model's device). */
 gapgb_status gapgb_surrogate_fallback_count(gapgb_model *model, int *count);

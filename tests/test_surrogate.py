@@ -313,3 +313,56 @@ def test_surrogate_gain_over_plain_gpu_path(gapgb_mod, trained):
     print("plain fp64 %.3f ms, surrogate %.3f ms per %d atoms: %.1fx" %
           (times["fp64"], times["surrogate"], N, gain))
     assert gain > 2.0
+
+
+def _with_contacts(seed, ncell=6, per_cell=4, r=2.3):
+    """Held-out alloy cells in which `per_cell` atoms are moved towards their
+    nearest neighbour until the pair is r apart (a short contact the training
+    cells do not contain)."""
+    import gapgb.synth as S
+    rng = np.random.default_rng(seed)
+    out = []
+    for c in range(ncell):
+        lat, pos, z = S.alloy512(seed=seed + c)
+        pos = pos.copy()
+        inv = np.linalg.inv(lat)
+        for a in rng.choice(len(pos), per_cell, replace=False):
+            d = (pos - pos[a]) @ inv
+            d -= np.round(d)
+            v = d @ lat
+            r2 = (v ** 2).sum(1)
+            r2[a] = np.inf
+            b = int(np.argmin(r2))
+            u = -v[b] / np.sqrt(r2[b])   # from b towards a
+            pos[a] = pos[a] + v[b] + u * r  # a at distance r from b's image
+        out.append((lat, pos, z))
+    return out
+
+
+@pytest.mark.gpu
+def test_contact_trigger_sends_short_contacts_to_the_gpr(gapgb_mod, trained):
+    """The force-sensitive trigger: with planted 2.3 A contacts, the atoms of
+    every contact take the exact GPR, the fallback count rises, and the
+    largest force error against the exact GPR falls within the bar."""
+    arrays, sur, _, _ = trained
+    zt, wt, ty, al, rc, ze, theta, mm, coeff = arrays
+    m = gapgb_mod.GapModel.create(zt, wt, ty, al, rc, theta, mm, coeff, sf_zeta=ze)
+    held = _with_contacts(91000)
+    E0, F0, _, ae0 = _eval(m, held, "fp64")
+    m.attach_surrogate(sur, threshold=0.005, contact=0.0)
+    _, F1, _, _ = _eval(m, held, "surrogate")
+    n1 = m.fallback_count()
+    m.attach_surrogate(sur, threshold=0.005, contact=2.45)
+    E2, F2, _, ae2 = _eval(m, held, "surrogate")
+    n2 = m.fallback_count()
+    d1, d2 = np.abs(F1 - F0).max(), np.abs(F2 - F0).max()
+    print("contacts: committee only F_max %.3g eV/A (%d fallbacks); with the contact "
+          "trigger F_max %.3g eV/A (%d fallbacks of %d atoms)" % (d1, n1, d2, n2, len(F0)))
+    assert n2 >= 2 * 6 * 4 and n2 > n1  # both atoms of every planted contact
+    assert d2 <= 0.020
+    assert d2 < d1
+    assert np.abs(E2 - E0).max() / 512 <= E_TOL
+    # r_contact must be >= 0
+    with pytest.raises(gapgb_mod.GapError):
+        m.attach_surrogate(sur, threshold=0.005, contact=-1.0)
+    m.close()
