@@ -660,6 +660,11 @@ def run_surrogate(args):
         nn = np.concatenate([nn_distances(lat[s_], pos[off[s_]:off[s_ + 1]])
                              for s_ in range(min(400, len(off) - 1))])
         contact = float(np.quantile(nn, 0.002))
+    # the gradient-spread trigger, calibrated on training atoms: quantiles of
+    # the members' dE/dG spread (the chosen one flags about 1 % of them)
+    gs = SU.grad_spread(sur, G[:1 << 20], Zd[:1 << 20]).double().cpu().numpy()
+    gq = {q: float(np.quantile(gs, q)) for q in (0.9, 0.97, 0.99, 0.997)}
+    gspread = gq[0.99]
     del G, e, t, Zd
     torch.cuda.empty_cache()
 
@@ -730,8 +735,8 @@ def run_surrogate(args):
     m_p = new_model("fp64")
     ae_p, F_p, E_p = outputs(m_p, chunks)
 
-    def with_fallback(m, thr, con):
-        m.attach_surrogate(sur, threshold=thr, contact=con)
+    def with_fallback(m, thr, con, gsp=0.0):
+        m.attach_surrogate(sur, threshold=thr, contact=con, grad_spread=gsp)
         m.set_precision("surrogate")
         ae, F, E = [], [], []
         nfb = 0
@@ -749,20 +754,23 @@ def run_surrogate(args):
     # and contact radii (the chosen configuration is the last entry)
     m_s = new_model("mixed")
     sweep = []
-    for thr, con in ((args.threshold, 0.0), (0.002, 0.0), (0.001, 0.0), (0.0005, 0.0),
-                     (0.0002, 0.0), (args.threshold, contact), (args.threshold, contact + 0.1),
-                     (0.001, contact + 0.1)):
-        ae_x, F_x, _, nfb_x = with_fallback(m_s, thr, con)
-        sweep.append({"threshold_eV": thr, "contact_A": con, "fallback_fraction": nfb_x / Nh,
+    configs = [(args.threshold, 0.0, 0.0), (0.001, 0.0, 0.0), (0.0002, 0.0, 0.0),
+               (args.threshold, contact, 0.0), (args.threshold, contact + 0.1, 0.0)]
+    configs += [(args.threshold, 0.0, gq[q]) for q in sorted(gq)]
+    configs += [(args.threshold, contact, gq[q]) for q in sorted(gq)]
+    for thr, con, gsp in configs:
+        ae_x, F_x, _, nfb_x = with_fallback(m_s, thr, con, gsp)
+        sweep.append({"threshold_eV": thr, "contact_A": con, "grad_spread": gsp,
+                      "fallback_fraction": nfb_x / Nh,
                       "F_max": float(np.abs(F_x - F_p).max()),
                       "F_p999": float(np.quantile(np.abs(F_x - F_p), 0.999)),
                       "e_atom_max": float(np.abs(ae_x - ae_p).max())})
-    ae_s, F_s, E_s, nfb = with_fallback(m_s, args.threshold, contact)
+    ae_s, F_s, E_s, nfb = with_fallback(m_s, args.threshold, contact, gspread)
     value, ms_total, clocks = timed(m_s, chunks, sampler=True)
     # stage times of the surrogate form on one chunk
     os.environ["GAPGB_PROFILE_STAGES"] = "1"
     prof = new_model("mixed")
-    prof.attach_surrogate(sur, threshold=args.threshold, contact=contact)
+    prof.attach_surrogate(sur, threshold=args.threshold, contact=contact, grad_spread=gspread)
     prof.set_precision("surrogate")
     stages = np.zeros(4)
     for it in range(6):
@@ -817,14 +825,17 @@ def run_surrogate(args):
                        "model": "alloy GAP M=4000 theta=%g std, D=64" % args.surrogate_theta,
                        "network": "per-species 64-128-128-1 SiLU, 4-member committee",
                        "threshold_eV": args.threshold, "contact_A": contact,
+                       "grad_spread": gspread,
+                       "grad_spread_training_quantiles": {str(k): v for k, v in gq.items()},
                        "l2": "flushed between steps (512 MB write)"},
             "train": {"structures": args.train_structs, "atoms": n_train, "epochs": args.epochs,
                       "rows_per_species": 1024, "label_s": t_label, "train_s": t_train,
                       "loss_first_last": [hist[0], hist[-1]]},
             "fallback": {"atoms": int(nfb), "fraction": nfb / Nh,
-                         "trigger": "committee std > threshold, or a neighbour closer than "
-                                    "contact_A (0.2% quantile of the training cells' "
-                                    "nearest-neighbour distances)"},
+                         "trigger": "committee std > threshold, members' dE/dG spread > "
+                                    "grad_spread (99% quantile over training atoms), or a "
+                                    "neighbour closer than contact_A (0.2% quantile of the "
+                                    "training cells' nearest-neighbour distances)"},
             "fallback_sweep": sweep,
             "errors_vs_fp64": {"e_atom_rms": float(np.sqrt(np.mean(de ** 2))),
                                "e_atom_p999": float(np.quantile(np.abs(de), 0.999)),

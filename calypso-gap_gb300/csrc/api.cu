@@ -278,12 +278,14 @@ gapgb_status ensure_surrogate(gapgb_model *m, int N) {
   if (m->live_graphs->load() > 0)
     return fail(GAPGB_ERR_ARG, "surrogate buffers would move while a CUDA graph is alive");
   free_dev(m->surr_std);
+  free_dev(m->surr_gstd);
   free_dev(m->fb_rows);
   free_dev(m->fb_count);
   free_dev(m->fb_scratch);
   m->surr_cap = 0;
   const int n = N + N / 8;
   if (cudaMalloc(&m->surr_std, sizeof(float) * n) != cudaSuccess ||
+      cudaMalloc(&m->surr_gstd, sizeof(float) * n) != cudaSuccess ||
       cudaMalloc(&m->fb_rows, sizeof(int) * n) != cudaSuccess ||
       cudaMalloc(&m->fb_count, sizeof(int)) != cudaSuccess ||
       cudaMalloc(&m->fb_scratch, gpr_rows_scratch_bytes(n, m->host.D)) != cudaSuccess) {
@@ -309,9 +311,10 @@ gapgb_status enqueue_tail(gapgb_model *m, int S, int N, int cap, int capS, int l
   if (m->precision == GAPGB_PREC_SURROGATE) {
     // committee for every atom, then the exact GPR for the atoms it flags
     surrogate_enqueue(m->surrogate, N, d_species, (const float *)ws.G, ws.e, m->surr_std,
-                      (float *)ws.dedg, ws.d_flags, st);
-    surrogate_select_fallback(N, m->surr_std, (float)m->surr_threshold, ws.nbr_cnt, ws.nbr_d32,
-                              cap, (float)m->surr_contact, m->fb_rows, m->fb_count, st);
+                      (float *)ws.dedg, m->surr_gstd, ws.d_flags, st);
+    surrogate_select_fallback(N, m->surr_std, (float)m->surr_threshold, m->surr_gstd,
+                              (float)m->surr_gspread, ws.nbr_cnt, ws.nbr_d32, cap,
+                              (float)m->surr_contact, m->fb_rows, m->fb_count, st);
     launch_gpr_rows(m, ws, m->surr_cap, m->fb_rows, m->fb_count, m->fb_scratch, st);
   }
   else if (m->precision == GAPGB_PREC_TC) {
@@ -626,6 +629,7 @@ void gapgb_model_free(gapgb_model *m) {
   free_dev(m->d_coeff);
   free_dev(m->d_coeff32);
   free_dev(m->surr_std);
+  free_dev(m->surr_gstd);
   free_dev(m->fb_rows);
   free_dev(m->fb_count);
   free_dev(m->fb_scratch);
@@ -996,11 +1000,14 @@ gapgb_status gapgb_model_set_surrogate(gapgb_model *m, gapgb_surrogate *s, doubl
   return GAPGB_OK;
 }
 
-gapgb_status gapgb_model_set_fallback_contact(gapgb_model *m, double r_contact) {
+gapgb_status gapgb_model_set_fallback_triggers(gapgb_model *m, double grad_spread,
+                                               double r_contact) {
   if (!m) return fail(GAPGB_ERR_ARG, "null model");
-  if (!(r_contact >= 0.0)) return fail(GAPGB_ERR_ARG, "r_contact must be >= 0");
+  if (!(grad_spread >= 0.0) || !(r_contact >= 0.0))
+    return fail(GAPGB_ERR_ARG, "grad_spread and r_contact must be >= 0");
   if (m->live_graphs->load() > 0)
     return fail(GAPGB_ERR_ARG, "the model is bound to a live CUDA graph (free it first)");
+  m->surr_gspread = grad_spread;
   m->surr_contact = r_contact;
   return GAPGB_OK;
 }

@@ -333,8 +333,10 @@ struct gapgb_model {
   gapgb_surrogate *surrogate = nullptr;
   double surr_threshold = 0.005;
   double surr_contact = 0.0;   // Angstrom: a neighbour closer than this forces the GPR
+  double surr_gspread = 0.0;   // eV per descriptor unit: a dE/dG spread above this forces it
   int surr_cap = 0;
   float *surr_std = nullptr;   // committee std per atom (eV)
+  float *surr_gstd = nullptr;  // members' dE/dG spread per atom (eV per descriptor unit)
   int *fb_rows = nullptr;      // atoms that take the GPR
   int *fb_count = nullptr;
   void *fb_scratch = nullptr;  // partial sums of the fallback GPR
@@ -435,10 +437,10 @@ gapgb_status md_clear_flags(gapgb_model *m);
 // mlp.cu (learned surrogate)
 gapgb_status surrogate_prepare(gapgb_surrogate *s, int N);
 void surrogate_enqueue(gapgb_surrogate *s, int N, const int *d_Z, const float *d_G, double *d_e,
-                       float *d_std, float *d_dedg, int *d_err, cudaStream_t st);
-void surrogate_select_fallback(int N, const float *d_std, float threshold, const int *d_cnt,
-                               const float4 *d_d32, int cap, float r_contact, int *d_rows,
-                               int *d_count, cudaStream_t st);
+                       float *d_std, float *d_dedg, float *d_gstd, int *d_err, cudaStream_t st);
+void surrogate_select_fallback(int N, const float *d_std, float threshold, const float *d_gstd,
+                               float grad_spread, const int *d_cnt, const float4 *d_d32, int cap,
+                               float r_contact, int *d_rows, int *d_count, cudaStream_t st);
 int surrogate_device(const gapgb_surrogate *s);
 // mlp_tc.cu (surrogate inference on the tensor cores)
 bool mlp_tc_eligible(int D, int H);

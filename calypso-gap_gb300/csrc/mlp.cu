@@ -374,17 +374,35 @@ __global__ void k_mlp_committee(int Mpad, int D, int members, const int *__restr
                                 const float *__restrict__ g, const float *__restrict__ isig,
                                 const float *__restrict__ e_shift, float e_scale,
                                 double *__restrict__ e_out, float *__restrict__ std_out,
-                                float *__restrict__ dedg_out) {
+                                float *__restrict__ dedg_out, float *__restrict__ gstd_out) {
   const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (row >= Mpad) return;
+  if (row >= Mpad) return;  // warp-uniform: a warp owns one row
   const int a = idx[row];
   if (a < 0) return;
   const int sp = tile_sp[row / kTile];
   const float sc = e_scale / members;
+  // mean dE/dG, and the members' spread of it: |std_q(dE/dG_q)| over the D
+  // components, in eV per descriptor unit (member q's dE/dG_d is
+  // g_qd e_scale isig_d)
+  float spread = 0.f;
   for (int d = lane; d < D; d += 32) {
     float s = 0.f;
     for (int q = 0; q < members; ++q) s += g[((size_t)q * Mpad + row) * D + d];
     dedg_out[(size_t)a * D + d] = s * sc * isig[d];
+    if (gstd_out) {  // two passes: no cancellation when the members agree closely
+      const float mean = __fdividef(s, (float)members);
+      float var = 0.f;
+      for (int q = 0; q < members; ++q) {
+        const float dv = g[((size_t)q * Mpad + row) * D + d] - mean;
+        var = fmaf(dv, dv, var);
+      }
+      spread = fmaf(isig[d] * isig[d], var / (float)(members > 1 ? members - 1 : 1), spread);
+    }
+  }
+  if (gstd_out) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) spread += __shfl_xor_sync(0xffffffffu, spread, o);
+    if (lane == 0) gstd_out[a] = e_scale * sqrtf(spread);
   }
   if (lane == 0) {
     // FP32 statistics (the FP64 pipe is narrow); the energy itself in FP64
@@ -401,15 +419,17 @@ __global__ void k_mlp_committee(int Mpad, int D, int members, const int *__restr
   }
 }
 
-// atom i takes the GPR when its committee std is above thr (or NaN), or when
-// a neighbour slot lies closer than r_contact (FP32 records, .w = distance)
+// atom i takes the GPR when its committee std is above thr (or NaN), when
+// the members' dE/dG spread is above gthr (> 0), or when a neighbour slot
+// lies closer than r_contact (FP32 records, .w = distance)
 __global__ void k_mlp_fallback(int N, const float *__restrict__ sd, float thr,
+                               const float *__restrict__ gsd, float gthr,
                                const int *__restrict__ cnt, const float4 *__restrict__ d32,
                                int cap, float rcon, int *__restrict__ rows,
                                int *__restrict__ count) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
-  bool fb = !(sd[i] <= thr);
+  bool fb = !(sd[i] <= thr) || (gthr > 0.f && !(gsd[i] <= gthr));
   if (!fb && rcon > 0.f) {
     const int P = min(cnt[i], cap);
     for (int q = 0; q < P && !fb; ++q) fb = d32[(size_t)i * cap + q].w < rcon;
@@ -580,7 +600,7 @@ gapgb_status surrogate_prepare(gapgb_surrogate *s, int N) {
 // d_G) on stream st: e (eV), committee std (eV) and mean dE/dG per atom.
 // Launch shapes depend on N only; no allocation, no synchronisation.
 void surrogate_enqueue(gapgb_surrogate *s, int N, const int *d_Z, const float *d_G, double *d_e,
-                       float *d_std, float *d_dedg, int *d_err, cudaStream_t st) {
+                       float *d_std, float *d_dedg, float *d_gstd, int *d_err, cudaStream_t st) {
   const int tiles = pad_tiles(N, s->nsp);
   const int Mpad = tiles * kTile;
   cudaMemsetAsync(s->p_cnt, 0, kMaxSurrSpecies * sizeof(int), st);
@@ -602,7 +622,8 @@ void surrogate_enqueue(gapgb_surrogate *s, int N, const int *d_Z, const float *d
   }
   k_mlp_committee<<<nblk((size_t)Mpad * 32), 256, 0, st>>>(Mpad, s->D, s->members, s->idx, s->p_tile,
                                                           s->y, s->Gx, s->isig, s->e_shift,
-                                                          s->e_scale, d_e, d_std, d_dedg);
+                                                          s->e_scale, d_e, d_std, d_dedg,
+                                                          d_gstd);
 }
 
 int surrogate_device(const gapgb_surrogate *s) { return s->device; }
@@ -612,13 +633,14 @@ bool surrogate_has_species(const gapgb_surrogate *s, int z) {
 }
 
 // rows[0 .. *count) = atoms whose committee std is above the threshold (or
-// NaN), or that have a neighbour closer than r_contact (0: no contact test)
-void surrogate_select_fallback(int N, const float *d_std, float threshold, const int *d_cnt,
-                               const float4 *d_d32, int cap, float r_contact, int *d_rows,
-                               int *d_count, cudaStream_t st) {
+// NaN), whose dE/dG spread is above grad_spread (0: off), or that have a
+// neighbour closer than r_contact (0: off)
+void surrogate_select_fallback(int N, const float *d_std, float threshold, const float *d_gstd,
+                               float grad_spread, const int *d_cnt, const float4 *d_d32, int cap,
+                               float r_contact, int *d_rows, int *d_count, cudaStream_t st) {
   cudaMemsetAsync(d_count, 0, sizeof(int), st);
-  k_mlp_fallback<<<nblk(N), 256, 0, st>>>(N, d_std, threshold, d_cnt, d_d32, cap, r_contact,
-                                          d_rows, d_count);
+  k_mlp_fallback<<<nblk(N), 256, 0, st>>>(N, d_std, threshold, d_gstd, grad_spread, d_cnt, d_d32,
+                                          cap, r_contact, d_rows, d_count);
 }
 
 }  // namespace gapgb
@@ -827,7 +849,7 @@ gapgb_status gapgb_surrogate_train_step(gapgb_surrogate *s, int rows_per_species
 
 gapgb_status gapgb_surrogate_predict(gapgb_surrogate *s, int natoms, const int *d_species,
                                      const float *d_G, double *d_e, float *d_std, float *d_dedg,
-                                     void *stream) {
+                                     float *d_gstd, void *stream) {
   if (!s || !d_species || !d_G || !d_e || !d_std || !d_dedg) return sfail(GAPGB_ERR_ARG, "null argument");
   if (natoms <= 0) return sfail(GAPGB_ERR_ARG, "natoms must be positive");
   GAPGB_CUDA_TRY(cudaSetDevice(s->device));
@@ -835,7 +857,7 @@ gapgb_status gapgb_surrogate_predict(gapgb_surrogate *s, int natoms, const int *
   if (st) return st;
   cudaStream_t cs = stream ? (cudaStream_t)stream : s->stream;
   GAPGB_CUDA_TRY(cudaMemsetAsync(s->p_err, 0, sizeof(int), cs));
-  surrogate_enqueue(s, natoms, d_species, d_G, d_e, d_std, d_dedg, s->p_err, cs);
+  surrogate_enqueue(s, natoms, d_species, d_G, d_e, d_std, d_dedg, d_gstd, s->p_err, cs);
   GAPGB_CUDA_TRY(cudaGetLastError());
   int err = 0;
   GAPGB_CUDA_TRY(cudaMemcpyAsync(&err, s->p_err, sizeof(int), cudaMemcpyDeviceToHost, cs));

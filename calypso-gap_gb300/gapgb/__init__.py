@@ -61,9 +61,9 @@ SYMBOLS = [
     ("gapgb_surrogate_set_norm", _I, [_P, _P, _P, _P, _D]),
     ("gapgb_surrogate_params", _I, [_P, _P, _P]),
     ("gapgb_surrogate_train_step", _I, [_P, _I, _P, _P, _P, _P, C.c_float, C.c_float, _I, _P, _P]),
-    ("gapgb_surrogate_predict", _I, [_P, _I, _P, _P, _P, _P, _P, _P]),
+    ("gapgb_surrogate_predict", _I, [_P, _I, _P, _P, _P, _P, _P, _P, _P]),
     ("gapgb_model_set_surrogate", _I, [_P, _P, _D]),
-    ("gapgb_model_set_fallback_contact", _I, [_P, _D]),
+    ("gapgb_model_set_fallback_triggers", _I, [_P, _D, _D]),
     ("gapgb_surrogate_fallback_count", _I, [_P, _P]),
     ("gapgb_gpr_labels", _I, [_P, _I, _P, _P, _P, _P, _P, _P, _P]),
     ("gapgb_md_create", _I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _D, _D, _I, C.POINTER(_P)]),
@@ -342,15 +342,18 @@ class GapModel:
                                          atom_energy or None, C.byref(h)), "gapgb_graph_create")
         return Graph(h, self)
 
-    def attach_surrogate(self, sur, threshold=0.005, contact=0.0):
+    def attach_surrogate(self, sur, threshold=0.005, contact=0.0, grad_spread=0.0):
         """Use a trained gapgb.surrogate.Surrogate at precision "surrogate";
-        atoms whose committee std exceeds `threshold` (eV), or with a
-        neighbour closer than `contact` (Angstrom, 0 = off), take the GPR."""
+        atoms whose committee std exceeds `threshold` (eV), whose members'
+        dE/dG spread exceeds `grad_spread` (eV per descriptor unit, 0 = off),
+        or with a neighbour closer than `contact` (Angstrom, 0 = off), take
+        the GPR."""
         _check(load().gapgb_model_set_surrogate(self._h, sur.handle if sur is not None else None,
                                                 float(threshold)), "gapgb_model_set_surrogate")
         self._surrogate = sur  # keeps it alive while attached
-        _check(load().gapgb_model_set_fallback_contact(self._h, float(contact)),
-               "gapgb_model_set_fallback_contact")
+        _check(load().gapgb_model_set_fallback_triggers(self._h, float(grad_spread),
+                                                        float(contact)),
+               "gapgb_model_set_fallback_triggers")
 
     def fallback_count(self):
         """Atoms sent to the GPR by the last surrogate evaluation."""

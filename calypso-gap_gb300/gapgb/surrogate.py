@@ -74,9 +74,10 @@ class Surrogate:
                "gapgb_surrogate_train_step")
         return loss
 
-    def predict_ptrs(self, natoms, d_species, d_G, d_e, d_std, d_dedg, stream=0):
+    def predict_ptrs(self, natoms, d_species, d_G, d_e, d_std, d_dedg, stream=0, d_gstd=0):
         _check(load().gapgb_surrogate_predict(self._h, int(natoms), d_species, d_G, d_e, d_std,
-                                              d_dedg, stream or None), "gapgb_surrogate_predict")
+                                              d_dedg, d_gstd or None, stream or None),
+               "gapgb_surrogate_predict")
 
     def predict(self, species, G):
         """Host convenience: (e[N], std[N], dedg[N, D]) for FP32 descriptors G."""
@@ -91,6 +92,27 @@ class Surrogate:
         self.predict_ptrs(n, Z.data_ptr(), Gd.data_ptr(), e.data_ptr(), sd.data_ptr(), dg.data_ptr(),
                           torch.cuda.current_stream().cuda_stream)
         return e.cpu().numpy(), sd.cpu().numpy(), dg.cpu().numpy()
+
+
+def grad_spread(sur, G, Z, chunk=1 << 18):
+    """The committee members' dE/dG spread of every row of the CUDA tensors
+    G [N, D] float32 and Z [N] int32 (eV per descriptor unit), as the
+    force-sensitive fallback trigger reads it: e.g. a high quantile of it
+    over training atoms calibrates that trigger."""
+    import torch
+    n = G.shape[0]
+    out = torch.empty(n, dtype=torch.float32, device=G.device)
+    e = torch.empty(min(n, chunk), dtype=torch.float64, device=G.device)
+    sd = torch.empty(min(n, chunk), dtype=torch.float32, device=G.device)
+    dg = torch.empty((min(n, chunk), sur.des_len), dtype=torch.float32, device=G.device)
+    for a in range(0, n, chunk):
+        b = min(n, a + chunk)
+        Gc = G[a:b].contiguous()
+        Zc = Z[a:b].contiguous()
+        sur.predict_ptrs(b - a, Zc.data_ptr(), Gc.data_ptr(), e.data_ptr(), sd.data_ptr(),
+                         dg.data_ptr(), torch.cuda.current_stream().cuda_stream,
+                         d_gstd=out[a:b].data_ptr())
+    return out
 
 
 def gpr_labels(model, atom_off, species, lat, pos, chunk_atoms=1 << 17):

@@ -355,12 +355,14 @@ gapgb_status gapgb_surrogate_train_step(gapgb_surrogate *s, int rows_per_species
 
 /* Committee prediction for natoms atoms (atomic numbers d_species, FP32
  * descriptors d_G, device): mean atomic energy d_e (eV), committee standard
- * deviation d_std (eV) and mean dE/dG d_dedg[natoms*D].  Waits for the
- * stream (NULL: the surrogate's own stream). */
+ * deviation d_std (eV), mean dE/dG d_dedg[natoms*D] and, when d_gstd is not
+ * NULL, the members' dE/dG spread per atom (as gapgb_model_set_fallback_
+ * triggers reads it).  Waits for the stream (NULL: the surrogate's own
+ * stream). */
 gapgb_status gapgb_surrogate_predict(gapgb_surrogate *s, int natoms,
                                      const int *d_species, const float *d_G,
                                      double *d_e, float *d_std, float *d_dedg,
-                                     void *stream);
+                                     float *d_gstd, void *stream);
 
 /* Attach a surrogate (not owned; NULL detaches) and the fallback threshold
  * on the committee standard deviation, in eV.  Its des_len must be the
@@ -370,14 +372,20 @@ gapgb_status gapgb_surrogate_predict(gapgb_surrogate *s, int natoms,
 gapgb_status gapgb_model_set_surrogate(gapgb_model *model, gapgb_surrogate *s,
                                        double threshold_ev);
 
-/* Force-sensitive fallback of the surrogate form (no counterpart in the
- * reference): at GAPGB_PREC_SURROGATE an atom also takes the exact GPR when
- * any of its neighbours is closer than r_contact (Angstrom), whatever its
- * committee spread.  Short contacts are where the descriptor Jacobian
- * amplifies a small dE/dG error into a large force error while the energy
- * committee stays quiet; both atoms of such a contact see it.  0 (the
- * default) turns the trigger off.  Refused while a graph of the model lives. */
-gapgb_status gapgb_model_set_fallback_contact(gapgb_model *model, double r_contact);
+/* Force-sensitive fallback triggers of the surrogate form (no counterpart in
+ * the reference).  At GAPGB_PREC_SURROGATE an atom also takes the exact GPR,
+ * whatever its energy-committee spread, when
+ *  - the committee members' dE/dG vectors spread by more than grad_spread
+ *    (the norm over the D components of their standard deviation, eV per
+ *    descriptor unit): a force error comes from a dE/dG error, which the
+ *    energy spread does not see; or
+ *  - any of its neighbours is closer than r_contact (Angstrom): at short
+ *    contacts the descriptor Jacobian amplifies a small dE/dG error into a
+ *    large force error; both atoms of such a contact see it.
+ * 0 (the default) turns a trigger off.  Refused while a graph of the model
+ * lives. */
+gapgb_status gapgb_model_set_fallback_triggers(gapgb_model *model, double grad_spread,
+                                               double r_contact);
 
 /* Number of atoms that took the GPR fallback in the model's last
  * GAPGB_PREC_SURROGATE evaluation (synchronises the model's device). */

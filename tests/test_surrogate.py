@@ -362,7 +362,48 @@ def test_contact_trigger_sends_short_contacts_to_the_gpr(gapgb_mod, trained):
     assert d2 <= 0.020
     assert d2 < d1
     assert np.abs(E2 - E0).max() / 512 <= E_TOL
-    # r_contact must be >= 0
+    # r_contact and the gradient spread must be >= 0
     with pytest.raises(gapgb_mod.GapError):
         m.attach_surrogate(sur, threshold=0.005, contact=-1.0)
+    with pytest.raises(gapgb_mod.GapError):
+        m.attach_surrogate(sur, threshold=0.005, grad_spread=-1.0)
+    m.close()
+
+
+@pytest.mark.gpu
+def test_gradient_spread_trigger(gapgb_mod, trained):
+    """The members' dE/dG spread (gapgb_surrogate_predict's d_gstd) equals its
+    definition on the committee's own members, and the trigger built on it
+    sends exactly the atoms above the threshold to the GPR."""
+    import torch
+    import gapgb.synth as S
+    import gapgb.surrogate as SU
+    arrays, sur, _, _ = trained
+    zt, wt, ty, al, rc, ze, theta, mm, coeff = arrays
+    m = gapgb_mod.GapModel.create(zt, wt, ty, al, rc, theta, mm, coeff, sf_zeta=ze)
+    held = [S.alloy512(seed=93000 + s) for s in range(4)]
+    off, sp, lat, pos = S.pack(held)
+    m.set_precision("fp32")
+    G = m.descriptors(off, sp, lat, pos).astype(np.float32)
+    dev = torch.device("cuda:0")
+    Gd = torch.from_numpy(G).to(dev)
+    Zd = torch.from_numpy(sp.astype(np.int32)).to(dev)
+    gs = SU.grad_spread(sur, Gd, Zd).cpu().numpy()
+    assert np.all(np.isfinite(gs)) and gs.max() > 0
+    # the definition: |std over members of dE/dG_q| with one member at a time
+    w = sur.params()
+    per = []
+    for q in range(sur.members):
+        one = SU.Surrogate(zt, sur.des_len, sur.hidden, 1, seed=0)
+        one.set_norm(*sur.norm)
+        one.set_params(w[q:q + 1])
+        per.append(one.predict(sp, G)[2].astype(np.float64))
+        one.close()
+    per = np.stack(per)
+    ref = np.sqrt(per.var(0, ddof=1).sum(1))
+    assert np.allclose(gs, ref, rtol=2e-3, atol=1e-6 * ref.max())
+    thr = float(np.quantile(gs, 0.95))
+    m.attach_surrogate(sur, threshold=np.inf, grad_spread=thr)
+    _eval(m, held, "surrogate")
+    assert m.fallback_count() == int((gs > thr).sum())
     m.close()
