@@ -64,11 +64,12 @@ __device__ __forceinline__ GLay grp_carve(unsigned char *raw, int warp, int capS
   return L;
 }
 
-// Stages atom i's slots from the FP32 records of the neighbour kernel.  The
-// cutoff function takes the fast intrinsics (its argument pi r / rc lies in
-// [0, pi], where __sincosf errs by about 4e-7), as do the exponentials and
-// 1/r; the forward and gradient kernels stage through this one routine, so
-// they differentiate the same function.
+// Stages atom i's slots from the FP32 records of the neighbour kernel; the
+// forward and gradient kernels stage through this one routine, so they
+// differentiate the same function.  The staged functions keep the accurate
+// libm forms: with __sincosf / __expf / __fdividef here the tensor-core form's
+// force error on a stiff Si model (forces ~150 eV/A) rose from within
+// 20 meV/A to 23 meV/A.
 __device__ __forceinline__ int grp_stage(const GLay &L, const SFT<float> &sf, int i, int cap,
                                          int capS, int lane, int rci, const int *__restrict__ cnt,
                                          const float4 *__restrict__ d32,
@@ -85,11 +86,11 @@ __device__ __forceinline__ int grp_stage(const GLay &L, const SFT<float> &sf, in
         const float x = sf.pi_over_rc[gr] * r;
         if (want_dfc) {
           float sn, cs;
-          __sincosf(x, &sn, &cs);
+          sincosf(x, &sn, &cs);
           fcv = 0.5f * (cs + 1.f);
           dfcv = -0.5f * sn * sf.pi_over_rc[gr];
         } else {
-          fcv = 0.5f * (__cosf(x) + 1.f);
+          fcv = 0.5f * (cosf(x) + 1.f);
         }
       }
       L.fc[(size_t)gr * capS + q] = fcv;
@@ -101,9 +102,9 @@ __device__ __forceinline__ int grp_stage(const GLay &L, const SFT<float> &sf, in
     }
     float ev[4];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) ev[t] = t < nal ? __expf(-sf.alpha_val[t] * r * r) : 0.f;
+    for (int t = 0; t < 4; ++t) ev[t] = t < nal ? expf(-sf.alpha_val[t] * r * r) : 0.f;
     L.a[q] = g;
-    L.b[q] = make_float4(__fdividef(1.f, r), w, fa, dfa);
+    L.b[q] = make_float4(1.f / r, w, fa, dfa);
     L.e[q] = make_float4(ev[0], ev[1], ev[2], ev[3]);
   }
   return P;
