@@ -477,14 +477,16 @@ struct AngCoef {
 };
 
 // Gradient of one angular pair's contribution sum_s dE/dG_s G_s(j, k) with
-// respect to the positions of slots j and k: vj and vk.
+// respect to the positions of slots j and k: vj and vk.  Slot j's records
+// (Aj, Bj, Ej) come from the caller, which keeps them across a run of pairs
+// that share j.
 template <int NAL, int NC, bool STD>
-__device__ __forceinline__ void pair_grad(const GLay &L, int j, int k, float pirc, int nal,
+__device__ __forceinline__ void pair_grad(const GLay &L, const float4 &Aj, const float4 &Bj,
+                                          const float4 &Ej, int k, float pirc, int nal,
                                           const float (&alv)[NAL], const float (&clam)[NC],
                                           const int (&ciz)[NC], const AngCoef<NAL, NC, STD> &U,
                                           float3 &vj, float3 &vk) {
-  const float4 Aj = L.a[j], Ak = L.a[k], Bj = L.b[j], Bk = L.b[k];
-  const float4 Ej = L.e[j], Ek = L.e[k];
+  const float4 Ak = L.a[k], Bk = L.b[k], Ek = L.e[k];
   const float cx = Aj.x - Ak.x, cy = Aj.y - Ak.y, cz = Aj.z - Ak.z;
   const float c2 = cx * cx + cy * cy + cz * cz;
   const float a = Aj.w, b = Ak.w;
@@ -621,14 +623,13 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
         int nxt = p0 < pe ? (int)prow[p0] : 0;
         int cur = -1;
         float gjx = 0.f, gjy = 0.f, gjz = 0.f;
+        float4 Aj = make_float4(0.f, 0.f, 0.f, 0.f), Bj = Aj, Ej = Aj;  // slot cur's records
         for (int t = 0; t < C; ++t) {
           const int p = p0 + t;
           const int jk = nxt;
           if (p + 1 < pe) nxt = (int)prow[p + 1];  // next pair's entry, loaded ahead
           if (p < pe) {
             const int j = jk & 0xff, k = jk >> 8;
-            float3 vj, vk;
-            pair_grad<NAL, NC, STD>(L, j, k, pirc, nal, alv, clam, ciz, U, vj, vk);
             if (j != cur) {
               if (cur >= 0) {
                 atomicAdd(&L.gx[cur], gjx);
@@ -637,7 +638,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
               }
               cur = j;
               gjx = gjy = gjz = 0.f;
+              Aj = L.a[j];
+              Bj = L.b[j];
+              Ej = L.e[j];
             }
+            float3 vj, vk;
+            pair_grad<NAL, NC, STD>(L, Aj, Bj, Ej, k, pirc, nal, alv, clam, ciz, U, vj, vk);
             gjx += vj.x;
             gjy += vj.y;
             gjz += vj.z;
@@ -655,7 +661,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
         pair_stream(L.a, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
           (void)c2;
           float3 vj, vk;
-          pair_grad<NAL, NC, STD>(L, j, k, pirc, nal, alv, clam, ciz, U, vj, vk);
+          pair_grad<NAL, NC, STD>(L, L.a[j], L.b[j], L.e[j], k, pirc, nal, alv, clam, ciz, U, vj,
+                                  vk);
           float vx = ok ? vj.x : 0.f, vy = ok ? vj.y : 0.f, vz = ok ? vj.z : 0.f;
           // slot j: equal j values are contiguous lanes of the batch, summed
           // by a segmented scan whose last lane adds the run
