@@ -378,8 +378,7 @@ P_SLOTS = 56.0
 T_PAIRS = 690.0  # contributing angular pairs per atom on this workload
 
 
-def stage_bytes_per_atom(D):
-    P, T = P_SLOTS, T_PAIRS
+def stage_bytes_per_atom(D, P=P_SLOTS, T=T_PAIRS):
     return {"neighbours": 32.0 + P * 28.0,
             "descriptors": P * 20.0 + D * 4.0 + T * 2.0,
             "gpr": D * 4.0 * 2 + 8.0,
@@ -394,20 +393,23 @@ def load_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def roofline(stages, N, D, precision, simt=None, plain_stages=None):
+def roofline(stages, N, D, precision, simt=None, plain_stages=None, P=P_SLOTS, T=T_PAIRS,
+             traffic_file=True):
     """Roofline entries from the per-stage device times (ms per step).
 
     `simt` holds the measured FP32 / FP64 FMA and MUFU ex2 rates of the device
     (gapgb.measure_peaks); `plain_stages` the stage times of the plain FP64
-    path on the same workload."""
+    path on the same workload; P and T the workload's slots and contributing
+    angular pairs per atom; `traffic_file` reads the DRAM bytes per atom of
+    the alloy512 capture (only meaningful on that workload)."""
     peaks, src = load_peaks()
     dom = int(np.argmax(stages))
     name = STAGES[dom]
-    bpa = stage_bytes_per_atom(D)
+    bpa = stage_bytes_per_atom(D, P, T)
     ach = bpa[name] * N / (stages[dom] * 1e-3) / 1e9
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "roofline_inputs.txt")
-    if os.path.exists(tpath):
+    if traffic_file and os.path.exists(tpath):
         per_atom = json.load(open(tpath)).get("dram_bytes_per_atom", {}).get(name)
         if per_atom is not None:
             traffic = per_atom * N
@@ -437,6 +439,17 @@ def roofline(stages, N, D, precision, simt=None, plain_stages=None):
                               "unit": "TFLOP/s", "frac": ach_t / peaks["bf16_tflops"],
                               "peak_source": src + " bf16_tflops",
                               "flops": "12 N M 64 (bf16 MMA, padded to 128)"}
+    elif precision == "tf32":
+        mp = ((m + 63) // 64) * 64
+        npad = ((N + 127) // 128) * 128
+        hw = 4.0 * npad * mp * 64  # 2 GEMMs x 1 product x 2 flops (padded)
+        ach_t = hw / (stages[2] * 1e-3) / 1e12
+        pk = 0.5 * peaks["bf16_tflops"]
+        roof["gpr_tensor"] = {"bound": "tensor", "achieved": ach_t, "peak": pk,
+                              "unit": "TFLOP/s", "frac": ach_t / pk,
+                              "peak_source": src + " bf16_tflops x 0.5 (the nominal TF32:BF16 "
+                                                   "dense ratio; no TF32 rate is measured)",
+                              "flops": "4 N M 64 (tf32 MMA, padded)"}
     roof["gpr_algorithmic_tflops"] = 4.0 * m * D * N / (stages[2] * 1e-3) / 1e12
     roof["fp32_nominal_tflops"] = nominal_fp32
     # the GPR's exp rate (one per atom and sparse point) against the measured
@@ -450,7 +463,7 @@ def roofline(stages, N, D, precision, simt=None, plain_stages=None):
     # flops (an FMA = 2): forward 70 per pair (geometry 10, the NAL exponential
     # factors 6, fc(r_jk) 4, Bernstein basis 10, 2 x NAL x 5 moment FMAs 40)
     # and 8 per radial term; gradient 150 per pair and 15 per radial term
-    P, T, R = P_SLOTS, T_PAIRS, 20
+    R = 20
     fl_fwd = N * (70.0 * T + 8.0 * P * R)
     fl_bwd = N * (150.0 * T + 15.0 * P * R)
     for name, fl, st in (("descriptors_fp32", fl_fwd, stages[1]), ("chain_rule_fp32", fl_bwd, stages[3])):
@@ -555,6 +568,59 @@ def run_population(args):
     torch.cuda.synchronize()
     m.check_device_status()
     ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
+    g.close()
+
+    # end to end through the host-buffer call: pinned host inputs and outputs,
+    # both copies inside the timed region
+    h = {k: v.cpu().pin_memory() for k, v in t.items()}
+    hE = torch.zeros(Sn, dtype=torch.float64).pin_memory()
+    hF = torch.zeros(N, 3, dtype=torch.float64).pin_memory()
+    hS = torch.zeros(Sn, 6, dtype=torch.float64).pin_memory()
+
+    def host_step():
+        m.eval_batch_host_ptrs(Sn, h["off"].data_ptr(), h["sp"].data_ptr(), h["lat"].data_ptr(),
+                               h["pos"].data_ptr(), 1, hE.data_ptr(), hF.data_ptr(),
+                               hS.data_ptr())
+
+    for _ in range(args.warmup):
+        host_step()
+    t_host = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        host_step()
+        t_host += time.perf_counter() - t0
+    e2e_s = t_host / args.steps
+    assert np.allclose(hE.numpy(), E.cpu().numpy(), rtol=0, atol=1e-9 * max(1.0, float(np.abs(E.cpu().numpy()).max())))
+    h2d = sum(v.numel() * v.element_size() for v in h.values())
+    d2h = (hE.numel() + hF.numel() + hS.numel()) * 8
+
+    # per-stage device times of the tuned configuration (library CUDA events)
+    os.environ["GAPGB_PROFILE_STAGES"] = "1"
+    prof = gapgb.GapModel.create(zt, wt, ty, al, rc, theta, mm, coeff, sf_zeta=ze)
+    tune._apply(prof, best)
+    prof.set_neighbour_cap(max(int(best["cap"]), 128))
+    stages = np.zeros(4)
+    maxa = int(np.diff(off).max())
+    for it in range(args.warmup + 3):
+        flush.zero_()
+        prof.eval_batch_ptrs(Sn, N, maxa, t["off"].data_ptr(), t["sp"].data_ptr(),
+                             t["lat"].data_ptr(), t["pos"].data_ptr(), 1, E.data_ptr(),
+                             F.data_ptr(), St.data_ptr(), 0, stream.cuda_stream)
+        prof.check_device_status()
+        if it >= args.warmup:
+            stages += np.array(prof.stage_times())
+    stages /= 3
+    # slots and contributing angular pairs per atom on 64 of the cells (the
+    # library's own neighbour list), for the per-atom byte and flop counts
+    P, T = population_pair_stats(prof, pop, 64, float(rc.max()))
+    prof.close()
+    os.environ["GAPGB_PROFILE_STAGES"] = "0"
+    roof = roofline(stages, N, D, best["precision"], simt=gapgb.measure_peaks(), P=P, T=T,
+                    traffic_file=False)
+    roof["slots_per_atom"], roof["pairs_per_atom"] = P, T
+
     line = {"metric": METRIC, "value": N / (ms * 1e-3), "unit": UNIT, "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -564,13 +630,57 @@ def run_population(args):
                        "autotuned": {k: best[k] for k in ("precision", "generic_kernels", "cap")},
                        "tune_errors": {"dE_per_atom": best["dE_per_atom"], "dF": best["dF"]},
                        "l2": "flushed between steps (512 MB write)"},
+            "e2e": {"value": N / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "call": "gapgb_eval_batch (host buffers)"},
+            "roofline": roof,
             # one graph launch per step holding the 9 kernels of a grouped-kernel
             # evaluation (see the headline workload's count); the generic
             # kernels add the reverse slots, the force gather and the orphans
             "gpu_launches": (12 if best["generic_kernels"] else 9) * args.steps}
-    print(json.dumps(line), flush=True)
-    g.close()
     m.close()
+    line["cpu_baseline"] = population_cpu_baseline(
+        (zt, wt, ty, al, rc, ze, theta, mm, coeff), pop, 256)
+    print(json.dumps(line), flush=True)
+
+
+def population_pair_stats(model, pop, count, rc):
+    """Mean slots and contributing angular pairs (j < k, r_ij, r_ik, r_jk <= rc)
+    per atom over the first `count` cells of a population."""
+    off, sp, lat, pos = pop
+    slots = pairs = atoms = 0
+    for s in range(count):
+        a, b = int(off[s]), int(off[s + 1])
+        cnt, nb = model.neighbors(sp[a:b], lat[s], pos[a:b], cap=400)
+        for i in range(b - a):
+            # rows (x, y, z, r, w, j + 1): the image position and its distance
+            v = nb[i, :cnt[i], :3][nb[i, :cnt[i], 3] <= rc]
+            d = np.linalg.norm(v[:, None, :] - v[None, :, :], axis=-1)
+            pairs += int(np.triu(d <= rc, 1).sum())
+            slots += int(cnt[i])
+        atoms += b - a
+    return slots / atoms, pairs / atoms
+
+
+def population_cpu_baseline(arrays, pop, count):
+    """The oracle on all host cores over the first `count` cells of the
+    population (a bounded sample of the same workload)."""
+    import tempfile
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import write_model_file
+    from oracle import oracle
+    zt, wt, ty, al, rc, ze, theta, mm, coeff = arrays
+    off, sp, lat, pos = pop
+    cores = len(os.sched_getaffinity(0))
+    n = int(off[count])
+    with tempfile.TemporaryDirectory() as d:
+        om = oracle.Model(write_model_file(os.path.join(d, "gp"), zt, wt, ty, al, rc, theta, mm,
+                                           coeff, ze))
+        t0 = time.perf_counter()
+        oracle.gap_calc_batch(om, off[:count + 1], sp[:n], lat[:count], pos[:n], 6.0, cores)
+        dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "the first %d population cells (%d atoms) on %d host threads, %.1f s"
+                      % (count, n, cores, dt)}
 
 
 def nn_distances(lat, pos):

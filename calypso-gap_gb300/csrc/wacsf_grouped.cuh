@@ -20,7 +20,11 @@
 // deterministic round-robin schedule) and scatters the forces with FP64
 // atomics in place of the reverse-slot gather.
 
-constexpr int kPairQ = 64;
+// per-warp ring queues of contributing pairs: the forward kernel screens two
+// 32-candidate batches per step (at most 31 + 64 entries pending), the
+// gradient kernel's overflow path one batch (at most 31 + 32)
+constexpr int kPairQFwd = 128;
+constexpr int kPairQBwd = 64;
 // resident blocks per SM the grouped kernels are compiled for (80 registers
 // a thread); their launchers ask for the largest shared-memory carve-out so
 // that the per-warp slot tables of 6 blocks fit
@@ -175,44 +179,62 @@ __device__ __forceinline__ void ang_powers(float cosv, const float *clam, const 
 // walked together (they hold P candidates between them, so a lane finds its
 // (j, k) with two comparisons and no loop); the pairs of one row j are
 // contiguous in the stream, so equal j values are contiguous in a batch.
-template <typename Work>
+template <int Q, typename Work>
 __device__ __forceinline__ void pair_stream(const float4 *__restrict__ A, int P, float rc, int lane,
                                             int *qjk, float *qc2, Work work) {
   const float rc2 = rc * rc;
   const unsigned lt = (1u << lane) - 1u;
   int qh = 0, qn = 0;  // ring queue: entries [qh, qn) are pending
+  // candidate t of the row pair (r, r2): its (j, k), whether it contributes,
+  // and r_jk^2
+  auto cand = [&](int r, int r2, int n1, int tot, int t, int &j, int &k, float &c2) {
+    j = r;
+    k = r + 1 + t;
+    if (t >= n1) {
+      j = r2;
+      k = r2 + 1 + (t - n1);
+    }
+    bool valid = false;
+    c2 = 0.f;
+    if (t < tot) {
+      const float4 aj = A[j], ak = A[k];
+      if (aj.w <= rc && ak.w <= rc) {
+        const float cx = aj.x - ak.x, cy = aj.y - ak.y, cz = aj.z - ak.z;
+        c2 = cx * cx + cy * cy + cz * cz;
+        valid = c2 <= rc2;
+      }
+    }
+    return valid;
+  };
+  auto push = [&](bool valid, int j, int k, float c2) {
+    const unsigned m = __ballot_sync(0xffffffffu, valid);
+    if (valid) {
+      const int e = (qn + __popc(m & lt)) & (Q - 1);
+      qjk[e] = j | (k << 16);
+      qc2[e] = c2;
+    }
+    qn += __popc(m);
+  };
   const int nfold = P / 2;  // row pairs (r, P - 2 - r); the middle row of an even P is alone
   for (int r = 0; r < nfold; ++r) {
     const int r2 = P - 2 - r;
     const int n1 = P - 1 - r;                // candidates of row r
     const int tot = r2 > r ? P : n1;         // with row r2's r + 1
-    for (int base = 0; base < tot; base += 32) {
-      const int t = base + lane;
-      bool valid = false;
-      float c2 = 0.f;
-      int j = r, k = r + 1 + t;
-      if (t >= n1) {
-        j = r2;
-        k = r2 + 1 + (t - n1);
-      }
-      if (t < tot) {
-        const float4 aj = A[j], ak = A[k];
-        if (aj.w <= rc && ak.w <= rc) {
-          const float cx = aj.x - ak.x, cy = aj.y - ak.y, cz = aj.z - ak.z;
-          c2 = cx * cx + cy * cy + cz * cz;
-          valid = c2 <= rc2;
-        }
-      }
-      const unsigned m = __ballot_sync(0xffffffffu, valid);
-      if (valid) {
-        const int e = (qn + __popc(m & lt)) & (kPairQ - 1);
-        qjk[e] = j | (k << 16);
-        qc2[e] = c2;
-      }
-      qn += __popc(m);
+    // with Q = 128, two batches of 32 candidates per step: their loads and
+    // distances are independent, which hides the shared-memory latency of
+    // the screen
+    constexpr int NB = Q >= 128 ? 2 : 1;
+    for (int base = 0; base < tot; base += 32 * NB) {
+      int j0, k0, j1 = 0, k1 = 0;
+      float c0, c1 = 0.f;
+      const bool v0 = cand(r, r2, n1, tot, base + lane, j0, k0, c0);
+      bool v1 = false;
+      if constexpr (NB == 2) v1 = cand(r, r2, n1, tot, base + 32 + lane, j1, k1, c1);
+      push(v0, j0, k0, c0);
+      if constexpr (NB == 2) push(v1, j1, k1, c1);
       __syncwarp();
-      if (qn - qh >= 32) {
-        const int e = (qh + lane) & (kPairQ - 1);
+      while (qn - qh >= 32) {
+        const int e = (qh + lane) & (Q - 1);
         const int jk = qjk[e];
         const float cc = qc2[e];
         __syncwarp();
@@ -222,7 +244,7 @@ __device__ __forceinline__ void pair_stream(const float4 *__restrict__ A, int P,
     }
   }
   if (qn > qh) {
-    const int e = (qh + lane) & (kPairQ - 1);
+    const int e = (qh + lane) & (Q - 1);
     const bool have = lane < qn - qh;
     const int jk = have ? qjk[e] : (0 | (1 << 16));
     const float cc = have ? qc2[e] : 1.f;
@@ -288,8 +310,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
   (void)nj;
   (void)apos;
   extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ int s_qjk[kWarpsPerBlock][kPairQ];
-  __shared__ float s_qc2[kWarpsPerBlock][kPairQ];
+  __shared__ int s_qjk[kWarpsPerBlock][kPairQFwd];
+  __shared__ float s_qc2[kWarpsPerBlock][kPairQFwd];
   __shared__ float s_acc[kWarpsPerBlock][2 * NAL * NC];
   __shared__ float s_out[kWarpsPerBlock][(STD && NC == 6) ? 2 * NAL * NC : 1];
   load_table<float>(smraw, sfg);
@@ -331,7 +353,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
     int np = 0;
     unsigned short *prow = pairs + (size_t)i * pcap;
     if (P > 1)
-      pair_stream(L.a, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
+      pair_stream<kPairQFwd>(L.a, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
         const unsigned vm = __ballot_sync(0xffffffffu, ok);
         if (ok && np + lane < pcap) prow[np + lane] = (unsigned short)(j | (k << 8));
         np += __popc(vm);
@@ -541,8 +563,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
   (void)xyzr;
   (void)apos;
   extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ int s_qjk[kWarpsPerBlock][kPairQ];
-  __shared__ float s_qc2[kWarpsPerBlock][kPairQ];
+  __shared__ int s_qjk[kWarpsPerBlock][kPairQBwd];
+  __shared__ float s_qc2[kWarpsPerBlock][kPairQBwd];
   __shared__ float s_u[kWarpsPerBlock][2 * NAL * NC];
   load_table<float>(smraw, sfg);
   const SFT<float> &sf = *reinterpret_cast<const SFT<float> *>(smraw);
@@ -658,7 +680,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
           atomicAdd(&L.gz[cur], gjz);
         }
       } else if (P > 1) {
-        pair_stream(L.a, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
+        pair_stream<kPairQBwd>(L.a, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
           (void)c2;
           float3 vj, vk;
           pair_grad<NAL, NC, STD>(L, L.a[j], L.b[j], L.e[j], k, pirc, nal, alv, clam, ciz, U, vj,

@@ -29,8 +29,35 @@ def test_roofline_entry_keys_and_arithmetic():
     assert t["bound"] == "tensor" and t["unit"] == "TFLOP/s"
     assert np.isclose(t["frac"], t["achieved"] / t["peak"])
     assert set(roof["stage_ms"]) == set(bench.STAGES)
-    # forms without the tensor-core GPR report no tensor entry
+    # forms without a tensor-core GPR report no tensor entry; TF32 has its own
     assert "gpr_tensor" not in bench.roofline(stages, N, D, "fp32")
+    t32 = bench.roofline(stages, N, D, "tf32")["gpr_tensor"]
+    assert np.isclose(t32["peak"], 0.5 * peaks["bf16_tflops"])
+    assert np.isclose(t32["achieved"], 4.0 * N * 4032 * 64 / 0.24e-3 / 1e12)
+
+
+def test_roofline_population_counts_and_no_alloy_traffic():
+    stages = [0.5, 1.0, 0.8, 1.2]
+    N, D, P, T = 100000, 64, 40.0, 300.0
+    roof = bench.roofline(stages, N, D, "tf32", P=P, T=T, traffic_file=False)
+    assert roof["traffic"] is None
+    assert np.isclose(roof["algorithmic_bytes_per_atom"],
+                      bench.stage_bytes_per_atom(D, P, T)["chain_rule"])
+    assert np.isclose(roof["chain_rule_fp32"]["flops_per_atom"], 150.0 * T + 15.0 * P * 20)
+
+
+def test_population_cpu_baseline_on_two_cells():
+    import gapgb.synth as S
+    pop = S.population(3, seed=5)
+    ty, al, rc, ze = S.sf_table()
+    zt = np.array([3, 8, 14, 26], np.int32)
+    D = 2 * len(ty)
+    rng = np.random.default_rng(0)
+    arrays = (zt, zt.astype(np.float64), ty, al, rc, ze, np.ones(D), rng.normal(size=(4, D)),
+              rng.normal(size=4) * 1e-3)
+    cb = bench.population_cpu_baseline(arrays, pop, 2)
+    assert cb["kind"] == "port" and cb["value"] > 0 and cb["unit"] == bench.UNIT
+    assert "%d atoms" % int(pop[0][2]) in cb["sample"]
 
 
 def test_roofline_uses_measured_simt_peaks_and_plain_stages():
