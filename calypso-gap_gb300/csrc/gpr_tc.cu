@@ -9,17 +9,25 @@
 //   s_ik  = |x''_i|^2 + |m''_k|^2 - 2 x''_i . m''_k
 //   GEMM1 (N x M, K = D):  x''.m'' ~ xh.mh + xh.ml + xl.mh  (3-term BF16 split,
 //                          x'' = xh + xl, m'' = mh + ml, every product exact in FP32)
+//                          as two MMAs per K step: xh.[mh; ml] (N = 128) into
+//                          columns [0, 64) and [64, 128), and xl.mh (N = 64)
+//                          into [0, 64); the epilogue adds the two halves
 //   w_ik  = c_k exp(-s_ik / 2),  e_i = sum_k w_ik  (compensated FP32, Kahan)
-//   GEMM2 (N x D, K = M):  (W M'')_id ~ wh.mh + wh.ml + wl.mh
+//   GEMM2 (N x D, K = M):  (W M'')_id ~ wh.mh + wh.ml + wl.mh, the same way:
+//                          wh.[mhT; mlT] (N = 128) and wl.mhT (N = 64)
 //   dE/dG_id = -(1/theta_d) (x''_id e_i - (W M'')_id)
 //
 // One CTA (8 warps) owns 128 atoms.  For each tile of 64 sparse points: one
 // 1-D bulk copy brings the pre-arranged operand tiles into shared memory,
-// one thread issues GEMM1 (12 tcgen05.mma, M=128 N=64 K=16) into a TMEM
-// accumulator, the eight warps read it back with tcgen05.ld (thread = atom
-// row), form w, accumulate e and write wh/wl into shared memory as GEMM2's A
-// operand, and one thread issues GEMM2 (12 tcgen05.mma, M=128 N=64 K=16)
-// accumulating over all sparse tiles in a second TMEM region.
+// one thread issues GEMM1 (8 tcgen05.mma, M=128 K=16, N=128 and N=64) into a
+// TMEM accumulator, the eight warps read it back with tcgen05.ld (thread =
+// atom row), form w, accumulate e and write wh/wl into shared memory as
+// GEMM2's A operand, and one thread issues GEMM2 (8 tcgen05.mma) accumulating
+// over all sparse tiles in a second TMEM region.  Fewer, wider MMAs: an
+// N = 128 MMA takes about 1.3 times as long as an N = 64 one on GB300, so the
+// 16 MMAs of a tile take about 0.76 times as long as 24 N = 64 MMAs.  The
+// [mh; ml] and [mhT; mlT] pairs are adjacent 64-row blocks in shared memory,
+// which is the 128-row B operand of the same canonical layout.
 //
 // Operand tiles use the no-swizzle K-major canonical layout: 8-row x 16-byte
 // core matrices, K-adjacent cores 128 B apart (LBO), 8-row groups
@@ -59,6 +67,10 @@ constexpr int kOffMh = kOffImg;
 constexpr int kOffMl = kOffMh + kMBytes16;
 constexpr int kOffMhT = kOffMl + kMBytes16;
 constexpr int kOffMlT = kOffMhT + kMBytes16;
+// [mh; ml] and [mhT; mlT] as one 128-row B operand: the second block starts
+// eight 8-row groups (the canonical layout's SBO apart) after the first
+static_assert(kOffMl - kOffMh == 8 * (kDP / 8) * 128, "mh / ml not one 128-row operand");
+static_assert(kOffMlT - kOffMhT == 8 * (kTileK / 8) * 128, "mhT / mlT not one 128-row operand");
 constexpr int kOffMnc = kOffMlT + kMBytes16;             // b2 and c, two tiles
 constexpr int kMncBytes = 2 * kTileK * 4;                 // one tile's mn and c
 constexpr int kOffWh = kOffMnc + 2 * kMncBytes;
@@ -67,7 +79,7 @@ constexpr int kOffBar = kOffWl + kWBytes;                 // 3 mbarriers + tmem 
 constexpr int kOffEp = kOffBar + 64;                      // partial energies [128] (FP64)
 constexpr int kSmemBytes = kOffEp + kRows * 8 + 1024;     // + alignment slack
 constexpr int kGprThreads = 256;  // warps w and w + 4 share TMEM lanes and split the columns
-constexpr int kTmemCols = 128;    // C1 (kTileK columns) and C2 (kDP columns)
+constexpr int kTmemCols = 256;    // C1 and C2, two 64-column halves each
 
 __global__ void __launch_bounds__(kGprThreads, 2)
     k_gpr_tc(int N, int ntiles, const unsigned char *__restrict__ img_model,
@@ -104,7 +116,7 @@ __global__ void __launch_bounds__(kGprThreads, 2)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const uint32_t tC1 = tmem, tC2 = tmem + kTileK;
+  const uint32_t tC1 = tmem, tC2 = tmem + 2 * kTileK;
   const uint32_t lane_base = (uint32_t)(quad * 32) << 16;  // this warp's TMEM lanes
   const int row = quad * 32 + lane;                         // atom row of this thread
   const int i = blockIdx.x * kRows + row;
@@ -116,7 +128,9 @@ __global__ void __launch_bounds__(kGprThreads, 2)
   // on each other.
   const float a2 = -0.5f * kLog2e * xnorm;
   float esum[4] = {0.f, 0.f, 0.f, 0.f}, ecmp[4] = {0.f, 0.f, 0.f, 0.f};
-  const uint32_t id1 = instr_desc(kRows, kTileK), id2 = instr_desc(kRows, kDP);
+  // N = 128: [mh; ml] (GEMM1) or [mhT; mlT] (GEMM2); N = 64: mh or mhT alone
+  const uint32_t id_pair = instr_desc(kRows, 128), id1 = instr_desc(kRows, kTileK),
+                 id2 = instr_desc(kRows, kDP);
   uint32_t ph_a = 0, ph_b = 0, ph_g1 = 0, ph_g2 = 0;
   bool pend_a = false, pend_b = false, pend_g1 = false, pend_g2 = false;
   bool ok = true;
@@ -155,16 +169,16 @@ __global__ void __launch_bounds__(kGprThreads, 2)
       pend_a = false;
     }
     if (!__syncthreads_and(ok)) break;
-    // GEMM1: C1[128 x 64] = xh.mh + xh.ml + xl.mh over K = 64 (4 steps of 16)
+    // GEMM1: C1[:, 0:64] + C1[:, 64:128] = xh.mh + xh.ml + xl.mh over K = 64
+    // (4 steps of 16): xh.[mh; ml] into both halves, then xl.mh into the first
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t a_off[3] = {kOffXh, kOffXh, kOffXl};
-      const uint32_t b_off[3] = {kOffMh, kOffMl, kOffMh};
-      for (int p = 0; p < 3; ++p)
+      const uint32_t a_off[2] = {kOffXh, kOffXl};
+      for (int p = 0; p < 2; ++p)
         for (int kk = 0; kk < kDP / 16; ++kk) {
           const uint64_t ad = smem_desc(s_base + a_off[p] + kk * 256, 128, (kDP / 8) * 128);
-          const uint64_t bd = smem_desc(s_base + b_off[p] + kk * 256, 128, (kDP / 8) * 128);
-          umma(tC1, ad, bd, id1, (p > 0 || kk > 0) ? 1u : 0u);
+          const uint64_t bd = smem_desc(s_base + kOffMh + kk * 256, 128, (kDP / 8) * 128);
+          umma(tC1, ad, bd, p == 0 ? id_pair : id1, (p > 0 || kk > 0) ? 1u : 0u);
         }
       umma_commit(bar_g1);
     }
@@ -184,7 +198,7 @@ __global__ void __launch_bounds__(kGprThreads, 2)
 #pragma unroll 1
     for (int cc = kHalfBlocks * half; cc < kHalfBlocks * (half + 1); ++cc) {
       float v[32];
-      tmem_ld32(tC1 + lane_base + cc * 32, v);
+      tmem_ld32_sum2(tC1 + lane_base + cc * 32, kTileK, v);
 #pragma unroll
       for (int g = 0; g < 4; ++g) {
         uint32_t hpk[4], lpk[4];
@@ -227,16 +241,16 @@ __global__ void __launch_bounds__(kGprThreads, 2)
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     if (!__syncthreads_and(ok)) break;
-    // GEMM2: C2[128 x 64] += wh.mhT + wh.mlT + wl.mhT over K = 64 (4 steps of 16)
+    // GEMM2: C2[:, 0:64] + C2[:, 64:128] += wh.mhT + wh.mlT + wl.mhT over
+    // K = 64 (4 steps of 16): wh.[mhT; mlT] into both halves, wl.mhT into the first
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t a_off[3] = {kOffWh, kOffWh, kOffWl};
-      const uint32_t b_off[3] = {kOffMhT, kOffMlT, kOffMhT};
-      for (int p = 0; p < 3; ++p)
+      const uint32_t a_off[2] = {kOffWh, kOffWl};
+      for (int p = 0; p < 2; ++p)
         for (int kk = 0; kk < kTileK / 16; ++kk) {
           const uint64_t ad = smem_desc(s_base + a_off[p] + kk * 256, 128, (kTileK / 8) * 128);
-          const uint64_t bd = smem_desc(s_base + b_off[p] + kk * 256, 128, (kTileK / 8) * 128);
-          umma(tC2, ad, bd, id2, (t > 0 || p > 0 || kk > 0) ? 1u : 0u);
+          const uint64_t bd = smem_desc(s_base + kOffMhT + kk * 256, 128, (kTileK / 8) * 128);
+          umma(tC2, ad, bd, p == 0 ? id_pair : id2, (t > 0 || p > 0 || kk > 0) ? 1u : 0u);
         }
       umma_commit(bar_g2);
     }
@@ -262,7 +276,7 @@ __global__ void __launch_bounds__(kGprThreads, 2)
     __syncthreads();
     const double etot = ep[row];
     float c2[32];
-    tmem_ld32(tC2 + lane_base + half * 32, c2);
+    tmem_ld32_sum2(tC2 + lane_base + half * 32, kDP, c2);
     if (i < N) {
       if (half == 0) e_out[i] = etot;
       const float ef = (float)etot;

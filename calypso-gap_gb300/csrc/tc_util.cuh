@@ -103,6 +103,30 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
 }
 
+// v = (32 columns at taddr) + (32 columns at taddr + off): the two halves of
+// an accumulator whose products were split across column blocks; both loads
+// are in flight before the one wait
+__device__ __forceinline__ void tmem_ld32_sum2(uint32_t taddr, uint32_t off, float *v) {
+  uint32_t r[32], s[32];
+#define GAPGB_LD32(dst, addr)                                                                     \
+  asm volatile(                                                                                  \
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"   \
+      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"         \
+      : "=r"(dst[0]), "=r"(dst[1]), "=r"(dst[2]), "=r"(dst[3]), "=r"(dst[4]), "=r"(dst[5]),     \
+        "=r"(dst[6]), "=r"(dst[7]), "=r"(dst[8]), "=r"(dst[9]), "=r"(dst[10]), "=r"(dst[11]),   \
+        "=r"(dst[12]), "=r"(dst[13]), "=r"(dst[14]), "=r"(dst[15]), "=r"(dst[16]),             \
+        "=r"(dst[17]), "=r"(dst[18]), "=r"(dst[19]), "=r"(dst[20]), "=r"(dst[21]),             \
+        "=r"(dst[22]), "=r"(dst[23]), "=r"(dst[24]), "=r"(dst[25]), "=r"(dst[26]),             \
+        "=r"(dst[27]), "=r"(dst[28]), "=r"(dst[29]), "=r"(dst[30]), "=r"(dst[31])              \
+      : "r"(addr))
+  GAPGB_LD32(r, taddr);
+  GAPGB_LD32(s, taddr + off);
+#undef GAPGB_LD32
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]) + __uint_as_float(s[q]);
+}
+
 constexpr float kLog2e = 1.4426950408889634f;
 
 // 2^x (PTX ex2.approx.ftz: relative error ~2^-22, flushes subnormal results)
