@@ -232,6 +232,9 @@ gapgb_status upload_model(gapgb_model *m) {
   GAPGB_CUDA_TRY(cudaMemcpy(m->d_coeff32, coeff32.data(), sizeof(float) * M, cudaMemcpyHostToDevice));
   GAPGB_CUDA_TRY(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
   for (auto &e : m->ev) GAPGB_CUDA_TRY(cudaEventCreate(&e));
+  GAPGB_CUDA_TRY(cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking));
+  GAPGB_CUDA_TRY(cudaEventCreateWithFlags(&m->ev_fork, cudaEventDisableTiming));
+  GAPGB_CUDA_TRY(cudaEventCreateWithFlags(&m->ev_join, cudaEventDisableTiming));
   const char *prof = std::getenv("GAPGB_PROFILE_STAGES");
   m->profile_stages = prof && prof[0] && prof[0] != '0';
   m->d_sf = d_sf;  // marks the model as uploaded
@@ -296,9 +299,53 @@ gapgb_status ensure_surrogate(gapgb_model *m, int N) {
   return GAPGB_OK;
 }
 
+// Two pipelines: atoms [0, h) on `st` and [h, N) on the model's side stream
+// (h a multiple of the 128-atom GPR tile), each running descriptors -> GPR ->
+// slot gradients, joined before the structure sums.  The halves touch
+// disjoint per-atom ranges of the workspace; the force scatter of both adds
+// into the one force array (FP64 atomics), zeroed before the fork.  The
+// fork / join are event waits, so the pair of streams is captured into a
+// CUDA graph like a single stream.
+constexpr int kSplitMinAtoms = 16384;
+
+bool split_applies(const gapgb_model *m, int N, int lgrad) {
+  return m->pipelines == 2 && !m->profile_stages && lgrad && N >= kSplitMinAtoms &&
+         (m->precision == GAPGB_PREC_TC || m->precision == GAPGB_PREC_TF32) &&
+         bwd_scatters_forces(m);
+}
+
+gapgb_status enqueue_split(gapgb_model *m, int S, int N, int cap, int capS,
+                           double *d_energy, double *d_force, double *d_stress,
+                           double *d_atom_e, cudaStream_t st) {
+  Workspace &ws = m->ws;
+  const bool tc = m->precision == GAPGB_PREC_TC;
+  gapgb_status s = tc ? build_tc_image(m) : build_tf32_image(m);  // first call only (allocates)
+  if (s) return s;
+  const int h = (N / 2) / 128 * 128;
+  cudaMemsetAsync(d_force, 0, sizeof(double) * 3 * (size_t)N, st);
+  cudaEventRecord(m->ev_fork, st);
+  cudaStreamWaitEvent(m->side, m->ev_fork, 0);
+  const int lo[2] = {0, h}, hi[2] = {h, N};
+  cudaStream_t ss[2] = {st, m->side};
+  for (int p = 0; p < 2; ++p) {
+    launch_wacsf_fwd<float>(m, ws, N, cap, capS, ss[p], lo[p], hi[p]);
+    if (tc) launch_gpr_tc(m, ws, N, ss[p], lo[p], hi[p]);
+    else launch_gpr_tf32(m, ws, N, ss[p], lo[p], hi[p]);
+    launch_wacsf_bwd<float>(m, ws, N, cap, capS, d_force, ss[p], lo[p], hi[p], false);
+  }
+  cudaEventRecord(m->ev_join, m->side);
+  cudaStreamWaitEvent(st, m->ev_join, 0);
+  launch_struct_reduce(ws, S, 1, d_energy, d_stress, d_atom_e, N, st);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(GAPGB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  return GAPGB_OK;
+}
+
 gapgb_status enqueue_tail(gapgb_model *m, int S, int N, int cap, int capS, int lgrad,
                           const int *d_species, double *d_energy, double *d_force,
                           double *d_stress, double *d_atom_e, cudaStream_t st) {
+  if (split_applies(m, N, lgrad))
+    return enqueue_split(m, S, N, cap, capS, d_energy, d_force, d_stress, d_atom_e, st);
   Workspace &ws = m->ws;
   const bool prof = m->profile_stages;
   // reverse slots serve the force gather only
@@ -638,7 +685,10 @@ void gapgb_model_free(gapgb_model *m) {
   variance_free(m->var);
   for (auto &e : m->ev)
     if (e) cudaEventDestroy(e);
+  if (m->ev_fork) cudaEventDestroy(m->ev_fork);
+  if (m->ev_join) cudaEventDestroy(m->ev_join);
   if (m->stream) cudaStreamDestroy(m->stream);
+  if (m->side) cudaStreamDestroy(m->side);
   delete m;
 }
 
@@ -701,6 +751,10 @@ gapgb_status gapgb_set_option(gapgb_model *m, gapgb_option opt, int64_t value) {
     case GAPGB_OPT_GENERIC_KERNELS:
       m->generic_kernels = value != 0;
       return GAPGB_OK;
+    case GAPGB_OPT_PIPELINES:
+      if (value != 1 && value != 2) return fail(GAPGB_ERR_ARG, "pipelines must be 1 or 2");
+      m->pipelines = (int)value;
+      return GAPGB_OK;
   }
   return fail(GAPGB_ERR_ARG, "unknown option");
 }
@@ -712,6 +766,7 @@ gapgb_status gapgb_get_option(const gapgb_model *m, gapgb_option opt, int64_t *v
     case GAPGB_OPT_NEIGHBOUR_CAP: *value = m->cap; return GAPGB_OK;
     case GAPGB_OPT_DEVICE: *value = m->device; return GAPGB_OK;
     case GAPGB_OPT_GENERIC_KERNELS: *value = m->generic_kernels ? 1 : 0; return GAPGB_OK;
+    case GAPGB_OPT_PIPELINES: *value = m->pipelines; return GAPGB_OK;
   }
   return fail(GAPGB_ERR_ARG, "unknown option");
 }

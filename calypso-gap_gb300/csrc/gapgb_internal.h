@@ -326,6 +326,9 @@ struct gapgb_model {
   bool generic_kernels = false;        // force the generic FP32 descriptor kernels
   cudaStream_t stream = nullptr;       // internal stream of the host-buffer calls
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  int pipelines = 2;                   // GAPGB_OPT_PIPELINES
+  cudaStream_t side = nullptr;         // second pipeline's stream
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;  // no timing
   bool profile_stages = false;
   float stage_ms[4] = {0, 0, 0, 0};
   gapgb::Workspace ws;
@@ -391,20 +394,27 @@ void launch_neighbors(Workspace &ws, int S, int N, int max_atoms, int cap, doubl
                       cudaStream_t st, bool exact = true);
 void launch_reverse(Workspace &ws, int N, int cap, cudaStream_t st);
 void launch_refresh(Workspace &ws, int N, int cap, cudaStream_t st, bool exact = true);
+// [a0, a1) restricts the grouped FP32 kernels to a range of atoms (a1 < 0:
+// up to N); the generic and FP64 kernels take the whole batch
 template <typename T>
 void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int cap_smem,
-                      cudaStream_t st);
+                      cudaStream_t st, int a0 = 0, int a1 = -1);
 // whether the FP32 gradient kernel of this model scatters the forces itself
 // (the reverse slots are then not needed)
 bool bwd_scatters_forces(const gapgb_model *m);
 // returns true when the kernel scattered the forces into d_force itself
 // (grouped FP32 kernels); otherwise launch_forces gathers the slot gradients
+// (zero_force: clear d_force first; a range call leaves that to its caller)
 template <typename T>
 bool launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int cap_smem,
-                      double *d_force, cudaStream_t st);
+                      double *d_force, cudaStream_t st, int a0 = 0, int a1 = -1,
+                      bool zero_force = true);
 template <typename T, typename TG>
 void launch_gpr(const gapgb_model *m, Workspace &ws, int N, cudaStream_t st);
-void launch_gpr_tc(gapgb_model *m, Workspace &ws, int N, cudaStream_t st);
+// the tensor-core GPRs over atoms [a0, a1) of an N-atom batch (a0 a multiple
+// of 128; a1 < 0: up to N)
+void launch_gpr_tc(gapgb_model *m, Workspace &ws, int N, cudaStream_t st, int a0 = 0,
+                   int a1 = -1);
 template <typename T>
 void launch_forces(Workspace &ws, int N, int cap, double *d_force, cudaStream_t st);
 void launch_struct_reduce(Workspace &ws, int S, int lgrad, double *d_energy, double *d_stress,
@@ -420,7 +430,8 @@ gapgb_status build_tc_image(gapgb_model *m, bool refresh = false);
 size_t tc_atom_scratch_bytes(int N);
 gapgb_status build_tf32_image(gapgb_model *m, bool refresh = false);
 size_t tf32_atom_scratch_bytes(int N);
-void launch_gpr_tf32(gapgb_model *m, Workspace &ws, int N, cudaStream_t st);
+void launch_gpr_tf32(gapgb_model *m, Workspace &ws, int N, cudaStream_t st, int a0 = 0,
+                     int a1 = -1);
 void launch_gpr_rows(const gapgb_model *m, Workspace &ws, int cap, const int *d_rows,
                      const int *d_count, void *scratch, cudaStream_t st);
 size_t gpr_rows_scratch_bytes(int cap, int D);

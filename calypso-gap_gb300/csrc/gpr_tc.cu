@@ -418,19 +418,25 @@ size_t tc_atom_scratch_bytes(int N) {
   return tiles * kImgAtoms + (size_t)N * kDP * sizeof(float) + (size_t)N * sizeof(float) + 1024;
 }
 
-void launch_gpr_tc(gapgb_model *m, Workspace &ws, int N, cudaStream_t st) {
+void launch_gpr_tc(gapgb_model *m, Workspace &ws, int N, cudaStream_t st, int a0, int a1) {
   const int D = m->host.D;
+  if (a1 < 0) a1 = N;
+  // the scratch layout is the whole batch's; the range's atoms start at tile a0 / 128
   const int tiles = (N + kRows - 1) / kRows;
   unsigned char *img_atoms = reinterpret_cast<unsigned char *>(ws.tc_scratch);
   float *xs = reinterpret_cast<float *>(img_atoms + (size_t)tiles * kImgAtoms);
   float *xn = xs + (size_t)N * kDP;
   const float *mu = reinterpret_cast<const float *>((const unsigned char *)m->d_tc + m->tc_bytes);
-  k_tc_prep_atoms<<<(tiles * kRows + 127) / 128, 128, 0, st>>>(N, D, (const float *)ws.G,
-                                                                m->d_invth32, mu, xs, xn, img_atoms);
+  const int n = a1 - a0, t0 = a0 / kRows, ct = (n + kRows - 1) / kRows;
+  if (n <= 0) return;
+  unsigned char *img_r = img_atoms + (size_t)t0 * kImgAtoms;
+  float *xs_r = xs + (size_t)a0 * kDP, *xn_r = xn + a0;
+  k_tc_prep_atoms<<<(ct * kRows + 127) / 128, 128, 0, st>>>(
+      n, D, (const float *)ws.G + (size_t)a0 * D, m->d_invth32, mu, xs_r, xn_r, img_r);
   kernel_smem((const void *)k_gpr_tc, kSmemBytes, true);
-  k_gpr_tc<<<tiles, kGprThreads, kSmemBytes, st>>>(N, m->tc_tiles, (const unsigned char *)m->d_tc,
-                                          img_atoms, xs, xn, m->d_invth32, D, ws.e,
-                                          (float *)ws.dedg, ws.d_flags);
+  k_gpr_tc<<<ct, kGprThreads, kSmemBytes, st>>>(n, m->tc_tiles, (const unsigned char *)m->d_tc,
+                                                img_r, xs_r, xn_r, m->d_invth32, D, ws.e + a0,
+                                                (float *)ws.dedg + (size_t)a0 * D, ws.d_flags);
 }
 
 }  // namespace gapgb

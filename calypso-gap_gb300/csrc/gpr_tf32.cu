@@ -350,20 +350,25 @@ size_t tf32_atom_scratch_bytes(int N) {
   return tiles * kXBytes + (size_t)N * kDP * sizeof(float) + (size_t)N * sizeof(float) + 256;
 }
 
-void launch_gpr_tf32(gapgb_model *m, Workspace &ws, int N, cudaStream_t st) {
+void launch_gpr_tf32(gapgb_model *m, Workspace &ws, int N, cudaStream_t st, int a0, int a1) {
   const int D = m->host.D;
+  if (a1 < 0) a1 = N;
+  // the scratch layout is the whole batch's; the range's atoms start at tile a0 / 128
   const int tiles = (N + kRows - 1) / kRows;
   unsigned char *img_atoms = reinterpret_cast<unsigned char *>(ws.tc_scratch);
   float *xs = reinterpret_cast<float *>(img_atoms + (size_t)tiles * kXBytes);
   float *xn = xs + (size_t)N * kDP;
   const float *mu = reinterpret_cast<const float *>((const unsigned char *)m->d_tf32 + m->tf32_bytes);
-  k_tf32_prep_atoms<<<(tiles * kRows + 127) / 128, 128, 0, st>>>(N, D, (const float *)ws.G,
-                                                                  m->d_invth32, mu, xs, xn,
-                                                                  img_atoms);
+  const int n = a1 - a0, t0 = a0 / kRows, ct = (n + kRows - 1) / kRows;
+  if (n <= 0) return;
+  unsigned char *img_r = img_atoms + (size_t)t0 * kXBytes;
+  float *xs_r = xs + (size_t)a0 * kDP, *xn_r = xn + a0;
+  k_tf32_prep_atoms<<<(ct * kRows + 127) / 128, 128, 0, st>>>(
+      n, D, (const float *)ws.G + (size_t)a0 * D, m->d_invth32, mu, xs_r, xn_r, img_r);
   kernel_smem((const void *)k_gpr_tf32, kSmem, true);
-  k_gpr_tf32<<<tiles, kThreads, kSmem, st>>>(N, m->tf32_tiles, (const unsigned char *)m->d_tf32,
-                                             img_atoms, xs, xn, m->d_invth32, D, ws.e,
-                                             (float *)ws.dedg, ws.d_flags);
+  k_gpr_tf32<<<ct, kThreads, kSmem, st>>>(n, m->tf32_tiles, (const unsigned char *)m->d_tf32,
+                                          img_r, xs_r, xn_r, m->d_invth32, D, ws.e + a0,
+                                          (float *)ws.dedg + (size_t)a0 * D, ws.d_flags);
 }
 
 }  // namespace gapgb

@@ -509,10 +509,13 @@ const SFT<float> *sft_of<float>(const gapgb_model *m) { return m->d_sft32; }
 
 template <typename T>
 void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int capS,
-                      cudaStream_t st) {
+                      cudaStream_t st, int a0, int a1) {
   const size_t smem = wacsf_smem_bytes(m->sfh, capS, true, sizeof(T));
+  if (a1 < 0) a1 = N;
+  const int D = m->sfh.D;
   if (m->sfh.D > 2 * m->sfh.nsf || m->sfh.nrad + m->sfh.nang < m->sfh.nsf)
-    cudaMemsetAsync(ws.G, 0, sizeof(T) * (size_t)N * m->sfh.D, st);  // never-written entries
+    cudaMemsetAsync((T *)ws.G + (size_t)a0 * D, 0, sizeof(T) * (size_t)(a1 - a0) * D,
+                    st);  // never-written entries
   if constexpr (std::is_same<T, float>::value) {
     GrpFwd gf;
     GrpBwd gb;
@@ -521,11 +524,16 @@ void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
                          (size_t)kWarpsPerBlock * 4 *
                              grp_warp_floats(capS, m->sfh.nrc, m->sfh.D, m->sfh.nrad, true);
       kernel_smem((const void *)gf, (int)smg, true);
-      const int grid = warp_grid(N, smg, (const void *)gf);
-      gf<<<grid, 32 * kWarpsPerBlock, smg, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
-                                                   ws.apos, ws.nbr_d32, ws.nbr_w32, m->d_sft32,
-                                                   (float *)ws.G, ws.pairs, ws.pair_cnt,
-                                                   capS <= 256 ? kPairCap : 0);
+      const int n = a1 - a0;
+      if (n <= 0) return;
+      const int grid = warp_grid(n, smg, (const void *)gf);
+      // atoms [a0, a1) through per-atom arrays offset to a0
+      const int pcap = capS <= 256 ? kPairCap : 0;
+      gf<<<grid, 32 * kWarpsPerBlock, smg, st>>>(
+          n, cap, capS, ws.nbr_cnt + a0, ws.nbr_xyz, ws.nbr_j, ws.apos,
+          ws.nbr_d32 + (size_t)a0 * cap, ws.nbr_w32 + (size_t)a0 * cap, m->d_sft32,
+          (float *)ws.G + (size_t)a0 * D, ws.pairs + (size_t)a0 * kPairCap, ws.pair_cnt + a0,
+          pcap);
       return;
     }
   }
@@ -546,8 +554,9 @@ bool bwd_scatters_forces(const gapgb_model *m) {
 
 template <typename T>
 bool launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int capS,
-                      double *d_force, cudaStream_t st) {
+                      double *d_force, cudaStream_t st, int a0, int a1, bool zero_force) {
   const size_t smem = wacsf_smem_bytes(m->sfh, capS, false, sizeof(T));
+  if (a1 < 0) a1 = N;
   if constexpr (std::is_same<T, float>::value) {
     GrpFwd gf;
     GrpBwd gb;
@@ -556,13 +565,19 @@ bool launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
                          (size_t)kWarpsPerBlock * 4 *
                              grp_warp_floats(capS, m->sfh.nrc, m->sfh.D, m->sfh.nrad, false);
       kernel_smem((const void *)gb, (int)smg, true);
-      const int grid = warp_grid(N, smg, (const void *)gb);
-      cudaMemsetAsync(d_force, 0, sizeof(double) * 3 * (size_t)N, st);
-      gb<<<grid, 32 * kWarpsPerBlock, smg, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
-                                                   ws.apos, ws.nbr_d32, ws.nbr_w32, m->d_sft32,
-                                                   (const float *)ws.dedg, d_force, ws.wvir,
-                                                   ws.pairs, ws.pair_cnt,
-                                                   capS <= 256 ? kPairCap : 0);
+      if (zero_force) cudaMemsetAsync(d_force, 0, sizeof(double) * 3 * (size_t)N, st);
+      const int n = a1 - a0;
+      if (n <= 0) return true;
+      const int grid = warp_grid(n, smg, (const void *)gb);
+      // atoms [a0, a1) through per-atom arrays offset to a0; the partner
+      // indices (nbr_j) and the force array stay global
+      const int D = m->sfh.D;
+      const int pcap = capS <= 256 ? kPairCap : 0;
+      gb<<<grid, 32 * kWarpsPerBlock, smg, st>>>(
+          n, a0, cap, capS, ws.nbr_cnt + a0, ws.nbr_xyz, ws.nbr_j + (size_t)a0 * cap, ws.apos,
+          ws.nbr_d32 + (size_t)a0 * cap, ws.nbr_w32 + (size_t)a0 * cap, m->d_sft32,
+          (const float *)ws.dedg + (size_t)a0 * D, d_force, ws.wvir + (size_t)a0 * 9,
+          ws.pairs + (size_t)a0 * kPairCap, ws.pair_cnt + a0, pcap);
       return true;  // forces scattered by the kernel
     }
   }
@@ -577,11 +592,13 @@ bool launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
   return false;  // slot gradients in ws.gslot: launch_forces gathers them
 }
 
-template void launch_wacsf_fwd<double>(const gapgb_model *, Workspace &, int, int, int, cudaStream_t);
-template void launch_wacsf_fwd<float>(const gapgb_model *, Workspace &, int, int, int, cudaStream_t);
+template void launch_wacsf_fwd<double>(const gapgb_model *, Workspace &, int, int, int, cudaStream_t,
+                                       int, int);
+template void launch_wacsf_fwd<float>(const gapgb_model *, Workspace &, int, int, int, cudaStream_t,
+                                      int, int);
 template bool launch_wacsf_bwd<double>(const gapgb_model *, Workspace &, int, int, int, double *,
-                                       cudaStream_t);
+                                       cudaStream_t, int, int, bool);
 template bool launch_wacsf_bwd<float>(const gapgb_model *, Workspace &, int, int, int, double *,
-                                      cudaStream_t);
+                                      cudaStream_t, int, int, bool);
 
 }  // namespace gapgb

@@ -553,7 +553,7 @@ __device__ __forceinline__ void pair_grad(const GLay &L, const float4 &Aj, const
 //    the j side by a segmented warp scan.
 template <int NAL, int NC, bool STD>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
-    k_wacsf_bwd_grp(int N, int cap, int capS, const int *__restrict__ cnt,
+    k_wacsf_bwd_grp(int N, int i0, int cap, int capS, const int *__restrict__ cnt,
                     const double4 *__restrict__ xyzr, const int *__restrict__ nj,
                     const double4 *__restrict__ apos, const float4 *__restrict__ d32,
                     const float *__restrict__ w32, const SFT<float> *__restrict__ sfg,
@@ -740,10 +740,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
     fx = warp_sum<float>(fx);
     fy = warp_sum<float>(fy);
     fz = warp_sum<float>(fz);
-    if (lane == 0) {
-      atomicAdd(force + (size_t)i * 3 + 0, (double)fx);
-      atomicAdd(force + (size_t)i * 3 + 1, (double)fy);
-      atomicAdd(force + (size_t)i * 3 + 2, (double)fz);
+    if (lane == 0) {  // atom i's own force: index i0 + i of the whole batch
+      atomicAdd(force + (size_t)(i0 + i) * 3 + 0, (double)fx);
+      atomicAdd(force + (size_t)(i0 + i) * 3 + 1, (double)fy);
+      atomicAdd(force + (size_t)(i0 + i) * 3 + 2, (double)fz);
     }
     // per-atom virial in FP32 (a sum over its own slots); the sums over
     // atoms are FP64 (k_struct_reduce)

@@ -12,7 +12,7 @@ import numpy as np
 from . import build as _build
 
 PREC_FP64, PREC_FP32, PREC_TC, PREC_MIXED, PREC_SURROGATE, PREC_TF32 = 0, 1, 2, 3, 4, 5
-OPT_PRECISION, OPT_NEIGHBOUR_CAP, OPT_DEVICE = 0, 1, 2
+OPT_PRECISION, OPT_NEIGHBOUR_CAP, OPT_DEVICE, OPT_GENERIC_KERNELS, OPT_PIPELINES = 0, 1, 2, 3, 4
 PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "tc": PREC_TC, "mixed": PREC_MIXED,
               "surrogate": PREC_SURROGATE, "tf32": PREC_TF32}
 
@@ -281,6 +281,11 @@ class GapModel:
 
     def set_neighbour_cap(self, cap):
         _check(load().gapgb_set_option(self._h, OPT_NEIGHBOUR_CAP, int(cap)), "gapgb_set_option")
+
+    def set_pipelines(self, n):
+        """1: one stream; 2 (default): large TC / TF32 batches run as two
+        halves on two streams (GAPGB_OPT_PIPELINES)."""
+        _check(load().gapgb_set_option(self._h, OPT_PIPELINES, int(n)), "gapgb_set_option")
 
     def get_option(self, opt):
         v = C.c_int64()

@@ -7,7 +7,11 @@ For a calibration batch it evaluates every candidate configuration:
     ones (GAPGB_OPT_GENERIC_KERNELS);
   - neighbour capacity: the tight bound (the largest count rounded up to 8)
     or 25 % headroom.  The capacity sets the per-warp shared-memory tiles of
-    the descriptor kernels, hence their occupancy.
+    the descriptor kernels, hence their occupancy;
+  - pipelines (GAPGB_OPT_PIPELINES): one stream, or two halves of the batch
+    on two streams, for the tensor-core forms with the grouped kernels on a
+    calibration batch of at least 16384 atoms (below that the library runs
+    one stream whatever the option).
 It keeps the candidates whose energies and forces lie within `tol_e`
 eV/atom and `tol_f` eV/A of the plain FP64 path (the drop-in parity path),
 times them on the device-buffer path, and applies the fastest to the model.
@@ -21,12 +25,13 @@ import time
 
 import numpy as np
 
-from . import GapModel, OPT_NEIGHBOUR_CAP, load
+from . import GapModel, OPT_GENERIC_KERNELS, OPT_NEIGHBOUR_CAP, OPT_PIPELINES, load
 
-OPT_GENERIC_KERNELS = 3
 # every precision form the tuner can return: the timed candidates, and the
 # plain FP64 path when no candidate passes the error gates
 FORMS = ("tc", "tf32", "fp32", "mixed", "fp64")
+# smallest batch the library splits into two pipelines (api.cu kSplitMinAtoms)
+SPLIT_MIN_ATOMS = 16384
 
 
 def _signature(model, off, device_name):
@@ -81,42 +86,47 @@ def autotune(model, off, species, lat, pos, tol_e=1e-3, tol_f=20e-3, reps=5, cac
     t_S = torch.zeros(S, 6, dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream(dev)
     results = []
+    grid = []
     for form in forms:
         for generic in (0, 1):
             for cap in caps:
-                cfg = {"precision": form, "generic_kernels": generic, "cap": cap}
-                _apply(model, cfg)
-                E, F, _ = model.eval_batch(off, species, lat, pos)
-                de = float(np.max(np.abs(E - E64) / natoms))
-                df = float(np.max(np.abs(F - F64)))
-                cfg.update(dE_per_atom=de, dF=df)
-                if de > tol_e or df > tol_f:
-                    cfg["ms"] = None
-                    results.append(cfg)
-                    continue
+                split = form in ("tc", "tf32") and generic == 0 and N >= SPLIT_MIN_ATOMS
+                for pipes in ((1, 2) if split else (1,)):
+                    grid.append({"precision": form, "generic_kernels": generic, "cap": cap,
+                                 "pipelines": pipes})
+    for cfg in grid:
+        _apply(model, cfg)
+        E, F, _ = model.eval_batch(off, species, lat, pos)
+        de = float(np.max(np.abs(E - E64) / natoms))
+        df = float(np.max(np.abs(F - F64)))
+        cfg.update(dE_per_atom=de, dF=df)
+        if de > tol_e or df > tol_f:
+            cfg["ms"] = None
+            results.append(cfg)
+            continue
 
-                def run():
-                    model.eval_batch_ptrs(S, N, int(natoms.max()), t_off.data_ptr(),
-                                          t_sp.data_ptr(), t_lat.data_ptr(), t_pos.data_ptr(), 1,
-                                          t_E.data_ptr(), t_F.data_ptr(), t_S.data_ptr(), 0,
-                                          stream.cuda_stream)
-                run()
-                model.check_device_status()
-                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record(stream)
-                for _ in range(reps):
-                    run()
-                b.record(stream)
-                torch.cuda.synchronize()
-                model.check_device_status()
-                cfg["ms"] = a.elapsed_time(b) / reps
-                results.append(cfg)
-                if verbose:
-                    print("autotune", cfg)
+        def run():
+            model.eval_batch_ptrs(S, N, int(natoms.max()), t_off.data_ptr(),
+                                  t_sp.data_ptr(), t_lat.data_ptr(), t_pos.data_ptr(), 1,
+                                  t_E.data_ptr(), t_F.data_ptr(), t_S.data_ptr(), 0,
+                                  stream.cuda_stream)
+        run()
+        model.check_device_status()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            run()
+        b.record(stream)
+        torch.cuda.synchronize()
+        model.check_device_status()
+        cfg["ms"] = a.elapsed_time(b) / reps
+        results.append(cfg)
+        if verbose:
+            print("autotune", cfg)
     ok = [r for r in results if r["ms"] is not None]
     if not ok:
-        best = {"precision": "fp64", "generic_kernels": 0, "cap": caps[-1], "dE_per_atom": 0.0,
-                "dF": 0.0, "ms": None}
+        best = {"precision": "fp64", "generic_kernels": 0, "cap": caps[-1], "pipelines": 2,
+                "dE_per_atom": 0.0, "dF": 0.0, "ms": None}
     else:
         best = min(ok, key=lambda r: r["ms"])
     _apply(model, best)
@@ -133,4 +143,5 @@ def autotune(model, off, species, lat, pos, tol_e=1e-3, tol_f=20e-3, reps=5, cac
 def _apply(model, cfg):
     model.set_precision(cfg["precision"])
     load().gapgb_set_option(model.handle, OPT_GENERIC_KERNELS, int(cfg.get("generic_kernels", 0)))
+    load().gapgb_set_option(model.handle, OPT_PIPELINES, int(cfg.get("pipelines", 2)))
     model.set_neighbour_cap(int(cfg["cap"]))

@@ -62,8 +62,14 @@ typedef enum {
   GAPGB_OPT_NEIGHBOUR_CAP = 1, /* slots per atom, default 256; grown on overflow
                                   by the host-buffer calls */
   GAPGB_OPT_DEVICE = 2,        /* CUDA device ordinal, default 0 */
-  GAPGB_OPT_GENERIC_KERNELS = 3 /* 1: FP32 descriptor kernels take the generic
-                                   path even when the fast path applies */
+  GAPGB_OPT_GENERIC_KERNELS = 3, /* 1: FP32 descriptor kernels take the generic
+                                    path even when the fast path applies */
+  GAPGB_OPT_PIPELINES = 4        /* 1 or 2 (default 2): a batch of at least
+                                    16384 atoms in the TC / TF32 forms (grouped
+                                    descriptor kernels, gradients on) is
+                                    evaluated as two halves on two streams, so
+                                    one half's kernels fill the SMs the other
+                                    half's leave idle; results are the same */
 } gapgb_option;
 
 typedef struct gapgb_model gapgb_model;
