@@ -378,6 +378,20 @@ P_SLOTS = 56.0
 T_PAIRS = 690.0  # contributing angular pairs per atom on this workload
 
 
+def step_kernels(precision, natoms, generic=False, pipelines=2):
+    """Kernels the library launches per evaluation with gradients: prep x2
+    and the neighbour build; per pipeline the descriptors, the GPR (tensor-core
+    forms: operand prep + kernel; SIMT forms: kernel + split reduce) and the
+    slot gradients (the grouped kernel scatters the forces itself); then the
+    structure partial and final sums.  Tensor-core batches of at least the
+    library's split threshold run two pipelines; the generic descriptor
+    kernels add the reverse slots, the force gather and the orphans."""
+    from gapgb.tune import SPLIT_MIN_ATOMS
+    two = (pipelines == 2 and precision in ("tc", "tf32") and not generic
+           and natoms >= SPLIT_MIN_ATOMS)
+    return 3 + 4 * (2 if two else 1) + 2 + (3 if generic else 0)
+
+
 def stage_bytes_per_atom(D, P=P_SLOTS, T=T_PAIRS):
     return {"neighbours": 32.0 + P * 28.0,
             "descriptors": P * 20.0 + D * 4.0 + T * 2.0,
@@ -420,6 +434,9 @@ def roofline(stages, N, D, precision, simt=None, plain_stages=None, P=P_SLOTS, T
                     "chain_rule_fp32 give their arithmetic rate against the measured FP32 "
                     "FMA rate",
             "stage_ms": {n: float(s) for n, s in zip(STAGES, stages)},
+            "stage_ms_note": "library stage events on one stream (the profiling path runs the "
+                             "stages in sequence); a timed tensor-core step of 16384 atoms or "
+                             "more runs two pipelines, so it is shorter than their sum",
             "algorithmic_bytes_per_atom": bpa[name]}
     # FP32 arithmetic of the chain-rule / descriptor kernels (counted FLOPs per
     # angular pair and radial term, 32 SFs) against the measured FP32 FMA rate
@@ -640,7 +657,8 @@ def run_population(args):
             # one graph launch per step holding the 9 kernels of a grouped-kernel
             # evaluation (see the headline workload's count); the generic
             # kernels add the reverse slots, the force gather and the orphans
-            "gpu_launches": (12 if best["generic_kernels"] else 9) * args.steps}
+            "gpu_launches": step_kernels(best["precision"], N, bool(best["generic_kernels"]),
+                                         int(best.get("pipelines", 2))) * args.steps}
     m.close()
     line["cpu_baseline"] = population_cpu_baseline(
         (zt, wt, ty, al, rc, ze, theta, mm, coeff), pop, 256)
@@ -1070,10 +1088,12 @@ def run_md(args):
                           "dstress_max_GPa": float(np.abs(St - Sp).max())}},
             # per step: kick+drift, wrap or skin check, prep x2, refresh,
             # descriptors, tensor-core GPR (prep + kernel), slot gradients with
-            # the force scatter, structure sums x2, kick, kinetic sums x2 = 14; a
-            # rebuild step adds the build, the bins (offsets, count, scan, fill)
-            # and the binned build in place of the refresh (+5)
-            "gpu_launches": 14 * args.md_steps + 5 * (args.md_steps // 10),
+            # the force scatter, structure sums x2, kick, kinetic sums x2 = 14,
+            # plus 4 for the second pipeline of a large batch; a rebuild step
+            # adds the build, the bins (offsets, count, scan, fill) and the
+            # binned build in place of the refresh (+5)
+            "gpu_launches": (14 + step_kernels("tc", N) - 9) * args.md_steps
+                            + 5 * (args.md_steps // 10),
             "clocks": tc["clocks"]}
     print(json.dumps(line), flush=True)
 
@@ -1147,7 +1167,7 @@ def run_precision(args):
             "config": {"workload": "precision forms on alloy512 x %d (D=64, M=4000)" % S,
                        "atoms": N, "l2": "flushed between steps (512 MB write)"},
             "forms": res, "errors_vs_oracle": orc,
-            "gpu_launches": 9 * args.steps}
+            "gpu_launches": step_kernels("tc", N) * args.steps}
     print(json.dumps(line), flush=True)
 
 
@@ -1513,11 +1533,8 @@ def main():
     }
     if gather is not None:
         line["gather_to_rank0"] = gather
-    # kernels launched per step (count from the library's launch sequence):
-    # prep x2, neighbour build, descriptors, GPR (tensor-core form: operand
-    # prep + kernel; SIMT forms: kernel + split reduce), slot gradients (the
-    # grouped kernel scatters the forces itself), structure partial + final sums
-    line["gpu_launches"] = args.steps * 9
+    # kernels launched per step (count from the library's launch sequence)
+    line["gpu_launches"] = args.steps * step_kernels(args.precision, N)
     if world == 1:
         line["cpu_baseline"] = cpu_baseline(arrays)
         line["dropin_latency_ms"] = dropin_latency()

@@ -84,3 +84,12 @@ def test_default_batch_is_one_gpr_wave(monkeypatch):
     assert bench.default_batch(args, 0) == 76  # 152 SMs x 2 CTAs x 128 atoms / 512
     args = types.SimpleNamespace(batch=64)
     assert bench.default_batch(args, 0) == 64  # an explicit --batch wins
+
+
+def test_step_kernel_counts():
+    # prep x2, neighbour build, structure sums x2, and 4 per pipeline
+    assert bench.step_kernels("tc", 38912) == 13        # two pipelines
+    assert bench.step_kernels("tc", 38912, pipelines=1) == 9
+    assert bench.step_kernels("tc", 8192) == 9          # below the split threshold
+    assert bench.step_kernels("fp32", 38912) == 9       # SIMT forms run one pipeline
+    assert bench.step_kernels("tf32", 10 ** 6, generic=True) == 12
