@@ -289,8 +289,10 @@ __device__ __forceinline__ float screen_r2(const float *L32, const float fd[3], 
 
 constexpr int kQueue = 256;  // survivors per warp per exact-test round
 
+// five blocks per SM (96 registers, no spills): 0.221 -> 0.217 ms per 38 912
+// alloy atoms against four at 116 registers; six spill and take 0.33 ms
 template <bool EXACT>
-__global__ void __launch_bounds__(128) k_nbr_build(int N, int cap, double rcut,
+__global__ void __launch_bounds__(128, 5) k_nbr_build(int N, int cap, double rcut,
                                                    const double4 *__restrict__ apos,
                                                    const float4 *__restrict__ frac32,
                                                    const int *__restrict__ atom_struct,
