@@ -51,6 +51,9 @@ def parse():
                         "GPR, two 128-atom CTAs per SM: 76 alloy512 cells on 152 SMs)")
     p.add_argument("--precision", default="tc", choices=["fp32", "tc", "tf32", "fp64", "mixed"])
     p.add_argument("--no-oracle", action="store_true", help="skip the oracle error check")
+    p.add_argument("--pipelines", type=int, default=2, choices=[1, 2],
+                   help="alloy workload: GAPGB_OPT_PIPELINES of the timed model (2: a large "
+                        "tensor-core batch runs as two halves on two streams)")
     p.add_argument("--workload", default="alloy", choices=["alloy", "population", "surrogate", "md", "precision",
                                              "variance", "fit"],
                    help="alloy: 512-atom ternary fcc cells (the headline metric); population: "
@@ -1367,6 +1370,7 @@ def main():
         m = gapgb.GapModel.create(zt, wt, ty, al, rc, theta, mm, coeff, sf_zeta=ze)
         m.set_precision(prec)
         m.set_neighbour_cap(96)
+        m.set_pipelines(args.pipelines)
         return m
 
     structs, (off, sp, lat, pos) = workload(rank, default_batch(args, dev))
@@ -1521,7 +1525,8 @@ def main():
         "config": {"workload": "alloy512 ternary fcc (Z 13/28/40), D=64, M=4000",
                    "structures_per_step": S, "atoms_per_step_per_gpu": N,
                    "batch_rule": "one wave of the tensor-core GPR: 2 CTAs x 128 atoms per SM",
-                   "precision": args.precision, "l2": "flushed between steps (512 MB write)"},
+                   "precision": args.precision, "pipelines": args.pipelines,
+                   "l2": "flushed between steps (512 MB write)"},
         "e2e": {"value": world * N / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "plain_fp64": {"value": plain_value, "unit": UNIT, "ms_per_step": ms_plain},
@@ -1534,7 +1539,7 @@ def main():
     if gather is not None:
         line["gather_to_rank0"] = gather
     # kernels launched per step (count from the library's launch sequence)
-    line["gpu_launches"] = args.steps * step_kernels(args.precision, N)
+    line["gpu_launches"] = args.steps * step_kernels(args.precision, N, pipelines=args.pipelines)
     if world == 1:
         line["cpu_baseline"] = cpu_baseline(arrays)
         line["dropin_latency_ms"] = dropin_latency()

@@ -220,18 +220,18 @@ __device__ __forceinline__ void pair_stream(const float4 *__restrict__ A, int P,
     const int r2 = P - 2 - r;
     const int n1 = P - 1 - r;                // candidates of row r
     const int tot = r2 > r ? P : n1;         // with row r2's r + 1
-    // with Q = 128, two batches of 32 candidates per step: their loads and
-    // distances are independent, which hides the shared-memory latency of
-    // the screen
-    constexpr int NB = Q >= 128 ? 2 : 1;
+    // Q / 64 batches of 32 candidates per step (at most 31 + 32 Q / 64 < Q
+    // entries pending): their loads and distances are independent, which
+    // hides the shared-memory latency of the screen
+    constexpr int NB = Q / 64 > 0 ? Q / 64 : 1;
     for (int base = 0; base < tot; base += 32 * NB) {
-      int j0, k0, j1 = 0, k1 = 0;
-      float c0, c1 = 0.f;
-      const bool v0 = cand(r, r2, n1, tot, base + lane, j0, k0, c0);
-      bool v1 = false;
-      if constexpr (NB == 2) v1 = cand(r, r2, n1, tot, base + 32 + lane, j1, k1, c1);
-      push(v0, j0, k0, c0);
-      if constexpr (NB == 2) push(v1, j1, k1, c1);
+      int jb[NB], kb[NB];
+      float cb[NB];
+      bool vb[NB];
+#pragma unroll
+      for (int b = 0; b < NB; ++b) vb[b] = cand(r, r2, n1, tot, base + 32 * b + lane, jb[b], kb[b], cb[b]);
+#pragma unroll
+      for (int b = 0; b < NB; ++b) push(vb[b], jb[b], kb[b], cb[b]);
       __syncwarp();
       while (qn - qh >= 32) {
         const int e = (qh + lane) & (Q - 1);
