@@ -362,6 +362,14 @@ gapgb_status fit_enqueue(gapgb_model *m, int S, int N, int cap, int capS, const 
 // launch_cache.cpp: launch attributes set / queried once per device
 // (a larger shared-memory size raises the limit; the limit never shrinks)
 void kernel_smem(const void *fn, int bytes, bool max_carveout = false);
+// The surrogate's BF16 training GEMMs on the tensor cores (mlp_gemm_tc.cu):
+// C[z] = beta C[z] + opA[z] opB[z]^T with mlp.cu's strided operand view.
+// Returns false, launching nothing, when the shape or strides are outside
+// what it stages (then the SIMT kernel runs).
+bool mlp_gemm_tc(cudaStream_t st, int Z, int M, int N, int K, const __nv_bfloat16 *A, int sAm,
+                 int sAk, size_t zA, const __nv_bfloat16 *B, int sBn, int sBk, size_t zB,
+                 const int *tile_sp, size_t sBsp, float *C, int ldc, size_t zC, float beta,
+                 int *flags);
 int kernel_occupancy(const void *fn, int threads, size_t smem);
 int device_sms();
 

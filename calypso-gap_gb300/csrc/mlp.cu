@@ -47,6 +47,7 @@
 #include <cstring>
 #include <numeric>
 #include <random>
+#include <type_traits>
 #include <vector>
 
 #include "gapgb_internal.h"
@@ -450,6 +451,7 @@ struct gapgb_surrogate {
   size_t P = 0;  // parameters per (member, species) block
   size_t W1 = 0, b1 = 0, W2 = 0, b2 = 0, w3 = 0, b3 = 0;
   float *w = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr;
+  int *t_err = nullptr;  // error flags of the training GEMMs (bounded tensor-core waits)
   __nv_bfloat16 *w16 = nullptr;
   float *mu = nullptr, *isig = nullptr, *sd = nullptr, *e_shift = nullptr;
   int *zt = nullptr;
@@ -483,10 +485,18 @@ gapgb_status sfail(gapgb_status st, const std::string &msg) {
   return st;
 }
 
+// tc_flags: the error flags of the tensor-core form (mlp_gemm_tc.cu), which
+// takes BF16 x BF16 products when its shape and stride rules hold; null keeps
+// the SIMT kernel (FP32 operands, or row tiles that may straddle species)
 template <typename TA, typename TB>
 void gemm(cudaStream_t st, int Z, int M, int N, int K, const TA *A, int sAm, int sAk, size_t zA,
           const TB *B, int sBn, int sBk, size_t zB, const int *tile_sp, size_t sBsp, float *C,
-          int ldc, size_t zC, float beta) {
+          int ldc, size_t zC, float beta, int *tc_flags = nullptr) {
+  if constexpr (std::is_same<TA, __nv_bfloat16>::value && std::is_same<TB, __nv_bfloat16>::value) {
+    if (tc_flags && mlp_gemm_tc(st, Z, M, N, K, A, sAm, sAk, zA, B, sBn, sBk, zB, tile_sp, sBsp,
+                                C, ldc, zC, beta, tc_flags))
+      return;
+  }
   dim3 g((N + kTile - 1) / kTile, (M + kTile - 1) / kTile, Z);
   k_mlp_gemm<TA, TB><<<g, 256, 0, st>>>(M, N, K, A, sAm, sAk, zA, B, sBn, sBk, zB, tile_sp, sBsp, C,
                                         ldc, zC, beta);
@@ -560,14 +570,16 @@ gapgb_status ensure_atoms(gapgb_surrogate *s, int N) {
 // Forward over `rows` rows per member (s->X filled); y and, with want_grad,
 // the input gradient Gx.  zX = 0 shares X across members (prediction).
 void forward(gapgb_surrogate *s, cudaStream_t st, int rows, const int *tile_sp, size_t zX,
-             bool want_grad) {
+             bool want_grad, int *tc_flags = nullptr) {
   const int D = s->D, H = s->H, Q = s->members;
   const size_t mstride = (size_t)s->nsp * s->P;  // member stride of the parameters
   const size_t zH = (size_t)rows * H, zD = (size_t)rows * D;
   RowMap rm{rows, s->nsp, s->P, tile_sp};
-  gemm(st, Q, rows, H, D, s->X, D, 1, zX, s->w16 + s->W1, D, 1, mstride, tile_sp, s->P, s->Z1, H, zH, 0.f);
+  gemm(st, Q, rows, H, D, s->X, D, 1, zX, s->w16 + s->W1, D, 1, mstride, tile_sp, s->P, s->Z1, H, zH,
+       0.f, tc_flags);
   k_mlp_bias_act<<<nblk(zH * Q), 256, 0, st>>>(rm, Q, H, s->b1, s->w, s->Z1, s->A1);
-  gemm(st, Q, rows, H, H, s->A1, H, 1, zH, s->w16 + s->W2, H, 1, mstride, tile_sp, s->P, s->Z2, H, zH, 0.f);
+  gemm(st, Q, rows, H, H, s->A1, H, 1, zH, s->w16 + s->W2, H, 1, mstride, tile_sp, s->P, s->Z2, H, zH,
+       0.f, tc_flags);
   k_mlp_bias_act<<<nblk(zH * Q), 256, 0, st>>>(rm, Q, H, s->b2, s->w, s->Z2, nullptr);
   k_mlp_out<<<nblk((size_t)rows * Q * 32), 256, 0, st>>>(rm, Q, H, s->w3, s->b3, s->w, s->Z2, s->y,
                                                          want_grad ? s->D2 : nullptr);
@@ -671,7 +683,10 @@ gapgb_status gapgb_surrogate_create(int nspecies, const int *species_z, int des_
   s->b2 = s->W2 + (size_t)hidden * hidden;
   s->w3 = s->b2 + hidden;
   s->b3 = s->w3 + hidden;
-  s->P = s->b3 + 1;
+  // blocks padded to 8 parameters, so that every block's BF16 weights start
+  // on a 16-byte boundary (the tensor-core training GEMMs load 16 bytes at a
+  // time); the padding stays zero
+  s->P = (s->b3 + 1 + 7) / 8 * 8;
   const size_t n = (size_t)members * nspecies * s->P;
   // variance-scaled normal initialisation, an independent draw per member
   std::vector<float> w(n, 0.f);
@@ -687,6 +702,7 @@ gapgb_status gapgb_surrogate_create(int nspecies, const int *species_z, int des_
   for (size_t i = 0; i < n; ++i) w16[i] = __float2bfloat16(w[i]);
   std::vector<float> zeros(std::max(des_len, kMaxSurrSpecies), 0.f), ones(des_len, 1.f);
   if (!(dalloc(&s->w, n) && dalloc(&s->m, n) && dalloc(&s->v, n) && dalloc(&s->grad, n) &&
+        dalloc(&s->t_err, 1) &&
         dalloc(&s->w16, n) && dalloc(&s->mu, des_len) && dalloc(&s->isig, des_len) &&
         dalloc(&s->sd, des_len) && dalloc(&s->e_shift, kMaxSurrSpecies) && dalloc(&s->zt, nspecies))) {
     cudaGetLastError();
@@ -697,6 +713,7 @@ gapgb_status gapgb_surrogate_create(int nspecies, const int *species_z, int des_
             cudaMemcpy(s->w16, w16.data(), n * 2, cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemset(s->m, 0, n * 4) == cudaSuccess && cudaMemset(s->v, 0, n * 4) == cudaSuccess &&
             cudaMemset(s->grad, 0, n * 4) == cudaSuccess &&
+            cudaMemset(s->t_err, 0, sizeof(int)) == cudaSuccess &&
             cudaMemcpy(s->mu, zeros.data(), des_len * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(s->isig, ones.data(), des_len * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(s->sd, ones.data(), des_len * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
@@ -715,7 +732,7 @@ gapgb_status gapgb_surrogate_create(int nspecies, const int *species_z, int des_
 void gapgb_surrogate_free(gapgb_surrogate *s) {
   if (!s) return;
   free_rows(s);
-  void *ps[] = {s->w, s->m, s->v, s->grad, s->w16, s->mu, s->isig, s->sd, s->e_shift, s->zt,
+  void *ps[] = {s->w, s->m, s->v, s->grad, s->t_err, s->w16, s->mu, s->isig, s->sd, s->e_shift, s->zt,
                 s->t_tile_sp, s->p_cnt, s->p_sp, s->p_slot, s->p_seg, s->p_tile, s->p_err,
                 s->w_img, s->x_img};
   for (void *p : ps)
@@ -802,31 +819,41 @@ gapgb_status gapgb_surrogate_train_step(gapgb_surrogate *s, int rows_per_species
   const size_t sH = (size_t)R * H, sD = (size_t)R * D;
   GAPGB_CUDA_TRY(cudaMemcpyAsync(s->idx, d_rows, total * sizeof(int), cudaMemcpyDeviceToDevice, cs));
   k_mlp_gather<<<nblk(total * D), 256, 0, cs>>>(total, D, s->idx, d_G, s->mu, s->isig, s->X);
-  forward(s, cs, rows, s->t_tile_sp, zD, true);
+  // tensor-core GEMMs when every 128-row tile lies in one species segment
+  int *tcf = (R % 128 == 0) ? s->t_err : nullptr;
+  forward(s, cs, rows, s->t_tile_sp, zD, true, tcf);
   LossArgs la{R, nsp, D, lambda, 1.f / s->e_scale, s->idx, s->y, s->Gx, d_e, d_dedg, s->sd,
               s->e_shift, s->eps, s->Rv, s->R16, s->lrows};
   k_mlp_loss<<<nblk(total * 32), 256, 0, cs>>>(la, total);
   const size_t mstride = (size_t)nsp * s->P;
   const int *ts = s->t_tile_sp;
   // tangent pass along r
-  gemm(cs, Q, rows, H, D, s->R16, D, 1, zD, s->w16 + s->W1, D, 1, mstride, ts, s->P, s->U1, H, zH, 0.f);
+  gemm(cs, Q, rows, H, D, s->R16, D, 1, zD, s->w16 + s->W1, D, 1, mstride, ts, s->P, s->U1, H, zH, 0.f,
+       tcf);
   k_mlp_dsilu<<<nblk(total * H), 256, 0, cs>>>(total * H, s->Z1, s->U1, nullptr, s->V1);
-  gemm(cs, Q, rows, H, H, s->V1, H, 1, zH, s->w16 + s->W2, H, 1, mstride, ts, s->P, s->U2, H, zH, 0.f);
+  gemm(cs, Q, rows, H, H, s->V1, H, 1, zH, s->w16 + s->W2, H, 1, mstride, ts, s->P, s->U2, H, zH, 0.f,
+       tcf);
   // reverse pass, layer 2
   RowMap rm{rows, nsp, s->P, ts};
   k_mlp_back2<<<nblk(total * H), 256, 0, cs>>>(rm, Q, H, s->w3, s->w, s->Z2, s->U2, s->eps, s->Zb2, s->Ub2);
   k_mlp_grad_w3<<<dim3(nblk(H), J), 256, 0, cs>>>(R, H, s->P, s->w3, s->b3, s->Z2, s->U2, s->eps, s->grad);
   // dW2 = zbar2^T a1 + ubar2^T v1 per segment (M = N = H, K = R)
-  gemm(cs, J, H, H, R, s->Zb2, 1, H, sH, s->A1, 1, H, sH, nullptr, 0, s->grad + s->W2, H, s->P, 0.f);
-  gemm(cs, J, H, H, R, s->Ub2, 1, H, sH, s->V1, 1, H, sH, nullptr, 0, s->grad + s->W2, H, s->P, 1.f);
+  gemm(cs, J, H, H, R, s->Zb2, 1, H, sH, s->A1, 1, H, sH, nullptr, 0, s->grad + s->W2, H, s->P, 0.f,
+       tcf);
+  gemm(cs, J, H, H, R, s->Ub2, 1, H, sH, s->V1, 1, H, sH, nullptr, 0, s->grad + s->W2, H, s->P, 1.f,
+       tcf);
   k_mlp_colsum<<<dim3(nblk(H), J), 256, 0, cs>>>(R, H, s->P, s->b2, s->Zb2, s->grad);
   // abar1 = W2^T zbar2, vbar1 = W2^T ubar2
-  gemm(cs, Q, rows, H, H, s->Zb2, H, 1, zH, s->w16 + s->W2, 1, H, mstride, ts, s->P, s->Ab1, H, zH, 0.f);
-  gemm(cs, Q, rows, H, H, s->Ub2, H, 1, zH, s->w16 + s->W2, 1, H, mstride, ts, s->P, s->Vb1, H, zH, 0.f);
+  gemm(cs, Q, rows, H, H, s->Zb2, H, 1, zH, s->w16 + s->W2, 1, H, mstride, ts, s->P, s->Ab1, H, zH, 0.f,
+       tcf);
+  gemm(cs, Q, rows, H, H, s->Ub2, H, 1, zH, s->w16 + s->W2, 1, H, mstride, ts, s->P, s->Vb1, H, zH, 0.f,
+       tcf);
   k_mlp_back1<<<nblk(total * H), 256, 0, cs>>>(total * H, s->Z1, s->U1, s->Ab1, s->Vb1, s->Zb1, s->Ub1);
   // dW1 = zbar1^T x + ubar1^T r per segment (M = H, N = D, K = R)
-  gemm(cs, J, H, D, R, s->Zb1, 1, H, sH, s->X, 1, D, sD, nullptr, 0, s->grad + s->W1, D, s->P, 0.f);
-  gemm(cs, J, H, D, R, s->Ub1, 1, H, sH, s->R16, 1, D, sD, nullptr, 0, s->grad + s->W1, D, s->P, 1.f);
+  gemm(cs, J, H, D, R, s->Zb1, 1, H, sH, s->X, 1, D, sD, nullptr, 0, s->grad + s->W1, D, s->P, 0.f,
+       tcf);
+  gemm(cs, J, H, D, R, s->Ub1, 1, H, sH, s->R16, 1, D, sD, nullptr, 0, s->grad + s->W1, D, s->P, 1.f,
+       tcf);
   k_mlp_colsum<<<dim3(nblk(H), J), 256, 0, cs>>>(R, H, s->P, s->b1, s->Zb1, s->grad);
   const size_t n = (size_t)J * s->P;
   if (d_grad) GAPGB_CUDA_TRY(cudaMemcpyAsync(d_grad, s->grad, n * 4, cudaMemcpyDeviceToDevice, cs));
@@ -839,8 +866,14 @@ gapgb_status gapgb_surrogate_train_step(gapgb_surrogate *s, int rows_per_species
   GAPGB_CUDA_TRY(cudaGetLastError());
   if (loss) {
     std::vector<double> lr_h(total);
+    int terr = 0;
     GAPGB_CUDA_TRY(cudaMemcpyAsync(lr_h.data(), s->lrows, total * sizeof(double), cudaMemcpyDeviceToHost, cs));
+    GAPGB_CUDA_TRY(cudaMemcpyAsync(&terr, s->t_err, sizeof(int), cudaMemcpyDeviceToHost, cs));
     GAPGB_CUDA_TRY(cudaStreamSynchronize(cs));
+    if (terr & kFlagTimeout) {
+      cudaMemsetAsync(s->t_err, 0, sizeof(int), cs);
+      return sfail(GAPGB_ERR_TIMEOUT, "a bounded tensor-core wait of the training GEMMs gave up");
+    }
     for (int z = 0; z < J; ++z)
       loss[z] = std::accumulate(lr_h.begin() + (size_t)z * R, lr_h.begin() + (size_t)(z + 1) * R, 0.0) / R;
   }

@@ -223,14 +223,23 @@ __device__ __forceinline__ int stage_slots(const Layout<T> &L, const SFT<T> &sf,
 
 // FP32: at least 4 blocks (16 warps) per SM; FP64 is FP64-pipe bound and
 // keeps its registers.
+// the parts an atom's pair (or round) loop is split into: a team of this
+// many warps runs them side by side, a single warp in turn
+constexpr int kTeam = kWarpsPerBlock;
+
+// team = 1: one warp per atom.  team = kWarpsPerBlock (small batches, which
+// would leave most SMs idle): the block's warps share one atom, each staging
+// its own copy of the slots and taking every team-th 32-pair stride of the
+// pair loop; their per-SF sums are added in warp order (deterministic).
 template <typename T>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, sizeof(T) == 4 ? 4 : 1)
     k_wacsf_fwd(int N, int cap, int capS, const int *__restrict__ cnt,
                 const double4 *__restrict__ xyzr, const int *__restrict__ nj,
                 const double4 *__restrict__ apos, const float4 *__restrict__ d32,
                 const float *__restrict__ w32, const SFT<T> *__restrict__ sfg,
-                T *__restrict__ G) {
+                T *__restrict__ G, int team) {
   extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ T s_part[kWarpsPerBlock][2 * kAngChunk];
   load_table<T>(smraw, sfg);
   const SFT<T> &sf = *reinterpret_cast<const SFT<T> *>(smraw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -238,12 +247,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, sizeof(T) == 4 ? 4 : 1)
   const int nrad = sf.nrad, nang = sf.nang, ngrp = sf.n_ang_grp;
   const Layout<T> L = carve<T>(smraw, warp, capS, nrc, nal, D, nang, true);
   const T maxrc = sf.max_ang_rc;
-  for (int i = blockIdx.x * kWarpsPerBlock + warp; i < N; i += gridDim.x * kWarpsPerBlock) {
+  const int tw = team > 1 ? warp : 0;  // this warp's place in its team
+  const int per_block = team > 1 ? 1 : kWarpsPerBlock;
+  for (int i = blockIdx.x * per_block + (team > 1 ? 0 : warp); i < N; i += gridDim.x * per_block) {
     const int P = stage_slots<T>(L, sf, i, cap, capS, lane, cnt, xyzr, nj, apos, d32, w32, false);
     __syncwarp();
     T *Gi = G + (size_t)i * D;
     // radial: one SF per lane, slots in the reference's order
-    for (int s = lane; s < nrad; s += 32) {
+    for (int s = lane + 32 * tw; s < nrad; s += 32 * team) {
       const int rci = sf.rad_rc[s];
       const T alpha = sf.rad_alpha[s], rs = sf.rad_rs[s];
       const T *fcr = L.fc + (size_t)rci * capS;
@@ -260,67 +271,89 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, sizeof(T) == 4 ? 4 : 1)
       Gi[d] = acc;
       Gi[d + nsf] = accw;
     }
-    // angular: chunks of kAngChunk SFs accumulated in registers
+    // angular: chunks of kAngChunk SFs accumulated in registers.  The pairs
+    // fall into kTeam parts (part w: the 32-pair strides w, w + kTeam, ...),
+    // each summed on its own and the parts added in order into s_part,
+    // whether one warp runs the parts in turn (team = 1) or the block's warps
+    // run one part each: the rounding is the same for every launch shape, so
+    // an atom's descriptors do not depend on the batch around it
     for (int c0 = 0; c0 < nang; c0 += kAngChunk) {
       int code[kAngChunk];
-      T accA[kAngChunk], accW[kAngChunk];
 #pragma unroll
-      for (int s = 0; s < kAngChunk; ++s) {
-        code[s] = (c0 + s < nang) ? sf.ang_code[c0 + s] : -1;
-        accA[s] = accW[s] = (T)0;
-      }
-      if (P > 1) {
-        const int npair = P * (P - 1) / 2;
-        int j = 0, k = 1 + lane;
-        while (j < P - 1 && k >= P) { const int o = k - P; ++j; k = j + 1 + o; }
-        for (int p = lane; p < npair; p += 32) {
-          const T a = L.r[j], b = L.r[k];
-          if (a <= maxrc && b <= maxrc) {
-            const T cx = L.dx[j] - L.dx[k], cy = L.dy[j] - L.dy[k], cz = L.dz[j] - L.dz[k];
-            const T c2 = cx * cx + cy * cy + cz * cz;
-            const T c = t_sqrt(c2);
-            if (c <= maxrc) {
-              // costheta = f/g, f = rjk^2 - rij^2 - rik^2, g = -2 rij rik (wacsf.f90:271-273)
-              const T cosv = (c2 - a * a - b * b) / ((T)-2 * a * b);
-              for (int g = 0; g < ngrp; ++g) {
-                const int rci = sf.ang_grp_rc[g];
-                const T fcc = (c <= sf.rc_val[rci])
-                                  ? (T)0.5 * (t_cos(sf.pi_over_rc[rci] * c) + (T)1) : (T)0;
-                L.Fp[rci * 32 + lane] =
-                    L.fc[(size_t)rci * capS + j] * L.fc[(size_t)rci * capS + k] * fcc;
-              }
-              for (int al = 0; al < nal; ++al)
-                L.Ep[al * 32 + lane] = L.ea[(size_t)al * capS + j] * L.ea[(size_t)al * capS + k] *
-                                       t_exp(-sf.alpha_val[al] * c2);
-              const T wjk = L.w[j] * L.w[k];
+      for (int s = 0; s < kAngChunk; ++s) code[s] = (c0 + s < nang) ? sf.ang_code[c0 + s] : -1;
+      if (lane < 2 * kAngChunk) s_part[warp][lane] = (T)0;
+      __syncwarp();
+      const int part0 = team > 1 ? tw : 0, part1 = team > 1 ? tw + 1 : kTeam;
+      for (int part = part0; part < part1; ++part) {
+        T accA[kAngChunk], accW[kAngChunk];
 #pragma unroll
-              for (int s = 0; s < kAngChunk; ++s) {
-                if (code[s] < 0) continue;
-                const int rci = code[s] & 255, al = (code[s] >> 8) & 255;
-                const int iz = (code[s] >> 16) & 255;
-                const T base = (code[s] >> 24) ? (T)1 - cosv : (T)1 + cosv;
-                T A, dA;
-                ang_pow<T>(base, iz, iz ? (T)1 : sf.ang_zeta[c0 + s], &A, &dA);
-                const T v = A * L.Ep[al * 32 + lane] * L.Fp[rci * 32 + lane];
-                accA[s] += v;
-                accW[s] += v * wjk;
+        for (int s = 0; s < kAngChunk; ++s) accA[s] = accW[s] = (T)0;
+        if (P > 1) {
+          const int npair = P * (P - 1) / 2;
+          int j = 0, k = 1 + lane + 32 * part;
+          while (j < P - 1 && k >= P) { const int o = k - P; ++j; k = j + 1 + o; }
+          for (int p = lane + 32 * part; p < npair; p += 32 * kTeam) {
+            const T a = L.r[j], b = L.r[k];
+            if (a <= maxrc && b <= maxrc) {
+              const T cx = L.dx[j] - L.dx[k], cy = L.dy[j] - L.dy[k], cz = L.dz[j] - L.dz[k];
+              const T c2 = cx * cx + cy * cy + cz * cz;
+              const T c = t_sqrt(c2);
+              if (c <= maxrc) {
+                // costheta = f/g, f = rjk^2 - rij^2 - rik^2, g = -2 rij rik (wacsf.f90:271-273)
+                const T cosv = (c2 - a * a - b * b) / ((T)-2 * a * b);
+                for (int g = 0; g < ngrp; ++g) {
+                  const int rci = sf.ang_grp_rc[g];
+                  const T fcc = (c <= sf.rc_val[rci])
+                                    ? (T)0.5 * (t_cos(sf.pi_over_rc[rci] * c) + (T)1) : (T)0;
+                  L.Fp[rci * 32 + lane] =
+                      L.fc[(size_t)rci * capS + j] * L.fc[(size_t)rci * capS + k] * fcc;
+                }
+                for (int al = 0; al < nal; ++al)
+                  L.Ep[al * 32 + lane] = L.ea[(size_t)al * capS + j] *
+                                         L.ea[(size_t)al * capS + k] *
+                                         t_exp(-sf.alpha_val[al] * c2);
+                const T wjk = L.w[j] * L.w[k];
+#pragma unroll
+                for (int s = 0; s < kAngChunk; ++s) {
+                  if (code[s] < 0) continue;
+                  const int rci = code[s] & 255, al = (code[s] >> 8) & 255;
+                  const int iz = (code[s] >> 16) & 255;
+                  const T base = (code[s] >> 24) ? (T)1 - cosv : (T)1 + cosv;
+                  T A, dA;
+                  ang_pow<T>(base, iz, iz ? (T)1 : sf.ang_zeta[c0 + s], &A, &dA);
+                  const T v = A * L.Ep[al * 32 + lane] * L.Fp[rci * 32 + lane];
+                  accA[s] += v;
+                  accW[s] += v * wjk;
+                }
               }
             }
+            k += 32 * kTeam;
+            while (j < P - 1 && k >= P) { const int o = k - P; ++j; k = j + 1 + o; }
           }
-          k += 32;
-          while (j < P - 1 && k >= P) { const int o = k - P; ++j; k = j + 1 + o; }
         }
-      }
 #pragma unroll
-      for (int s = 0; s < kAngChunk; ++s) {
-        if (c0 + s >= nang) continue;
-        const T x = warp_sum(accA[s]), y = warp_sum(accW[s]);
-        if (lane == 0) {
-          const int d = sf.ang_d[c0 + s];
-          Gi[d] = sf.ang_pref[c0 + s] * x;
-          Gi[d + nsf] = sf.ang_pref[c0 + s] * y;
+        for (int s = 0; s < kAngChunk; ++s) {
+          const T x = warp_sum(accA[s]), y = warp_sum(accW[s]);
+          if (lane == 0) {
+            s_part[warp][s] += x;
+            s_part[warp][kAngChunk + s] += y;
+          }
         }
+        __syncwarp();
       }
+      if (team > 1) __syncthreads();
+      if ((team > 1 ? warp == 0 : true) && lane < kAngChunk && c0 + lane < nang) {
+        T x = (T)0, y = (T)0;
+        for (int w = 0; w < team; ++w) {
+          x += s_part[team > 1 ? w : warp][lane];
+          y += s_part[team > 1 ? w : warp][kAngChunk + lane];
+        }
+        const int d = sf.ang_d[c0 + lane];
+        Gi[d] = sf.ang_pref[c0 + lane] * x;
+        Gi[d + nsf] = sf.ang_pref[c0 + lane] * y;
+      }
+      if (team > 1) __syncthreads();
+      else __syncwarp();
     }
     __syncwarp();
   }
@@ -333,7 +366,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
                 const double4 *__restrict__ apos, const float4 *__restrict__ d32,
                 const float *__restrict__ w32, const SFT<T> *__restrict__ sfg,
                 const T *__restrict__ dedg, typename Vec4<T>::type *__restrict__ gslot,
-                double *__restrict__ wvir) {
+                double *__restrict__ wvir, int team) {
   using V4 = typename Vec4<T>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
   load_table<T>(smraw, sfg);
@@ -343,7 +376,18 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
   const int nrad = sf.nrad, nang = sf.nang, ngrp = sf.n_ang_grp;
   const Layout<T> L = carve<T>(smraw, warp, capS, nrc, nal, D, nang, false);
   const T maxrc = sf.max_ang_rc;
-  for (int i = blockIdx.x * kWarpsPerBlock + warp; i < N; i += gridDim.x * kWarpsPerBlock) {
+  // The rounds fall into kTeam parts (part w: rounds w, w + kTeam, ...), each
+  // summed into slot-gradient arrays of its own and the parts added in order.
+  // team > 1: the block's warps share one atom and run one part each (warp
+  // 0's arrays also hold the radial terms), added in warp order before warp 0
+  // writes the slot gradients and the virial.  team = 1: the warp runs the
+  // parts in turn, part 0 into its arrays and each later part into the
+  // atom's row of gslot (global scratch until the final slot gradients are
+  // written there), added after it.  The rounding is the same for every
+  // launch shape.
+  const int tw = team > 1 ? warp : 0;
+  const int per_block = team > 1 ? 1 : kWarpsPerBlock;
+  for (int i = blockIdx.x * per_block + (team > 1 ? 0 : warp); i < N; i += gridDim.x * per_block) {
     const int P = stage_slots<T>(L, sf, i, cap, capS, lane, cnt, xyzr, nj, apos, d32, w32, true);
     for (int d = lane; d < D; d += 32) L.dg[d] = dedg[(size_t)i * D + d];
     for (int q = lane; q < P; q += 32) L.gx[q] = L.gy[q] = L.gz[q] = (T)0;
@@ -354,8 +398,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
       L.cA[s] = sf.ang_pref[s] * L.dg[d];
       L.cB[s] = sf.ang_pref[s] * L.dg[d + nsf];
     }
-    // radial terms: lanes own slots
-    for (int q = lane; q < P; q += 32) {
+    // radial terms: lanes own slots (the team's first warp)
+    for (int q = lane; q < P && tw == 0; q += 32) {
       const T r = L.r[q], w = L.w[q];
       T S = (T)0;
       for (int s = 0; s < nrad; ++s) {
@@ -379,7 +423,30 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
     if (nang > 0 && P > 1) {
       const int Pp = P + (P & 1);
       const int half = Pp >> 1;
-      for (int round = 0; round < Pp - 1; ++round) {
+      const int part0 = team > 1 ? tw : 0, part1 = team > 1 ? tw + 1 : kTeam;
+      for (int part = part0; part < part1; ++part) {
+      const bool own = team > 1 || part == 0;
+      V4 *tmp = gslot + (size_t)i * cap;  // this part's scratch when !own
+      if (!own) {
+        for (int q = lane; q < P; q += 32) {
+          V4 z;
+          z.x = z.y = z.z = z.w = (T)0;
+          tmp[q] = z;
+        }
+        __syncwarp();
+      }
+      auto add = [&](int q, T vx, T vy, T vz) {
+        if (own) {
+          L.gx[q] += vx;
+          L.gy[q] += vy;
+          L.gz[q] += vz;
+        } else {
+          tmp[q].x += vx;
+          tmp[q].y += vy;
+          tmp[q].z += vz;
+        }
+      };
+      for (int round = part; round < Pp - 1; round += kTeam) {
         for (int t = lane; t < half; t += 32) {
           int j, k;
           if (t == 0) {
@@ -439,17 +506,42 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock)
             S3 += F * (SP * dcdc - (T)2 * SU * c) + SQ * (fa * fb * dfcc);
           }
           const T s1 = S1 * ia, s2 = S2 * ib, s3 = S3 * ic;
-          L.gx[j] += s1 * djx + s3 * cx;
-          L.gy[j] += s1 * djy + s3 * cy;
-          L.gz[j] += s1 * djz + s3 * cz;
-          L.gx[k] += s2 * dkx - s3 * cx;
-          L.gy[k] += s2 * dky - s3 * cy;
-          L.gz[k] += s2 * dkz - s3 * cz;
+          add(j, s1 * djx + s3 * cx, s1 * djy + s3 * cy, s1 * djz + s3 * cz);
+          add(k, s2 * dkx - s3 * cx, s2 * dky - s3 * cy, s2 * dkz - s3 * cz);
         }
         __syncwarp();
       }
+      if (!own) {
+        __syncwarp();
+        for (int q = lane; q < P; q += 32) {
+          const V4 t = tmp[q];
+          L.gx[q] += t.x;
+          L.gy[q] += t.y;
+          L.gz[q] += t.z;
+        }
+        __syncwarp();
+      }
+      }
     }
     __syncwarp();
+    if (team > 1) {
+      __syncthreads();
+      const Layout<T> L0 = carve<T>(smraw, 0, capS, nrc, nal, D, nang, false);
+      for (int q = threadIdx.x; q < P; q += blockDim.x) {
+        T gx = L0.gx[q], gy = L0.gy[q], gz = L0.gz[q];
+        for (int w = 1; w < team; ++w) {
+          const Layout<T> Lw = carve<T>(smraw, w, capS, nrc, nal, D, nang, false);
+          gx += Lw.gx[q];
+          gy += Lw.gy[q];
+          gz += Lw.gz[q];
+        }
+        L0.gx[q] = gx;
+        L0.gy[q] = gy;
+        L0.gz[q] = gz;
+      }
+      __syncthreads();
+      if (warp != 0) continue;
+    }
     // slot gradients and the per-atom virial (lanes in T, the warp sum in FP64)
     T W[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int q = lane; q < P; q += 32) {
@@ -489,6 +581,22 @@ int warp_grid(int N, size_t smem_per_block, const void *fn) {
   int need = (N + kWarpsPerBlock - 1) / kWarpsPerBlock;
   int maxb = sms * per_sm;
   return need < maxb ? (need > 0 ? need : 1) : maxb;
+}
+
+// Launch shape of the generic kernels: a batch of fewer than 8 atoms per SM
+// (a single drop-in structure, say) would occupy a few warps per SM, so each
+// atom gets a whole block (team = its kWarpsPerBlock warps); otherwise one
+// warp per atom.
+int team_grid(int N, size_t smem_per_block, const void *fn, int *team) {
+  const int sms = device_sms();
+  if (N < 8 * sms) {
+    *team = kWarpsPerBlock;
+    const int per_sm = kernel_occupancy(fn, 32 * kWarpsPerBlock, smem_per_block);
+    const int maxb = sms * (per_sm > 0 ? per_sm : 1);
+    return N < maxb ? (N > 0 ? N : 1) : maxb;
+  }
+  *team = 1;
+  return warp_grid(N, smem_per_block, fn);
 }
 
 }  // namespace
@@ -539,10 +647,11 @@ void launch_wacsf_fwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
   }
   auto fn = k_wacsf_fwd<T>;
   kernel_smem((const void *)fn, (int)smem);
-  const int grid = warp_grid(N, smem, (const void *)fn);
+  int team = 1;
+  const int grid = team_grid(N, smem, (const void *)fn, &team);
   fn<<<grid, 32 * kWarpsPerBlock, smem, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
                                                ws.apos, ws.nbr_d32, ws.nbr_w32, sft_of<T>(m),
-                                               (T *)ws.G);
+                                               (T *)ws.G, team);
 }
 
 bool bwd_scatters_forces(const gapgb_model *m) {
@@ -583,11 +692,12 @@ bool launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
   }
   auto fn = k_wacsf_bwd<T>;
   kernel_smem((const void *)fn, (int)smem);
-  const int grid = warp_grid(N, smem, (const void *)fn);
+  int team = 1;
+  const int grid = team_grid(N, smem, (const void *)fn, &team);
   fn<<<grid, 32 * kWarpsPerBlock, smem, st>>>(N, cap, capS, ws.nbr_cnt, ws.nbr_xyz, ws.nbr_j,
                                                ws.apos, ws.nbr_d32, ws.nbr_w32, sft_of<T>(m),
                                                (const T *)ws.dedg,
-                                               (typename Vec4<T>::type *)ws.gslot, ws.wvir);
+                                               (typename Vec4<T>::type *)ws.gslot, ws.wvir, team);
   (void)d_force;
   return false;  // slot gradients in ws.gslot: launch_forces gathers them
 }

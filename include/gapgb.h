@@ -337,8 +337,9 @@ gapgb_status gapgb_surrogate_set_norm(gapgb_surrogate *s, const double *g_mean,
 
 /* FP32 master weights, members * nspecies blocks of params_per_block floats
  * in the order block (q * nspecies + s) = {W1[H][D], b1[H], W2[H][H], b2[H],
- * w3[H], b3}.  `get` copies them out, `set` replaces them (and resets Adam);
- * either may be NULL. */
+ * w3[H], b3, zeros}: params_per_block is rounded up to a multiple of 8 and the
+ * tail stays zero.  `get` copies them out, `set` replaces them (and resets
+ * Adam); either may be NULL. */
 gapgb_status gapgb_surrogate_params(gapgb_surrogate *s, float *get,
                                     const float *set);
 

@@ -11,7 +11,8 @@ the GPU result can be compared tightly; `emulate_bf16=False` is the exact
 float64 function, checked against finite differences by the CPU tests.
 
 Parameter block layout (one member, one species), flat float vector:
-W1[H][D], b1[H], W2[H][H], b2[H], w3[H], b3.
+W1[H][D], b1[H], W2[H][H], b2[H], w3[H], b3, then zeros up to a multiple of
+8 parameters (the library's block size).
 """
 import numpy as np
 
@@ -35,7 +36,9 @@ def layout(D, H):
     b2 = W2 + H * H
     w3 = b2 + H
     b3 = w3 + H
-    return dict(W1=W1, b1=b1, W2=W2, b2=b2, w3=w3, b3=b3, P=b3 + 1)
+    # the library pads each (member, species) block to a multiple of 8
+    # parameters (16-byte aligned BF16 weights); the padding is zero
+    return dict(W1=W1, b1=b1, W2=W2, b2=b2, w3=w3, b3=b3, P=(b3 + 1 + 7) // 8 * 8)
 
 
 def unpack(p, D, H):
@@ -47,7 +50,9 @@ def unpack(p, D, H):
 
 
 def pack(W1, b1, W2, b2, w3, b3):
-    return np.concatenate([W1.ravel(), b1, W2.ravel(), b2, w3, [b3]])
+    p = np.concatenate([W1.ravel(), b1, W2.ravel(), b2, w3, [b3]])
+    P = layout(W1.shape[1], W1.shape[0])["P"]
+    return np.concatenate([p, np.zeros(P - p.size)])
 
 
 def _sig(z):
