@@ -25,10 +25,9 @@
 // Set-up, once per device, is done by the first call on that device with
 // that device current: the device address of the array (cudaGetSymbolAddress;
 // in host code the array's name is only a host-side stand-in) and the
-// kernel's shared-memory limit for the largest descriptor length.  That
-// first call should come before any stream capture.  The coefficients are
-// read from the model's device copy: finish (synchronise) every call of this
-// entry point before gapgb_model_set_coeff rewrites them.
+// kernel's shared-memory limit for the largest descriptor length.  The
+// coefficients are read from the model's device copy: finish (synchronise)
+// every call of this entry point before gapgb_model_set_coeff rewrites them.
 #include <mutex>
 
 #include "gapgb_internal.h"

@@ -295,12 +295,11 @@ gapgb_status gapgb_measure_peaks(double out[3]);
  * until the process exits; calls with natoms * (D + 1) > 1048576 (16131 atoms
  * at D = 64) return GAPGB_ERR_CAP_EXCEEDED.  The model must already be
  * resident on the device (any evaluation uploads it; this call never does).
- * The first call on a device does a one-time set-up (the array's device
- * address, the kernel's shared-memory limit), so make that first call before
- * any stream capture.  All calls share the array: calls that overlap on the
- * GPU (other streams, other host threads) race and must be serialised by the
- * caller, and every call must have finished before gapgb_model_set_coeff
- * rewrites the coefficients it reads. */
+ * The first call on a device also does a one-time set-up (the array's device
+ * address, the kernel's shared-memory limit).  All calls share the array:
+ * calls that overlap on the GPU (other streams, other host threads) race and
+ * must be serialised by the caller, and every call must have finished before
+ * gapgb_model_set_coeff rewrites the coefficients it reads. */
 gapgb_status gapgb_gpr_noalloc(gapgb_model *model, int natoms,
                                const double *d_G, double *d_e, double *d_dedg,
                                void *stream);
