@@ -365,11 +365,12 @@ void kernel_smem(const void *fn, int bytes, bool max_carveout = false);
 // The surrogate's BF16 training GEMMs on the tensor cores (mlp_gemm_tc.cu):
 // C[z] = beta C[z] + opA[z] opB[z]^T with mlp.cu's strided operand view.
 // Returns false, launching nothing, when the shape or strides are outside
-// what it stages (then the SIMT kernel runs).
+// what it stages (then the SIMT kernel runs).  `part` (part_elems floats, may
+// be null) is scratch for splitting K when there are few row tiles.
 bool mlp_gemm_tc(cudaStream_t st, int Z, int M, int N, int K, const __nv_bfloat16 *A, int sAm,
                  int sAk, size_t zA, const __nv_bfloat16 *B, int sBn, int sBk, size_t zB,
                  const int *tile_sp, size_t sBsp, float *C, int ldc, size_t zC, float beta,
-                 int *flags);
+                 int *flags, float *part = nullptr, size_t part_elems = 0);
 int kernel_occupancy(const void *fn, int threads, size_t smem);
 int device_sms();
 

@@ -452,6 +452,8 @@ struct gapgb_surrogate {
   size_t W1 = 0, b1 = 0, W2 = 0, b2 = 0, w3 = 0, b3 = 0;
   float *w = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr;
   int *t_err = nullptr;  // error flags of the training GEMMs (bounded tensor-core waits)
+  float *t_part = nullptr;  // split-K partials of the weight-gradient GEMMs
+  size_t t_part_n = 0;
   __nv_bfloat16 *w16 = nullptr;
   float *mu = nullptr, *isig = nullptr, *sd = nullptr, *e_shift = nullptr;
   int *zt = nullptr;
@@ -491,10 +493,11 @@ gapgb_status sfail(gapgb_status st, const std::string &msg) {
 template <typename TA, typename TB>
 void gemm(cudaStream_t st, int Z, int M, int N, int K, const TA *A, int sAm, int sAk, size_t zA,
           const TB *B, int sBn, int sBk, size_t zB, const int *tile_sp, size_t sBsp, float *C,
-          int ldc, size_t zC, float beta, int *tc_flags = nullptr) {
+          int ldc, size_t zC, float beta, int *tc_flags = nullptr, float *tc_part = nullptr,
+          size_t tc_part_n = 0) {
   if constexpr (std::is_same<TA, __nv_bfloat16>::value && std::is_same<TB, __nv_bfloat16>::value) {
     if (tc_flags && mlp_gemm_tc(st, Z, M, N, K, A, sAm, sAk, zA, B, sBn, sBk, zB, tile_sp, sBsp,
-                                C, ldc, zC, beta, tc_flags))
+                                C, ldc, zC, beta, tc_flags, tc_part, tc_part_n))
       return;
   }
   dim3 g((N + kTile - 1) / kTile, (M + kTile - 1) / kTile, Z);
@@ -732,7 +735,7 @@ gapgb_status gapgb_surrogate_create(int nspecies, const int *species_z, int des_
 void gapgb_surrogate_free(gapgb_surrogate *s) {
   if (!s) return;
   free_rows(s);
-  void *ps[] = {s->w, s->m, s->v, s->grad, s->t_err, s->w16, s->mu, s->isig, s->sd, s->e_shift, s->zt,
+  void *ps[] = {s->w, s->m, s->v, s->grad, s->t_err, s->t_part, s->w16, s->mu, s->isig, s->sd, s->e_shift, s->zt,
                 s->t_tile_sp, s->p_cnt, s->p_sp, s->p_slot, s->p_seg, s->p_tile, s->p_err,
                 s->w_img, s->x_img};
   for (void *p : ps)
@@ -819,8 +822,17 @@ gapgb_status gapgb_surrogate_train_step(gapgb_surrogate *s, int rows_per_species
   const size_t sH = (size_t)R * H, sD = (size_t)R * D;
   GAPGB_CUDA_TRY(cudaMemcpyAsync(s->idx, d_rows, total * sizeof(int), cudaMemcpyDeviceToDevice, cs));
   k_mlp_gather<<<nblk(total * D), 256, 0, cs>>>(total, D, s->idx, d_G, s->mu, s->isig, s->X);
-  // tensor-core GEMMs when every 128-row tile lies in one species segment
+  // tensor-core GEMMs when every 128-row tile lies in one species segment;
+  // split-K scratch for the weight gradients (J blocks x up to 16 splits)
   int *tcf = (R % 128 == 0) ? s->t_err : nullptr;
+  const size_t part_n = (size_t)Q * nsp * 16 * H * std::max(H, D);
+  if (tcf && s->t_part_n < part_n) {
+    if (s->t_part) cudaFree(s->t_part);
+    s->t_part = nullptr;
+    s->t_part_n = 0;
+    if (dalloc(&s->t_part, part_n)) s->t_part_n = part_n;
+    else cudaGetLastError();  // no scratch: the GEMMs run without splitting K
+  }
   forward(s, cs, rows, s->t_tile_sp, zD, true, tcf);
   LossArgs la{R, nsp, D, lambda, 1.f / s->e_scale, s->idx, s->y, s->Gx, d_e, d_dedg, s->sd,
               s->e_shift, s->eps, s->Rv, s->R16, s->lrows};
@@ -839,9 +851,9 @@ gapgb_status gapgb_surrogate_train_step(gapgb_surrogate *s, int rows_per_species
   k_mlp_grad_w3<<<dim3(nblk(H), J), 256, 0, cs>>>(R, H, s->P, s->w3, s->b3, s->Z2, s->U2, s->eps, s->grad);
   // dW2 = zbar2^T a1 + ubar2^T v1 per segment (M = N = H, K = R)
   gemm(cs, J, H, H, R, s->Zb2, 1, H, sH, s->A1, 1, H, sH, nullptr, 0, s->grad + s->W2, H, s->P, 0.f,
-       tcf);
+       tcf, s->t_part, s->t_part_n);
   gemm(cs, J, H, H, R, s->Ub2, 1, H, sH, s->V1, 1, H, sH, nullptr, 0, s->grad + s->W2, H, s->P, 1.f,
-       tcf);
+       tcf, s->t_part, s->t_part_n);
   k_mlp_colsum<<<dim3(nblk(H), J), 256, 0, cs>>>(R, H, s->P, s->b2, s->Zb2, s->grad);
   // abar1 = W2^T zbar2, vbar1 = W2^T ubar2
   gemm(cs, Q, rows, H, H, s->Zb2, H, 1, zH, s->w16 + s->W2, 1, H, mstride, ts, s->P, s->Ab1, H, zH, 0.f,
@@ -851,9 +863,9 @@ gapgb_status gapgb_surrogate_train_step(gapgb_surrogate *s, int rows_per_species
   k_mlp_back1<<<nblk(total * H), 256, 0, cs>>>(total * H, s->Z1, s->U1, s->Ab1, s->Vb1, s->Zb1, s->Ub1);
   // dW1 = zbar1^T x + ubar1^T r per segment (M = H, N = D, K = R)
   gemm(cs, J, H, D, R, s->Zb1, 1, H, sH, s->X, 1, D, sD, nullptr, 0, s->grad + s->W1, D, s->P, 0.f,
-       tcf);
+       tcf, s->t_part, s->t_part_n);
   gemm(cs, J, H, D, R, s->Ub1, 1, H, sH, s->R16, 1, D, sD, nullptr, 0, s->grad + s->W1, D, s->P, 1.f,
-       tcf);
+       tcf, s->t_part, s->t_part_n);
   k_mlp_colsum<<<dim3(nblk(H), J), 256, 0, cs>>>(R, H, s->P, s->b1, s->Zb1, s->grad);
   const size_t n = (size_t)J * s->P;
   if (d_grad) GAPGB_CUDA_TRY(cudaMemcpyAsync(d_grad, s->grad, n * 4, cudaMemcpyDeviceToDevice, cs));

@@ -23,11 +23,19 @@
 // frees its tensor memory and returns).  The epilogue reads the accumulator
 // with tcgen05.ld, thread = row.
 //
+// A launch with few row tiles (the weight gradients: one 128-row tile per
+// (member, species) block, K = the batch's rows) splits K over CTAs: CTA x of
+// a tile takes chunks [x ks, (x + 1) ks), writes its partial product to a
+// scratch array, and a second kernel adds the partials in split order (so
+// the result does not depend on scheduling) into C.
+//
 // Row tiles follow mlp.cu's species segments, which are padded to 128 rows:
 // a 128-row tile lies in one segment, and a tile whose table entries are
 // both negative (padding) is skipped, as the SIMT kernel skips its 64-row
 // padding tiles.
 #include <cuda_bf16.h>
+
+#include <algorithm>
 
 #include "gapgb_internal.h"
 #include "tc_util.cuh"
@@ -85,7 +93,8 @@ __global__ void __launch_bounds__(128)
     k_mlp_gemm_tc(int M, int N, int K, const __nv_bfloat16 *__restrict__ A, int sAm, int sAk,
                   size_t zA, const __nv_bfloat16 *__restrict__ B, int sBn, int sBk, size_t zB,
                   const int *__restrict__ tile_sp, size_t sBsp, float *__restrict__ C, int ldc,
-                  size_t zC, float beta, int *__restrict__ flags) {
+                  size_t zC, float beta, int *__restrict__ flags, int ks,
+                  float *__restrict__ part) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   unsigned char *sm = reinterpret_cast<unsigned char *>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -121,7 +130,10 @@ __global__ void __launch_bounds__(128)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
   const uint32_t idesc = instr_desc(kGM, BN);
-  const int nk = (K + kGK - 1) / kGK;
+  // this CTA's chunks of K: all of them, or split x's run of ks
+  const int nk_all = (K + kGK - 1) / kGK;
+  const int cb = part ? blockIdx.x * ks : 0;
+  const int nk = part ? min(ks, nk_all - cb) : nk_all;
   bool ok = true;
   int waited[2] = {0, 0};  // commits of each stage waited for
   int issued[2] = {0, 0};  // commits of each stage issued
@@ -134,8 +146,8 @@ __global__ void __launch_bounds__(128)
     }
     if (!__syncthreads_and(ok)) break;
     unsigned char *st = sm + s * kGStage;
-    load_chunk(st, A, sAm, sAk, m0, M, kGM, c * kGK, K, tid);
-    load_chunk(st + kGA, B, sBn, sBk, 0, N, BN, c * kGK, K, tid);
+    load_chunk(st, A, sAm, sAk, m0, M, kGM, (cb + c) * kGK, K, tid);
+    load_chunk(st + kGA, B, sBn, sBk, 0, N, BN, (cb + c) * kGK, K, tid);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -169,7 +181,13 @@ __global__ void __launch_bounds__(128)
     for (int c0 = 0; c0 < BN; c0 += 32) {
       float v[32];
       tmem_ld32(tmem + lane_base + c0, v);
-      if (live) {
+      if (live && part) {
+        // partial [z][split][m][n] of the whole (padded-free) M x N product
+        float *prow = part + (((size_t)blockIdx.z * gridDim.x + blockIdx.x) * M + m) * N;
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (c0 + j < N) prow[c0 + j] = v[j];
+      } else if (live) {
         float *crow = C + (size_t)m * ldc;
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
@@ -186,12 +204,28 @@ __global__ void __launch_bounds__(128)
                  : "memory");
 }
 
+// C[z][m][n] = beta C + sum over splits (in order) of the partials
+__global__ void k_mlp_splitk_reduce(int Z, int M, int N, int splits, const float *__restrict__ part,
+                                    float *__restrict__ C, int ldc, size_t zC, float beta) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t mn = (size_t)M * N;
+  if (t >= (size_t)Z * mn) return;
+  const int z = (int)(t / mn);
+  const size_t r = t % mn;
+  const int m = (int)(r / N), n = (int)(r % N);
+  const float *p = part + (size_t)z * splits * mn + r;
+  float acc = p[0];
+  for (int x = 1; x < splits; ++x) acc += p[(size_t)x * mn];
+  float *c = C + z * zC + (size_t)m * ldc + n;
+  *c = (beta == 0.f ? 0.f : beta * *c) + acc;
+}
+
 }  // namespace
 
 bool mlp_gemm_tc(cudaStream_t st, int Z, int M, int N, int K, const __nv_bfloat16 *A, int sAm,
                  int sAk, size_t zA, const __nv_bfloat16 *B, int sBn, int sBk, size_t zB,
                  const int *tile_sp, size_t sBsp, float *C, int ldc, size_t zC, float beta,
-                 int *flags) {
+                 int *flags, float *part, size_t part_elems) {
   // shapes and strides the staging covers: N <= 128 in one tile, each operand
   // K-contiguous with 16-byte rows or row-contiguous with 16-byte K rows,
   // 16-byte aligned bases and batch offsets
@@ -205,15 +239,31 @@ bool mlp_gemm_tc(cudaStream_t st, int Z, int M, int N, int K, const __nv_bfloat1
   const bool b_k = sBk == 1 && mult8((size_t)sBn) && K % 8 == 0;
   const bool b_n = sBn == 1 && mult8((size_t)sBk) && N % 8 == 0;
   if (!(a_k || a_m) || !(b_k || b_n)) return false;
-  const dim3 grid(1, (M + kGM - 1) / kGM, Z);
+  // split K when the row tiles alone would leave most SMs idle (at least
+  // two chunks per split, about two CTAs per SM, within the scratch)
+  const int mt = (M + kGM - 1) / kGM, nk = (K + kGK - 1) / kGK;
+  int splits = 1, ks = nk;
+  if (part && !tile_sp && mt * Z < device_sms() && nk >= 4) {
+    splits = std::min(nk / 2, (2 * device_sms() + mt * Z - 1) / (mt * Z));
+    while (splits > 1 && (size_t)Z * splits * M * N > part_elems) --splits;
+    ks = (nk + splits - 1) / splits;
+    splits = (nk + ks - 1) / ks;
+  }
+  float *pp = splits > 1 ? part : nullptr;
+  const dim3 grid(splits, mt, Z);
   if (N <= 64) {
     kernel_smem((const void *)k_mlp_gemm_tc<64>, kGSmem, true);
     k_mlp_gemm_tc<64><<<grid, 128, kGSmem, st>>>(M, N, K, A, sAm, sAk, zA, B, sBn, sBk, zB,
-                                                  tile_sp, sBsp, C, ldc, zC, beta, flags);
+                                                  tile_sp, sBsp, C, ldc, zC, beta, flags, ks, pp);
   } else {
     kernel_smem((const void *)k_mlp_gemm_tc<128>, kGSmem, true);
     k_mlp_gemm_tc<128><<<grid, 128, kGSmem, st>>>(M, N, K, A, sAm, sAk, zA, B, sBn, sBk, zB,
-                                                   tile_sp, sBsp, C, ldc, zC, beta, flags);
+                                                   tile_sp, sBsp, C, ldc, zC, beta, flags, ks, pp);
+  }
+  if (pp) {
+    const size_t n = (size_t)Z * M * N;
+    k_mlp_splitk_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(Z, M, N, splits, pp, C, ldc,
+                                                                      zC, beta);
   }
   return true;
 }
