@@ -306,7 +306,7 @@ gapgb_status ensure_surrogate(gapgb_model *m, int N) {
 // into the one force array (FP64 atomics), zeroed before the fork.  The
 // fork / join are event waits, so the pair of streams is captured into a
 // CUDA graph like a single stream.
-constexpr int kSplitMinAtoms = 16384;
+constexpr int kSplitMinAtoms = 20480;
 
 bool split_applies(const gapgb_model *m, int N, int lgrad) {
   return m->pipelines == 2 && !m->profile_stages && lgrad && N >= kSplitMinAtoms &&

@@ -10,7 +10,7 @@ For a calibration batch it evaluates every candidate configuration:
     the descriptor kernels, hence their occupancy;
   - pipelines (GAPGB_OPT_PIPELINES): one stream, or two halves of the batch
     on two streams, for the tensor-core forms with the grouped kernels on a
-    calibration batch of at least 16384 atoms (below that the library runs
+    calibration batch of at least 20480 atoms (below that the library runs
     one stream whatever the option).
 It keeps the candidates whose energies and forces lie within `tol_e`
 eV/atom and `tol_f` eV/A of the plain FP64 path (the drop-in parity path),
@@ -31,7 +31,7 @@ from . import GapModel, OPT_GENERIC_KERNELS, OPT_NEIGHBOUR_CAP, OPT_PIPELINES, l
 # plain FP64 path when no candidate passes the error gates
 FORMS = ("tc", "tf32", "fp32", "mixed", "fp64")
 # smallest batch the library splits into two pipelines (api.cu kSplitMinAtoms)
-SPLIT_MIN_ATOMS = 16384
+SPLIT_MIN_ATOMS = 20480
 
 
 def _signature(model, off, device_name):

@@ -65,7 +65,7 @@ typedef enum {
   GAPGB_OPT_GENERIC_KERNELS = 3, /* 1: FP32 descriptor kernels take the generic
                                     path even when the fast path applies */
   GAPGB_OPT_PIPELINES = 4        /* 1 or 2 (default 2): a batch of at least
-                                    16384 atoms in the TC / TF32 forms (grouped
+                                    20480 atoms in the TC / TF32 forms (grouped
                                     descriptor kernels, gradients on) is
                                     evaluated as two halves on two streams, so
                                     one half's kernels fill the SMs the other

@@ -34,6 +34,9 @@ def test_roofline_entry_keys_and_arithmetic():
     t32 = bench.roofline(stages, N, D, "tf32")["gpr_tensor"]
     assert np.isclose(t32["peak"], 0.5 * peaks["bf16_tflops"])
     assert np.isclose(t32["achieved"], 4.0 * N * 4032 * 64 / 0.24e-3 / 1e12)
+    # a measured TF32 rate replaces the nominal ratio
+    t32m = bench.roofline(stages, N, D, "tf32", tf32_tflops=900.0)["gpr_tensor"]
+    assert t32m["peak"] == 900.0 and "measured" in t32m["peak_source"]
 
 
 def test_roofline_population_counts_and_no_alloy_traffic():

@@ -14,7 +14,7 @@ from helpers import write_model_file
 
 pytestmark = pytest.mark.gpu
 
-NCELLS = 41  # 20 992 atoms: above the 16 384-atom threshold, split inside cell 20
+NCELLS = 41  # 20 992 atoms: above the 20 480-atom threshold, split inside cell 20
 
 
 @pytest.fixture(scope="module")
