@@ -186,33 +186,24 @@ __device__ __forceinline__ void pair_stream(const float4 *__restrict__ A, int P,
   const unsigned lt = (1u << lane) - 1u;
   int qh = 0, qn = 0;  // ring queue: entries [qh, qn) are pending
   // candidate t of the row pair (r, r2): its (j, k), whether it contributes,
-  // and r_jk^2
+  // and r_jk^2.  Branch-free: a lane past the row pair's end reads slots 0
+  // and 1 (P > 1) and reports no pair
   auto cand = [&](int r, int r2, int n1, int tot, int t, int &j, int &k, float &c2) {
-    j = r;
-    k = r + 1 + t;
-    if (t >= n1) {
-      j = r2;
-      k = r2 + 1 + (t - n1);
-    }
-    bool valid = false;
-    c2 = 0.f;
-    if (t < tot) {
-      const float4 aj = A[j], ak = A[k];
-      if (aj.w <= rc && ak.w <= rc) {
-        const float cx = aj.x - ak.x, cy = aj.y - ak.y, cz = aj.z - ak.z;
-        c2 = cx * cx + cy * cy + cz * cz;
-        valid = c2 <= rc2;
-      }
-    }
-    return valid;
+    const bool in = t < tot, second = t >= n1;
+    j = in ? (second ? r2 : r) : 0;
+    k = in ? (second ? r2 + 1 + (t - n1) : r + 1 + t) : 1;
+    const float4 aj = A[j], ak = A[k];
+    const float cx = aj.x - ak.x, cy = aj.y - ak.y, cz = aj.z - ak.z;
+    c2 = cx * cx + cy * cy + cz * cz;
+    return in & (aj.w <= rc) & (ak.w <= rc) & (c2 <= rc2);
   };
+  // queue the contributing candidates in lane order; every lane stores, the
+  // others into their own spare entry past the ring (entries Q + lane)
   auto push = [&](bool valid, int j, int k, float c2) {
     const unsigned m = __ballot_sync(0xffffffffu, valid);
-    if (valid) {
-      const int e = (qn + __popc(m & lt)) & (Q - 1);
-      qjk[e] = j | (k << 16);
-      qc2[e] = c2;
-    }
+    const int e = valid ? (qn + __popc(m & lt)) & (Q - 1) : Q + lane;
+    qjk[e] = j | (k << 16);
+    qc2[e] = c2;
     qn += __popc(m);
   };
   const int nfold = P / 2;  // row pairs (r, P - 2 - r); the middle row of an even P is alone
@@ -310,8 +301,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
   (void)nj;
   (void)apos;
   extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ int s_qjk[kWarpsPerBlock][kPairQFwd];
-  __shared__ float s_qc2[kWarpsPerBlock][kPairQFwd];
+  __shared__ int s_qjk[kWarpsPerBlock][kPairQFwd + 32];  // ring + the lanes' spare entries
+  __shared__ float s_qc2[kWarpsPerBlock][kPairQFwd + 32];
   __shared__ float s_acc[kWarpsPerBlock][2 * NAL * NC];
   __shared__ float s_out[kWarpsPerBlock][(STD && NC == 6) ? 2 * NAL * NC : 1];
   load_table<float>(smraw, sfg);
@@ -563,8 +554,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
   (void)xyzr;
   (void)apos;
   extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ int s_qjk[kWarpsPerBlock][kPairQBwd];
-  __shared__ float s_qc2[kWarpsPerBlock][kPairQBwd];
+  __shared__ int s_qjk[kWarpsPerBlock][kPairQBwd + 32];  // ring + the lanes' spare entries
+  __shared__ float s_qc2[kWarpsPerBlock][kPairQBwd + 32];
   __shared__ float s_u[kWarpsPerBlock][2 * NAL * NC];
   load_table<float>(smraw, sfg);
   const SFT<float> &sf = *reinterpret_cast<const SFT<float> *>(smraw);
