@@ -301,8 +301,10 @@ __global__ void __launch_bounds__(128, 5) k_nbr_build(int N, int cap, double rcu
                                                    int *__restrict__ nj, int *__restrict__ ns,
                                                    float4 *__restrict__ d32, float *__restrict__ w32,
                                                    int *__restrict__ flags) {
-  __shared__ int s_qj[kWarpsPerBlock][kQueue];
-  __shared__ int s_qs[kWarpsPerBlock][kQueue];
+  // the ring queue and, past it, one spare entry per lane for the branch-free
+  // store of a lane without a survivor
+  __shared__ int s_qj[kWarpsPerBlock][kQueue + 32];
+  __shared__ int s_qs[kWarpsPerBlock][kQueue + 32];
   __shared__ double s_dn[2 * kMaxImage + 1];  // s_dn[n + kMaxImage] = (double)n
   for (int t = threadIdx.x; t < 2 * kMaxImage + 1; t += blockDim.x) s_dn[t] = (double)(t - kMaxImage);
   __syncthreads();
@@ -392,28 +394,27 @@ __global__ void __launch_bounds__(128, 5) k_nbr_build(int N, int cap, double rcu
       const int j = si.a0 + jl;
       const float4 fj = fj_next;
       if (jl + 32 < si.na) fj_next = frac32[j + 32];
-      int lo[3] = {0, 0, 0}, hi[3] = {-1, -1, -1};
-      float fd[3] = {0.f, 0.f, 0.f};
-      if (valid) {
-        fd[0] = fj.x - fi.x;
-        fd[1] = fj.y - fi.y;
-        fd[2] = fj.z - fi.z;
-        image_box(ext, si.nabc, fi, fj, lo, hi);
+      // (branch-free: a lane past the structure's atoms has an empty box)
+      int lo[3], hi[3];
+      const float fd[3] = {fj.x - fi.x, fj.y - fi.y, fj.z - fi.z};
+      image_box(ext, si.nabc, fi, fj, lo, hi);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        lo[a] = valid ? lo[a] : 0;
+        hi[a] = valid ? hi[a] : -1;
       }
       // Every lane's box holds at most one image (cells wider than twice the
       // cutoff): one screen per lane, survivors queued in lane order - the
       // candidates and the order of the general loops below, without them
-      const bool none = hi[0] < lo[0] || hi[1] < lo[1] || hi[2] < lo[2];
-      const bool one = hi[0] == lo[0] && hi[1] == lo[1] && hi[2] == lo[2];
+      const bool none = (hi[0] < lo[0]) | (hi[1] < lo[1]) | (hi[2] < lo[2]);
+      const bool one = (hi[0] == lo[0]) & (hi[1] == lo[1]) & (hi[2] == lo[2]);
       if (__all_sync(0xffffffffu, none || one)) {
-        const bool keep = one && !(j == i && lo[0] == 0 && lo[1] == 0 && lo[2] == 0) &&
-                          screen_r2(L32, fd, lo[0], lo[1], lo[2]) <= r2max;
+        const bool self = (j == i) & (lo[0] == 0) & (lo[1] == 0) & (lo[2] == 0);
+        const bool keep = one & !self & (screen_r2(L32, fd, lo[0], lo[1], lo[2]) <= r2max);
         const unsigned m = __ballot_sync(0xffffffffu, keep);
-        if (keep) {
-          const int e = (qt + __popc(m & lt_mask)) & (kQueue - 1);
-          qj[e] = j;
-          qs[e] = ((lo[0] + 128) << 16) | ((lo[1] + 128) << 8) | (lo[2] + 128);
-        }
+        const int e = keep ? (qt + __popc(m & lt_mask)) & (kQueue - 1) : kQueue + lane;
+        qj[e] = j;
+        qs[e] = ((lo[0] + 128) << 16) | ((lo[1] + 128) << 8) | (lo[2] + 128);
         qt += __popc(m);
         __syncwarp();
         drain(false);
