@@ -343,27 +343,26 @@ __global__ void __launch_bounds__(128, 5) k_nbr_build(int N, int cap, double rcu
     // `all`), hits appended in queue order = the reference order
     auto drain = [&](bool all) {
       while (qt - qh >= 32 || (all && qt > qh)) {
+        // branch-free: a lane past the queue's end tests the batch's first
+        // entry (queued, so in range) and reports no hit
         const int t = qh + lane;
-        bool hit = false;
+        const bool in = t < qt;
+        bool hit;
         double xyz[3] = {0, 0, 0};
         double dis = 0;
         float4 fr = make_float4(0.f, 0.f, 0.f, 0.f);
-        int jj = 0, sh = 0;
-        if (t < qt) {
-          const int e = t & (kQueue - 1);
-          jj = qj[e];
-          sh = qs[e];
-          const int n1 = ((sh >> 16) & 255) - 128, n2 = ((sh >> 8) & 255) - 128,
-                    n3 = (sh & 255) - 128;
-          if (EXACT) {
-            dis = ref_image(pi, apos[jj], si.lat, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
-                            s_dn[n3 + kMaxImage], xyz);
-            hit = !(dis > rcut);
-          } else {
-            fr = fast_rel(pi, apos[jj], si.lat, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
-                          s_dn[n3 + kMaxImage]);
-            hit = fr.w <= rc2f;
-          }
+        const int e = (in ? t : qh) & (kQueue - 1);
+        const int jj = qj[e], sh = qs[e];
+        const int n1 = ((sh >> 16) & 255) - 128, n2 = ((sh >> 8) & 255) - 128,
+                  n3 = (sh & 255) - 128;
+        if (EXACT) {
+          dis = ref_image(pi, apos[jj], si.lat, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
+                          s_dn[n3 + kMaxImage], xyz);
+          hit = in & !(dis > rcut);
+        } else {
+          fr = fast_rel(pi, apos[jj], si.lat, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
+                        s_dn[n3 + kMaxImage]);
+          hit = in & (fr.w <= rc2f);
         }
         __syncwarp();
         const unsigned m = __ballot_sync(0xffffffffu, hit);
