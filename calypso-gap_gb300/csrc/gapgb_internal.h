@@ -219,6 +219,12 @@ struct StructInfo {
   double linv[9];  // inverse: fractional f = d * linv (row vector)
   double ext[3];   // conservative |f_a + n_a| bound: rcut * |column a of linv|
   double volume;   // |det(lat)| (gap_calc.f90:201)
+  // FP32 forms of the screen's constants, formed once per structure (the
+  // conversions run on the narrow FP64 pipe): the lattice, ext, the squared
+  // screen bound (rcut plus the fractional rounding margin) and rcut^2
+  float lat32[9];
+  float ext32[3];
+  float r2max32, rc2_32;
   int nabc[3];     // gap_calc.f90:85-88
   int a0, na;
   // spatial bins of a large cell (nb[0] == 0: not binned): nb[a] bins of

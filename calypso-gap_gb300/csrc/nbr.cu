@@ -85,6 +85,17 @@ __global__ void k_prep_struct(int S, const int *__restrict__ atom_off,
     // for their rounding (|f| < 1e3 keeps the error below 1e-4)
     si.ext[a] = rcut * cl * (1.0 + 1e-9) + 2e-4;
   }
+  {
+    float lsum = 0.f;
+    for (int q = 0; q < 9; ++q) {
+      si.lat32[q] = (float)si.lat[q];
+      lsum += fabsf(si.lat32[q]);
+    }
+    const float rs = (float)rcut + 2.5e-4f * lsum + 1e-3f;
+    si.r2max32 = rs * rs;
+    si.rc2_32 = (float)(rcut * rcut);
+    for (int a = 0; a < 3; ++a) si.ext32[a] = (float)si.ext[a];
+  }
   si.a0 = atom_off[s];
   si.na = atom_off[s + 1] - atom_off[s];
   // bins of fractional width >= ext (+ 1e-3 for the FP32 coordinates of the
@@ -317,18 +328,12 @@ __global__ void __launch_bounds__(128, 5) k_nbr_build(int N, int cap, double rcu
     if (si.nb[0] != 0) continue;  // large cells: k_nbr_build_binned
     const double4 pi = apos[i];
     const float4 fi = frac32[i];
-    float L32[9];
-    float lsum = 0.f;
-#pragma unroll
-    for (int q = 0; q < 9; ++q) {
-      L32[q] = (float)si.lat[q];
-      lsum += fabsf(L32[q]);
-    }
-    // FP32 screen bound: rcut plus the fractional rounding margin in Angstrom
-    const float rs = (float)rcut + 2.5e-4f * lsum + 1e-3f;
-    const float r2max = rs * rs;
-    const float rc2f = (float)(rcut * rcut);
-    const float ext[3] = {(float)si.ext[0], (float)si.ext[1], (float)si.ext[2]};
+    // FP32 screen constants of the structure (k_prep_struct): the lattice,
+    // the squared bound rcut plus the fractional rounding margin, rcut^2
+    const float *L32 = si.lat32;
+    const float r2max = si.r2max32;
+    const float rc2f = si.rc2_32;
+    const float *ext = si.ext32;
     double4 *oxyz = xyzr + (size_t)i * cap;
     int *oj = nj + (size_t)i * cap;
     int *os = ns + (size_t)i * cap;
@@ -505,16 +510,9 @@ __global__ void __launch_bounds__(128) k_nbr_build_binned(
     if (si.nb[0] == 0) continue;
     const double4 pi = apos[i];
     const float4 fi = frac32[i];
-    float L32[9];
-    float lsum = 0.f;
-#pragma unroll
-    for (int q = 0; q < 9; ++q) {
-      L32[q] = (float)si.lat[q];
-      lsum += fabsf(L32[q]);
-    }
-    const float rs = (float)rcut + 2.5e-4f * lsum + 1e-3f;
-    const float r2max = rs * rs;
-    const float rc2f = (float)(rcut * rcut);
+    const float *L32 = si.lat32;  // FP32 screen constants (k_prep_struct)
+    const float r2max = si.r2max32;
+    const float rc2f = si.rc2_32;
     const int mi = atom_m[i];
     const int mi3[3] = {((mi >> 16) & 255) - 128, ((mi >> 8) & 255) - 128, (mi & 255) - 128};
     const int local = atom_bin[i] - si.bin0;
