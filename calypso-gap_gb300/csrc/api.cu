@@ -253,12 +253,19 @@ bool finite_all(const double *p, size_t n) {
   return true;
 }
 
-gapgb_status check_batch_host(int nstruct, const int *atom_off, const double *lat,
-                              const double *pos) {
+// the batch's structure offsets (cheap: one pass over nstruct entries)
+gapgb_status check_offsets_host(int nstruct, const int *atom_off) {
   if (nstruct <= 0 || !atom_off) return fail(GAPGB_ERR_ARG, "nstruct must be positive");
   if (atom_off[0] != 0) return fail(GAPGB_ERR_ARG, "atom_off[0] must be 0");
   for (int s = 0; s < nstruct; ++s)
     if (atom_off[s + 1] <= atom_off[s]) return fail(GAPGB_ERR_ARG, "every structure needs at least one atom");
+  return GAPGB_OK;
+}
+
+// finite lattices and positions, non-singular lattices (one pass over the
+// positions: the host path runs it while the inputs are being copied)
+gapgb_status check_geometry_host(int nstruct, const int *atom_off, const double *lat,
+                                 const double *pos) {
   if (!finite_all(lat, (size_t)nstruct * 9)) return fail(GAPGB_ERR_ARG, "non-finite lattice");
   if (!finite_all(pos, (size_t)atom_off[nstruct] * 3)) return fail(GAPGB_ERR_ARG, "non-finite position");
   for (int s = 0; s < nstruct; ++s) {
@@ -268,6 +275,12 @@ gapgb_status check_batch_host(int nstruct, const int *atom_off, const double *la
     if (!(std::fabs(det) > 0.0)) return fail(GAPGB_ERR_ARG, "singular lattice");
   }
   return GAPGB_OK;
+}
+
+gapgb_status check_batch_host(int nstruct, const int *atom_off, const double *lat,
+                              const double *pos) {
+  gapgb_status st = check_offsets_host(nstruct, atom_off);
+  return st ? st : check_geometry_host(nstruct, atom_off, lat, pos);
 }
 
 // Everything after the neighbour list, enqueued on `st`.
@@ -424,8 +437,9 @@ void read_stage_times(gapgb_model *m) {
 gapgb_status eval_host(gapgb_model *m, int S, const int *atom_off, const int *species,
                        const double *lat, const double *pos, int lgrad, double *energy,
                        double *force, double *stress, double *atom_e, double **d_G_out) {
-  gapgb_status st = check_batch_host(S, atom_off, lat, pos);
+  gapgb_status st = check_offsets_host(S, atom_off);
   if (st) return st;
+  if (!lat || !pos) return fail(GAPGB_ERR_ARG, "null argument");
   const int N = atom_off[S];
   st = upload_model(m);
   if (st) return st;
@@ -438,6 +452,13 @@ gapgb_status eval_host(gapgb_model *m, int S, const int *atom_off, const int *sp
   GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_species, species, sizeof(int) * N, cudaMemcpyHostToDevice, s));
   GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_lat, lat, sizeof(double) * 9 * S, cudaMemcpyHostToDevice, s));
   GAPGB_CUDA_TRY(cudaMemcpyAsync(ws.d_pos, pos, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, s));
+  // the geometry checks run on the host while the copies are in flight; no
+  // kernel is launched before they pass
+  st = check_geometry_host(S, atom_off, lat, pos);
+  if (st) {
+    cudaStreamSynchronize(s);  // the copies read the caller's buffers
+    return st;
+  }
   const int maxa = max_struct_atoms(S, atom_off);
   // the slot count the descriptor kernels are sized for: the previous call's
   // maximum, or on a model's first call the whole capacity (a bound on any
