@@ -31,21 +31,21 @@ constexpr int kPairQBwd = 64;
 constexpr int kGrpMinBlocks = 6;
 
 // Per-warp shared-memory layout of the grouped kernels: packed slot records
-// (a pair reads its two slots with six 128-bit loads) and the per-cutoff
-// tables of the radial terms.
+// (a pair reads its two slots with four 128-bit loads; the angular
+// exponential exp(-alpha (rij^2 + rik^2 + rjk^2)) is formed per pair from the
+// three squared lengths) and the per-cutoff tables of the radial terms.
 //   a[q] = (dx, dy, dz, r)        b[q] = (1/r, w, fc, fc') at the angular cutoff
-//   e[q] = exp(-alpha_t r^2), t < 4
 //   fc[g][q], dfc[g][q]           cutoff function of every cutoff group g
 //   rco[s]                        (kx, rs, dE/dG_d, dE/dG_{d+nsf}) of radial SF s
 //                                 (gradient kernel)
 //   gx, gy, gz [q], dg[D]         slot gradients and dE/dG (gradient kernel)
 struct GLay {
-  float4 *a, *b, *e, *rco;
+  float4 *a, *b, *rco;
   float *fc, *dfc, *gx, *gy, *gz, *dg;
 };
 
 __host__ __device__ inline size_t grp_warp_floats(int capS, int nrc, int D, int nrad, bool fwd) {
-  const size_t n = (size_t)12 * capS + (size_t)nrc * capS * (fwd ? 1 : 2) +
+  const size_t n = (size_t)8 * capS + (size_t)nrc * capS * (fwd ? 1 : 2) +
                    (fwd ? 0 : (size_t)4 * nrad + (size_t)3 * capS + D);
   return (n + 3) / 4 * 4;  // keeps every warp's records 16-byte aligned
 }
@@ -57,9 +57,8 @@ __device__ __forceinline__ GLay grp_carve(unsigned char *raw, int warp, int capS
   GLay L;
   L.a = reinterpret_cast<float4 *>(base);
   L.b = L.a + capS;
-  L.e = L.b + capS;
-  L.rco = fwd ? nullptr : L.e + capS;  // gradient kernel: per-SF radial records
-  L.fc = reinterpret_cast<float *>(fwd ? L.e + capS : L.rco + nrad);
+  L.rco = fwd ? nullptr : L.b + capS;  // gradient kernel: per-SF radial records
+  L.fc = reinterpret_cast<float *>(fwd ? L.b + capS : L.rco + nrad);
   L.dfc = fwd ? nullptr : L.fc + (size_t)nrc * capS;
   L.gx = fwd ? nullptr : L.dfc + (size_t)nrc * capS;
   L.gy = fwd ? nullptr : L.gx + capS;
@@ -104,12 +103,8 @@ __device__ __forceinline__ int grp_stage(const GLay &L, const SFT<float> &sf, in
         dfa = dfcv;
       }
     }
-    float ev[4];
-#pragma unroll
-    for (int t = 0; t < 4; ++t) ev[t] = t < nal ? expf(-sf.alpha_val[t] * r * r) : 0.f;
     L.a[q] = g;
     L.b[q] = make_float4(1.f / r, w, fa, dfa);
-    L.e[q] = make_float4(ev[0], ev[1], ev[2], ev[3]);
   }
   return P;
 }
@@ -312,10 +307,13 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
   const GLay L = grp_carve(smraw, warp, capS, sf.nrc, D, sf.nrad, true);
   const int rci = nang > 0 ? sf.ang_grp_rc[0] : 0;
   const float rc = sf.rc_val[rci], pirc = sf.pi_over_rc[rci];
-  float alv[NAL], clam[NC];
+  float alv[NAL], kal[NAL], clam[NC];
   int ciz[NC];
 #pragma unroll
-  for (int q = 0; q < NAL; ++q) alv[q] = q < nal ? sf.alpha_val[q] : 0.f;
+  for (int q = 0; q < NAL; ++q) {
+    alv[q] = q < nal ? sf.alpha_val[q] : 0.f;
+    kal[q] = -alv[q] * kLog2e;
+  }
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
     clam[c] = sf.comb_lam[c];
@@ -350,16 +348,18 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
         np += __popc(vm);
         if (!ok) return;
         const float a = L.a[j].w, b = L.a[k].w;
-        const float4 Bj = L.b[j], Bk = L.b[k], Ej = L.e[j], Ek = L.e[k];
+        const float4 Bj = L.b[j], Bk = L.b[k];
         const float c = c2 > 0.f ? c2 * rsqrtf(c2) : 0.f;
         // costheta = (rij^2 + rik^2 - rjk^2) / (2 rij rik) (wacsf.f90:271-273)
-        const float cosv = (a * a + b * b - c2) * 0.5f * Bj.x * Bk.x;
+        const float sab = a * a + b * b;
+        const float cosv = (sab - c2) * 0.5f * Bj.x * Bk.x;
         const float F = Bj.z * Bk.z * (0.5f * (__cosf(pirc * c) + 1.f));
         const float wjk = Bj.y * Bk.y;
+        // exp(-alpha (rij^2 + rik^2 + rjk^2)) as one 2^x (kal = -alpha log2 e)
+        const float s3 = sab + c2;
         float EF[NAL];
 #pragma unroll
-        for (int q = 0; q < NAL; ++q)
-          EF[q] = q < nal ? f4get(Ej, q) * f4get(Ek, q) * __expf(-alv[q] * c2) * F : 0.f;
+        for (int q = 0; q < NAL; ++q) EF[q] = q < nal ? ex2f(kal[q] * s3) * F : 0.f;
         float basis[NB];
         if constexpr (kB) {
           const float u = fmaf(0.5f, cosv, 0.5f), w = fmaf(-0.5f, cosv, 0.5f);
@@ -491,21 +491,24 @@ struct AngCoef {
 
 // Gradient of one angular pair's contribution sum_s dE/dG_s G_s(j, k) with
 // respect to the positions of slots j and k: vj and vk.  Slot j's records
-// (Aj, Bj, Ej) come from the caller, which keeps them across a run of pairs
-// that share j.
+// (Aj, Bj) come from the caller, which keeps them across a run of pairs that
+// share j.  The exponential factor exp(-alpha (rij^2 + rik^2 + rjk^2)) is one
+// 2^x with kal = -alpha log2 e.
 template <int NAL, int NC, bool STD>
 __device__ __forceinline__ void pair_grad(const GLay &L, const float4 &Aj, const float4 &Bj,
-                                          const float4 &Ej, int k, float pirc, int nal,
-                                          const float (&alv)[NAL], const float (&clam)[NC],
+                                          int k, float pirc, int nal,
+                                          const float (&alv)[NAL], const float (&kal)[NAL],
+                                          const float (&clam)[NC],
                                           const int (&ciz)[NC], const AngCoef<NAL, NC, STD> &U,
                                           float3 &vj, float3 &vk) {
-  const float4 Ak = L.a[k], Bk = L.b[k], Ek = L.e[k];
+  const float4 Ak = L.a[k], Bk = L.b[k];
   const float cx = Aj.x - Ak.x, cy = Aj.y - Ak.y, cz = Aj.z - Ak.z;
   const float c2 = cx * cx + cy * cy + cz * cz;
   const float a = Aj.w, b = Ak.w;
   const float ic = c2 > 0.f ? rsqrtf(c2) : 0.f, c = c2 * ic;
   const float ia = Bj.x, ib = Bk.x;
-  const float cosv = (a * a + b * b - c2) * 0.5f * ia * ib;
+  const float sab = a * a + b * b, sum2 = sab + c2;
+  const float cosv = (sab - c2) * 0.5f * ia * ib;
   const float dcda = ib - cosv * ia, dcdb = ia - cosv * ib, dcdc = -c * ia * ib;
   float sn, cs;
   __sincosf(pirc * c, &sn, &cs);
@@ -517,7 +520,7 @@ __device__ __forceinline__ void pair_grad(const GLay &L, const float4 &Aj, const
   float SP = 0.f, SQ = 0.f, SU = 0.f;
 #pragma unroll
   for (int q = 0; q < NAL; ++q) {
-    const float E = q < nal ? f4get(Ej, q) * f4get(Ek, q) * __expf(-alv[q] * c2) : 0.f;
+    const float E = q < nal ? ex2f(kal[q] * sum2) : 0.f;
     SP += E * Pd[q];
     SQ += E * Pv[q];
     SU += alv[q] * E * Pv[q];
@@ -564,10 +567,13 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
   const GLay L = grp_carve(smraw, warp, capS, sf.nrc, D, nrad, false);
   const int rci = nang > 0 ? sf.ang_grp_rc[0] : 0;
   const float rc = sf.rc_val[rci], pirc = sf.pi_over_rc[rci];
-  float alv[NAL], clam[NC];
+  float alv[NAL], kal[NAL], clam[NC];
   int ciz[NC];
 #pragma unroll
-  for (int q = 0; q < NAL; ++q) alv[q] = q < nal ? sf.alpha_val[q] : 0.f;
+  for (int q = 0; q < NAL; ++q) {
+    alv[q] = q < nal ? sf.alpha_val[q] : 0.f;
+    kal[q] = -alv[q] * kLog2e;
+  }
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
     clam[c] = sf.comb_lam[c];
@@ -636,7 +642,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
         int nxt = p0 < pe ? (int)prow[p0] : 0;
         int cur = -1;
         float gjx = 0.f, gjy = 0.f, gjz = 0.f;
-        float4 Aj = make_float4(0.f, 0.f, 0.f, 0.f), Bj = Aj, Ej = Aj;  // slot cur's records
+        float4 Aj = make_float4(0.f, 0.f, 0.f, 0.f), Bj = Aj;  // slot cur's records
         for (int t = 0; t < C; ++t) {
           const int p = p0 + t;
           const int jk = nxt;
@@ -653,10 +659,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
               gjx = gjy = gjz = 0.f;
               Aj = L.a[j];
               Bj = L.b[j];
-              Ej = L.e[j];
             }
             float3 vj, vk;
-            pair_grad<NAL, NC, STD>(L, Aj, Bj, Ej, k, pirc, nal, alv, clam, ciz, U, vj, vk);
+            pair_grad<NAL, NC, STD>(L, Aj, Bj, k, pirc, nal, alv, kal, clam, ciz, U, vj, vk);
             gjx += vj.x;
             gjy += vj.y;
             gjz += vj.z;
@@ -674,8 +679,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
         pair_stream<kPairQBwd>(L.a, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
           (void)c2;
           float3 vj, vk;
-          pair_grad<NAL, NC, STD>(L, L.a[j], L.b[j], L.e[j], k, pirc, nal, alv, clam, ciz, U, vj,
-                                  vk);
+          pair_grad<NAL, NC, STD>(L, L.a[j], L.b[j], k, pirc, nal, alv, kal, clam, ciz, U, vj, vk);
           float vx = ok ? vj.x : 0.f, vy = ok ? vj.y : 0.f, vz = ok ? vj.z : 0.f;
           // slot j: equal j values are contiguous lanes of the batch, summed
           // by a segmented scan whose last lane adds the run
