@@ -123,9 +123,9 @@ __global__ void __launch_bounds__(kGprThreads, 2)
   const float xnorm = (i < N) ? xn[i] : 0.f;
   // w = c exp(-s/2) = c 2^(log2e v + a2_i + b2_k) with a2_i = -log2e |x''_i|^2 / 2
   // and b2_k = -log2e |m''_k|^2 / 2 (the image stores b2): one add, one FMA
-  // and ex2 per element.  e = sum w in four independent Kahan chains, one per
-  // element pair of a core-matrix row, so consecutive elements do not wait
-  // on each other.
+  // and ex2 per element.  e = sum w: each thread sums its 32 elements of a
+  // tile into four plain partial sums (8 elements each), which enter four
+  // independent Kahan chains once per tile.
   const float a2 = -0.5f * kLog2e * xnorm;
   float esum[4] = {0.f, 0.f, 0.f, 0.f}, ecmp[4] = {0.f, 0.f, 0.f, 0.f};
   // N = 128: [mh; ml] (GEMM1) or [mhT; mlT] (GEMM2); N = 64: mh or mhT alone
@@ -199,6 +199,7 @@ __global__ void __launch_bounds__(kGprThreads, 2)
     for (int cc = kHalfBlocks * half; cc < kHalfBlocks * (half + 1); ++cc) {
       float v[32];
       tmem_ld32_sum2(tC1 + lane_base + cc * 32, kTileK, v);
+      float part[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
       for (int g = 0; g < 4; ++g) {
         uint32_t hpk[4], lpk[4];
@@ -216,10 +217,7 @@ __global__ void __launch_bounds__(kGprThreads, 2)
           for (int u = 0; u < 2; ++u) {
             const int q = h * 2 + u;
             const float w = cv[q] * ex2_approx(fmaf(v[g * 8 + q], kLog2e, a2 + bv[q]));
-            const float y = w - ecmp[h];  // Kahan
-            const float tt = esum[h] + y;
-            ecmp[h] = (tt - esum[h]) - y;
-            esum[h] = tt;
+            part[h] += w;
             w2[u] = w;
           }
           const __nv_bfloat162 hi = __floats2bfloat162_rn(w2[0], w2[1]);
@@ -231,6 +229,13 @@ __global__ void __launch_bounds__(kGprThreads, 2)
         const int off = kmajor_off(row, k0, kTileK / 8);
         *reinterpret_cast<uint4 *>(wh + off) = make_uint4(hpk[0], hpk[1], hpk[2], hpk[3]);
         *reinterpret_cast<uint4 *>(wl + off) = make_uint4(lpk[0], lpk[1], lpk[2], lpk[3]);
+      }
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {  // Kahan
+        const float y = part[h] - ecmp[h];
+        const float tt = esum[h] + y;
+        ecmp[h] = (tt - esum[h]) - y;
+        esum[h] = tt;
       }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
