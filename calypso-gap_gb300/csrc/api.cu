@@ -422,6 +422,9 @@ gapgb_status flags_to_status(const int *f) {
   if (f[0] & kFlagTimeout) return fail(GAPGB_ERR_TIMEOUT, "a bounded device wait gave up");
   if (f[0] & kFlagNotPositiveDefinite)
     return fail(GAPGB_ERR_ARG, "the fit's normal matrix is not positive definite (raise the jitter)");
+  if (f[0] & kFlagForceRange)
+    return fail(GAPGB_ERR_CAP_EXCEEDED,
+                "a slot-gradient term beyond 2047 eV/A or not finite (FP32 forms); use the FP64 form");
   if (f[0] & kFlagSkinExceeded)
     return fail(GAPGB_ERR_CAP_EXCEEDED, "an atom moved more than half the Verlet skin between rebuilds");
   return GAPGB_OK;

@@ -49,6 +49,7 @@ enum : int {
   kFlagTimeout = 16,
   kFlagSkinExceeded = 32,  // MD: an atom moved more than half the skin since the last rebuild
   kFlagNotPositiveDefinite = 64,  // fit: a Cholesky pivot was not positive
+  kFlagForceRange = 128,  // FP32 gradient: a slot-gradient term beyond the fixed-point range
 };
 
 // Symmetry-function table as the kernels read it.  Angular SFs are grouped by

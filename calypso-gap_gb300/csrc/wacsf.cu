@@ -686,7 +686,7 @@ bool launch_wacsf_bwd(const gapgb_model *m, Workspace &ws, int N, int cap, int c
           n, a0, cap, capS, ws.nbr_cnt + a0, ws.nbr_xyz, ws.nbr_j + (size_t)a0 * cap, ws.apos,
           ws.nbr_d32 + (size_t)a0 * cap, ws.nbr_w32 + (size_t)a0 * cap, m->d_sft32,
           (const float *)ws.dedg + (size_t)a0 * D, d_force, ws.wvir + (size_t)a0 * 9,
-          ws.pairs + (size_t)a0 * kPairCap, ws.pair_cnt + a0, pcap);
+          ws.pairs + (size_t)a0 * kPairCap, ws.pair_cnt + a0, pcap, ws.d_flags);
       return true;  // forces scattered by the kernel
     }
   }

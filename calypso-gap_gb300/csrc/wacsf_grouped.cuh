@@ -15,10 +15,11 @@
 //    so the pair's chain-rule scalars need NAL x NC multiply-adds in total.
 // Pairs beyond the cutoff are dropped by a per-warp ballot queue before the
 // arithmetic, so all lanes work on contributing pairs.  The gradient kernel
-// accumulates slot gradients with shared-memory FP32 atomics (summation
-// order, hence the last bits, may vary between runs; the FP64 path keeps the
-// deterministic round-robin schedule) and scatters the forces with FP64
-// atomics in place of the reverse-slot gather.
+// accumulates slot gradients in fixed point by int32 shared-memory atomics
+// (exact integer sums, so the same in every run) and scatters the forces
+// with FP64 atomics in place of the reverse-slot gather (their order, hence
+// the forces' last bits, may vary between runs; the FP64 path keeps the
+// deterministic round-robin schedule).
 
 // per-warp ring queues of contributing pairs: the forward kernel screens two
 // 32-candidate batches per step (at most 31 + 64 entries pending), the
@@ -35,18 +36,24 @@ constexpr int kGrpMinBlocks = 6;
 // exponential exp(-alpha (rij^2 + rik^2 + rjk^2)) is formed per pair from the
 // three squared lengths) and the per-cutoff tables of the radial terms.
 //   a[q] = (dx, dy, dz, r)        b[q] = (1/r, w, fc, fc') at the angular cutoff
-//   fc[g][q], dfc[g][q]           cutoff function of every cutoff group g
+//   fc[g][q], dfc[g][q]           cutoff function of every cutoff group g, kept
+//                                 only with several groups (with one, b holds it)
 //   rco[s]                        (kx, rs, dE/dG_d, dE/dG_{d+nsf}) of radial SF s
 //                                 (gradient kernel)
-//   gx, gy, gz [q], dg[D]         slot gradients and dE/dG (gradient kernel)
+//   gh[c][q], gl[c][q]            slot gradient component c in fixed point,
+//                                 gh 2^-9 + gl 2^-29 (gradient kernel)
+//   dg[D]                         dE/dG (gradient kernel)
 struct GLay {
   float4 *a, *b, *rco;
-  float *fc, *dfc, *gx, *gy, *gz, *dg;
+  float *fc, *dfc, *dg;
+  int *gh, *gl;
 };
 
+__host__ __device__ inline int grp_fc_groups(int nrc) { return nrc > 1 ? nrc : 0; }
+
 __host__ __device__ inline size_t grp_warp_floats(int capS, int nrc, int D, int nrad, bool fwd) {
-  const size_t n = (size_t)8 * capS + (size_t)nrc * capS * (fwd ? 1 : 2) +
-                   (fwd ? 0 : (size_t)4 * nrad + (size_t)3 * capS + D);
+  const size_t n = (size_t)8 * capS + (size_t)grp_fc_groups(nrc) * capS * (fwd ? 1 : 2) +
+                   (fwd ? 0 : (size_t)4 * nrad + (size_t)6 * capS + D);
   return (n + 3) / 4 * 4;  // keeps every warp's records 16-byte aligned
 }
 
@@ -59,11 +66,11 @@ __device__ __forceinline__ GLay grp_carve(unsigned char *raw, int warp, int capS
   L.b = L.a + capS;
   L.rco = fwd ? nullptr : L.b + capS;  // gradient kernel: per-SF radial records
   L.fc = reinterpret_cast<float *>(fwd ? L.b + capS : L.rco + nrad);
-  L.dfc = fwd ? nullptr : L.fc + (size_t)nrc * capS;
-  L.gx = fwd ? nullptr : L.dfc + (size_t)nrc * capS;
-  L.gy = fwd ? nullptr : L.gx + capS;
-  L.gz = fwd ? nullptr : L.gy + capS;
-  L.dg = fwd ? nullptr : L.gz + capS;
+  const size_t nfc = (size_t)grp_fc_groups(nrc) * capS;
+  L.dfc = fwd ? nullptr : L.fc + nfc;
+  L.gh = fwd ? nullptr : reinterpret_cast<int *>(L.dfc + nfc);
+  L.gl = fwd ? nullptr : L.gh + 3 * capS;
+  L.dg = fwd ? nullptr : reinterpret_cast<float *>(L.gl + 3 * capS);
   return L;
 }
 
@@ -96,8 +103,10 @@ __device__ __forceinline__ int grp_stage(const GLay &L, const SFT<float> &sf, in
           fcv = 0.5f * (cosf(x) + 1.f);
         }
       }
-      L.fc[(size_t)gr * capS + q] = fcv;
-      if (want_dfc) L.dfc[(size_t)gr * capS + q] = dfcv;
+      if (nrc > 1) {
+        L.fc[(size_t)gr * capS + q] = fcv;
+        if (want_dfc) L.dfc[(size_t)gr * capS + q] = dfcv;
+      }
       if (gr == rci) {
         fa = fcv;
         dfa = dfcv;
@@ -248,6 +257,54 @@ __device__ __forceinline__ float ex2f(float x) {
   float y;
   asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
+}
+
+// Slot gradients in fixed point.  A term v is split as
+//   v = h 2^-9 + l 2^-29 + e,  |e| <= 2^-30,  |h| <= 2^20,  |l| <= 2^19,
+// and h and l are summed by native int32 shared-memory atomic adds (an FP32
+// atomic add is a compare-and-swap loop).  Integer sums do not depend on the
+// order of the adds, so the slot gradients are the same in every run.  The
+// rounding uses the 1.5 2^23 shifter (exact for |x| < 2^22), so the split
+// stays on the FP32 and integer pipes.  A slot receives at most 2047 terms
+// (one radial write, at most capS - 1 k-side pairs and capS - 1 j-side
+// partial sums; capS <= 1024, since the gradient kernel's per-warp tables
+// take at least 56 bytes per slot and four warps share the 227 KB of a
+// block), so with |v| <= kFxMax both sums fit int32.  A
+// term beyond kFxMax, or not finite, marks the atom (`bad`), and the kernel
+// raises kFlagForceRange.
+constexpr float kFxShift = 12582912.f;  // 1.5 2^23
+constexpr int kFxShiftBits = 0x4B400000;
+constexpr float kFxMax = 2047.f;  // eV/A per term
+__device__ __forceinline__ void fx_split(float v, int &h, int &l, bool &bad) {
+  bad |= !(fabsf(v) <= kFxMax);
+  const float ts = fmaf(v, 512.f, kFxShift);              // v 2^9 rounded, plus the shifter
+  h = __float_as_int(ts) - kFxShiftBits;
+  const float hf = ts - kFxShift;                          // exact
+  const float u = fmaf(hf, -1048576.f, v * 536870912.f);  // (v 2^9 - hf) 2^20, exact
+  l = __float_as_int(u + kFxShift) - kFxShiftBits;
+}
+__device__ __forceinline__ void slot_add(const GLay &L, int capS, int q, float x, float y,
+                                         float z, bool &bad) {
+  int h, l;
+  fx_split(x, h, l, bad);
+  atomicAdd(&L.gh[q], h);
+  atomicAdd(&L.gl[q], l);
+  fx_split(y, h, l, bad);
+  atomicAdd(&L.gh[capS + q], h);
+  atomicAdd(&L.gl[capS + q], l);
+  fx_split(z, h, l, bad);
+  atomicAdd(&L.gh[2 * capS + q], h);
+  atomicAdd(&L.gl[2 * capS + q], l);
+}
+__device__ __forceinline__ void slot_set(const GLay &L, int capS, int q, float x, float y,
+                                         float z, bool &bad) {
+  const float v[3] = {x, y, z};
+#pragma unroll
+  for (int c = 0; c < 3; ++c) fx_split(v[c], L.gh[c * capS + q], L.gl[c * capS + q], bad);
+}
+__device__ __forceinline__ float slot_get(const GLay &L, int capS, int q, int c) {
+  return fmaf((float)L.gh[c * capS + q], 0.001953125f,
+              (float)L.gl[c * capS + q] * 1.86264514923095703125e-09f);
 }
 
 // radial part of the forward kernel: one SF per lane over the slots in
@@ -553,7 +610,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
                     const float *__restrict__ w32, const SFT<float> *__restrict__ sfg,
                     const float *__restrict__ dedg, double *__restrict__ force,
                     double *__restrict__ wvir, const unsigned short *__restrict__ pairs,
-                    const int *__restrict__ pcount, int pcap) {
+                    const int *__restrict__ pcount, int pcap, int *__restrict__ flags) {
   (void)xyzr;
   (void)apos;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -579,10 +636,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
     clam[c] = sf.comb_lam[c];
     ciz[c] = sf.comb_iz[c];
   }
+  bool bad = false;  // a slot-gradient term outside the fixed-point range
   for (int i = blockIdx.x * kWarpsPerBlock + warp; i < N; i += gridDim.x * kWarpsPerBlock) {
     const int P = grp_stage(L, sf, i, cap, capS, lane, rci, cnt, d32, w32, true);
     for (int d = lane; d < D; d += 32) L.dg[d] = dedg[(size_t)i * D + d];
-    for (int q = lane; q < P; q += 32) L.gx[q] = L.gy[q] = L.gz[q] = 0.f;
     for (int e = lane; e < 2 * NAL * NC; e += 32) s_u[warp][e] = 0.f;
     __syncwarp();
     // per-atom radial records: (kx, rs, dE/dG_d, dE/dG_{d+nsf})
@@ -626,10 +683,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
         }
       }
       const float ir = S / r;
-      L.gx[q] += ir * aq.x;
-      L.gy[q] += ir * aq.y;
-      L.gz[q] += ir * aq.z;
+      slot_set(L, capS, q, ir * aq.x, ir * aq.y, ir * aq.z, bad);  // every slot's first write
     }
+    __syncwarp();
     if (nang > 0) {
       AngCoef<NAL, NC, STD> U;
       U.load(s_u[warp]);
@@ -650,11 +706,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
           if (p < pe) {
             const int j = jk & 0xff, k = jk >> 8;
             if (j != cur) {
-              if (cur >= 0) {
-                atomicAdd(&L.gx[cur], gjx);
-                atomicAdd(&L.gy[cur], gjy);
-                atomicAdd(&L.gz[cur], gjz);
-              }
+              if (cur >= 0) slot_add(L, capS, cur, gjx, gjy, gjz, bad);
               cur = j;
               gjx = gjy = gjz = 0.f;
               Aj = L.a[j];
@@ -665,16 +717,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
             gjx += vj.x;
             gjy += vj.y;
             gjz += vj.z;
-            atomicAdd(&L.gx[k], vk.x);
-            atomicAdd(&L.gy[k], vk.y);
-            atomicAdd(&L.gz[k], vk.z);
+            slot_add(L, capS, k, vk.x, vk.y, vk.z, bad);
           }
         }
-        if (cur >= 0) {
-          atomicAdd(&L.gx[cur], gjx);
-          atomicAdd(&L.gy[cur], gjy);
-          atomicAdd(&L.gz[cur], gjz);
-        }
+        if (cur >= 0) slot_add(L, capS, cur, gjx, gjy, gjz, bad);
       } else if (P > 1) {
         pair_stream<kPairQBwd>(L.a, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
           (void)c2;
@@ -696,16 +742,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
               vz += tz;
             }
           }
-          if (ok && lane == last) {
-            atomicAdd(&L.gx[j], vx);
-            atomicAdd(&L.gy[j], vy);
-            atomicAdd(&L.gz[j], vz);
-          }
-          if (ok) {
-            atomicAdd(&L.gx[k], vk.x);
-            atomicAdd(&L.gy[k], vk.y);
-            atomicAdd(&L.gz[k], vk.z);
-          }
+          if (ok && lane == last) slot_add(L, capS, j, vx, vy, vz, bad);
+          if (ok) slot_add(L, capS, k, vk.x, vk.y, vk.z, bad);
         });
       }
     }
@@ -716,7 +754,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
     float W[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     float fx = 0.f, fy = 0.f, fz = 0.f;
     for (int q = lane; q < P; q += 32) {
-      const float gx = L.gx[q], gy = L.gy[q], gz = L.gz[q];
+      const float gx = slot_get(L, capS, q, 0), gy = slot_get(L, capS, q, 1),
+                  gz = slot_get(L, capS, q, 2);
       const int j = nj[(size_t)i * cap + q];
       atomicAdd(force + (size_t)j * 3 + 0, -(double)gx);
       atomicAdd(force + (size_t)j * 3 + 1, -(double)gy);
@@ -753,6 +792,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
     }
     __syncwarp();
   }
+  if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flags, kFlagForceRange);
 }
 
 // Kernel pointers of every (NAL, NC) instantiation.

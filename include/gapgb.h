@@ -56,6 +56,13 @@ typedef enum {
   GAPGB_PREC_TF32 = 5      /* FP32 descriptors, tensor-core GPR with single
                               TF32 products and FP32 accumulation; D <= 64 */
 } gapgb_precision;
+/* In the forms other than FP64, the fast descriptor-gradient kernel (taken
+ * when every angular SF shares one cutoff, up to 4 angular alphas and 8
+ * (lambda, zeta) combinations) sums each neighbour slot's gradient in fixed
+ * point: every pair term is rounded to 2^-29 eV/A, and a term beyond 2047
+ * eV/A or not finite makes the call return GAPGB_ERR_CAP_EXCEEDED (the FP64
+ * form has no such limit).  These slot sums do not depend on the order of
+ * the device's atomic adds. */
 
 typedef enum {
   GAPGB_OPT_PRECISION = 0,     /* gapgb_precision, default GAPGB_PREC_FP64 */

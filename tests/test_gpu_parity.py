@@ -664,9 +664,12 @@ def test_graph_follows_new_coefficients_and_pins_its_buffers(gapgb_mod, oracle_m
     torch.cuda.synchronize()
     m.check_device_status()
     E2, F2 = t["E"].cpu().numpy(), t["F"].cpu().numpy()
-    # the energy is linear in c; forces too (their FP64 atomic sums reorder)
+    # the energy is linear in c; forces too, to the resolution of the
+    # gradient kernel's fixed-point slot sums (each term rounded to 2^-29
+    # eV/A, a few hundred terms per force); a stale image would be off by
+    # |F1|, here about 0.07 eV/A
     assert np.allclose(E2, 2.0 * E1, rtol=1e-12, atol=0.0)
-    assert np.abs(F2 - 2.0 * F1).max() <= 1e-9 * np.abs(F2).max()
+    assert np.abs(F2 - 2.0 * F1).max() <= 1e-6
     # the host-buffer path (same sizes: the workspace stays) agrees; a stale
     # image would be off by a factor of two
     Eh, Fh, _ = m.eval_batch(off, sp, lat, pos)

@@ -36,3 +36,36 @@ def test_non_finite_and_singular_inputs_are_refused(gapgb_mod):
         assert E1 == E0 and np.array_equal(F1, F0) and np.array_equal(S1, S0)
     finally:
         m.close()
+
+
+ERR_CAP = 3  # GAPGB_ERR_CAP_EXCEEDED
+
+
+def test_fp32_gradient_range_is_reported(gapgb_mod):
+    """The FP32 forms sum slot gradients in fixed point, for terms up to 2047
+    eV/A.  A model whose terms exceed that (coefficients scaled by 1e8) is
+    refused with GAPGB_ERR_CAP_EXCEEDED in an FP32 form; the FP64 form
+    evaluates it, and once the coefficients are restored the FP32 form gives
+    its earlier results again."""
+    import gapgb.synth as S
+    zt, wt, ty, al, rc, ze, theta, mm, coeff = S.alloy_model(M=200, seed=2, ncells=2)
+    m = gapgb_mod.GapModel.create(zt, wt, ty, al, rc, theta, mm, coeff, sf_zeta=ze)
+    try:
+        m.set_neighbour_cap(96)
+        off, sp, lat, pos = S.pack([S.alloy512(seed=7)])
+        m.set_precision("fp32")
+        E0, F0, S0 = m.eval_batch(off, sp, lat, pos)
+        m.set_coeff(coeff * 1e8)
+        with pytest.raises(gapgb_mod.GapError) as e:
+            m.eval_batch(off, sp, lat, pos)
+        assert e.value.status == ERR_CAP
+        m.set_precision("fp64")
+        _, F64, _ = m.eval_batch(off, sp, lat, pos)
+        assert np.abs(F64).max() > 2047.0
+        m.set_precision("fp32")
+        m.set_coeff(coeff)
+        E1, F1, S1 = m.eval_batch(off, sp, lat, pos)
+        assert np.array_equal(E1, E0) and np.array_equal(S1, S0)
+        np.testing.assert_allclose(F1, F0, rtol=0, atol=1e-12)  # FP64 scatter order
+    finally:
+        m.close()
