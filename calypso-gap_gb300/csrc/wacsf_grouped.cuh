@@ -26,10 +26,17 @@
 // gradient kernel's overflow path one batch (at most 31 + 32)
 constexpr int kPairQFwd = 128;
 constexpr int kPairQBwd = 64;
-// resident blocks per SM the grouped kernels are compiled for (80 registers
-// a thread); their launchers ask for the largest shared-memory carve-out so
-// that the per-warp slot tables of 6 blocks fit
+// resident blocks per SM the grouped kernels are compiled for: the forward
+// kernel 6 (80 registers a thread; at 7 and 72 registers it ran 4 % slower),
+// the gradient kernel 7 (72 registers) where the instantiation compiles
+// without spilling, 6 otherwise.  The launchers ask for the largest
+// shared-memory carve-out so that the per-warp slot tables of those blocks
+// fit, and size the grid by the occupancy the compiled kernel reaches.
 constexpr int kGrpMinBlocks = 6;
+template <int NAL, int NC, bool STD>
+constexpr int grp_bwd_blocks() {
+  return ((NAL <= 2 && (STD || NC <= 2)) || (NAL == 1 && NC <= 4)) ? 7 : 6;
+}
 
 // Per-warp shared-memory layout of the grouped kernels: packed slot records
 // (a pair reads its two slots with four 128-bit loads; the angular
@@ -603,7 +610,7 @@ __device__ __forceinline__ void pair_grad(const GLay &L, const float4 &Aj, const
 //    whose list overflowed re-enumerate their pairs (pair_stream) and sum
 //    the j side by a segmented warp scan.
 template <int NAL, int NC, bool STD>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock, kGrpMinBlocks)
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, (grp_bwd_blocks<NAL, NC, STD>()))
     k_wacsf_bwd_grp(int N, int i0, int cap, int capS, const int *__restrict__ cnt,
                     const double4 *__restrict__ xyzr, const int *__restrict__ nj,
                     const double4 *__restrict__ apos, const float4 *__restrict__ d32,

@@ -92,3 +92,19 @@ def test_straddling_cell_matches_oracle(alloy, oracle_mod, tmp_path):
     assert abs(E[s] - oE) / len(p) <= 1e-3
     assert np.abs(F[off[s]:off[s + 1]] - oF).max() <= 20e-3
     assert np.abs(St[s] - oS).max() <= 1e-2
+
+
+def test_slot_sums_repeat(alloy):
+    """The grouped gradient kernel sums slot gradients in fixed point, so the
+    per-atom virials, hence the stresses, are the same bit for bit in every
+    run; only the forces' FP64 scatter atomics may add in another order."""
+    import gapgb.synth as S
+    m, _, structs = alloy
+    off, sp, lat, pos = S.pack(structs[:8])
+    m.set_precision("tc")
+    m.set_pipelines(1)
+    runs = [m.eval_batch(off, sp, lat, pos) for _ in range(3)]
+    for E, F, St in runs[1:]:
+        assert np.array_equal(E, runs[0][0])
+        assert np.array_equal(St, runs[0][2])
+        np.testing.assert_allclose(F, runs[0][1], rtol=0, atol=1e-12)
