@@ -608,12 +608,18 @@ def run_population(args):
     m.check_device_status()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
            for _ in range(args.steps)]
+    stop, lines = threading.Event(), []
+    th = threading.Thread(target=clocks_sampler, args=(stop, lines), daemon=True)
+    th.start()
+    time.sleep(0.3)
     for a, b in evs:
         flush.zero_()
         a.record(stream)
         g.launch(stream.cuda_stream)
         b.record(stream)
     torch.cuda.synchronize()
+    stop.set()
+    th.join()
     m.check_device_status()
     ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
     g.close()
@@ -687,7 +693,8 @@ def run_population(args):
             # evaluation (see the headline workload's count); the generic
             # kernels add the reverse slots, the force gather and the orphans
             "gpu_launches": step_kernels(best["precision"], N, bool(best["generic_kernels"]),
-                                         int(best.get("pipelines", 2))) * args.steps}
+                                         int(best.get("pipelines", 2))) * args.steps,
+            "clocks": summarize_clocks(lines)}
     m.close()
     line["cpu_baseline"] = population_cpu_baseline(
         (zt, wt, ty, al, rc, ze, theta, mm, coeff), pop, 256)
