@@ -14,6 +14,7 @@
 // sizes shared memory and grows the capacity.  The device-buffer call never
 // synchronises.
 #include <cmath>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <algorithm>
@@ -247,9 +248,24 @@ int max_struct_atoms(int S, const int *atom_off) {
   return mx;
 }
 
+// A double is not finite exactly when its exponent field (bits 20..30 of the
+// high 32-bit word) is all ones.  The largest masked high word of a block is
+// an unsigned-max reduction the host compiler vectorises (one pass over the
+// positions of the call, on its critical path before the first launch).
 bool finite_all(const double *p, size_t n) {
-  for (size_t i = 0; i < n; ++i)
-    if (!std::isfinite(p[i])) return false;
+  constexpr uint32_t kExp = 0x7FF00000u;
+  constexpr size_t kBlock = 4096;
+  for (size_t b = 0; b < n; b += kBlock) {
+    const size_t e = std::min(n, b + kBlock);
+    uint32_t mx = 0;
+    for (size_t i = b; i < e; ++i) {
+      uint64_t u;
+      std::memcpy(&u, p + i, sizeof(u));
+      const uint32_t x = static_cast<uint32_t>(u >> 32) & kExp;
+      mx = x > mx ? x : mx;
+    }
+    if (mx == kExp) return false;
+  }
   return true;
 }
 
