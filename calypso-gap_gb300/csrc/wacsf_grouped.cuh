@@ -47,13 +47,16 @@ constexpr int grp_bwd_blocks() {
 //                                 only with several groups (with one, b holds it)
 //   rco[s]                        (kx, rs, dE/dG_d, dE/dG_{d+nsf}) of radial SF s
 //                                 (gradient kernel)
-//   gh[c][q], gl[c][q]            slot gradient component c in fixed point,
-//                                 gh 2^-9 + gl 2^-29 (gradient kernel)
+//   g6[q][c][2]                   slot gradient component c in fixed point,
+//                                 g6[q][c][0] 2^-9 + g6[q][c][1] 2^-29
+//                                 (gradient kernel): a slot's six words are
+//                                 adjacent, so a pair's six atomic adds share
+//                                 one address
 //   dg[D]                         dE/dG (gradient kernel)
 struct GLay {
   float4 *a, *b, *rco;
   float *fc, *dfc, *dg;
-  int *gh, *gl;
+  int *g6;
 };
 
 __host__ __device__ inline int grp_fc_groups(int nrc) { return nrc > 1 ? nrc : 0; }
@@ -72,12 +75,12 @@ __device__ __forceinline__ GLay grp_carve(unsigned char *raw, int warp, int capS
   L.a = reinterpret_cast<float4 *>(base);
   L.b = L.a + capS;
   L.rco = fwd ? nullptr : L.b + capS;  // gradient kernel: per-SF radial records
-  L.fc = reinterpret_cast<float *>(fwd ? L.b + capS : L.rco + nrad);
+  // g6 follows the 16-byte records, so every slot's words are 8-byte aligned
+  L.g6 = fwd ? nullptr : reinterpret_cast<int *>(L.rco + nrad);
+  L.fc = fwd ? reinterpret_cast<float *>(L.b + capS) : reinterpret_cast<float *>(L.g6 + 6 * capS);
   const size_t nfc = (size_t)grp_fc_groups(nrc) * capS;
   L.dfc = fwd ? nullptr : L.fc + nfc;
-  L.gh = fwd ? nullptr : reinterpret_cast<int *>(L.dfc + nfc);
-  L.gl = fwd ? nullptr : L.gh + 3 * capS;
-  L.dg = fwd ? nullptr : reinterpret_cast<float *>(L.gl + 3 * capS);
+  L.dg = fwd ? nullptr : L.dfc + nfc;
   return L;
 }
 
@@ -278,40 +281,46 @@ __device__ __forceinline__ float ex2f(float x) {
 // take at least 56 bytes per slot and four warps share the 227 KB of a
 // block), so with |v| <= kFxMax both sums fit int32.  A
 // term beyond kFxMax, or not finite, marks the atom (`bad`), and the kernel
-// raises kFlagForceRange.
+// raises kFlagForceRange (tested once per vector, as |x| + |y| + |z|).
 constexpr float kFxShift = 12582912.f;  // 1.5 2^23
 constexpr int kFxShiftBits = 0x4B400000;
 constexpr float kFxMax = 2047.f;  // eV/A per term
-__device__ __forceinline__ void fx_split(float v, int &h, int &l, bool &bad) {
-  bad |= !(fabsf(v) <= kFxMax);
+__device__ __forceinline__ void fx_split(float v, int &h, int &l) {
   const float ts = fmaf(v, 512.f, kFxShift);              // v 2^9 rounded, plus the shifter
   h = __float_as_int(ts) - kFxShiftBits;
   const float hf = ts - kFxShift;                          // exact
   const float u = fmaf(hf, -1048576.f, v * 536870912.f);  // (v 2^9 - hf) 2^20, exact
   l = __float_as_int(u + kFxShift) - kFxShiftBits;
 }
-__device__ __forceinline__ void slot_add(const GLay &L, int capS, int q, float x, float y,
-                                         float z, bool &bad) {
+__device__ __forceinline__ void slot_add(const GLay &L, int q, float x, float y, float z,
+                                         bool &bad) {
+  bad |= !(fabsf(x) + fabsf(y) + fabsf(z) <= kFxMax);
+  int *w = L.g6 + 6 * q;
   int h, l;
-  fx_split(x, h, l, bad);
-  atomicAdd(&L.gh[q], h);
-  atomicAdd(&L.gl[q], l);
-  fx_split(y, h, l, bad);
-  atomicAdd(&L.gh[capS + q], h);
-  atomicAdd(&L.gl[capS + q], l);
-  fx_split(z, h, l, bad);
-  atomicAdd(&L.gh[2 * capS + q], h);
-  atomicAdd(&L.gl[2 * capS + q], l);
+  fx_split(x, h, l);
+  atomicAdd(w + 0, h);
+  atomicAdd(w + 1, l);
+  fx_split(y, h, l);
+  atomicAdd(w + 2, h);
+  atomicAdd(w + 3, l);
+  fx_split(z, h, l);
+  atomicAdd(w + 4, h);
+  atomicAdd(w + 5, l);
 }
-__device__ __forceinline__ void slot_set(const GLay &L, int capS, int q, float x, float y,
-                                         float z, bool &bad) {
-  const float v[3] = {x, y, z};
-#pragma unroll
-  for (int c = 0; c < 3; ++c) fx_split(v[c], L.gh[c * capS + q], L.gl[c * capS + q], bad);
+__device__ __forceinline__ void slot_set(const GLay &L, int q, float x, float y, float z,
+                                         bool &bad) {
+  bad |= !(fabsf(x) + fabsf(y) + fabsf(z) <= kFxMax);
+  int2 *w = reinterpret_cast<int2 *>(L.g6 + 6 * q);
+  int h, l;
+  fx_split(x, h, l);
+  w[0] = make_int2(h, l);
+  fx_split(y, h, l);
+  w[1] = make_int2(h, l);
+  fx_split(z, h, l);
+  w[2] = make_int2(h, l);
 }
-__device__ __forceinline__ float slot_get(const GLay &L, int capS, int q, int c) {
-  return fmaf((float)L.gh[c * capS + q], 0.001953125f,
-              (float)L.gl[c * capS + q] * 1.86264514923095703125e-09f);
+__device__ __forceinline__ float fx_value(int2 v) {
+  return fmaf((float)v.x, 0.001953125f, (float)v.y * 1.86264514923095703125e-09f);
 }
 
 // radial part of the forward kernel: one SF per lane over the slots in
@@ -690,7 +699,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, (grp_bwd_blocks<NAL, NC, 
         }
       }
       const float ir = S / r;
-      slot_set(L, capS, q, ir * aq.x, ir * aq.y, ir * aq.z, bad);  // every slot's first write
+      slot_set(L, q, ir * aq.x, ir * aq.y, ir * aq.z, bad);  // every slot's first write
     }
     __syncwarp();
     if (nang > 0) {
@@ -713,7 +722,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, (grp_bwd_blocks<NAL, NC, 
           if (p < pe) {
             const int j = jk & 0xff, k = jk >> 8;
             if (j != cur) {
-              if (cur >= 0) slot_add(L, capS, cur, gjx, gjy, gjz, bad);
+              if (cur >= 0) slot_add(L, cur, gjx, gjy, gjz, bad);
               cur = j;
               gjx = gjy = gjz = 0.f;
               Aj = L.a[j];
@@ -724,10 +733,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, (grp_bwd_blocks<NAL, NC, 
             gjx += vj.x;
             gjy += vj.y;
             gjz += vj.z;
-            slot_add(L, capS, k, vk.x, vk.y, vk.z, bad);
+            slot_add(L, k, vk.x, vk.y, vk.z, bad);
           }
         }
-        if (cur >= 0) slot_add(L, capS, cur, gjx, gjy, gjz, bad);
+        if (cur >= 0) slot_add(L, cur, gjx, gjy, gjz, bad);
       } else if (P > 1) {
         pair_stream<kPairQBwd>(L.a, P, rc, lane, s_qjk[warp], s_qc2[warp], [&](int j, int k, float c2, bool ok) {
           (void)c2;
@@ -749,8 +758,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, (grp_bwd_blocks<NAL, NC, 
               vz += tz;
             }
           }
-          if (ok && lane == last) slot_add(L, capS, j, vx, vy, vz, bad);
-          if (ok) slot_add(L, capS, k, vk.x, vk.y, vk.z, bad);
+          if (ok && lane == last) slot_add(L, j, vx, vy, vz, bad);
+          if (ok) slot_add(L, k, vk.x, vk.y, vk.z, bad);
         });
       }
     }
@@ -761,8 +770,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, (grp_bwd_blocks<NAL, NC, 
     float W[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     float fx = 0.f, fy = 0.f, fz = 0.f;
     for (int q = lane; q < P; q += 32) {
-      const float gx = slot_get(L, capS, q, 0), gy = slot_get(L, capS, q, 1),
-                  gz = slot_get(L, capS, q, 2);
+      const int2 *w = reinterpret_cast<const int2 *>(L.g6 + 6 * q);
+      const float gx = fx_value(w[0]), gy = fx_value(w[1]), gz = fx_value(w[2]);
       const int j = nj[(size_t)i * cap + q];
       atomicAdd(force + (size_t)j * 3 + 0, -(double)gx);
       atomicAdd(force + (size_t)j * 3 + 1, -(double)gy);
