@@ -232,6 +232,9 @@ struct StructInfo {
   // fractional width >= ext[a] per axis, global bin ids bin0 .. bin0 + nb0 nb1 nb2 - 1
   int nb[3];
   int bin0;
+  // 1 when 2 ext[a] < 1 on every axis (a cell wider than twice the cutoff):
+  // then at most one image of an atom, the nearest, can lie within the cutoff
+  int single;
 };
 
 constexpr int kPairCap = 1024;  // recorded angular pairs per atom

@@ -95,6 +95,7 @@ __global__ void k_prep_struct(int S, const int *__restrict__ atom_off,
     si.r2max32 = rs * rs;
     si.rc2_32 = (float)(rcut * rcut);
     for (int a = 0; a < 3; ++a) si.ext32[a] = (float)si.ext[a];
+    si.single = (2.f * si.ext32[0] < 1.f) & (2.f * si.ext32[1] < 1.f) & (2.f * si.ext32[2] < 1.f);
   }
   si.a0 = atom_off[s];
   si.na = atom_off[s + 1] - atom_off[s];
@@ -398,9 +399,39 @@ __global__ void __launch_bounds__(128, 5) k_nbr_build(int N, int cap, double rcu
       const int j = si.a0 + jl;
       const float4 fj = fj_next;
       if (jl + 32 < si.na) fj_next = frac32[j + 32];
+      const float fd[3] = {fj.x - fi.x, fj.y - fi.y, fj.z - fi.z};
+      if (si.single) {
+        // the box [-d - ext, -d + ext] of each axis is narrower than 1, so it
+        // holds at most one integer, the nearest to -d: n = rint(-d) is the
+        // one candidate image when |d + n| <= ext on every axis and |n| <=
+        // nabc - the candidates of image_box below without its bounds.  The
+        // screen is screen_r2's, on the same d + n.
+        float dn[3];
+        int n[3];
+        bool keep = valid;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const float m = rintf(-fd[a]);
+          dn[a] = fd[a] + m;
+          n[a] = __float_as_int(m + 12582912.f) - 0x4B400000;  // m exactly, |m| < 2^22
+          keep &= (fabsf(dn[a]) <= ext[a]) & (abs(n[a]) <= si.nabc[a]);
+        }
+        keep &= !((j == i) & (n[0] == 0) & (n[1] == 0) & (n[2] == 0));
+        const float x = dn[0] * L32[0] + dn[1] * L32[3] + dn[2] * L32[6];
+        const float y = dn[0] * L32[1] + dn[1] * L32[4] + dn[2] * L32[7];
+        const float z = dn[0] * L32[2] + dn[1] * L32[5] + dn[2] * L32[8];
+        keep &= x * x + y * y + z * z <= r2max;
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        const int e = keep ? (qt + __popc(m & lt_mask)) & (kQueue - 1) : kQueue + lane;
+        qj[e] = j;
+        qs[e] = ((n[0] + 128) << 16) | ((n[1] + 128) << 8) | (n[2] + 128);
+        qt += __popc(m);
+        __syncwarp();
+        drain(false);
+        continue;
+      }
       // (branch-free: a lane past the structure's atoms has an empty box)
       int lo[3], hi[3];
-      const float fd[3] = {fj.x - fi.x, fj.y - fi.y, fj.z - fi.z};
       image_box(ext, si.nabc, fi, fj, lo, hi);
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
