@@ -279,7 +279,9 @@ struct Workspace {
   // spatial bins of large cells (neighbour build)
   int *bin_count = nullptr, *bin_start = nullptr, *bin_atoms = nullptr;
   int *atom_bin = nullptr, *atom_slot = nullptr, *atom_m = nullptr;
-  int *d_flags = nullptr;     // [0] error bits, [1] max neighbour count, [2] orphan count
+  int *d_flags = nullptr;     // [0] error bits, [1] max neighbour count, [2] orphan count,
+                              // [3] / [4] nonzero when the batch has unbinned cells that are
+                              // not / are wider than twice the cutoff (k_prep_struct)
   int *orphans = nullptr;     // orphan slot list
   int orphan_cap = 0;
   int *h_flags = nullptr;     // pinned mirror of d_flags

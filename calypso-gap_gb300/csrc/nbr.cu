@@ -116,6 +116,8 @@ __global__ void k_prep_struct(int S, const int *__restrict__ atom_off,
     if (ok && prod <= si.na)
       for (int a = 0; a < 3; ++a) si.nb[a] = nb[a];
   }
+  // which of the two neighbour kernels has work (the other returns at once)
+  if (si.nb[0] == 0) atomicOr(flags + (si.single ? 4 : 3), 1);
   out[s] = si;
 }
 
@@ -301,10 +303,16 @@ __device__ __forceinline__ float screen_r2(const float *L32, const float fd[3], 
 
 constexpr int kQueue = 256;  // survivors per warp per exact-test round
 
-// five blocks per SM (96 registers, no spills): 0.221 -> 0.217 ms per 38 912
-// alloy atoms against four at 116 registers; six spill and take 0.33 ms
-template <bool EXACT>
-__global__ void __launch_bounds__(128, 5) k_nbr_build(int N, int cap, double rcut,
+// Two kernels share this code.  WIDE: the atoms of unbinned cells wider than
+// twice the cutoff on every axis (StructInfo::single), screened by their
+// nearest image alone; without the general image loops the FP32 form fits
+// six blocks per SM (80 registers; 0.160 -> 0.141 ms per 38 912 alloy atoms
+// against one kernel at five).  !WIDE: the other unbinned cells, five blocks
+// per SM (96 registers; six spill and took 0.33 ms).  Each kernel returns at
+// once when the batch has no cell of its kind, and skips the others' atoms.
+template <bool EXACT, bool WIDE>
+__global__ void __launch_bounds__(128, (WIDE && !EXACT) ? 6 : 5)
+    k_nbr_build(int N, int cap, double rcut,
                                                    const double4 *__restrict__ apos,
                                                    const float4 *__restrict__ frac32,
                                                    const int *__restrict__ atom_struct,
@@ -318,6 +326,7 @@ __global__ void __launch_bounds__(128, 5) k_nbr_build(int N, int cap, double rcu
   __shared__ int s_qj[kWarpsPerBlock][kQueue + 32];
   __shared__ int s_qs[kWarpsPerBlock][kQueue + 32];
   __shared__ double s_dn[2 * kMaxImage + 1];  // s_dn[n + kMaxImage] = (double)n
+  if (flags[WIDE ? 4 : 3] == 0) return;  // no cell of this kernel's kind (block-uniform)
   for (int t = threadIdx.x; t < 2 * kMaxImage + 1; t += blockDim.x) s_dn[t] = (double)(t - kMaxImage);
   __syncthreads();
   const int lane = threadIdx.x & 31;
@@ -325,8 +334,10 @@ __global__ void __launch_bounds__(128, 5) k_nbr_build(int N, int cap, double rcu
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int i = gw; i < N; i += nw) {
-    const StructInfo si = sinfo[atom_struct[i]];
-    if (si.nb[0] != 0) continue;  // large cells: k_nbr_build_binned
+    const int sidx = atom_struct[i];
+    // large cells: k_nbr_build_binned; cells of the other kind: the other kernel
+    if (sinfo[sidx].nb[0] != 0 || (sinfo[sidx].single != 0) != WIDE) continue;
+    const StructInfo si = sinfo[sidx];
     const double4 pi = apos[i];
     const float4 fi = frac32[i];
     // FP32 screen constants of the structure (k_prep_struct): the lattice,
@@ -400,7 +411,7 @@ __global__ void __launch_bounds__(128, 5) k_nbr_build(int N, int cap, double rcu
       const float4 fj = fj_next;
       if (jl + 32 < si.na) fj_next = frac32[j + 32];
       const float fd[3] = {fj.x - fi.x, fj.y - fi.y, fj.z - fi.z};
-      if (si.single) {
+      if constexpr (WIDE) {
         // the box [-d - ext, -d + ext] of each axis is narrower than 1, so it
         // holds at most one integer, the nearest to -d: n = rint(-d) is the
         // one candidate image when |d + n| <= ext on every axis and |n| <=
@@ -429,73 +440,75 @@ __global__ void __launch_bounds__(128, 5) k_nbr_build(int N, int cap, double rcu
         __syncwarp();
         drain(false);
         continue;
-      }
-      // (branch-free: a lane past the structure's atoms has an empty box)
-      int lo[3], hi[3];
-      image_box(ext, si.nabc, fi, fj, lo, hi);
+      } else {
+        // (branch-free: a lane past the structure's atoms has an empty box)
+        int lo[3], hi[3];
+        image_box(ext, si.nabc, fi, fj, lo, hi);
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        lo[a] = valid ? lo[a] : 0;
-        hi[a] = valid ? hi[a] : -1;
-      }
-      // Every lane's box holds at most one image (cells wider than twice the
-      // cutoff): one screen per lane, survivors queued in lane order - the
-      // candidates and the order of the general loops below, without them
-      const bool none = (hi[0] < lo[0]) | (hi[1] < lo[1]) | (hi[2] < lo[2]);
-      const bool one = (hi[0] == lo[0]) & (hi[1] == lo[1]) & (hi[2] == lo[2]);
-      if (__all_sync(0xffffffffu, none || one)) {
-        const bool self = (j == i) & (lo[0] == 0) & (lo[1] == 0) & (lo[2] == 0);
-        const bool keep = one & !self & (screen_r2(L32, fd, lo[0], lo[1], lo[2]) <= r2max);
-        const unsigned m = __ballot_sync(0xffffffffu, keep);
-        const int e = keep ? (qt + __popc(m & lt_mask)) & (kQueue - 1) : kQueue + lane;
-        qj[e] = j;
-        qs[e] = ((lo[0] + 128) << 16) | ((lo[1] + 128) << 8) | (lo[2] + 128);
-        qt += __popc(m);
-        __syncwarp();
-        drain(false);
-        continue;
-      }
-      // FP32 screen: survivors of this lane's image box, in (n1, n2, n3) order
-      int c = 0;
-      if (valid)
-        for (int n1 = lo[0]; n1 <= hi[0]; ++n1)
-          for (int n2 = lo[1]; n2 <= hi[1]; ++n2)
-            for (int n3 = lo[2]; n3 <= hi[2]; ++n3) {
-              if (j == i && n1 == 0 && n2 == 0 && n3 == 0) continue;
-              if (screen_r2(L32, fd, n1, n2, n3) <= r2max) ++c;
-            }
-      int incl = c;
-#pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, incl, off);
-        if (lane >= off) incl += t;
-      }
-      const int excl = incl - c;
-      const int T = __shfl_sync(0xffffffffu, incl, 31);
-      // survivors in canonical order (lane = j order, then shifts) enter a
-      // per-warp ring queue that spans chunks; the exact FP64 test runs on
-      // 32 queued candidates at a time
-      for (int r0 = 0; r0 < T; r0 += kQueue - 32) {
-        const int take = min(kQueue - 32, T - r0);
-        if (c > 0 && excl < r0 + take && excl + c > r0) {
-          int idx = excl;
-          for (int n1 = lo[0]; n1 <= hi[0] && idx < r0 + take; ++n1)
-            for (int n2 = lo[1]; n2 <= hi[1] && idx < r0 + take; ++n2)
-              for (int n3 = lo[2]; n3 <= hi[2] && idx < r0 + take; ++n3) {
-                if (j == i && n1 == 0 && n2 == 0 && n3 == 0) continue;
-                if (screen_r2(L32, fd, n1, n2, n3) > r2max) continue;
-                if (idx >= r0) {
-                  const int e = (qt + idx - r0) & (kQueue - 1);
-                  qj[e] = j;
-                  qs[e] = ((n1 + 128) << 16) | ((n2 + 128) << 8) | (n3 + 128);
-                }
-                ++idx;
-              }
+        for (int a = 0; a < 3; ++a) {
+          lo[a] = valid ? lo[a] : 0;
+          hi[a] = valid ? hi[a] : -1;
         }
-        qt += take;
-        __syncwarp();
-        drain(false);
-      }
+        // Every lane's box holds at most one image (this chunk of j of a cell
+        // narrower than twice the cutoff on some axis): one screen per lane,
+        // survivors queued in lane order - the candidates and the order of the
+        // general loops below, without them
+        const bool none = (hi[0] < lo[0]) | (hi[1] < lo[1]) | (hi[2] < lo[2]);
+        const bool one = (hi[0] == lo[0]) & (hi[1] == lo[1]) & (hi[2] == lo[2]);
+        if (__all_sync(0xffffffffu, none || one)) {
+          const bool self = (j == i) & (lo[0] == 0) & (lo[1] == 0) & (lo[2] == 0);
+          const bool keep = one & !self & (screen_r2(L32, fd, lo[0], lo[1], lo[2]) <= r2max);
+          const unsigned m = __ballot_sync(0xffffffffu, keep);
+          const int e = keep ? (qt + __popc(m & lt_mask)) & (kQueue - 1) : kQueue + lane;
+          qj[e] = j;
+          qs[e] = ((lo[0] + 128) << 16) | ((lo[1] + 128) << 8) | (lo[2] + 128);
+          qt += __popc(m);
+          __syncwarp();
+          drain(false);
+          continue;
+        }
+        // FP32 screen: survivors of this lane's image box, in (n1, n2, n3) order
+        int c = 0;
+        if (valid)
+          for (int n1 = lo[0]; n1 <= hi[0]; ++n1)
+            for (int n2 = lo[1]; n2 <= hi[1]; ++n2)
+              for (int n3 = lo[2]; n3 <= hi[2]; ++n3) {
+                if (j == i && n1 == 0 && n2 == 0 && n3 == 0) continue;
+                if (screen_r2(L32, fd, n1, n2, n3) <= r2max) ++c;
+              }
+        int incl = c;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, incl, off);
+          if (lane >= off) incl += t;
+        }
+        const int excl = incl - c;
+        const int T = __shfl_sync(0xffffffffu, incl, 31);
+        // survivors in canonical order (lane = j order, then shifts) enter a
+        // per-warp ring queue that spans chunks; the exact FP64 test runs on
+        // 32 queued candidates at a time
+        for (int r0 = 0; r0 < T; r0 += kQueue - 32) {
+          const int take = min(kQueue - 32, T - r0);
+          if (c > 0 && excl < r0 + take && excl + c > r0) {
+            int idx = excl;
+            for (int n1 = lo[0]; n1 <= hi[0] && idx < r0 + take; ++n1)
+              for (int n2 = lo[1]; n2 <= hi[1] && idx < r0 + take; ++n2)
+                for (int n3 = lo[2]; n3 <= hi[2] && idx < r0 + take; ++n3) {
+                  if (j == i && n1 == 0 && n2 == 0 && n3 == 0) continue;
+                  if (screen_r2(L32, fd, n1, n2, n3) > r2max) continue;
+                  if (idx >= r0) {
+                    const int e = (qt + idx - r0) & (kQueue - 1);
+                    qj[e] = j;
+                    qs[e] = ((n1 + 128) << 16) | ((n2 + 128) << 8) | (n3 + 128);
+                  }
+                  ++idx;
+                }
+          }
+          qt += take;
+          __syncwarp();
+          drain(false);
+        }
+      }  // !WIDE
     }
     drain(true);
     if (lane == 0) {
@@ -796,11 +809,14 @@ void launch_prep(const gapgb_model *m, Workspace &ws, int S, int N, const int *d
 
 void launch_neighbors(Workspace &ws, int S, int N, int max_atoms, int cap, double rcut,
                       cudaStream_t st, bool exact) {
-  auto build = exact ? k_nbr_build<true> : k_nbr_build<false>;
+  auto build_wide = exact ? k_nbr_build<true, true> : k_nbr_build<false, true>;
+  auto build = exact ? k_nbr_build<true, false> : k_nbr_build<false, false>;
   auto build_binned = exact ? k_nbr_build_binned<true> : k_nbr_build_binned<false>;
-  build<<<grid_for_warps(N), 32 * kWarpsPerBlock, 0, st>>>(
-      N, cap, rcut, ws.apos, ws.frac32, ws.atom_struct, ws.sinfo, ws.nbr_cnt, ws.nbr_xyz,
-      ws.nbr_j, ws.nbr_s, ws.nbr_d32, ws.nbr_w32, ws.d_flags);
+  // cells wider than twice the cutoff, then the other unbinned cells
+  for (auto fn : {build_wide, build})
+    fn<<<grid_for_warps(N), 32 * kWarpsPerBlock, 0, st>>>(
+        N, cap, rcut, ws.apos, ws.frac32, ws.atom_struct, ws.sinfo, ws.nbr_cnt, ws.nbr_xyz,
+        ws.nbr_j, ws.nbr_s, ws.nbr_d32, ws.nbr_w32, ws.d_flags);
   if (max_atoms < kBinMinAtoms) return;  // no structure was binned (launch_prep)
   int *total = ws.bin_count + N;  // last entry of the count array holds the bin total
   cudaMemsetAsync(ws.bin_count, 0, sizeof(int) * (size_t)(N + 1), st);
