@@ -383,7 +383,9 @@ T_PAIRS = 690.0  # contributing angular pairs per atom on this workload
 
 def step_kernels(precision, natoms, generic=False, pipelines=2):
     """Kernels the library launches per evaluation with gradients: prep x2
-    and the neighbour build; per pipeline the descriptors, the GPR (tensor-core
+    and the two neighbour-build kernels (cells wider than twice the cutoff,
+    then the others; the one with no cell of its kind returns at once); per
+    pipeline the descriptors, the GPR (tensor-core
     forms: operand prep + kernel; SIMT forms: kernel + split reduce) and the
     slot gradients (the grouped kernel scatters the forces itself); then the
     structure partial and final sums.  Tensor-core batches of at least the
@@ -392,7 +394,7 @@ def step_kernels(precision, natoms, generic=False, pipelines=2):
     from gapgb.tune import SPLIT_MIN_ATOMS
     two = (pipelines == 2 and precision in ("tc", "tf32") and not generic
            and natoms >= SPLIT_MIN_ATOMS)
-    return 3 + 4 * (2 if two else 1) + 2 + (3 if generic else 0)
+    return 4 + 4 * (2 if two else 1) + 2 + (3 if generic else 0)
 
 
 def stage_bytes_per_atom(D, P=P_SLOTS, T=T_PAIRS):
@@ -689,7 +691,7 @@ def run_population(args):
             "e2e": {"value": N / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "call": "gapgb_eval_batch (host buffers)"},
             "roofline": roof,
-            # one graph launch per step holding the 9 kernels of a grouped-kernel
+            # one graph launch per step holding the 10 kernels of a grouped-kernel
             # evaluation (see the headline workload's count); the generic
             # kernels add the reverse slots, the force gather and the orphans
             "gpu_launches": step_kernels(best["precision"], N, bool(best["generic_kernels"]),

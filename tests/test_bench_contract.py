@@ -90,9 +90,10 @@ def test_default_batch_is_one_gpr_wave(monkeypatch):
 
 
 def test_step_kernel_counts():
-    # prep x2, neighbour build, structure sums x2, and 4 per pipeline
-    assert bench.step_kernels("tc", 38912) == 13        # two pipelines
-    assert bench.step_kernels("tc", 38912, pipelines=1) == 9
-    assert bench.step_kernels("tc", 8192) == 9          # below the split threshold
-    assert bench.step_kernels("fp32", 38912) == 9       # SIMT forms run one pipeline
-    assert bench.step_kernels("tf32", 10 ** 6, generic=True) == 12
+    # prep x2, neighbour build x2 (wide and other cells), structure sums x2,
+    # and 4 per pipeline
+    assert bench.step_kernels("tc", 38912) == 14        # two pipelines
+    assert bench.step_kernels("tc", 38912, pipelines=1) == 10
+    assert bench.step_kernels("tc", 8192) == 10         # below the split threshold
+    assert bench.step_kernels("fp32", 38912) == 10      # SIMT forms run one pipeline
+    assert bench.step_kernels("tf32", 10 ** 6, generic=True) == 13
