@@ -236,6 +236,50 @@ def test_batch_equals_single(synth_si):
         assert np.abs(St[s] - s1).max() <= 1e-10
 
 
+def _wide_si(seed, outside=0):
+    """216-atom Si cell (16.3 A, wider than twice the 6 A cutoff on every
+    axis); `outside` atoms moved past the cell's faces."""
+    import gapgb.synth as S
+    rng = np.random.default_rng(seed)
+    lat, pos = S._supercell(S._diamond_basis(), 5.43, (3, 3, 3))
+    pos = pos + rng.normal(0.0, 0.05, pos.shape)
+    pos[:outside] += lat[0] * 1.04 - lat[2] * 0.03
+    return lat, pos, np.full(len(pos), 14, np.int32)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "tc"])
+def test_mixed_wide_and_narrow_batch(synth_si, oracle_mod, prec):
+    """Cells wider than twice the cutoff and narrower ones in one batch: the
+    two neighbour-build kernels each take their own cells' atoms and skip the
+    others', so every structure's results equal its evaluation alone, and
+    the wide cell with atoms outside the cell has the oracle's list and
+    results."""
+    import gapgb.synth as S
+    g, o = synth_si
+    g.set_precision(prec)
+    structs = [_wide_si(1), S.si64(seed=41), _wide_si(2, outside=7), S.si64(seed=42)]
+    off, sp, lat, pos = S.pack(structs)
+    E, F, St = g.eval_batch(off, sp, lat, pos)
+    for s, (l, p, z) in enumerate(structs):
+        e1, f1, s1, _ = g.eval(z, l, p)
+        assert abs(E[s] - e1) <= 1e-12 * max(1.0, abs(e1)), s
+        assert np.abs(F[off[s]:off[s + 1]] - f1).max() <= 1e-10, s
+        assert np.abs(St[s] - s1).max() <= 1e-10, s
+    l, p, z = structs[2]
+    gcnt, gnb = g.neighbors(z, l, p, cap=400)
+    ocnt, onb = oracle_mod.neighbors(l, p, o.weights(z), 6.0, 400)
+    _assert_nbr_equal(gcnt, gnb, ocnt, onb)
+    oE, oF, oS, _ = oracle_mod.gap_calc(o, z, l, p, 6.0, True)
+    # this stiff model's cell carries stresses near 280 GPa: the reduced-
+    # precision bar is 1e-2 GPa or 1e-4 of the largest component
+    e_tol, f_tol, s_tol = ((E_REL, F_ABS, S_ABS) if prec == "fp64"
+                           else (1e-3, 20e-3, max(1e-2, 1e-4 * np.abs(oS).max())))
+    assert abs(E[2] - oE) <= (e_tol * max(1.0, abs(oE)) if prec == "fp64" else e_tol * len(z))
+    assert np.abs(F[off[2]:off[3]] - oF).max() <= f_tol
+    assert np.abs(St[2] - oS).max() <= s_tol
+    g.set_precision("fp64")
+
+
 def test_lgrad_false(golden_model, frames):
     golden_model.set_precision("fp64")
     E, F, S, _ = golden_model.eval(frames["numbers"][0], frames["cell"][0], frames["positions"][0],
