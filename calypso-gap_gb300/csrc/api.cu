@@ -52,6 +52,7 @@ void free_ws(Workspace &ws) {
   free_dev(ws.d_atom_e);
   free_dev(ws.apos);
   free_dev(ws.frac32);
+  free_dev(ws.pos2f);
   free_dev(ws.atom_struct);
   free_dev(ws.sinfo);
   free_dev(ws.nbr_cnt);
@@ -122,6 +123,7 @@ gapgb_status ensure_ws(gapgb_model *m, int N, int S, int cap) {
   WS_ALLOC(ws.d_atom_e, nN);
   WS_ALLOC(ws.apos, nN);
   WS_ALLOC(ws.frac32, nN);
+  WS_ALLOC(ws.pos2f, (size_t)nN * 2);
   WS_ALLOC(ws.atom_struct, nN);
   WS_ALLOC(ws.sinfo, nS);
   WS_ALLOC(ws.nbr_cnt, nN);

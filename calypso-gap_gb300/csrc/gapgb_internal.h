@@ -224,6 +224,7 @@ struct StructInfo {
   // conversions run on the narrow FP64 pipe): the lattice, ext, the squared
   // screen bound (rcut plus the fractional rounding margin) and rcut^2
   float lat32[9];
+  float latl32[9];  // lat - lat32, rounded to FP32: the lattice as a double-float pair
   float ext32[3];
   float r2max32, rc2_32;
   int nabc[3];     // gap_calc.f90:85-88
@@ -267,6 +268,8 @@ struct Workspace {
   // internal
   double4 *apos = nullptr;
   float4 *frac32 = nullptr;   // fractional coordinates (FP32) for image pruning
+  float4 *pos2f = nullptr;    // each position as FP32 high [2 i] and low [2 i + 1] parts
+                              // (the FP32 neighbour form's relative vectors)
   int *atom_struct = nullptr;
   StructInfo *sinfo = nullptr;
   int *nbr_cnt = nullptr, *nbr_j = nullptr, *nbr_s = nullptr, *nbr_rev = nullptr;

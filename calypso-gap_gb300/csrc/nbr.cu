@@ -89,6 +89,7 @@ __global__ void k_prep_struct(int S, const int *__restrict__ atom_off,
     float lsum = 0.f;
     for (int q = 0; q < 9; ++q) {
       si.lat32[q] = (float)si.lat[q];
+      si.latl32[q] = (float)(si.lat[q] - (double)si.lat32[q]);
       lsum += fabsf(si.lat32[q]);
     }
     const float rs = (float)rcut + 2.5e-4f * lsum + 1e-3f;
@@ -200,7 +201,8 @@ __global__ void k_prep_atoms(int N, int S, const int *__restrict__ atom_off,
                              const int *__restrict__ species, const double *__restrict__ pos,
                              const SFDev *__restrict__ sf, const StructInfo *__restrict__ sinfo,
                              int *__restrict__ atom_struct, double4 *__restrict__ apos,
-                             float4 *__restrict__ frac32, int *__restrict__ flags) {
+                             float4 *__restrict__ frac32, float4 *__restrict__ pos2f,
+                             int *__restrict__ flags) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   int lo = 0, hi = S;  // largest s with atom_off[s] <= i
@@ -217,6 +219,10 @@ __global__ void k_prep_atoms(int N, int S, const int *__restrict__ atom_off,
   if (!found) atomicOr(flags, kFlagUnknownSpecies);
   double x = pos[3 * (size_t)i], y = pos[3 * (size_t)i + 1], zc = pos[3 * (size_t)i + 2];
   apos[i] = make_double4(x, y, zc, w);
+  const float xh = (float)x, yh = (float)y, zh = (float)zc;
+  pos2f[2 * (size_t)i] = make_float4(xh, yh, zh, 0.f);
+  pos2f[2 * (size_t)i + 1] = make_float4((float)(x - (double)xh), (float)(y - (double)yh),
+                                         (float)(zc - (double)zh), 0.f);
   const double *inv = sinfo[lo].linv;
   frac32[i] = make_float4((float)(x * inv[0] + y * inv[3] + zc * inv[6]),
                           (float)(x * inv[1] + y * inv[4] + zc * inv[7]),
@@ -278,6 +284,47 @@ __device__ __forceinline__ float4 fast_rel(const double4 &pi, const double4 &pj,
   return make_float4(d[0], d[1], d[2], d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
 }
 
+// s + e == a + b exactly (Knuth's two-sum; the _rn intrinsics keep the
+// compiler from contracting or reordering it)
+__device__ __forceinline__ float two_sum(float a, float b, float &e) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return s;
+}
+
+// The FP32 form's relative vector for an image n with every |n_a| <= 1 (the
+// cells wider than twice the cutoff), in double-float FP32 arithmetic: the
+// positions and the lattice as high + low FP32 parts, the high parts summed
+// exactly by two-sums (n L_hi is exact for |n| <= 1), the low parts and the
+// two-sum errors added to a low word, and the pair rounded once to FP32.
+// It carries about 48 bits, so it rounds like fast_rel's FP64 vector but
+// needs no FP64 operation (GB300's FP64 rate is 1/74 of its FP32 rate).
+// Every step is odd under negation, so the reverse pair's vector is the
+// exact negation.
+__device__ __forceinline__ float4 df_rel(const float4 &pih, const float4 &pil, const float4 &pjh,
+                                         const float4 &pjl, const float *Lh, const float *Ll,
+                                         int n1, int n2, int n3) {
+  const float f1 = (float)n1, f2 = (float)n2, f3 = (float)n3;
+  const float hj[3] = {pjh.x, pjh.y, pjh.z}, hi[3] = {pih.x, pih.y, pih.z};
+  const float lj[3] = {pjl.x, pjl.y, pjl.z}, li[3] = {pil.x, pil.y, pil.z};
+  float d[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float e0, e1, e2, e3;
+    float sum = two_sum(hj[k], -hi[k], e0);
+    sum = two_sum(sum, f1 * Lh[k], e1);
+    sum = two_sum(sum, f2 * Lh[3 + k], e2);
+    sum = two_sum(sum, f3 * Lh[6 + k], e3);
+    float lo = __fsub_rn(lj[k], li[k]);
+    lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(e0, e1), __fadd_rn(e2, e3)));
+    lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(__fmul_rn(f1, Ll[k]), __fmul_rn(f2, Ll[3 + k])),
+                                 __fmul_rn(f3, Ll[6 + k])));
+    d[k] = __fadd_rn(sum, lo);
+  }
+  return make_float4(d[0], d[1], d[2], d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+}
+
 __device__ __forceinline__ void image_box(const float ext[3], const int nabc[3], const float4 &fi,
                                           const float4 &fj, int lo[3], int hi[3]) {
   const float d[3] = {fj.x - fi.x, fj.y - fi.y, fj.z - fi.z};
@@ -315,6 +362,7 @@ __global__ void __launch_bounds__(128, (WIDE && !EXACT) ? 6 : 5)
     k_nbr_build(int N, int cap, double rcut,
                                                    const double4 *__restrict__ apos,
                                                    const float4 *__restrict__ frac32,
+                                                   const float4 *__restrict__ pos2f,
                                                    const int *__restrict__ atom_struct,
                                                    const StructInfo *__restrict__ sinfo,
                                                    int *__restrict__ cnt, double4 *__restrict__ xyzr,
@@ -340,6 +388,12 @@ __global__ void __launch_bounds__(128, (WIDE && !EXACT) ? 6 : 5)
     const StructInfo si = sinfo[sidx];
     const double4 pi = apos[i];
     const float4 fi = frac32[i];
+    // the double-float position of atom i (the FP32 form of wide cells)
+    float4 pih = make_float4(0.f, 0.f, 0.f, 0.f), pil = pih;
+    if constexpr (WIDE && !EXACT) {
+      pih = pos2f[2 * (size_t)i];
+      pil = pos2f[2 * (size_t)i + 1];
+    }
     // FP32 screen constants of the structure (k_prep_struct): the lattice,
     // the squared bound rcut plus the fractional rounding margin, rcut^2
     const float *L32 = si.lat32;
@@ -377,8 +431,12 @@ __global__ void __launch_bounds__(128, (WIDE && !EXACT) ? 6 : 5)
                           s_dn[n3 + kMaxImage], xyz);
           hit = in & !(dis > rcut);
         } else {
-          fr = fast_rel(pi, apos[jj], si.lat, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
-                        s_dn[n3 + kMaxImage]);
+          if constexpr (WIDE)  // every |n| <= nabc = 1 in a wide cell
+            fr = df_rel(pih, pil, pos2f[2 * (size_t)jj], pos2f[2 * (size_t)jj + 1], si.lat32,
+                        si.latl32, n1, n2, n3);
+          else
+            fr = fast_rel(pi, apos[jj], si.lat, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
+                          s_dn[n3 + kMaxImage]);
           hit = in & (fr.w <= rc2f);
         }
         __syncwarp();
@@ -804,7 +862,7 @@ void launch_prep(const gapgb_model *m, Workspace &ws, int S, int N, const int *d
                                                  ws.sinfo, ws.d_flags);
   k_prep_atoms<<<(N + 255) / 256, 256, 0, st>>>(N, S, d_atom_off, d_species, d_pos, m->d_sf,
                                                  ws.sinfo, ws.atom_struct, ws.apos, ws.frac32,
-                                                 ws.d_flags);
+                                                 ws.pos2f, ws.d_flags);
 }
 
 void launch_neighbors(Workspace &ws, int S, int N, int max_atoms, int cap, double rcut,
@@ -815,8 +873,8 @@ void launch_neighbors(Workspace &ws, int S, int N, int max_atoms, int cap, doubl
   // cells wider than twice the cutoff, then the other unbinned cells
   for (auto fn : {build_wide, build})
     fn<<<grid_for_warps(N), 32 * kWarpsPerBlock, 0, st>>>(
-        N, cap, rcut, ws.apos, ws.frac32, ws.atom_struct, ws.sinfo, ws.nbr_cnt, ws.nbr_xyz,
-        ws.nbr_j, ws.nbr_s, ws.nbr_d32, ws.nbr_w32, ws.d_flags);
+        N, cap, rcut, ws.apos, ws.frac32, ws.pos2f, ws.atom_struct, ws.sinfo, ws.nbr_cnt,
+        ws.nbr_xyz, ws.nbr_j, ws.nbr_s, ws.nbr_d32, ws.nbr_w32, ws.d_flags);
   if (max_atoms < kBinMinAtoms) return;  // no structure was binned (launch_prep)
   int *total = ws.bin_count + N;  // last entry of the count array holds the bin total
   cudaMemsetAsync(ws.bin_count, 0, sizeof(int) * (size_t)(N + 1), st);
