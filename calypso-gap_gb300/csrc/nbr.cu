@@ -293,15 +293,16 @@ __device__ __forceinline__ float two_sum(float a, float b, float &e) {
   return s;
 }
 
-// The FP32 form's relative vector for an image n with every |n_a| <= 1 (the
-// cells wider than twice the cutoff), in double-float FP32 arithmetic: the
+// The FP32 form's relative vector in double-float FP32 arithmetic: the
 // positions and the lattice as high + low FP32 parts, the high parts summed
-// exactly by two-sums (n L_hi is exact for |n| <= 1), the low parts and the
-// two-sum errors added to a low word, and the pair rounded once to FP32.
-// It carries about 48 bits, so it rounds like fast_rel's FP64 vector but
-// needs no FP64 operation (GB300's FP64 rate is 1/74 of its FP32 rate).
-// Every step is odd under negation, so the reverse pair's vector is the
-// exact negation.
+// exactly by two-sums, the low parts and the two-sum errors added to a low
+// word, and the pair rounded once to FP32.  n L_hi is exact when every
+// |n_a| <= 1 (UNIT: the cells wider than twice the cutoff); otherwise each
+// product is split exactly by an FMA (p + e = n L_hi, |n| < 2^7).  It carries
+// about 48 bits, so it rounds like fast_rel's FP64 vector but needs no FP64
+// operation (GB300's FP64 rate is 1/74 of its FP32 rate).  Every step is odd
+// under negation, so the reverse pair's vector is the exact negation.
+template <bool UNIT>
 __device__ __forceinline__ float4 df_rel(const float4 &pih, const float4 &pil, const float4 &pjh,
                                          const float4 &pjl, const float *Lh, const float *Ll,
                                          int n1, int n2, int n3) {
@@ -312,12 +313,17 @@ __device__ __forceinline__ float4 df_rel(const float4 &pih, const float4 &pil, c
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     float e0, e1, e2, e3;
+    const float p1 = __fmul_rn(f1, Lh[k]), p2 = __fmul_rn(f2, Lh[3 + k]),
+                p3 = __fmul_rn(f3, Lh[6 + k]);
     float sum = two_sum(hj[k], -hi[k], e0);
-    sum = two_sum(sum, f1 * Lh[k], e1);
-    sum = two_sum(sum, f2 * Lh[3 + k], e2);
-    sum = two_sum(sum, f3 * Lh[6 + k], e3);
+    sum = two_sum(sum, p1, e1);
+    sum = two_sum(sum, p2, e2);
+    sum = two_sum(sum, p3, e3);
     float lo = __fsub_rn(lj[k], li[k]);
     lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(e0, e1), __fadd_rn(e2, e3)));
+    if constexpr (!UNIT)  // the products' rounding errors
+      lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(__fmaf_rn(f1, Lh[k], -p1), __fmaf_rn(f2, Lh[3 + k], -p2)),
+                                   __fmaf_rn(f3, Lh[6 + k], -p3)));
     lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(__fmul_rn(f1, Ll[k]), __fmul_rn(f2, Ll[3 + k])),
                                  __fmul_rn(f3, Ll[6 + k])));
     d[k] = __fadd_rn(sum, lo);
@@ -432,8 +438,8 @@ __global__ void __launch_bounds__(128, (WIDE && !EXACT) ? 6 : 5)
           hit = in & !(dis > rcut);
         } else {
           if constexpr (WIDE)  // every |n| <= nabc = 1 in a wide cell
-            fr = df_rel(pih, pil, pos2f[2 * (size_t)jj], pos2f[2 * (size_t)jj + 1], si.lat32,
-                        si.latl32, n1, n2, n3);
+            fr = df_rel<true>(pih, pil, pos2f[2 * (size_t)jj], pos2f[2 * (size_t)jj + 1],
+                              si.lat32, si.latl32, n1, n2, n3);
           else
             fr = fast_rel(pi, apos[jj], si.lat, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
                           s_dn[n3 + kMaxImage]);
@@ -778,7 +784,7 @@ __global__ void k_nbr_reverse(int N, int cap, const int *__restrict__ cnt,
 template <bool EXACT>
 __global__ void k_nbr_refresh(int N, int cap, const int *__restrict__ cnt,
                               const int *__restrict__ nj, const int *__restrict__ ns,
-                              const double4 *__restrict__ apos,
+                              const double4 *__restrict__ apos, const float4 *__restrict__ pos2f,
                               const int *__restrict__ atom_struct,
                               const StructInfo *__restrict__ sinfo, double4 *__restrict__ xyzr,
                               float4 *__restrict__ d32) {
@@ -802,8 +808,11 @@ __global__ void k_nbr_refresh(int N, int cap, const int *__restrict__ cnt,
       d32[idx] = make_float4(d2f_rn(xyz[0] - pi.x), d2f_rn(xyz[1] - pi.y),
                              d2f_rn(xyz[2] - pi.z), d2f_rn(dis));
     } else {
-      const float4 fr = fast_rel(pi, apos[j], L, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
-                                 s_dn[n3 + kMaxImage]);
+      // double-float, as the wide build kernel: no FP64 operation per slot
+      const StructInfo &si = sinfo[atom_struct[i]];
+      const float4 fr = df_rel<false>(pos2f[2 * (size_t)i], pos2f[2 * (size_t)i + 1],
+                                      pos2f[2 * (size_t)j], pos2f[2 * (size_t)j + 1], si.lat32,
+                                      si.latl32, n1, n2, n3);
       d32[idx] = make_float4(fr.x, fr.y, fr.z, sqrtf(fr.w));
     }
   }
@@ -903,8 +912,8 @@ void launch_refresh(Workspace &ws, int N, int cap, cudaStream_t st, bool exact) 
   const size_t want = (total + 255) / 256;
   const int grid = (int)std::min<size_t>(want > 0 ? want : 1, (size_t)sms * 8);
   auto fn = exact ? k_nbr_refresh<true> : k_nbr_refresh<false>;
-  fn<<<grid, 256, 0, st>>>(N, cap, ws.nbr_cnt, ws.nbr_j, ws.nbr_s, ws.apos, ws.atom_struct,
-                           ws.sinfo, ws.nbr_xyz, ws.nbr_d32);
+  fn<<<grid, 256, 0, st>>>(N, cap, ws.nbr_cnt, ws.nbr_j, ws.nbr_s, ws.apos, ws.pos2f,
+                           ws.atom_struct, ws.sinfo, ws.nbr_xyz, ws.nbr_d32);
 }
 
 void launch_reverse(Workspace &ws, int N, int cap, cudaStream_t st) {
