@@ -394,9 +394,9 @@ __global__ void __launch_bounds__(128, (WIDE && !EXACT) ? 6 : 5)
     const StructInfo si = sinfo[sidx];
     const double4 pi = apos[i];
     const float4 fi = frac32[i];
-    // the double-float position of atom i (the FP32 form of wide cells)
+    // the double-float position of atom i (the FP32 form)
     float4 pih = make_float4(0.f, 0.f, 0.f, 0.f), pil = pih;
-    if constexpr (WIDE && !EXACT) {
+    if constexpr (!EXACT) {
       pih = pos2f[2 * (size_t)i];
       pil = pos2f[2 * (size_t)i + 1];
     }
@@ -437,12 +437,8 @@ __global__ void __launch_bounds__(128, (WIDE && !EXACT) ? 6 : 5)
                           s_dn[n3 + kMaxImage], xyz);
           hit = in & !(dis > rcut);
         } else {
-          if constexpr (WIDE)  // every |n| <= nabc = 1 in a wide cell
-            fr = df_rel<true>(pih, pil, pos2f[2 * (size_t)jj], pos2f[2 * (size_t)jj + 1],
-                              si.lat32, si.latl32, n1, n2, n3);
-          else
-            fr = fast_rel(pi, apos[jj], si.lat, s_dn[n1 + kMaxImage], s_dn[n2 + kMaxImage],
-                          s_dn[n3 + kMaxImage]);
+          fr = df_rel<WIDE>(pih, pil, pos2f[2 * (size_t)jj], pos2f[2 * (size_t)jj + 1],
+                            si.lat32, si.latl32, n1, n2, n3);
           hit = in & (fr.w <= rc2f);
         }
         __syncwarp();
