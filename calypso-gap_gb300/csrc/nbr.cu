@@ -269,12 +269,14 @@ __device__ __forceinline__ double ref_image(const double4 &pi, const double4 &pj
                               __dmul_rn(dr[2], dr[2])));
 }
 
-// FP32 forms of the evaluation: relative vector d = (p_j - p_i) + n L with
-// FP64 fused multiply-adds (12 FP64 operations instead of the reference
-// formula's ~40 with the square root), rounded once to FP32; the cutoff test
-// runs on the FP32 squared length.  The reverse pair's vector is the exact
-// negation, so both members of a pair agree.  Only where bit-identical
-// lists are not required (fc and fc' vanish at the cutoff).
+// FP32 forms of the evaluation in the binned build of large cells: relative
+// vector d = (p_j - p_i) + n L with FP64 fused multiply-adds (12 FP64
+// operations instead of the reference formula's ~40 with the square root),
+// rounded once to FP32; the cutoff test runs on the FP32 squared length.  The
+// reverse pair's vector is the exact negation, so both members of a pair
+// agree.  Only where bit-identical lists are not required (fc and fc' vanish
+// at the cutoff).  The unbinned builds and the MD refresh use df_rel below,
+// which rounds the same way without FP64 operations.
 __device__ __forceinline__ float4 fast_rel(const double4 &pi, const double4 &pj, const double *L,
                                            double dn1, double dn2, double dn3) {
   const double p[3] = {pj.x - pi.x, pj.y - pi.y, pj.z - pi.z};
